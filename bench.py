@@ -1,0 +1,448 @@
+"""Benchmark of the sparse x dense mul! hot path on one GB300 (or N replicas under torchrun).
+
+Headline: plain Float64 CSR SpMV ``mul!(y, A, x)`` of the 2D 5-point Laplacian on a 2048 x 2048
+grid (n = 4,194,304, nnz = 20,963,328, Int32 indices, alpha = 1, beta = 0), synthetic and
+generated on the host from the stated formula.  Metric: algorithmic HBM GB/s under the
+minimal-bytes model  nnz*(8+4) + (m+1)*4 + n*8 + m*8 = 335.45 MB per SpMV.
+
+* ``value``     device time of K SpMVs with A, x, y resident in HBM; L2 is flushed (a 512 MB
+                write) before every timed SpMV and only the SpMV sits between the events
+* ``roofline``  the dominant kernel (merge-path gather) timed by events the library records
+                right around it; algorithmic bytes / its average duration vs the measured
+                HBM copy bandwidth in MEASURED_PEAKS.json
+* ``e2e``       the same metric through the public API from pinned host buffers: per step the
+                host->device copy of x, mul!, the device->host copy of y
+* ``cpu_baseline``  the oracle's C restatement of the reference kernel (OpenMP, all host
+                cores) on the same matrix, a bounded number of SpMVs
+* ``extras``    the other benchmark rows (CSC, SpMM k=16, F32, Int64 indices, power-law
+                ComplexF64 CSR/COO, n=1e5 random CSR/CSC/COO, COO->CSR conversion)
+
+``--impl reference`` times the CPU restatement of the reference (the reference itself is
+Julia, absent on this machine) on the same workload and prints the same JSON line.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+L2_FLUSH_BYTES = 512 << 20
+METRIC = "SpMV/SpMM HBM GB/s (% of peak); batched mul!/s + p99 vs plain GPU at 1e-12"
+
+
+def spmv_bytes(m, n, nnz, vs, is_, k=1, beta_read=False):
+    b = nnz * (vs + is_) + (m + 1) * is_ + n * k * vs + m * k * vs
+    return b + (m * k * vs if beta_read else 0)
+
+
+def measured_peak():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def committed_traffic(key):
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
+            return json.load(f).get(key)
+    except Exception:
+        return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 100 ms while running."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.thread.join(timeout=2)
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 8:
+                continue
+            try:
+                sm.append(float(p[0]))
+                mx.append(float(p[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, p[4:8]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def cpu_spmv_sample(oracle, m, n, rp, cv, nz, x, budget_s=10.0, max_reps=200):
+    """Time the C restatement of kernel_spmatmul_csr_N! (OpenMP, all host threads)."""
+    threads = oracle.max_threads()
+    y = np.zeros(m)
+    oracle.mul("csr", "N", m, n, rp, cv, nz, 1, x, y, nthreads=threads)  # warm-up
+    times = []
+    t_end = time.perf_counter() + budget_s
+    while len(times) < max_reps and (time.perf_counter() < t_end or len(times) < 3):
+        t0 = time.perf_counter()
+        oracle.mul("csr", "N", m, n, rp, cv, nz, 1, x, y, nthreads=threads)
+        times.append(time.perf_counter() - t0)
+    return statistics.median(times), len(times), threads
+
+
+def run_reference(args, world, rank):
+    """CPU restatement of the reference on the headline workload (rank 0 only)."""
+    if rank != 0:
+        return
+    from oracle import oracle
+    import genericsparsearrays_gb300  # noqa: F401  (registered by __graft_entry__)
+    wl = genericsparsearrays_gb300.workloads
+    m, n, rp, cv, nz = wl.laplacian_2d(2048, itype=np.int32, dtype=np.float64)
+    x = np.random.default_rng(0).uniform(-1, 1, n)
+    threads = oracle.max_threads()
+    y = np.zeros(m)
+    for _ in range(args.warmup):
+        oracle.mul("csr", "N", m, n, rp, cv, nz, 1, x, y, nthreads=threads)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        oracle.mul("csr", "N", m, n, rp, cv, nz, 1, x, y, nthreads=threads)
+        times.append(time.perf_counter() - t0)
+    nbytes = spmv_bytes(m, n, cv.size, 8, 4)
+    total = sum(times)
+    value = nbytes * len(times) / total / 1e9
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(value, 2), "unit": "GB/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(total / len(times) * 1e3, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "laplacian_2048x2048_csr_spmv_f64_i32", "n": m, "nnz": int(cv.size),
+                   "bytes_per_step": nbytes, "impl_note":
+                   "C/OpenMP restatement of kernel_spmatmul_csr_N! (Julia reference absent)"},
+        "cpu_baseline": {"value": round(value, 2), "unit": "GB/s", "cores": threads, "kind": "port",
+                         "sample": f"{len(times)} full SpMVs of the 2048^2 Laplacian"},
+        "e2e": {"value": round(value, 2), "unit": "GB/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+
+class DeviceTimer:
+    """Per-step CUDA-event timing on the current stream, with an L2 flush between steps."""
+
+    def __init__(self, torch, device):
+        self.torch = torch
+        self.flush_buf = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=device)
+
+    def flush(self):
+        self.flush_buf.fill_(1.0)
+
+    def run(self, fn, steps, warmup, flush=True, kernel_events=None, lib=None):
+        torch = self.torch
+        for _ in range(warmup):
+            fn()
+        torch.cuda.synchronize()
+        starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+        ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+        kb = [torch.cuda.Event(enable_timing=True) for _ in range(steps)] if kernel_events else None
+        ka = [torch.cuda.Event(enable_timing=True) for _ in range(steps)] if kernel_events else None
+        torch.cuda.synchronize()
+        for i in range(steps):
+            if flush:
+                self.flush()
+            if kernel_events:
+                lib.gsa_set_kernel_timer(ctypes.c_void_p(kb[i].cuda_event), ctypes.c_void_p(ka[i].cuda_event))
+            starts[i].record()
+            fn()
+            ends[i].record()
+        if kernel_events:
+            lib.gsa_set_kernel_timer(None, None)
+        torch.cuda.synchronize()
+        total_ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
+        kern_ms = sum(b.elapsed_time(a) for b, a in zip(kb, ka)) if kernel_events else None
+        return total_ms, kern_ms
+
+
+def run_gpu(args, world, rank, local):
+    import torch
+    import __graft_entry__
+    gsa = __graft_entry__.load_package()
+    from genericsparsearrays_gb300 import workloads as wl
+    from genericsparsearrays_gb300 import _lib
+
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    lib = _lib.load()
+    timer = DeviceTimer(torch, dev)
+    peak, peak_kind = measured_peak()
+
+    # ---- headline workload ------------------------------------------------
+    m, n, rp, cv, nz = wl.laplacian_2d(2048, itype=np.int32, dtype=np.float64)
+    nnz = int(cv.size)
+    nbytes = spmv_bytes(m, n, nnz, 8, 4)
+    rng = np.random.default_rng(0)
+    x_host = rng.uniform(-1, 1, n)
+    A = gsa.adapt(dev, gsa.GenericSparseMatrixCSR(m, n, rp, cv, nz))
+    x = torch.from_numpy(x_host).to(dev)
+    y = torch.empty(m, dtype=torch.float64, device=dev)
+    ws_bytes = lib.gsa_mul_workspace_size(0, _lib.F64, _lib.IDX32, m, n, nnz, 0, 1, 0)
+    ws = torch.empty(max(ws_bytes, 1), dtype=torch.uint8, device=dev)
+    one, zero = np.array([1.0]), np.array([0.0])
+    pone, pzero = one.ctypes.data_as(ctypes.c_void_p), zero.ctypes.data_as(ctypes.c_void_p)
+
+    def spmv_capi(algo=0):
+        st = lib.gsa_csr_mul(ctypes.c_void_p(torch.cuda.current_stream().cuda_stream), _lib.F64,
+                             _lib.IDX32, m, n, nnz, ctypes.c_void_p(A.rowptr.data_ptr()),
+                             ctypes.c_void_p(A.colval.data_ptr()), ctypes.c_void_p(A.nzval.data_ptr()),
+                             1, 0, 1, ctypes.c_void_p(x.data_ptr()), n, 0,
+                             ctypes.c_void_p(y.data_ptr()), m, pone, pzero, algo,
+                             ctypes.c_void_p(ws.data_ptr()), ws.numel())
+        if st:
+            raise RuntimeError(_lib.last_error())
+
+    # correctness guard on the benchmarked call
+    spmv_capi()
+    torch.cuda.synchronize()
+    import scipy.sparse as sp
+    S = sp.csr_matrix((nz, cv.astype(np.int64) - 1, rp.astype(np.int64) - 1), shape=(m, n))
+    ref = S @ x_host
+    scale = abs(S) @ np.abs(x_host)
+    err = float(np.max(np.abs(y.cpu().numpy() - ref) / scale))
+    if err > 1e-12:
+        raise SystemExit(f"benchmark result check failed: max rel error {err}")
+
+    with ClockSampler(local) as clocks:
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        total_ms, kern_ms = timer.run(spmv_capi, args.steps, args.warmup, flush=True,
+                                      kernel_events=True, lib=lib)
+        t_rank = torch.tensor([total_ms], dtype=torch.float64, device=dev)
+        if world > 1:
+            torch.distributed.all_reduce(t_rank, op=torch.distributed.ReduceOp.MAX)
+        max_ms = float(t_rank.item())
+        value = world * nbytes * args.steps / (max_ms / 1e3) / 1e9
+        kern_avg_s = kern_ms / args.steps / 1e3
+        achieved = nbytes / kern_avg_s / 1e9
+
+        # e2e through the public API: pinned host x -> device, mul!, device -> pinned host y
+        xh = torch.from_numpy(x_host).pin_memory()
+        yh = torch.empty(m, dtype=torch.float64).pin_memory()
+        xd = torch.empty(n, dtype=torch.float64, device=dev)
+        yd = torch.empty(m, dtype=torch.float64, device=dev)
+
+        def e2e_step():
+            xd.copy_(xh, non_blocking=True)
+            gsa.mul_(yd, A, xd)
+            yh.copy_(yd, non_blocking=True)
+            torch.cuda.current_stream().synchronize()
+
+        for _ in range(args.warmup):
+            e2e_step()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            e2e_step()
+        e2e_s = time.perf_counter() - t0
+        e2e_ok = float(np.max(np.abs(yh.numpy() - ref) / scale)) <= 1e-12
+        e2e_value = nbytes * args.steps / e2e_s / 1e9
+
+        extras = {} if args.no_extras else run_extras(gsa, wl, torch, dev, lib, timer, args)
+
+    clk = clocks.summary()
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        from oracle import oracle
+        t_cpu, reps, threads = cpu_spmv_sample(oracle, m, n, rp, cv, nz, x_host, budget_s=args.cpu_budget)
+        cpu = {"value": round(nbytes / t_cpu / 1e9, 2), "unit": "GB/s", "cores": threads,
+               "kind": "port",
+               "sample": f"{reps} full SpMVs of the 2048^2 Laplacian (median), C/OpenMP restatement"}
+    traffic = committed_traffic("gather_merge_kernel/laplacian_2048_csr_spmv_f64_i32")
+    line = {
+        "metric": METRIC, "value": round(value, 2), "unit": "GB/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(max_ms / args.steps, 5),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded 2048x2048 5-point Laplacian, x U(-1,1))",
+        "config": {"workload": "laplacian_2048x2048_csr_spmv_f64_i32", "n": m, "nnz": nnz,
+                   "bytes_per_step": nbytes, "l2": "flushed (512 MB write) before every timed step",
+                   "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+                   "pct_of_peak": round(100 * value / world / peak, 1), "max_rel_error": err},
+        "roofline": {"bound": "hbm", "kernel": "gather_merge_kernel<double,int,false>",
+                     "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
+                     "kernel_us": round(kern_avg_s * 1e6, 2),
+                     "traffic": traffic},
+        "e2e": {"value": round(e2e_value, 2), "unit": "GB/s", "h2d_bytes_per_step": n * 8,
+                "d2h_bytes_per_step": m * 8, "ms_per_step": round(e2e_s / args.steps * 1e3, 4),
+                "matches_oracle": e2e_ok, "api": "genericsparsearrays_gb300.mul_"},
+        "gpu_launches": 3 * args.steps,
+        "clocks": clk,
+        "cpu_baseline": cpu,
+        "extras": extras,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def run_extras(gsa, wl, torch, dev, lib, timer, args):
+    """Other benchmark rows, fewer steps each: GB/s under the minimal-bytes model."""
+    out = {}
+    steps, warm = max(5, args.steps // 4), 3
+
+    def time_call(fn):
+        total_ms, kern_ms = timer.run(fn, steps, warm, flush=True, kernel_events=True, lib=lib)
+        return total_ms / steps / 1e3, kern_ms / steps / 1e3
+
+    rng = np.random.default_rng(1)
+    # Laplacian: F64/I64, F32/I32, F32/I64 CSR; CSC F64/I32; SpMM k=16; COO->CSR
+    for it, dt, tag in ((np.int64, np.float64, "f64_i64"), (np.int32, np.float32, "f32_i32"),
+                        (np.int64, np.float32, "f32_i64")):
+        m, n, rp, cv, nz = wl.laplacian_2d(2048, itype=it, dtype=dt)
+        A = gsa.adapt(dev, gsa.GenericSparseMatrixCSR(m, n, rp, cv, nz))
+        x = torch.from_numpy(rng.uniform(-1, 1, n).astype(dt)).to(dev)
+        y = torch.empty(m, dtype=x.dtype, device=dev)
+        t, tk = time_call(lambda: gsa.mul_(y, A, x))
+        b = spmv_bytes(m, n, cv.size, np.dtype(dt).itemsize, np.dtype(it).itemsize)
+        out[f"laplacian_csr_spmv_{tag}"] = {"GBps": round(b / t / 1e9, 1), "kernel_GBps": round(b / tk / 1e9, 1),
+                                             "us": round(t * 1e6, 2)}
+        del A
+    m, n, rp, cv, nz = wl.laplacian_2d(2048, itype=np.int32, dtype=np.float64)
+    A = gsa.adapt(dev, gsa.GenericSparseMatrixCSR(m, n, rp, cv, nz))
+    x = torch.from_numpy(rng.uniform(-1, 1, n)).to(dev)
+    y = torch.empty(m, dtype=torch.float64, device=dev)
+    b1 = spmv_bytes(m, n, cv.size, 8, 4)
+    t, tk = time_call(lambda: gsa.mul_(y, A, x, algo=gsa.ALGO_VECTOR))
+    out["laplacian_csr_spmv_f64_i32_vector"] = {"GBps": round(b1 / t / 1e9, 1), "kernel_GBps": round(b1 / tk / 1e9, 1),
+                                                 "us": round(t * 1e6, 2)}
+    _, _, cp, rv, cz = wl.csr_to_csc(m, n, rp, cv, nz)
+    K = gsa.adapt(dev, gsa.GenericSparseMatrixCSC(m, n, cp, rv, cz))
+    t, tk = time_call(lambda: gsa.mul_(y, K, x))
+    out["laplacian_csc_spmv_f64_i32"] = {"GBps": round(b1 / t / 1e9, 1), "kernel_GBps": round(b1 / tk / 1e9, 1),
+                                          "us": round(t * 1e6, 2)}
+    del K
+    X = torch.empty((16, n), dtype=torch.float64, device=dev).t()
+    X.copy_(torch.from_numpy(rng.uniform(-1, 1, (n, 16))))
+    Y = torch.empty((16, m), dtype=torch.float64, device=dev).t()
+    bk = spmv_bytes(m, n, cv.size, 8, 4, k=16)
+    t, tk = time_call(lambda: gsa.mul_(Y, A, X))
+    out["laplacian_csr_spmm_k16_f64_i32"] = {"GBps": round(bk / t / 1e9, 1), "kernel_GBps": round(bk / tk / 1e9, 1),
+                                              "us": round(t * 1e6, 2)}
+    del X, Y
+    _, _, r, c, v = wl.permuted_coo(m, n, rp, cv, nz, seed=7)
+    C = gsa.adapt(dev, gsa.GenericSparseMatrixCOO(m, n, r.astype(np.int64), c.astype(np.int64), v))
+    bc = cv.size * (8 + 16) + cv.size * (8 + 8) + (m + 1) * 8
+    t, tk = time_call(lambda: gsa.GenericSparseMatrixCSR(C))
+    out["laplacian_coo_to_csr_f64_i64"] = {"GBps": round(bc / t / 1e9, 1), "us": round(t * 1e6, 1)}
+    del C, A
+    # power-law ComplexF64 CSR and COO
+    m, n, rp, cv, nz = wl.power_law(1_000_000, seed=0, itype=np.int64, dtype=np.complex128)
+    A = gsa.adapt(dev, gsa.GenericSparseMatrixCSR(m, n, rp, cv, nz))
+    x = torch.from_numpy(rng.standard_normal(n) + 1j * rng.standard_normal(n)).to(dev)
+    y = torch.empty(m, dtype=torch.complex128, device=dev)
+    bp = spmv_bytes(m, n, cv.size, 16, 8)
+    t, tk = time_call(lambda: gsa.mul_(y, A, x))
+    out["powerlaw_csr_spmv_c64_i64"] = {"GBps": round(bp / t / 1e9, 1), "kernel_GBps": round(bp / tk / 1e9, 1),
+                                         "us": round(t * 1e6, 2), "nnz": int(cv.size)}
+    Cp = gsa.adapt(dev, gsa.GenericSparseMatrixCOO(m, n, wl.csr_rows(rp), cv, nz))
+    bq = cv.size * (16 + 16) + n * 16 + m * 16
+    t, tk = time_call(lambda: gsa.mul_(y, Cp, x))
+    out["powerlaw_coo_spmv_c64_i64"] = {"GBps": round(bq / t / 1e9, 1), "kernel_GBps": round(bq / tk / 1e9, 1),
+                                         "us": round(t * 1e6, 2)}
+    del A, Cp
+    # n = 1e5 Poisson(10): CSR / CSC / COO (18 MB: L2-resident unless flushed; flushed here)
+    m, n, rp, cv, nz = wl.random_poisson(100_000, seed=0)
+    A = gsa.adapt(dev, gsa.GenericSparseMatrixCSR(m, n, rp, cv, nz))
+    _, _, cp, rv, cz = wl.csr_to_csc(m, n, rp, cv, nz)
+    K = gsa.adapt(dev, gsa.GenericSparseMatrixCSC(m, n, cp, rv, cz))
+    Co = gsa.GenericSparseMatrixCOO(K)
+    x = torch.from_numpy(rng.uniform(-1, 1, n)).to(dev)
+    y = torch.empty(m, dtype=torch.float64, device=dev)
+    br = spmv_bytes(m, n, cv.size, 8, 8)
+    for name, M in (("csr", A), ("csc", K), ("coo", Co)):
+        t, tk = time_call(lambda: gsa.mul_(y, M, x))
+        out[f"random1e5_{name}_spmv_f64_i64"] = {"GBps": round(br / t / 1e9, 1), "us": round(t * 1e6, 2)}
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gsa", choices=["gsa", "reference"])
+    ap.add_argument("--no-extras", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-budget", type=float, default=10.0)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    world, rank, local = dist_setup()
+    import __graft_entry__
+    __graft_entry__.load_package()
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+        return
+    run_gpu(args, world, rank, local)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,36 @@
+"""GB300-native sparse x dense ``mul!`` and COO -> CSR/CSC conversion for GenericSparseArrays.jl.
+
+The compute lives in ``libgsa.so`` (hand-written sm_103a CUDA behind the C ABI of
+``include/gsa.h``); this package is the host-side mirror of the reference's Julia API for
+that path.  Import it as ``genericsparsearrays_gb300`` (``__graft_entry__.load_package()``
+registers the directory under that name, since its folder name is not an identifier).
+"""
+from . import _lib, workloads
+from .errors import ArgumentError, DimensionMismatch
+from .sparse import (
+    AbstractGenericSparseMatrix,
+    Adjoint,
+    GenericSparseMatrixCOO,
+    GenericSparseMatrixCSC,
+    GenericSparseMatrixCSR,
+    SparseMatrixCSC,
+    Transpose,
+    adapt,
+    adjoint,
+    collect,
+    mul,
+    mul_,
+    nnz,
+    size,
+    transpose,
+    validate,
+)
+
+ALGO_AUTO, ALGO_MERGE, ALGO_VECTOR = _lib.ALGO_AUTO, _lib.ALGO_MERGE, _lib.ALGO_VECTOR
+
+__all__ = [
+    "AbstractGenericSparseMatrix", "Adjoint", "ArgumentError", "DimensionMismatch",
+    "GenericSparseMatrixCOO", "GenericSparseMatrixCSC", "GenericSparseMatrixCSR",
+    "SparseMatrixCSC", "Transpose", "adapt", "adjoint", "collect", "mul", "mul_", "nnz", "size",
+    "transpose", "validate", "ALGO_AUTO", "ALGO_MERGE", "ALGO_VECTOR",
+]

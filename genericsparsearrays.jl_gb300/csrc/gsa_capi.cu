@@ -1,0 +1,397 @@
+// extern "C" entry points of libgsa (declared in include/gsa.h): argument and
+// dimension checks in the order the reference's mul! methods make them,
+// dispatch to the kernels, stream-ordered workspace, error strings.
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include "gsa_internal.cuh"
+
+namespace gsa {
+
+static thread_local char g_err[512] = "";
+static thread_local cudaEvent_t g_timer_before = nullptr, g_timer_after = nullptr;
+
+void timer_before(cudaStream_t s) {
+    if (g_timer_before) cudaEventRecord(g_timer_before, s);
+}
+void timer_after(cudaStream_t s) {
+    if (g_timer_after) cudaEventRecord(g_timer_after, s);
+}
+
+void set_error(const char *fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof(g_err), fmt, ap);
+    va_end(ap);
+}
+
+int fail(int status, const char *fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof(g_err), fmt, ap);
+    va_end(ap);
+    return status;
+}
+
+int check_cuda(cudaError_t e, const char *what) {
+    if (e == cudaSuccess) return GSA_OK;
+    return fail(GSA_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+// Workspace: the caller's, or a stream-ordered allocation released on the
+// same stream once the enqueued work is done with it.
+struct Workspace {
+    void *p = nullptr;
+    size_t bytes = 0;
+    bool owned = false;
+    cudaStream_t s = nullptr;
+    int acquire(cudaStream_t stream, void *user, size_t user_bytes, size_t need) {
+        s = stream;
+        if (need == 0) { p = user; bytes = user_bytes; return GSA_OK; }
+        if (user) {
+            if (user_bytes < need)
+                return fail(GSA_ERR_INVALID_ARG, "workspace of %zu bytes is smaller than the %zu needed",
+                            user_bytes, need);
+            p = user;
+            bytes = user_bytes;
+            return GSA_OK;
+        }
+        cudaError_t e = cudaMallocAsync(&p, need, stream);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return fail(GSA_ERR_ALLOC, "stream-ordered workspace allocation of %zu bytes failed: %s",
+                        need, cudaGetErrorString(e));
+        }
+        owned = true;
+        bytes = need;
+        return GSA_OK;
+    }
+    ~Workspace() {
+        if (owned && p) cudaFreeAsync(p, s);
+    }
+};
+
+static bool misaligned(const void *p, size_t a) { return a && ((uintptr_t)p % a) != 0; }
+
+// Shared checks of the mul! entry points: sizes of op(A), op(B), C.
+static int check_mul_args(int dtype, int itype, int64_t m, int64_t n, int64_t nnz, int opA,
+                          int64_t k, int64_t ldb, int opB, int64_t ldc, const void *alpha,
+                          const void *beta, const void *B, const void *C, const void *const *arrs,
+                          int narr) {
+    size_t vs = dtype_size(dtype), is = itype_size(itype);
+    if (!vs || !is) return fail(GSA_ERR_UNSUPPORTED, "unsupported dtype %d / itype %d", dtype, itype);
+    if (opA < 0 || opA > 2 || opB < 0 || opB > 2)
+        return fail(GSA_ERR_INVALID_ARG, "op must be 0 (N), 1 (T) or 2 (C)");
+    if (m < 0 || n < 0 || nnz < 0 || k < 0)
+        return fail(GSA_ERR_INVALID_ARG, "negative size (m=%lld n=%lld nnz=%lld k=%lld)",
+                    (long long)m, (long long)n, (long long)nnz, (long long)k);
+    if (!alpha || !beta) return fail(GSA_ERR_INVALID_ARG, "alpha and beta must be host pointers");
+    int64_t rows_out = opA == GSA_OP_N ? m : n;
+    int64_t inner = opA == GSA_OP_N ? n : m;
+    int64_t need_ldb = opB == GSA_OP_N ? inner : k;
+    if (ldb < (need_ldb > 1 ? need_ldb : 1))
+        return fail(GSA_ERR_DIM, "ldb=%lld is smaller than %lld", (long long)ldb, (long long)need_ldb);
+    if (ldc < (rows_out > 1 ? rows_out : 1))
+        return fail(GSA_ERR_DIM, "ldc=%lld is smaller than %lld", (long long)ldc, (long long)rows_out);
+    if (rows_out > 0 && k > 0 && !C) return fail(GSA_ERR_INVALID_ARG, "C is NULL");
+    if (inner > 0 && k > 0 && !B) return fail(GSA_ERR_INVALID_ARG, "B is NULL");
+    if (misaligned(B, vs) || misaligned(C, vs))
+        return fail(GSA_ERR_INVALID_ARG, "dense operands must be aligned to their element size");
+    for (int i = 0; i < narr; ++i) {
+        size_t a = (i == narr - 1) ? vs : is;
+        if (misaligned(arrs[i], a))
+            return fail(GSA_ERR_INVALID_ARG, "sparse arrays must be aligned to their element size");
+    }
+    return GSA_OK;
+}
+
+template <typename V> static DenseIn<V> make_in(const void *B, int64_t ldb, int opB) {
+    DenseIn<V> d;
+    d.p = (const V *)B;
+    d.rs = opB == GSA_OP_N ? 1 : ldb;
+    d.cs = opB == GSA_OP_N ? ldb : 1;
+    d.conj = opB == GSA_OP_C;
+    return d;
+}
+
+template <typename V>
+static DenseOut<V> make_out(void *C, int64_t ldc, const void *alpha, const void *beta) {
+    DenseOut<V> d;
+    d.p = (V *)C;
+    d.ld = ldc;
+    memcpy(&d.alpha, alpha, sizeof(V));
+    memcpy(&d.beta, beta, sizeof(V));
+    d.beta_mode = beta_mode_of(d.beta);
+    return d;
+}
+
+struct CompressedMulBody {
+    cudaStream_t s; bool gather; int64_t outer_n, inner_n, nnz, k, rows_out;
+    const void *ptr, *idx, *val, *B, *alpha, *beta; void *C; int base, opA, opB, algo;
+    int64_t ldb, ldc; void *ws; size_t ws_bytes;
+    template <typename V, typename I> int operator()() {
+        CompressedArgs<V, I> a;
+        a.outer_n = outer_n; a.inner_n = inner_n; a.nnz = nnz;
+        a.ptr = (const I *)ptr; a.idx = (const I *)idx; a.val = (const V *)val;
+        a.base = base; a.conjA = (opA == GSA_OP_C);
+        DenseIn<V> Bv = make_in<V>(B, ldb, opB);
+        DenseOut<V> Cv = make_out<V>(C, ldc, alpha, beta);
+        if (rows_out == 0 || k == 0) return GSA_OK;
+        Workspace w;
+        size_t need = gather ? gather_workspace_size<V, I>(outer_n, nnz, k, algo)
+                             : scatter_workspace_size<V, I>(outer_n, nnz, k);
+        int rc = w.acquire(s, ws, ws_bytes, need);
+        if (rc) return rc;
+        if (gather) return launch_gather<V, I>(s, a, k, Bv, Cv, algo, w.p, w.bytes);
+        return launch_scatter<V, I>(s, a, k, Bv, Cv, rows_out, w.p, w.bytes);
+    }
+};
+
+struct CooMulBody {
+    cudaStream_t s; bool trans; int64_t nnz, k, rows_out, in_rows;
+    const void *rowind, *colind, *val, *B, *alpha, *beta; void *C; int base, opA, opB;
+    int64_t ldb, ldc;
+    template <typename V, typename I> int operator()() {
+        DenseIn<V> Bv = make_in<V>(B, ldb, opB);
+        DenseOut<V> Cv = make_out<V>(C, ldc, alpha, beta);
+        if (rows_out == 0 || k == 0) return GSA_OK;
+        const I *out_idx = (const I *)(trans ? colind : rowind);
+        const I *in_idx = (const I *)(trans ? rowind : colind);
+        return launch_coo<V, I>(s, nnz, out_idx, in_idx, (const V *)val, base, opA == GSA_OP_C, k,
+                                Bv, Cv, rows_out, in_rows);
+    }
+};
+
+struct MulWsBody {
+    bool gather; int64_t outer_n, nnz, k; int algo; size_t out;
+    template <typename V, typename I> int operator()() {
+        out = gather ? gather_workspace_size<V, I>(outer_n, nnz, k, algo)
+                     : scatter_workspace_size<V, I>(outer_n, nnz, k);
+        return 0;
+    }
+};
+
+struct CooToCompressedBody {
+    cudaStream_t s; bool colmajor; int64_t m, n, nnz; const void *r, *c, *v; int base;
+    void *po, *io, *vo, *ws; size_t ws_bytes;
+    template <typename V, typename I> int operator()() {
+        Workspace w;
+        int rc = w.acquire(s, ws, ws_bytes, coo_to_compressed_workspace_size<V, I>(m, n, nnz, colmajor));
+        if (rc) return rc;
+        return launch_coo_to_compressed<V, I>(s, colmajor, m, n, nnz, (const I *)r, (const I *)c,
+                                              (const V *)v, base, (I *)po, (I *)io, (V *)vo, w.p,
+                                              w.bytes);
+    }
+};
+
+struct CooToCompressedWsBody {
+    bool colmajor; int64_t m, n, nnz; size_t out;
+    template <typename V, typename I> int operator()() {
+        out = coo_to_compressed_workspace_size<V, I>(m, n, nnz, colmajor);
+        return 0;
+    }
+};
+
+// CSR and CSC share one body: 'compressed rows' decides whether opA == N is a
+// gather (CSR) or a scatter (CSC).
+static int compressed_mul(bool csr, void *stream, int dtype, int itype, int64_t m, int64_t n,
+                          int64_t nnz, const void *ptr, const void *idx, const void *val, int base,
+                          int opA, int64_t k, const void *B, int64_t ldb, int opB, void *C,
+                          int64_t ldc, const void *alpha, const void *beta, int algo, void *ws,
+                          size_t ws_bytes) {
+    const void *arrs[3] = {ptr, idx, val};
+    int rc = check_mul_args(dtype, itype, m, n, nnz, opA, k, ldb, opB, ldc, alpha, beta, B, C, arrs, 3);
+    if (rc) return rc;
+    if (!ptr) return fail(GSA_ERR_INVALID_ARG, "pointer array is NULL");
+    if (nnz > 0 && (!idx || !val)) return fail(GSA_ERR_INVALID_ARG, "index/value arrays are NULL");
+    if (algo < 0 || algo > 2) return fail(GSA_ERR_INVALID_ARG, "unknown algo %d", algo);
+    cudaStream_t s = (cudaStream_t)stream;
+    const bool gather = csr ? (opA == GSA_OP_N) : (opA != GSA_OP_N);
+    const int64_t outer_n = csr ? m : n, inner_n = csr ? n : m;
+    const int64_t rows_out = opA == GSA_OP_N ? m : n;
+    CompressedMulBody body{s, gather, outer_n, inner_n, nnz, k, rows_out, ptr, idx, val, B, alpha,
+                           beta, C, base, opA, opB, algo, ldb, ldc, ws, ws_bytes};
+    return dispatch_vi(dtype, itype, body);
+}
+
+}  // namespace gsa
+
+using namespace gsa;
+
+extern "C" {
+
+int gsa_version(void) { return 100; }
+
+const char *gsa_last_error_string(void) { return g_err; }
+
+void gsa_set_kernel_timer(void *before, void *after) {
+    g_timer_before = (cudaEvent_t)before;
+    g_timer_after = (cudaEvent_t)after;
+}
+
+int gsa_csr_mul(void *stream, int dtype, int itype, int64_t m, int64_t n, int64_t nnz,
+                const void *rowptr, const void *colval, const void *nzval, int base, int opA,
+                int64_t k, const void *B, int64_t ldb, int opB, void *C, int64_t ldc,
+                const void *alpha, const void *beta, int algo, void *workspace,
+                size_t workspace_bytes) {
+    return compressed_mul(true, stream, dtype, itype, m, n, nnz, rowptr, colval, nzval, base, opA,
+                          k, B, ldb, opB, C, ldc, alpha, beta, algo, workspace, workspace_bytes);
+}
+
+int gsa_csc_mul(void *stream, int dtype, int itype, int64_t m, int64_t n, int64_t nnz,
+                const void *colptr, const void *rowval, const void *nzval, int base, int opA,
+                int64_t k, const void *B, int64_t ldb, int opB, void *C, int64_t ldc,
+                const void *alpha, const void *beta, int algo, void *workspace,
+                size_t workspace_bytes) {
+    return compressed_mul(false, stream, dtype, itype, m, n, nnz, colptr, rowval, nzval, base, opA,
+                          k, B, ldb, opB, C, ldc, alpha, beta, algo, workspace, workspace_bytes);
+}
+
+int gsa_coo_mul(void *stream, int dtype, int itype, int64_t m, int64_t n, int64_t nnz,
+                const void *rowind, const void *colind, const void *nzval, int base, int opA,
+                int64_t k, const void *B, int64_t ldb, int opB, void *C, int64_t ldc,
+                const void *alpha, const void *beta) {
+    const void *arrs[3] = {rowind, colind, nzval};
+    int rc = check_mul_args(dtype, itype, m, n, nnz, opA, k, ldb, opB, ldc, alpha, beta, B, C, arrs, 3);
+    if (rc) return rc;
+    if (nnz > 0 && (!rowind || !colind || !nzval))
+        return fail(GSA_ERR_INVALID_ARG, "COO arrays are NULL");
+    cudaStream_t s = (cudaStream_t)stream;
+    const bool trans = opA != GSA_OP_N;
+    const int64_t rows_out = trans ? n : m, in_rows = trans ? m : n;
+    CooMulBody body{s, trans, nnz, k, rows_out, in_rows, rowind, colind, nzval, B, alpha, beta, C,
+                    base, opA, opB, ldb, ldc};
+    return dispatch_vi(dtype, itype, body);
+}
+
+size_t gsa_mul_workspace_size(int format, int dtype, int itype, int64_t m, int64_t n, int64_t nnz,
+                              int opA, int64_t k, int algo) {
+    if (format != 0 && format != 1) return 0;
+    const bool csr = format == 0;
+    const bool gather = csr ? (opA == GSA_OP_N) : (opA != GSA_OP_N);
+    const int64_t outer_n = csr ? m : n;
+    MulWsBody body{gather, outer_n, nnz, k, algo, 0};
+    if (dispatch_vi(dtype, itype, body)) return 0;
+    return body.out;
+}
+
+static int coo_to_compressed(bool colmajor, void *stream, int dtype, int itype, int64_t m, int64_t n,
+                             int64_t nnz, const void *rowind, const void *colind, const void *nzval,
+                             int base, void *ptr_out, void *idx_out, void *val_out, void *ws,
+                             size_t ws_bytes) {
+    size_t vs = dtype_size(dtype), is = itype_size(itype);
+    if (!vs || !is) return fail(GSA_ERR_UNSUPPORTED, "unsupported dtype %d / itype %d", dtype, itype);
+    if (m < 0 || n < 0 || nnz < 0) return fail(GSA_ERR_INVALID_ARG, "negative size");
+    if (!ptr_out) return fail(GSA_ERR_INVALID_ARG, "pointer output is NULL");
+    if (nnz > 0 && (!rowind || !colind || !nzval || !idx_out || !val_out))
+        return fail(GSA_ERR_INVALID_ARG, "NULL array");
+    if (misaligned(rowind, is) || misaligned(colind, is) || misaligned(ptr_out, is) ||
+        misaligned(idx_out, is) || misaligned(nzval, vs) || misaligned(val_out, vs))
+        return fail(GSA_ERR_INVALID_ARG, "arrays must be aligned to their element size");
+    cudaStream_t s = (cudaStream_t)stream;
+    CooToCompressedBody body{s, colmajor, m, n, nnz, rowind, colind, nzval, base, ptr_out, idx_out,
+                             val_out, ws, ws_bytes};
+    return dispatch_vi(dtype, itype, body);
+}
+
+int gsa_coo_to_csr(void *stream, int dtype, int itype, int64_t m, int64_t n, int64_t nnz,
+                   const void *rowind, const void *colind, const void *nzval, int base,
+                   void *rowptr_out, void *colval_out, void *nzval_out, void *workspace,
+                   size_t workspace_bytes) {
+    return coo_to_compressed(false, stream, dtype, itype, m, n, nnz, rowind, colind, nzval, base,
+                             rowptr_out, colval_out, nzval_out, workspace, workspace_bytes);
+}
+
+int gsa_coo_to_csc(void *stream, int dtype, int itype, int64_t m, int64_t n, int64_t nnz,
+                   const void *rowind, const void *colind, const void *nzval, int base,
+                   void *colptr_out, void *rowval_out, void *nzval_out, void *workspace,
+                   size_t workspace_bytes) {
+    return coo_to_compressed(true, stream, dtype, itype, m, n, nnz, rowind, colind, nzval, base,
+                             colptr_out, rowval_out, nzval_out, workspace, workspace_bytes);
+}
+
+size_t gsa_coo_to_compressed_workspace_size(int colmajor, int dtype, int itype, int64_t m, int64_t n,
+                                            int64_t nnz) {
+    CooToCompressedWsBody body{colmajor != 0, m, n, nnz, 0};
+    if (dispatch_vi(dtype, itype, body)) return 0;
+    return body.out;
+}
+
+static int compressed_to_coo(bool colmajor, void *stream, int dtype, int itype, int64_t m, int64_t n,
+                             int64_t nnz, const void *ptr, const void *idx, const void *val, int base,
+                             void *rowind_out, void *colind_out, void *val_out) {
+    size_t vs = dtype_size(dtype), is = itype_size(itype);
+    if (!vs || !is) return fail(GSA_ERR_UNSUPPORTED, "unsupported dtype %d / itype %d", dtype, itype);
+    if (m < 0 || n < 0 || nnz < 0) return fail(GSA_ERR_INVALID_ARG, "negative size");
+    if (!ptr) return fail(GSA_ERR_INVALID_ARG, "pointer array is NULL");
+    if (nnz > 0 && (!idx || !val || !rowind_out || !colind_out || !val_out))
+        return fail(GSA_ERR_INVALID_ARG, "NULL array");
+    if (misaligned(ptr, is) || misaligned(idx, is) || misaligned(rowind_out, is) ||
+        misaligned(colind_out, is) || misaligned(val, vs) || misaligned(val_out, vs))
+        return fail(GSA_ERR_INVALID_ARG, "arrays must be aligned to their element size");
+    if (nnz == 0) return GSA_OK;
+    cudaStream_t s = (cudaStream_t)stream;
+    const int64_t outer_n = colmajor ? n : m;
+    void *major_out = colmajor ? colind_out : rowind_out;
+    void *minor_out = colmajor ? rowind_out : colind_out;
+    int rc = check_cuda(cudaMemcpyAsync(minor_out, idx, (size_t)nnz * is, cudaMemcpyDeviceToDevice, s),
+                        "index copy");
+    if (rc) return rc;
+    rc = check_cuda(cudaMemcpyAsync(val_out, val, (size_t)nnz * vs, cudaMemcpyDeviceToDevice, s),
+                    "value copy");
+    if (rc) return rc;
+    Workspace w;
+    rc = w.acquire(s, nullptr, 0, expand_major_workspace_size(outer_n, nnz));
+    if (rc) return rc;
+    if (itype == GSA_IDX32)
+        return launch_expand_major<int32_t>(s, outer_n, nnz, (const int32_t *)ptr, base,
+                                            (int32_t *)major_out, w.p, w.bytes);
+    return launch_expand_major<int64_t>(s, outer_n, nnz, (const int64_t *)ptr, base,
+                                        (int64_t *)major_out, w.p, w.bytes);
+}
+
+int gsa_csr_to_coo(void *stream, int dtype, int itype, int64_t m, int64_t n, int64_t nnz,
+                   const void *rowptr, const void *colval, const void *nzval, int base,
+                   void *rowind_out, void *colind_out, void *nzval_out) {
+    return compressed_to_coo(false, stream, dtype, itype, m, n, nnz, rowptr, colval, nzval, base,
+                             rowind_out, colind_out, nzval_out);
+}
+
+int gsa_csc_to_coo(void *stream, int dtype, int itype, int64_t m, int64_t n, int64_t nnz,
+                   const void *colptr, const void *rowval, const void *nzval, int base,
+                   void *rowind_out, void *colind_out, void *nzval_out) {
+    return compressed_to_coo(true, stream, dtype, itype, m, n, nnz, colptr, rowval, nzval, base,
+                             rowind_out, colind_out, nzval_out);
+}
+
+int gsa_validate_compressed(void *stream, int itype, int64_t outer_n, int64_t inner_n, int64_t nnz,
+                            const void *ptr, const void *idx, int base) {
+    size_t is = itype_size(itype);
+    if (!is) return fail(GSA_ERR_UNSUPPORTED, "unsupported itype %d", itype);
+    if (outer_n < 0 || inner_n < 0 || nnz < 0) return fail(GSA_ERR_INVALID_ARG, "negative size");
+    if (!ptr || (nnz > 0 && !idx)) return fail(GSA_ERR_INVALID_ARG, "NULL array");
+    cudaStream_t s = (cudaStream_t)stream;
+    int *d_flag = nullptr;
+    int rc = check_cuda(cudaMallocAsync((void **)&d_flag, sizeof(int), s), "validate flag");
+    if (rc) return rc;
+    cudaMemsetAsync(d_flag, 0, sizeof(int), s);
+    rc = itype == GSA_IDX32
+             ? launch_validate<int32_t>(s, outer_n, inner_n, nnz, (const int32_t *)ptr,
+                                        (const int32_t *)idx, base, d_flag)
+             : launch_validate<int64_t>(s, outer_n, inner_n, nnz, (const int64_t *)ptr,
+                                        (const int64_t *)idx, base, d_flag);
+    int h_flag = 0;
+    if (!rc) rc = check_cuda(cudaMemcpyAsync(&h_flag, d_flag, sizeof(int), cudaMemcpyDeviceToHost, s),
+                             "validate readback");
+    cudaFreeAsync(d_flag, s);
+    if (!rc) rc = check_cuda(cudaStreamSynchronize(s), "validate sync");
+    if (rc) return rc;
+    if (h_flag)
+        return fail(GSA_ERR_STRUCTURE, "malformed compressed structure (%s%s%s%s)",
+                    (h_flag & 1) ? "ptr[0] != base; " : "", (h_flag & 2) ? "ptr[end] != nnz+base; " : "",
+                    (h_flag & 4) ? "decreasing ptr; " : "", (h_flag & 8) ? "index out of range" : "");
+    return GSA_OK;
+}
+
+}  // extern "C"

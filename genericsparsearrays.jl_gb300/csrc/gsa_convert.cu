@@ -1,0 +1,447 @@
+// Format conversions.
+//
+// COO -> CSR / CSC (src/conversions/conversions.jl:171-212,282-323).  The
+// reference builds key = major*minor_dim + minor in the index type (wrapping
+// for Int32 once major_dim*minor_dim >= 2^31), sortperms the keys with
+// AcceleratedKernels, gathers the three arrays and binary-searches every
+// major index.  Here:
+//   1. make_keys_kernel: key = (major << minor_bits) | minor as an unsigned
+//      64-bit word (no multiply, no wrap), payload = the entry's position
+//   2. LSD radix sort, 8-bit digits, only over the key bits that can be set;
+//      each pass = per-tile digit histograms, one exclusive scan, a stable
+//      scatter (warp match_any ranking in storage order)
+//   3. finalize_kernel: minor index straight from the key, value gathered by
+//      the payload; pointer_kernel: pointer entries from the boundaries of the
+//      sorted major indices (every entry written exactly once)
+// LSD radix sort is stable, so duplicate (row, col) pairs keep input order.
+//
+// CSR / CSC -> COO (src/conversions/conversion_kernels.jl:2-35): the major
+// index of every entry is written by merge-path tiles (balanced for any row
+// length mix); minor indices and values are plain copies.
+#include "gsa_internal.cuh"
+
+namespace gsa {
+
+constexpr int RS_THREADS = 256;
+constexpr int RS_WARPS = RS_THREADS / 32;
+constexpr int RS_ROUNDS = 8;                       // 32-entry rounds per warp
+constexpr int RS_TILE = RS_THREADS * RS_ROUNDS;    // entries per tile
+constexpr int RS_BITS = 8;
+constexpr int RS_BINS = 1 << RS_BITS;
+
+static int bits_for(int64_t count) {  // bits needed for values 0..count-1
+    int b = 0;
+    while (b < 63 && ((int64_t)1 << b) < count) ++b;
+    return b;
+}
+
+template <typename I>
+__global__ void make_keys_kernel(int64_t nnz, const I *__restrict__ major, const I *__restrict__ minor,
+                                 int base, int minor_bits, uint64_t *__restrict__ keys,
+                                 uint32_t *__restrict__ perm) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nnz;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        uint64_t hi = (uint64_t)((int64_t)ld_stream(major + i) - base);
+        uint64_t lo = (uint64_t)((int64_t)ld_stream(minor + i) - base);
+        keys[i] = minor_bits >= 64 ? lo : ((hi << minor_bits) | lo);
+        perm[i] = (uint32_t)i;
+    }
+}
+
+__device__ __forceinline__ unsigned lanemask_lt() {
+    unsigned m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+// Per-tile digit histograms, digit-major: hist[d * num_tiles + tile].
+__global__ void __launch_bounds__(RS_THREADS)
+radix_upsweep_kernel(const uint64_t *__restrict__ keys, int64_t n, int shift, uint32_t mask,
+                     uint32_t *__restrict__ hist, int64_t num_tiles) {
+    __shared__ uint32_t s_h[RS_BINS];
+    const int tid = threadIdx.x, lane = tid & 31;
+    for (int d = tid; d < RS_BINS; d += RS_THREADS) s_h[d] = 0;
+    __syncthreads();
+    const int64_t t0 = (int64_t)blockIdx.x * RS_TILE;
+#pragma unroll
+    for (int r = 0; r < RS_ROUNDS; ++r) {
+        int64_t e = t0 + (int64_t)r * RS_THREADS + tid;
+        uint32_t d = e < n ? (uint32_t)(keys[e] >> shift) & mask : RS_BINS;
+        unsigned peers = __match_any_sync(0xffffffffu, d);
+        if (d < RS_BINS && lane == __ffs(peers) - 1) atomicAdd(&s_h[d], __popc(peers));
+    }
+    __syncthreads();
+    for (int d = tid; d < RS_BINS; d += RS_THREADS) hist[(int64_t)d * num_tiles + blockIdx.x] = s_h[d];
+}
+
+// Stable scatter.  Warp w of a tile owns entries [w*32*ROUNDS, (w+1)*32*ROUNDS)
+// of the tile and ranks them round by round; per-warp digit counts then give
+// each (warp, digit) its offset inside the tile's slice of the digit bucket.
+__global__ void __launch_bounds__(RS_THREADS)
+radix_downsweep_kernel(const uint64_t *__restrict__ keys_in, const uint32_t *__restrict__ perm_in,
+                       uint64_t *__restrict__ keys_out, uint32_t *__restrict__ perm_out, int64_t n,
+                       int shift, uint32_t mask, const uint32_t *__restrict__ offsets,
+                       int64_t num_tiles) {
+    __shared__ uint32_t s_wh[RS_WARPS][RS_BINS];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    for (int t = tid; t < RS_WARPS * RS_BINS; t += RS_THREADS) (&s_wh[0][0])[t] = 0;
+    __syncthreads();
+    const int64_t w0 = (int64_t)blockIdx.x * RS_TILE + (int64_t)warp * 32 * RS_ROUNDS;
+    const unsigned lt = lanemask_lt();
+    uint64_t key[RS_ROUNDS];
+    uint32_t pv[RS_ROUNDS], rank[RS_ROUNDS], dig[RS_ROUNDS];
+#pragma unroll
+    for (int r = 0; r < RS_ROUNDS; ++r) {
+        int64_t e = w0 + r * 32 + lane;
+        bool valid = e < n;
+        key[r] = valid ? keys_in[e] : 0;
+        pv[r] = valid ? perm_in[e] : 0;
+        dig[r] = valid ? (uint32_t)(key[r] >> shift) & mask : RS_BINS;
+    }
+#pragma unroll
+    for (int r = 0; r < RS_ROUNDS; ++r) {
+        uint32_t d = dig[r];
+        unsigned peers = __match_any_sync(0xffffffffu, d);
+        uint32_t before = d < RS_BINS ? s_wh[warp][d] : 0;
+        rank[r] = before + __popc(peers & lt);
+        __syncwarp();
+        if (d < RS_BINS && lane == __ffs(peers) - 1) s_wh[warp][d] = before + __popc(peers);
+        __syncwarp();
+    }
+    __syncthreads();
+    for (int d = tid; d < RS_BINS; d += RS_THREADS) {
+        uint32_t run = offsets[(int64_t)d * num_tiles + blockIdx.x];
+        for (int w = 0; w < RS_WARPS; ++w) {
+            uint32_t c = s_wh[w][d];
+            s_wh[w][d] = run;
+            run += c;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < RS_ROUNDS; ++r) {
+        if (dig[r] < RS_BINS) {
+            uint32_t pos = s_wh[warp][dig[r]] + rank[r];
+            keys_out[pos] = key[r];
+            perm_out[pos] = pv[r];
+        }
+    }
+}
+
+// ---- exclusive scan of uint32 counts (reduce, scan of block sums, downsweep)
+constexpr int SC_THREADS = 512;
+constexpr int SC_ITEMS = 8;
+constexpr int SC_TILE = SC_THREADS * SC_ITEMS;
+
+__device__ __forceinline__ uint32_t block_excl_scan_u32(uint32_t v, uint32_t *s_warp, uint32_t &total) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    constexpr int W = SC_THREADS / 32;
+    uint32_t x = v;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        uint32_t y = __shfl_up_sync(0xffffffffu, x, off);
+        if (lane >= off) x += y;
+    }
+    if (lane == 31) s_warp[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t s = lane < W ? s_warp[lane] : 0;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            uint32_t y = __shfl_up_sync(0xffffffffu, s, off);
+            if (lane >= off) s += y;
+        }
+        if (lane < W) s_warp[lane] = s;
+    }
+    __syncthreads();
+    uint32_t warp_prefix = warp > 0 ? s_warp[warp - 1] : 0;
+    total = s_warp[W - 1];
+    __syncthreads();
+    return warp_prefix + x - v;
+}
+
+__global__ void __launch_bounds__(SC_THREADS)
+scan_reduce_kernel(const uint32_t *__restrict__ in, int64_t n, uint32_t *__restrict__ block_sums) {
+    __shared__ uint32_t s_warp[SC_THREADS / 32];
+    const int64_t t0 = (int64_t)blockIdx.x * SC_TILE;
+    uint32_t sum = 0;
+#pragma unroll
+    for (int u = 0; u < SC_ITEMS; ++u) {
+        int64_t e = t0 + (int64_t)u * SC_THREADS + threadIdx.x;
+        if (e < n) sum += in[e];
+    }
+    uint32_t total;
+    block_excl_scan_u32(sum, s_warp, total);
+    if (threadIdx.x == 0) block_sums[blockIdx.x] = total;
+}
+
+// Single CTA: exclusive scan of the block sums in place (any count).
+__global__ void __launch_bounds__(SC_THREADS)
+scan_block_sums_kernel(uint32_t *__restrict__ sums, int64_t nb) {
+    __shared__ uint32_t s_warp[SC_THREADS / 32];
+    uint32_t carry = 0;
+    for (int64_t b0 = 0; b0 < nb; b0 += SC_THREADS) {
+        int64_t e = b0 + threadIdx.x;
+        uint32_t v = e < nb ? sums[e] : 0;
+        uint32_t total;
+        uint32_t ex = block_excl_scan_u32(v, s_warp, total);
+        if (e < nb) sums[e] = carry + ex;
+        carry += total;
+    }
+}
+
+// Each thread scans SC_ITEMS consecutive entries (blocked arrangement).
+__global__ void __launch_bounds__(SC_THREADS)
+scan_downsweep_kernel(const uint32_t *__restrict__ in, uint32_t *__restrict__ out, int64_t n,
+                      const uint32_t *__restrict__ block_prefix) {
+    __shared__ uint32_t s_warp[SC_THREADS / 32];
+    const int64_t t0 = (int64_t)blockIdx.x * SC_TILE + (int64_t)threadIdx.x * SC_ITEMS;
+    uint32_t v[SC_ITEMS], sum = 0;
+#pragma unroll
+    for (int u = 0; u < SC_ITEMS; ++u) {
+        v[u] = t0 + u < n ? in[t0 + u] : 0;
+        sum += v[u];
+    }
+    uint32_t total;
+    uint32_t run = block_excl_scan_u32(sum, s_warp, total) + block_prefix[blockIdx.x];
+#pragma unroll
+    for (int u = 0; u < SC_ITEMS; ++u) {
+        if (t0 + u < n) out[t0 + u] = run;
+        run += v[u];
+    }
+}
+
+// The reduce kernel sums each SC_TILE slice in striped order and the downsweep
+// scans the same slice in blocked order: both cover [b*SC_TILE, (b+1)*SC_TILE).
+static int exclusive_scan_u32(cudaStream_t s, const uint32_t *in, uint32_t *out, int64_t n,
+                              uint32_t *block_sums) {
+    if (n == 0) return GSA_OK;
+    int64_t nb = ceil_div(n, SC_TILE);
+    scan_reduce_kernel<<<(unsigned)nb, SC_THREADS, 0, s>>>(in, n, block_sums);
+    scan_block_sums_kernel<<<1, SC_THREADS, 0, s>>>(block_sums, nb);
+    scan_downsweep_kernel<<<(unsigned)nb, SC_THREADS, 0, s>>>(in, out, n, block_sums);
+    return check_cuda(cudaGetLastError(), "exclusive_scan_u32");
+}
+
+template <typename V, typename I>
+__global__ void finalize_kernel(int64_t nnz, const uint64_t *__restrict__ keys,
+                                const uint32_t *__restrict__ perm, int minor_bits, int base,
+                                const V *__restrict__ val_in, I *__restrict__ idx_out,
+                                V *__restrict__ val_out) {
+    const uint64_t mask = minor_bits >= 64 ? ~0ull : ((1ull << minor_bits) - 1);
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nnz;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        idx_out[i] = (I)((int64_t)(keys[i] & mask) + base);
+        val_out[i] = ldg(val_in + perm[i]);
+    }
+}
+
+template <typename I>
+__global__ void pointer_kernel(int64_t nnz, const uint64_t *__restrict__ keys, int minor_bits,
+                               int64_t major_n, int base, I *__restrict__ ptr_out) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i <= nnz;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        int64_t prev = i == 0 ? -1 : (int64_t)(keys[i - 1] >> minor_bits);
+        int64_t cur = i == nnz ? major_n : (int64_t)(keys[i] >> minor_bits);
+        if (cur > major_n) cur = major_n;
+        for (int64_t r = prev + 1; r <= cur; ++r) ptr_out[r] = (I)(i + base);
+    }
+}
+
+struct SortLayout {
+    int64_t num_tiles, hist_n;
+    size_t bytes;
+};
+static SortLayout sort_layout(int64_t nnz) {
+    SortLayout L;
+    L.num_tiles = ceil_div(nnz, RS_TILE);
+    L.hist_n = L.num_tiles * RS_BINS;
+    Carver cv(nullptr);
+    cv.take<uint64_t>(nnz);
+    cv.take<uint64_t>(nnz);
+    cv.take<uint32_t>(nnz);
+    cv.take<uint32_t>(nnz);
+    cv.take<uint32_t>(L.hist_n);
+    cv.take<uint32_t>(ceil_div(L.hist_n, SC_TILE) + 1);
+    L.bytes = align_up(cv.off, 256);
+    return L;
+}
+
+template <typename V, typename I>
+size_t coo_to_compressed_workspace_size(int64_t m, int64_t n, int64_t nnz, bool colmajor) {
+    (void)m; (void)n; (void)colmajor;
+    if (nnz == 0) return 0;
+    return sort_layout(nnz).bytes;
+}
+
+static unsigned grid_for(int64_t n, int threads) {
+    int64_t b = ceil_div(n, threads);
+    if (b > 152 * 32) b = 152 * 32;
+    return (unsigned)(b > 0 ? b : 1);
+}
+
+template <typename V, typename I>
+int launch_coo_to_compressed(cudaStream_t s, bool colmajor, int64_t m, int64_t n, int64_t nnz,
+                             const I *rowind, const I *colind, const V *val, int base,
+                             I *ptr_out, I *idx_out, V *val_out, void *ws, size_t ws_bytes) {
+    const I *major = colmajor ? colind : rowind;
+    const I *minor = colmajor ? rowind : colind;
+    const int64_t major_n = colmajor ? n : m, minor_n = colmajor ? m : n;
+    const int minor_bits = bits_for(minor_n), major_bits = bits_for(major_n);
+    if (minor_bits + major_bits > 64)
+        return fail(GSA_ERR_UNSUPPORTED, "matrix too large for 64-bit sort keys (%lld x %lld)",
+                    (long long)m, (long long)n);
+    if (nnz > 0xffffffffLL)
+        return fail(GSA_ERR_UNSUPPORTED, "conversion supports at most 2^32-1 stored entries");
+    if (nnz == 0) {
+        pointer_kernel<I><<<1, 256, 0, s>>>(0, nullptr, minor_bits, major_n, base, ptr_out);
+        return check_cuda(cudaGetLastError(), "pointer_kernel");
+    }
+    SortLayout L = sort_layout(nnz);
+    if (ws_bytes < L.bytes) return fail(GSA_ERR_INVALID_ARG, "conversion workspace too small");
+    Carver cv(ws);
+    uint64_t *ka = cv.take<uint64_t>(nnz), *kb = cv.take<uint64_t>(nnz);
+    uint32_t *pa = cv.take<uint32_t>(nnz), *pb = cv.take<uint32_t>(nnz);
+    uint32_t *hist = cv.take<uint32_t>(L.hist_n);
+    uint32_t *bsums = cv.take<uint32_t>(ceil_div(L.hist_n, SC_TILE) + 1);
+
+    timer_before(s);
+    make_keys_kernel<I><<<grid_for(nnz, 256), 256, 0, s>>>(nnz, major, minor, base, minor_bits, ka, pa);
+    int rc = check_cuda(cudaGetLastError(), "make_keys_kernel");
+    if (rc) return rc;
+    const int total_bits = minor_bits + major_bits;
+    for (int shift = 0; shift < total_bits; shift += RS_BITS) {
+        int w = total_bits - shift < RS_BITS ? total_bits - shift : RS_BITS;
+        uint32_t mask = (1u << w) - 1;
+        radix_upsweep_kernel<<<(unsigned)L.num_tiles, RS_THREADS, 0, s>>>(ka, nnz, shift, mask, hist,
+                                                                          L.num_tiles);
+        rc = exclusive_scan_u32(s, hist, hist, L.hist_n, bsums);
+        if (rc) return rc;
+        radix_downsweep_kernel<<<(unsigned)L.num_tiles, RS_THREADS, 0, s>>>(
+            ka, pa, kb, pb, nnz, shift, mask, hist, L.num_tiles);
+        rc = check_cuda(cudaGetLastError(), "radix pass");
+        if (rc) return rc;
+        uint64_t *tk = ka; ka = kb; kb = tk;
+        uint32_t *tp = pa; pa = pb; pb = tp;
+    }
+    finalize_kernel<V, I><<<grid_for(nnz, 256), 256, 0, s>>>(nnz, ka, pa, minor_bits, base, val,
+                                                             idx_out, val_out);
+    pointer_kernel<I><<<grid_for(nnz + 1, 256), 256, 0, s>>>(nnz, ka, minor_bits, major_n, base, ptr_out);
+    timer_after(s);
+    return check_cuda(cudaGetLastError(), "finalize/pointer kernels");
+}
+
+// ---------------------------------------------------------------------------
+// CSR / CSC -> COO: major index of every stored entry, merge-path tiles.
+constexpr int EX_THREADS = 256, EX_IPT = 8, EX_TILE = EX_THREADS * EX_IPT;
+
+template <typename I>
+__global__ void __launch_bounds__(EX_THREADS)
+expand_major_kernel(int64_t outer_n, int64_t nnz, const I *__restrict__ ptr, int base,
+                    const int64_t *__restrict__ coords, I *__restrict__ major_out) {
+    __shared__ int s_rowend[EX_TILE];
+    __shared__ int s_outer[EX_TILE];
+    const int64_t tile = blockIdx.x;
+    const int64_t total = outer_n + nnz;
+    const int64_t d0 = tile * EX_TILE;
+    const int64_t d1 = d0 + EX_TILE < total ? d0 + EX_TILE : total;
+    const int64_t rs = coords[tile], re = coords[tile + 1];
+    const int64_t js = d0 - rs, je = d1 - re;
+    const int tile_rows = (int)(re - rs), tile_nnz = (int)(je - js);
+    const int tid = threadIdx.x;
+    for (int e = tid; e < tile_rows; e += EX_THREADS)
+        s_rowend[e] = (int)((int64_t)__ldg(ptr + rs + 1 + e) - base - js);
+    __syncthreads();
+    const int items = tile_rows + tile_nnz;
+    int d = tid * EX_IPT < items ? tid * EX_IPT : items;
+    int lo = d - tile_nnz > 0 ? d - tile_nnz : 0;
+    int hi = d < tile_rows ? d : tile_rows;
+    while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if (s_rowend[mid] + mid < d) lo = mid + 1;
+        else hi = mid;
+    }
+    int i = lo, j = d - lo;
+#pragma unroll
+    for (int step = 0; step < EX_IPT; ++step) {
+        if (i < tile_rows && s_rowend[i] <= j) ++i;
+        else if (j < tile_nnz) s_outer[j++] = i;
+    }
+    __syncthreads();
+    for (int e = tid; e < tile_nnz; e += EX_THREADS) major_out[js + e] = (I)(rs + s_outer[e] + base);
+}
+
+size_t expand_major_workspace_size(int64_t outer_n, int64_t nnz) {
+    if (nnz == 0) return 0;
+    return align_up((size_t)(ceil_div(outer_n + nnz, EX_TILE) + 1) * sizeof(int64_t), 256);
+}
+
+template <typename I>
+int launch_expand_major(cudaStream_t s, int64_t outer_n, int64_t nnz, const I *ptr, int base,
+                        I *major_out, void *ws, size_t ws_bytes) {
+    if (nnz == 0) return GSA_OK;
+    if (ws_bytes < expand_major_workspace_size(outer_n, nnz))
+        return fail(GSA_ERR_INVALID_ARG, "expansion workspace too small");
+    int64_t T = ceil_div(outer_n + nnz, EX_TILE);
+    int64_t *coords = (int64_t *)ws;
+    int rc = launch_merge_partition<I>(s, ptr, base, outer_n, nnz, EX_TILE, T, coords);
+    if (rc) return rc;
+    expand_major_kernel<I><<<(unsigned)T, EX_THREADS, 0, s>>>(outer_n, nnz, ptr, base, coords, major_out);
+    return check_cuda(cudaGetLastError(), "expand_major_kernel");
+}
+
+// ---------------------------------------------------------------------------
+// Structure check; flag bits: 1 ptr[0], 2 ptr[end], 4 decreasing ptr, 8 index out of range.
+template <typename I>
+__global__ void validate_kernel(int64_t outer_n, int64_t inner_n, int64_t nnz, const I *__restrict__ ptr,
+                                const I *__restrict__ idx, int base, int *__restrict__ flag) {
+    int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    int64_t t0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t0 == 0) {
+        if ((int64_t)ptr[0] != base) atomicOr(flag, 1);
+        if ((int64_t)ptr[outer_n] != nnz + base) atomicOr(flag, 2);
+    }
+    for (int64_t o = t0; o < outer_n; o += stride)
+        if (ptr[o + 1] < ptr[o]) atomicOr(flag, 4);
+    for (int64_t j = t0; j < nnz; j += stride) {
+        int64_t v = (int64_t)idx[j] - base;
+        if (v < 0 || v >= inner_n) atomicOr(flag, 8);
+    }
+}
+
+template <typename I>
+int launch_validate(cudaStream_t s, int64_t outer_n, int64_t inner_n, int64_t nnz, const I *ptr,
+                    const I *idx, int base, int *d_flag) {
+    validate_kernel<I><<<grid_for(outer_n > nnz ? outer_n : nnz, 256), 256, 0, s>>>(
+        outer_n, inner_n, nnz, ptr, idx, base, d_flag);
+    return check_cuda(cudaGetLastError(), "validate_kernel");
+}
+
+#define GSA_INST_CONVERT(V, I)                                                                  \
+    template int launch_coo_to_compressed<V, I>(cudaStream_t, bool, int64_t, int64_t, int64_t,  \
+                                                const I *, const I *, const V *, int, I *, I *, \
+                                                V *, void *, size_t);                           \
+    template size_t coo_to_compressed_workspace_size<V, I>(int64_t, int64_t, int64_t, bool);
+GSA_INST_CONVERT(float, int32_t)
+GSA_INST_CONVERT(float, int64_t)
+GSA_INST_CONVERT(double, int32_t)
+GSA_INST_CONVERT(double, int64_t)
+GSA_INST_CONVERT(cf32, int32_t)
+GSA_INST_CONVERT(cf32, int64_t)
+GSA_INST_CONVERT(cf64, int32_t)
+GSA_INST_CONVERT(cf64, int64_t)
+GSA_INST_CONVERT(int32_t, int32_t)
+GSA_INST_CONVERT(int32_t, int64_t)
+GSA_INST_CONVERT(int64_t, int32_t)
+GSA_INST_CONVERT(int64_t, int64_t)
+
+template int launch_expand_major<int32_t>(cudaStream_t, int64_t, int64_t, const int32_t *, int,
+                                          int32_t *, void *, size_t);
+template int launch_expand_major<int64_t>(cudaStream_t, int64_t, int64_t, const int64_t *, int,
+                                          int64_t *, void *, size_t);
+template int launch_validate<int32_t>(cudaStream_t, int64_t, int64_t, int64_t, const int32_t *,
+                                      const int32_t *, int, int *);
+template int launch_validate<int64_t>(cudaStream_t, int64_t, int64_t, int64_t, const int64_t *,
+                                      const int64_t *, int, int *);
+
+}  // namespace gsa

@@ -1,0 +1,321 @@
+// Internal definitions shared by the libgsa translation units: value types,
+// arithmetic in the reference's conventions, dense-operand accessors, error
+// reporting and the dtype x itype dispatch.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stddef.h>
+
+#include "../../include/gsa.h"
+
+namespace gsa {
+
+// ---------------------------------------------------------------------------
+// Value types.  Complex numbers are (re, im) pairs aligned to twice the real
+// size, matching Julia's ComplexF32/ComplexF64 arrays and numpy/torch complex.
+struct alignas(8) cf32 { float re, im; };
+struct alignas(16) cf64 { double re, im; };
+
+template <typename V> struct VT;
+template <> struct VT<float> {
+    static constexpr bool is_complex = false;
+    __host__ __device__ static float zero() { return 0.0f; }
+};
+template <> struct VT<double> {
+    static constexpr bool is_complex = false;
+    __host__ __device__ static double zero() { return 0.0; }
+};
+template <> struct VT<cf32> {
+    static constexpr bool is_complex = true;
+    __host__ __device__ static cf32 zero() { return cf32{0.0f, 0.0f}; }
+};
+template <> struct VT<cf64> {
+    static constexpr bool is_complex = true;
+    __host__ __device__ static cf64 zero() { return cf64{0.0, 0.0}; }
+};
+template <> struct VT<int32_t> {
+    static constexpr bool is_complex = false;
+    __host__ __device__ static int32_t zero() { return 0; }
+};
+template <> struct VT<int64_t> {
+    static constexpr bool is_complex = false;
+    __host__ __device__ static int64_t zero() { return 0; }
+};
+
+// Arithmetic.  Integers wrap (Julia's Int32/Int64 semantics), complex products
+// use the textbook formula Julia uses.
+__host__ __device__ __forceinline__ float add(float a, float b) { return a + b; }
+__host__ __device__ __forceinline__ double add(double a, double b) { return a + b; }
+__host__ __device__ __forceinline__ cf32 add(cf32 a, cf32 b) { return cf32{a.re + b.re, a.im + b.im}; }
+__host__ __device__ __forceinline__ cf64 add(cf64 a, cf64 b) { return cf64{a.re + b.re, a.im + b.im}; }
+__host__ __device__ __forceinline__ int32_t add(int32_t a, int32_t b) {
+    return (int32_t)((uint32_t)a + (uint32_t)b);
+}
+__host__ __device__ __forceinline__ int64_t add(int64_t a, int64_t b) {
+    return (int64_t)((uint64_t)a + (uint64_t)b);
+}
+
+__host__ __device__ __forceinline__ float mul(float a, float b) { return a * b; }
+__host__ __device__ __forceinline__ double mul(double a, double b) { return a * b; }
+__host__ __device__ __forceinline__ cf32 mul(cf32 a, cf32 b) {
+    return cf32{a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re};
+}
+__host__ __device__ __forceinline__ cf64 mul(cf64 a, cf64 b) {
+    return cf64{a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re};
+}
+__host__ __device__ __forceinline__ int32_t mul(int32_t a, int32_t b) {
+    return (int32_t)((uint32_t)a * (uint32_t)b);
+}
+__host__ __device__ __forceinline__ int64_t mul(int64_t a, int64_t b) {
+    return (int64_t)((uint64_t)a * (uint64_t)b);
+}
+
+template <typename V> __host__ __device__ __forceinline__ V conj_if(V a, bool c) { return a; }
+template <> __host__ __device__ __forceinline__ cf32 conj_if(cf32 a, bool c) {
+    return c ? cf32{a.re, -a.im} : a;
+}
+template <> __host__ __device__ __forceinline__ cf64 conj_if(cf64 a, bool c) {
+    return c ? cf64{a.re, -a.im} : a;
+}
+
+template <typename V> __host__ __device__ __forceinline__ bool is_zero(V a) { return a == V(0); }
+template <> __host__ __device__ __forceinline__ bool is_zero(cf32 a) { return a.re == 0.0f && a.im == 0.0f; }
+template <> __host__ __device__ __forceinline__ bool is_zero(cf64 a) { return a.re == 0.0 && a.im == 0.0; }
+template <typename V> __host__ __device__ __forceinline__ bool is_one(V a) { return a == V(1); }
+template <> __host__ __device__ __forceinline__ bool is_one(cf32 a) { return a.re == 1.0f && a.im == 0.0f; }
+template <> __host__ __device__ __forceinline__ bool is_one(cf64 a) { return a.re == 1.0 && a.im == 0.0; }
+
+// Read-only (non-coherent) loads for operands the kernel never writes.
+template <typename T> __device__ __forceinline__ T ldg(const T *p) { return __ldg(p); }
+template <> __device__ __forceinline__ cf32 ldg(const cf32 *p) {
+    float2 v = __ldg(reinterpret_cast<const float2 *>(p));
+    return cf32{v.x, v.y};
+}
+template <> __device__ __forceinline__ cf64 ldg(const cf64 *p) {
+    double2 v = __ldg(reinterpret_cast<const double2 *>(p));
+    return cf64{v.x, v.y};
+}
+
+// Streaming loads for data read exactly once (matrix entries): evict-first.
+template <typename T> __device__ __forceinline__ T ld_stream(const T *p) { return __ldcs(p); }
+template <> __device__ __forceinline__ cf32 ld_stream(const cf32 *p) {
+    float2 v = __ldcs(reinterpret_cast<const float2 *>(p));
+    return cf32{v.x, v.y};
+}
+template <> __device__ __forceinline__ cf64 ld_stream(const cf64 *p) {
+    double2 v = __ldcs(reinterpret_cast<const double2 *>(p));
+    return cf64{v.x, v.y};
+}
+
+// Atomic accumulate (complex: one atomic per component).
+__device__ __forceinline__ void atomic_add(float *p, float v) { atomicAdd(p, v); }
+__device__ __forceinline__ void atomic_add(double *p, double v) { atomicAdd(p, v); }
+__device__ __forceinline__ void atomic_add(cf32 *p, cf32 v) {
+    atomicAdd(&p->re, v.re);
+    atomicAdd(&p->im, v.im);
+}
+__device__ __forceinline__ void atomic_add(cf64 *p, cf64 v) {
+    atomicAdd(&p->re, v.re);
+    atomicAdd(&p->im, v.im);
+}
+__device__ __forceinline__ void atomic_add(int32_t *p, int32_t v) { atomicAdd((int *)p, (int)v); }
+__device__ __forceinline__ void atomic_add(int64_t *p, int64_t v) {
+    atomicAdd((unsigned long long *)p, (unsigned long long)v);
+}
+
+// Warp shuffles for every value type.
+template <typename V> __device__ __forceinline__ V shfl_up(V v, int d) {
+    return __shfl_up_sync(0xffffffffu, v, d);
+}
+template <> __device__ __forceinline__ cf32 shfl_up(cf32 v, int d) {
+    return cf32{__shfl_up_sync(0xffffffffu, v.re, d), __shfl_up_sync(0xffffffffu, v.im, d)};
+}
+template <> __device__ __forceinline__ cf64 shfl_up(cf64 v, int d) {
+    return cf64{__shfl_up_sync(0xffffffffu, v.re, d), __shfl_up_sync(0xffffffffu, v.im, d)};
+}
+template <typename V> __device__ __forceinline__ V shfl_xor(V v, int m, int w = 32) {
+    return __shfl_xor_sync(0xffffffffu, v, m, w);
+}
+template <> __device__ __forceinline__ cf32 shfl_xor(cf32 v, int m, int w) {
+    return cf32{__shfl_xor_sync(0xffffffffu, v.re, m, w), __shfl_xor_sync(0xffffffffu, v.im, m, w)};
+}
+template <> __device__ __forceinline__ cf64 shfl_xor(cf64 v, int m, int w) {
+    return cf64{__shfl_xor_sync(0xffffffffu, v.re, m, w), __shfl_xor_sync(0xffffffffu, v.im, m, w)};
+}
+template <typename V> __device__ __forceinline__ V shfl_down(V v, int d) {
+    return __shfl_down_sync(0xffffffffu, v, d);
+}
+template <> __device__ __forceinline__ cf32 shfl_down(cf32 v, int d) {
+    return cf32{__shfl_down_sync(0xffffffffu, v.re, d), __shfl_down_sync(0xffffffffu, v.im, d)};
+}
+template <> __device__ __forceinline__ cf64 shfl_down(cf64 v, int d) {
+    return cf64{__shfl_down_sync(0xffffffffu, v.re, d), __shfl_down_sync(0xffffffffu, v.im, d)};
+}
+
+// ---------------------------------------------------------------------------
+// Dense operand views.  op(B)(i, c) = B[i*rs + c*cs], conjugated if conj.
+template <typename V> struct DenseIn {
+    const V *p;
+    int64_t rs, cs;
+    bool conj;
+    __device__ __forceinline__ V at(int64_t i, int64_t c) const {
+        return conj_if(ldg(p + i * rs + c * cs), conj);
+    }
+};
+
+// C column-major with leading dimension ld; beta handled per LinearAlgebra's
+// _rmul_or_fill!: beta == 1 keeps C, beta == 0 overwrites without reading.
+template <typename V> struct DenseOut {
+    V *p;
+    int64_t ld;
+    V alpha, beta;
+    int beta_mode;  // 0: beta == 0, 1: beta == 1, 2: general
+    // C[i, c] = beta*C[i, c] + acc*alpha
+    __device__ __forceinline__ void store(int64_t i, int64_t c, V acc) const {
+        V *q = p + i * 1 + c * ld;
+        V t = mul(acc, alpha);
+        if (beta_mode == 0) *q = add(VT<V>::zero(), t);
+        else if (beta_mode == 1) *q = add(*q, t);
+        else *q = add(mul(*q, beta), t);
+    }
+    // C[i, c] += v (for values already multiplied by alpha)
+    __device__ __forceinline__ void accumulate(int64_t i, int64_t c, V v) const {
+        V *q = p + i + c * ld;
+        *q = add(*q, v);
+    }
+};
+
+template <typename V> inline int beta_mode_of(V beta) {
+    return is_zero(beta) ? 0 : (is_one(beta) ? 1 : 2);
+}
+
+// ---------------------------------------------------------------------------
+// Errors.
+void set_error(const char *fmt, ...);
+int fail(int status, const char *fmt, ...);
+int check_cuda(cudaError_t e, const char *what);
+
+// Optional events recorded right before and after the main compute kernel of the next
+// calls on this host thread (set by gsa_set_kernel_timer).
+void timer_before(cudaStream_t s);
+void timer_after(cudaStream_t s);
+
+inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
+inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+// Splits one workspace into aligned sub-buffers.
+struct Carver {
+    char *base;
+    size_t off = 0;
+    explicit Carver(void *b) : base((char *)b) {}
+    template <typename T> T *take(size_t count) {
+        off = align_up(off, 256);
+        T *p = base ? (T *)(base + off) : nullptr;
+        off += count * sizeof(T);
+        return p;
+    }
+};
+
+// Dispatch helpers: call F.template operator()<V, I>() for runtime codes.
+template <typename F> int dispatch_vi(int dtype, int itype, F &&f) {
+    if (itype == GSA_IDX32) {
+        switch (dtype) {
+        case GSA_F32: return f.template operator()<float, int32_t>();
+        case GSA_F64: return f.template operator()<double, int32_t>();
+        case GSA_C32: return f.template operator()<cf32, int32_t>();
+        case GSA_C64: return f.template operator()<cf64, int32_t>();
+        case GSA_I32: return f.template operator()<int32_t, int32_t>();
+        case GSA_I64: return f.template operator()<int64_t, int32_t>();
+        }
+    } else if (itype == GSA_IDX64) {
+        switch (dtype) {
+        case GSA_F32: return f.template operator()<float, int64_t>();
+        case GSA_F64: return f.template operator()<double, int64_t>();
+        case GSA_C32: return f.template operator()<cf32, int64_t>();
+        case GSA_C64: return f.template operator()<cf64, int64_t>();
+        case GSA_I32: return f.template operator()<int32_t, int64_t>();
+        case GSA_I64: return f.template operator()<int64_t, int64_t>();
+        }
+    }
+    return fail(GSA_ERR_UNSUPPORTED, "unsupported dtype %d / itype %d", dtype, itype);
+}
+
+inline size_t dtype_size(int dtype) {
+    switch (dtype) {
+    case GSA_F32: return 4;
+    case GSA_F64: return 8;
+    case GSA_C32: return 8;
+    case GSA_C64: return 16;
+    case GSA_I32: return 4;
+    case GSA_I64: return 8;
+    }
+    return 0;
+}
+inline size_t itype_size(int itype) { return itype == GSA_IDX32 ? 4 : (itype == GSA_IDX64 ? 8 : 0); }
+
+// ---------------------------------------------------------------------------
+// Kernel entry points implemented in the .cu files (host-side launchers).
+
+// Arguments of one sparse x dense product in "compressed outer" form: the
+// outer dimension is the one ptr compresses (rows for CSR, columns for CSC).
+template <typename V, typename I> struct CompressedArgs {
+    int64_t outer_n;   // number of compressed rows/columns
+    int64_t inner_n;   // range of idx (entries outside it are skipped, never read or written)
+    int64_t nnz;
+    const I *ptr;      // outer_n + 1 entries
+    const I *idx;      // nnz entries
+    const V *val;      // nnz entries
+    int base;
+    bool conjA;
+};
+
+// Gather: out[o, c] = beta*out[o, c] + alpha * sum_j conj?(val_j) * op(B)(idx_j, c)
+template <typename V, typename I>
+int launch_gather(cudaStream_t s, const CompressedArgs<V, I> &a, int64_t k, DenseIn<V> B,
+                  DenseOut<V> C, int algo, void *ws, size_t ws_bytes);
+template <typename V, typename I>
+size_t gather_workspace_size(int64_t outer_n, int64_t nnz, int64_t k, int algo);
+
+// Scatter: out[idx_j, c] += conj?(val_j) * (op(B)(o, c) * alpha), after the beta pass.
+template <typename V, typename I>
+int launch_scatter(cudaStream_t s, const CompressedArgs<V, I> &a, int64_t k, DenseIn<V> B,
+                   DenseOut<V> C, int64_t out_rows, void *ws, size_t ws_bytes);
+template <typename V, typename I>
+size_t scatter_workspace_size(int64_t outer_n, int64_t nnz, int64_t k);
+
+// COO: out[key_i, c] += conj?(val_i) * (op(B)(other_i, c) * alpha), after the beta pass.
+template <typename V, typename I>
+int launch_coo(cudaStream_t s, int64_t nnz, const I *out_idx, const I *in_idx, const V *val,
+               int base, bool conjA, int64_t k, DenseIn<V> B, DenseOut<V> C, int64_t out_rows,
+               int64_t in_rows);
+
+// beta pass of LinearAlgebra._rmul_or_fill! over an out_rows x k block of C.
+template <typename V>
+int launch_rmul_or_fill(cudaStream_t s, DenseOut<V> C, int64_t out_rows, int64_t k);
+
+// Conversions.
+template <typename V, typename I>
+int launch_coo_to_compressed(cudaStream_t s, bool colmajor, int64_t m, int64_t n, int64_t nnz,
+                             const I *rowind, const I *colind, const V *val, int base,
+                             I *ptr_out, I *idx_out, V *val_out, void *ws, size_t ws_bytes);
+template <typename V, typename I>
+size_t coo_to_compressed_workspace_size(int64_t m, int64_t n, int64_t nnz, bool colmajor);
+
+template <typename I>
+int launch_expand_major(cudaStream_t s, int64_t outer_n, int64_t nnz, const I *ptr, int base,
+                        I *major_out, void *ws, size_t ws_bytes);
+size_t expand_major_workspace_size(int64_t outer_n, int64_t nnz);
+
+template <typename I>
+int launch_validate(cudaStream_t s, int64_t outer_n, int64_t inner_n, int64_t nnz, const I *ptr,
+                    const I *idx, int base, int *d_flag);
+
+// Merge-path partition shared by gather, scatter and expansion: for each tile
+// boundary d = t * tile_items (t = 0..num_tiles), the number of outer entries
+// whose end offset is consumed before diagonal d.
+template <typename I>
+int launch_merge_partition(cudaStream_t s, const I *ptr, int base, int64_t outer_n, int64_t nnz,
+                           int64_t tile_items, int64_t num_tiles, int64_t *coords);
+
+}  // namespace gsa

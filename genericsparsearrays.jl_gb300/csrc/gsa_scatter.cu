@@ -1,0 +1,228 @@
+// Scatter products and the beta pass.
+//
+// * Compressed scatter: C[idx_j, c] += a_j * (op(B)(o, c) * alpha) for every
+//   stored entry j of outer o -- kernel_spmatmul_csr_T!
+//   (src/matrix_csr/matrix_csr_kernels.jl:24-45) and kernel_spmatmul_csc_N!
+//   (src/matrix_csc/matrix_csc_kernels.jl:1-22).  Those give one work item per
+//   outer entry, so one long column serialises a thread.  Here the entries are
+//   cut into the same nnz-balanced merge-path tiles as the gather; a tile
+//   first labels each of its entries with its outer index (shared memory),
+//   then streams the entries coalesced and adds them with atomics.
+// * COO: kernel_spmatmul_coo_N! / _T! (src/matrix_coo/matrix_coo_kernels.jl:1-43),
+//   one atomic per entry there.  Here each warp takes 32 consecutive entries,
+//   reduces runs of equal output rows with a segmented shuffle scan and issues
+//   one atomic per run (row-sorted COO: about one per row; any order: correct).
+// * rmul_or_fill: LinearAlgebra._rmul_or_fill!(C, beta) as the reference calls
+//   it before its atomic kernels (src/matrix_csr/matrix_csr.jl:192).
+//
+// Complex values use one atomic per component (the reference's KA @atomic
+// cannot do Complex, so its CSR-T / CSC-N / COO products skip Complex).
+#include "gsa_internal.cuh"
+
+namespace gsa {
+
+template <typename V>
+__global__ void rmul_or_fill_kernel(DenseOut<V> C, int64_t rows, int64_t k) {
+    int64_t total = rows * k;
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+         t += (int64_t)gridDim.x * blockDim.x) {
+        int64_t r = t % rows, c = t / rows;
+        V *q = C.p + r + c * C.ld;
+        if (C.beta_mode == 0) *q = VT<V>::zero();
+        else *q = mul(*q, C.beta);
+    }
+}
+
+template <typename V>
+int launch_rmul_or_fill(cudaStream_t s, DenseOut<V> C, int64_t rows, int64_t k) {
+    if (C.beta_mode == 1 || rows == 0 || k == 0) return GSA_OK;
+    int64_t blocks = ceil_div(rows * k, 256);
+    if (blocks > 152 * 32) blocks = 152 * 32;
+    rmul_or_fill_kernel<V><<<(unsigned)blocks, 256, 0, s>>>(C, rows, k);
+    return check_cuda(cudaGetLastError(), "rmul_or_fill_kernel");
+}
+
+// ---------------------------------------------------------------------------
+template <typename V> struct ScatterShape {
+    static constexpr int THREADS = 256;
+    static constexpr int IPT = 8;
+    static constexpr int TILE = THREADS * IPT;
+};
+
+template <typename V, typename I>
+__global__ void __launch_bounds__(ScatterShape<V>::THREADS)
+scatter_merge_kernel(CompressedArgs<V, I> a, int64_t k, DenseIn<V> B, DenseOut<V> C,
+                     const int64_t *__restrict__ coords) {
+    constexpr int THREADS = ScatterShape<V>::THREADS;
+    constexpr int IPT = ScatterShape<V>::IPT;
+    constexpr int TILE = ScatterShape<V>::TILE;
+    __shared__ int s_rowend[TILE];
+    __shared__ int s_outer[TILE];
+
+    const int64_t tile = blockIdx.x;
+    const int64_t total = a.outer_n + a.nnz;
+    const int64_t d0 = tile * TILE;
+    const int64_t d1 = d0 + TILE < total ? d0 + TILE : total;
+    const int64_t rs = coords[tile], re = coords[tile + 1];
+    const int64_t js = d0 - rs, je = d1 - re;
+    const int64_t tile_rows64 = re - rs, tile_nnz64 = je - js;
+    if (tile_rows64 < 0 || tile_nnz64 < 0 || tile_rows64 + tile_nnz64 > TILE) return;
+    const int tile_rows = (int)tile_rows64, tile_nnz = (int)tile_nnz64;
+    const int tid = threadIdx.x;
+
+    for (int e = tid; e < tile_rows; e += THREADS)
+        s_rowend[e] = (int)((int64_t)__ldg(a.ptr + rs + 1 + e) - a.base - js);
+    __syncthreads();
+
+    // label every entry of the tile with its (local) outer index
+    const int items = tile_rows + tile_nnz;
+    int d = tid * IPT < items ? tid * IPT : items;
+    int lo = d - tile_nnz > 0 ? d - tile_nnz : 0;
+    int hi = d < tile_rows ? d : tile_rows;
+    while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if (s_rowend[mid] + mid < d) lo = mid + 1;
+        else hi = mid;
+    }
+    int i = lo, j = d - lo;
+#pragma unroll
+    for (int step = 0; step < IPT; ++step) {
+        if (i < tile_rows && s_rowend[i] <= j) ++i;
+        else if (j < tile_nnz) s_outer[j++] = i;
+    }
+    __syncthreads();
+
+    I idx[IPT];
+    V av[IPT];
+#pragma unroll
+    for (int u = 0; u < IPT; ++u) {
+        int e = tid + u * THREADS;
+        if (e < tile_nnz) {
+            idx[u] = ld_stream(a.idx + js + e);
+            av[u] = conj_if(ld_stream(a.val + js + e), a.conjA);
+        }
+    }
+    for (int64_t c = 0; c < k; ++c) {
+#pragma unroll
+        for (int u = 0; u < IPT; ++u) {
+            int e = tid + u * THREADS;
+            int64_t r = (int64_t)idx[u] - a.base;
+            if (e < tile_nnz && (uint64_t)r < (uint64_t)a.inner_n) {
+                V axj = mul(B.at(rs + s_outer[e], c), C.alpha);
+                atomic_add(C.p + r + c * C.ld, mul(av[u], axj));
+            }
+        }
+    }
+}
+
+template <typename V, typename I>
+size_t scatter_workspace_size(int64_t outer_n, int64_t nnz, int64_t k) {
+    if (outer_n == 0 || nnz == 0 || k == 0) return 0;
+    int64_t T = ceil_div(outer_n + nnz, ScatterShape<V>::TILE);
+    return align_up((size_t)(T + 1) * sizeof(int64_t), 256);
+}
+
+template <typename V, typename I>
+int launch_scatter(cudaStream_t s, const CompressedArgs<V, I> &a, int64_t k, DenseIn<V> B,
+                   DenseOut<V> C, int64_t out_rows, void *ws, size_t ws_bytes) {
+    int rc = launch_rmul_or_fill<V>(s, C, out_rows, k);
+    if (rc) return rc;
+    if (a.outer_n == 0 || a.nnz == 0 || k == 0) return GSA_OK;
+    constexpr int TILE = ScatterShape<V>::TILE;
+    const int64_t T = ceil_div(a.outer_n + a.nnz, TILE);
+    if (ws_bytes < scatter_workspace_size<V, I>(a.outer_n, a.nnz, k))
+        return fail(GSA_ERR_INVALID_ARG, "scatter workspace too small");
+    if (T > 0x7fffffffLL) return fail(GSA_ERR_UNSUPPORTED, "too many tiles");
+    int64_t *coords = (int64_t *)ws;
+    rc = launch_merge_partition<I>(s, a.ptr, a.base, a.outer_n, a.nnz, TILE, T, coords);
+    if (rc) return rc;
+    timer_before(s);
+    scatter_merge_kernel<V, I><<<(unsigned)T, ScatterShape<V>::THREADS, 0, s>>>(a, k, B, C, coords);
+    timer_after(s);
+    return check_cuda(cudaGetLastError(), "scatter_merge_kernel");
+}
+
+// ---------------------------------------------------------------------------
+// COO: each warp covers CHUNK consecutive entries in groups of 32.
+template <typename V, typename I>
+__global__ void __launch_bounds__(256)
+coo_kernel(int64_t nnz, const I *__restrict__ out_idx, const I *__restrict__ in_idx,
+           const V *__restrict__ val, int base, bool conjA, int64_t k, DenseIn<V> B,
+           DenseOut<V> C, int64_t out_rows, int64_t in_rows) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t g = warp; g * 32 < nnz; g += nwarps) {
+        const int64_t e = g * 32 + lane;
+        bool valid = e < nnz;
+        int64_t key = -1, in = 0;
+        V av = VT<V>::zero();
+        if (valid) {
+            key = (int64_t)ld_stream(out_idx + e) - base;
+            in = (int64_t)ld_stream(in_idx + e) - base;
+            av = conj_if(ld_stream(val + e), conjA);
+            // entries outside the matrix are skipped, never read or written
+            if ((uint64_t)key >= (uint64_t)out_rows || (uint64_t)in >= (uint64_t)in_rows) {
+                valid = false;
+                key = -1;
+            }
+        }
+        const int64_t next_key = __shfl_down_sync(0xffffffffu, key, 1);
+        const bool tail = valid && (lane == 31 || next_key != key);
+        for (int64_t c = 0; c < k; ++c) {
+            V v = valid ? mul(av, mul(B.at(in, c), C.alpha)) : VT<V>::zero();
+#pragma unroll
+            for (int off = 1; off < 32; off <<= 1) {
+                V ov = shfl_up(v, off);
+                int64_t ok = __shfl_up_sync(0xffffffffu, key, off);
+                if (lane >= off && ok == key) v = add(ov, v);
+            }
+            if (tail) atomic_add(C.p + key + c * C.ld, v);
+        }
+    }
+}
+
+template <typename V, typename I>
+int launch_coo(cudaStream_t s, int64_t nnz, const I *out_idx, const I *in_idx, const V *val,
+               int base, bool conjA, int64_t k, DenseIn<V> B, DenseOut<V> C, int64_t out_rows,
+               int64_t in_rows) {
+    int rc = launch_rmul_or_fill<V>(s, C, out_rows, k);
+    if (rc) return rc;
+    if (nnz == 0 || k == 0) return GSA_OK;
+    int64_t warps = ceil_div(nnz, 32);
+    int64_t blocks = ceil_div(warps, 8);
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    timer_before(s);
+    coo_kernel<V, I><<<(unsigned)blocks, 256, 0, s>>>(nnz, out_idx, in_idx, val, base, conjA, k, B,
+                                                       C, out_rows, in_rows);
+    timer_after(s);
+    return check_cuda(cudaGetLastError(), "coo_kernel");
+}
+
+#define GSA_INST_SCATTER(V, I)                                                                  \
+    template int launch_scatter<V, I>(cudaStream_t, const CompressedArgs<V, I> &, int64_t,      \
+                                      DenseIn<V>, DenseOut<V>, int64_t, void *, size_t);        \
+    template size_t scatter_workspace_size<V, I>(int64_t, int64_t, int64_t);                    \
+    template int launch_coo<V, I>(cudaStream_t, int64_t, const I *, const I *, const V *, int, \
+                                  bool, int64_t, DenseIn<V>, DenseOut<V>, int64_t, int64_t);
+GSA_INST_SCATTER(float, int32_t)
+GSA_INST_SCATTER(float, int64_t)
+GSA_INST_SCATTER(double, int32_t)
+GSA_INST_SCATTER(double, int64_t)
+GSA_INST_SCATTER(cf32, int32_t)
+GSA_INST_SCATTER(cf32, int64_t)
+GSA_INST_SCATTER(cf64, int32_t)
+GSA_INST_SCATTER(cf64, int64_t)
+GSA_INST_SCATTER(int32_t, int32_t)
+GSA_INST_SCATTER(int32_t, int64_t)
+GSA_INST_SCATTER(int64_t, int32_t)
+GSA_INST_SCATTER(int64_t, int64_t)
+
+template int launch_rmul_or_fill<float>(cudaStream_t, DenseOut<float>, int64_t, int64_t);
+template int launch_rmul_or_fill<double>(cudaStream_t, DenseOut<double>, int64_t, int64_t);
+template int launch_rmul_or_fill<cf32>(cudaStream_t, DenseOut<cf32>, int64_t, int64_t);
+template int launch_rmul_or_fill<cf64>(cudaStream_t, DenseOut<cf64>, int64_t, int64_t);
+template int launch_rmul_or_fill<int32_t>(cudaStream_t, DenseOut<int32_t>, int64_t, int64_t);
+template int launch_rmul_or_fill<int64_t>(cudaStream_t, DenseOut<int64_t>, int64_t, int64_t);
+
+}  // namespace gsa

@@ -1,0 +1,648 @@
+"""Host mirror of GenericSparseArrays.jl's sparse x dense API over libgsa.
+
+The reference's user-facing surface for this path is kept, with Python spelling:
+
+=========================================  ===============================================
+Julia (reference)                          here
+=========================================  ===============================================
+``GenericSparseMatrixCSR(m,n,rowptr,...)``  ``GenericSparseMatrixCSR(m, n, rowptr, colval, nzval)``
+``GenericSparseMatrixCSC(...)`` / ``COO``   same names
+``adapt(CuArray, A)``                       ``adapt("cuda", A)`` (``adapt("cpu", A)`` back)
+``mul!(C, A, B, α, β)``, ``mul!(C, A, B)``  ``mul_(C, A, B, alpha, beta)``, ``mul_(C, A, B)``
+``A * x``                                   ``A @ x`` or ``mul(A, x)``
+``transpose(A)``, ``adjoint(A)`` / ``A'``    ``transpose(A)``, ``adjoint(A)`` (also on dense tensors)
+``GenericSparseMatrixCSR(A_coo)`` etc.      same constructors, one argument
+``SparseMatrixCSC(A)``, ``collect(A)``      ``SparseMatrixCSC(A)`` (scipy), ``collect(A)`` (numpy)
+``nnz(A)``, ``size(A)``                     ``nnz(A)``, ``A.shape`` / ``size(A)``
+=========================================  ===============================================
+
+Buffers are torch tensors (device memory on CUDA; host tensors before ``adapt``);
+indices are 1-based, as in the reference (``rowptr[0] == 1``).  Dense operands are torch
+tensors; any 2-D tensor with one unit stride is used in place (column-major as given, a
+row-major tensor as the transpose of its column-major parent).
+
+Products and COO -> CSR/CSC conversions run only in libgsa on the GPU.  A call on host
+buffers raises ``ArgumentError``: there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+from typing import Optional, Tuple
+
+import numpy as np
+import torch
+
+from . import _lib
+from .errors import ArgumentError, DimensionMismatch
+
+_DTYPE = {torch.float32: _lib.F32, torch.float64: _lib.F64, torch.complex64: _lib.C32,
+          torch.complex128: _lib.C64, torch.int32: _lib.I32, torch.int64: _lib.I64}
+_ITYPE = {torch.int32: _lib.IDX32, torch.int64: _lib.IDX64}
+_NP_OF = {torch.float32: np.float32, torch.float64: np.float64, torch.complex64: np.complex64,
+          torch.complex128: np.complex128, torch.int32: np.int32, torch.int64: np.int64}
+_IMAX = {torch.int32: 2**31 - 1, torch.int64: 2**63 - 1}
+
+# Index base of every buffer this layer creates or accepts (Julia's).
+BASE = 1
+
+
+def _tensor(x, dtype=None) -> torch.Tensor:
+    if isinstance(x, torch.Tensor):
+        return x if dtype is None else x.to(dtype)
+    if isinstance(x, np.ndarray):
+        t = torch.from_numpy(np.ascontiguousarray(x))
+        return t if dtype is None else t.to(dtype)
+    return torch.as_tensor(x, dtype=dtype)
+
+
+def _stream_ptr(device: torch.device) -> ctypes.c_void_p:
+    return ctypes.c_void_p(torch.cuda.current_stream(device).cuda_stream)
+
+
+def _ptr(t: Optional[torch.Tensor]) -> ctypes.c_void_p:
+    return ctypes.c_void_p(t.data_ptr() if t is not None and t.numel() else 0)
+
+
+def _check_Ti(m: int, n: int, itype: torch.dtype) -> None:
+    """SparseArrays.sparse_check_Ti as called by the reference constructors."""
+    if not (0 <= m <= _IMAX[itype]):
+        raise ArgumentError(f"number of rows (m = {m}) does not fit in Ti = {itype}")
+    if not (0 <= n <= _IMAX[itype]):
+        raise ArgumentError(f"number of columns (n = {n}) does not fit in Ti = {itype}")
+
+
+class AbstractGenericSparseMatrix:
+    """Common part of the three storage formats (src/core.jl:11-22)."""
+
+    m: int
+    n: int
+    nzval: torch.Tensor
+
+    @property
+    def shape(self) -> Tuple[int, int]:
+        return (self.m, self.n)
+
+    @property
+    def dtype(self) -> torch.dtype:
+        return self.nzval.dtype
+
+    @property
+    def device(self) -> torch.device:
+        return self.nzval.device
+
+    def __len__(self):
+        return self.m * self.n
+
+    def __matmul__(self, B):
+        return mul(self, B)
+
+    @property
+    def T(self):
+        return transpose(self)
+
+    @property
+    def H(self):
+        return adjoint(self)
+
+
+def _check_same_device(*ts):
+    devs = {t.device for t in ts}
+    if len(devs) != 1:
+        raise ArgumentError("All storage vectors must be on the same device/backend.")
+
+
+class GenericSparseMatrixCSR(AbstractGenericSparseMatrix):
+    """CSR matrix with generic storage (src/matrix_csr/matrix_csr.jl:17-63).
+
+    ``GenericSparseMatrixCSR(m, n, rowptr, colval, nzval)`` copies the three buffers, as the
+    reference constructor does.  One argument converts: a COO or CSC matrix (on the GPU), a
+    ``Transpose``/``Adjoint`` of a CSC matrix, or a scipy sparse matrix (host).
+    """
+
+    def __init__(self, *args):
+        if len(args) == 1:
+            src = _convert_to(GenericSparseMatrixCSR, args[0])
+            self.m, self.n = src.m, src.n
+            self.rowptr, self.colval, self.nzval = src.rowptr, src.colval, src.nzval
+            return
+        if len(args) != 5:
+            raise TypeError("GenericSparseMatrixCSR(m, n, rowptr, colval, nzval) or (A)")
+        m, n, rowptr, colval, nzval = args
+        rowptr, colval, nzval = _tensor(rowptr), _tensor(colval), _tensor(nzval)
+        _check_same_device(rowptr, colval, nzval)
+        if rowptr.dtype not in _ITYPE or colval.dtype != rowptr.dtype:
+            raise ArgumentError("rowptr and colval must share an index type (int32 or int64)")
+        if m < 0:
+            raise ArgumentError("m must be non-negative")
+        if n < 0:
+            raise ArgumentError("n must be non-negative")
+        _check_Ti(m, n, rowptr.dtype)
+        if rowptr.numel() != m + 1:
+            raise ArgumentError("rowptr length must be m+1")
+        if colval.numel() != nzval.numel():
+            raise ArgumentError("colval and nzval must have same length")
+        self.m, self.n = int(m), int(n)
+        self.rowptr = rowptr.clone().contiguous()
+        self.colval = colval.clone().contiguous()
+        self.nzval = nzval.clone().contiguous()
+
+    @property
+    def itype(self) -> torch.dtype:
+        return self.rowptr.dtype
+
+    def __repr__(self):
+        return f"GenericSparseMatrixCSR({self.m}x{self.n}, nnz={nnz(self)}, {self.dtype}, {self.device})"
+
+
+class GenericSparseMatrixCSC(AbstractGenericSparseMatrix):
+    """CSC matrix with generic storage (src/matrix_csc/matrix_csc.jl:17-63)."""
+
+    def __init__(self, *args):
+        if len(args) == 1:
+            src = _convert_to(GenericSparseMatrixCSC, args[0])
+            self.m, self.n = src.m, src.n
+            self.colptr, self.rowval, self.nzval = src.colptr, src.rowval, src.nzval
+            return
+        if len(args) != 5:
+            raise TypeError("GenericSparseMatrixCSC(m, n, colptr, rowval, nzval) or (A)")
+        m, n, colptr, rowval, nzval = args
+        colptr, rowval, nzval = _tensor(colptr), _tensor(rowval), _tensor(nzval)
+        _check_same_device(colptr, rowval, nzval)
+        if colptr.dtype not in _ITYPE or rowval.dtype != colptr.dtype:
+            raise ArgumentError("colptr and rowval must share an index type (int32 or int64)")
+        if m < 0:
+            raise ArgumentError("m must be non-negative")
+        if n < 0:
+            raise ArgumentError("n must be non-negative")
+        _check_Ti(m, n, colptr.dtype)
+        if colptr.numel() != n + 1:
+            raise ArgumentError("colptr length must be n+1")
+        if rowval.numel() != nzval.numel():
+            raise ArgumentError("rowval and nzval must have same length")
+        self.m, self.n = int(m), int(n)
+        self.colptr = colptr.clone().contiguous()
+        self.rowval = rowval.clone().contiguous()
+        self.nzval = nzval.clone().contiguous()
+
+    @property
+    def itype(self) -> torch.dtype:
+        return self.colptr.dtype
+
+    def __repr__(self):
+        return f"GenericSparseMatrixCSC({self.m}x{self.n}, nnz={nnz(self)}, {self.dtype}, {self.device})"
+
+
+class GenericSparseMatrixCOO(AbstractGenericSparseMatrix):
+    """COO matrix with generic storage, any entry order (src/matrix_coo/matrix_coo.jl:17-61)."""
+
+    def __init__(self, *args):
+        if len(args) == 1:
+            src = _convert_to(GenericSparseMatrixCOO, args[0])
+            self.m, self.n = src.m, src.n
+            self.rowind, self.colind, self.nzval = src.rowind, src.colind, src.nzval
+            return
+        if len(args) != 5:
+            raise TypeError("GenericSparseMatrixCOO(m, n, rowind, colind, nzval) or (A)")
+        m, n, rowind, colind, nzval = args
+        rowind, colind, nzval = _tensor(rowind), _tensor(colind), _tensor(nzval)
+        _check_same_device(rowind, colind, nzval)
+        if rowind.dtype not in _ITYPE or colind.dtype != rowind.dtype:
+            raise ArgumentError("rowind and colind must share an index type (int32 or int64)")
+        if m < 0:
+            raise ArgumentError("m must be non-negative")
+        if n < 0:
+            raise ArgumentError("n must be non-negative")
+        _check_Ti(m, n, rowind.dtype)
+        if not (rowind.numel() == colind.numel() == nzval.numel()):
+            raise ArgumentError("rowind, colind, and nzval must have same length")
+        self.m, self.n = int(m), int(n)
+        self.rowind = rowind.clone().contiguous()
+        self.colind = colind.clone().contiguous()
+        self.nzval = nzval.clone().contiguous()
+
+    @property
+    def itype(self) -> torch.dtype:
+        return self.rowind.dtype
+
+    def __repr__(self):
+        return f"GenericSparseMatrixCOO({self.m}x{self.n}, nnz={nnz(self)}, {self.dtype}, {self.device})"
+
+
+# ---------------------------------------------------------------------------
+# Lazy Transpose / Adjoint wrappers (LinearAlgebra.Transpose / Adjoint)
+
+class Transpose:
+    def __init__(self, parent):
+        self.parent = parent
+
+    @property
+    def shape(self):
+        s = tuple(self.parent.shape)
+        return (s[1], s[0]) if len(s) == 2 else (1, s[0])
+
+    def __matmul__(self, B):
+        return mul(self, B)
+
+
+class Adjoint(Transpose):
+    pass
+
+
+def _is_real(dtype) -> bool:
+    return not dtype.is_complex
+
+
+def transpose(A):
+    """``transpose(A)``: lazy for sparse matrices and dense tensors; ``transpose(transpose(A)) === A``."""
+    if isinstance(A, Adjoint):
+        p = A.parent
+        return p if _is_real(p.dtype) else _conj_copy(p)
+    if isinstance(A, Transpose):
+        return A.parent
+    return Transpose(A)
+
+
+def adjoint(A):
+    """``adjoint(A)`` (``A'``): conjugate transpose, lazy; for real element types it is ``transpose``."""
+    if isinstance(A, Adjoint):
+        return A.parent
+    if isinstance(A, Transpose):
+        p = A.parent
+        return p if _is_real(p.dtype) else _conj_copy(p)
+    return Adjoint(A)
+
+
+def _conj_copy(p):
+    if isinstance(p, torch.Tensor):
+        return p.conj().resolve_conj()
+    q = _same_structure(p, p.nzval.conj().resolve_conj())
+    return q
+
+
+def _same_structure(A, nzval):
+    if isinstance(A, GenericSparseMatrixCSR):
+        return GenericSparseMatrixCSR(A.m, A.n, A.rowptr, A.colval, nzval)
+    if isinstance(A, GenericSparseMatrixCSC):
+        return GenericSparseMatrixCSC(A.m, A.n, A.colptr, A.rowval, nzval)
+    return GenericSparseMatrixCOO(A.m, A.n, A.rowind, A.colind, nzval)
+
+
+# ---------------------------------------------------------------------------
+
+def nnz(A) -> int:
+    if isinstance(A, Transpose):
+        return nnz(A.parent)
+    return int(A.nzval.numel())
+
+
+def size(A, dim: Optional[int] = None):
+    s = tuple(A.shape)
+    if len(s) == 1:
+        s = (s[0], 1)
+    return s if dim is None else s[dim - 1]
+
+
+def _to_device(t: torch.Tensor, to) -> torch.Tensor:
+    return t.to(to).contiguous() if t.device != torch.device(to) else t
+
+
+def adapt(to, A):
+    """``Adapt.adapt_structure(to, A)`` (src/matrix_csr/matrix_csr.jl:65-71 and the CSC/COO
+    equivalents): the same matrix with every buffer moved to ``to`` ("cuda", "cuda:1", "cpu",
+    or a torch.device).  The constructor copies the buffers, as the reference's does."""
+    dev = torch.device(to)
+    if dev.type == "cuda" and dev.index is None:
+        dev = torch.device("cuda", torch.cuda.current_device())
+    if isinstance(A, Transpose):
+        return type(A)(adapt(to, A.parent))
+    if isinstance(A, torch.Tensor):
+        return A.to(dev)
+    if isinstance(A, GenericSparseMatrixCSR):
+        return GenericSparseMatrixCSR(A.m, A.n, A.rowptr.to(dev), A.colval.to(dev), A.nzval.to(dev))
+    if isinstance(A, GenericSparseMatrixCSC):
+        return GenericSparseMatrixCSC(A.m, A.n, A.colptr.to(dev), A.rowval.to(dev), A.nzval.to(dev))
+    if isinstance(A, GenericSparseMatrixCOO):
+        return GenericSparseMatrixCOO(A.m, A.n, A.rowind.to(dev), A.colind.to(dev), A.nzval.to(dev))
+    raise ArgumentError(f"cannot adapt {type(A).__name__}")
+
+
+# ---------------------------------------------------------------------------
+# mul!
+
+def _unwrap_sparse(A):
+    """(parent, opA) following trans_adj_wrappers (src/core.jl:102-113)."""
+    if isinstance(A, Adjoint):
+        return A.parent, (_lib.OP_T if _is_real(A.parent.dtype) else _lib.OP_C)
+    if isinstance(A, Transpose):
+        return A.parent, _lib.OP_T
+    return A, _lib.OP_N
+
+
+def _dense_operand(B) -> Tuple[torch.Tensor, int, int, int, int]:
+    """op(B) as (buffer, ldb, opB, rows, cols) for the C ABI.
+
+    The C ABI reads op(B)(i, c) = buf[i + c*ld] for opB == N and buf[c + i*ld] (conjugated for
+    opB == C) otherwise.  A column-major parent P is used as is; a row-major P is the
+    transpose of a column-major buffer, so the op flips.  Only a conjugated row-major parent
+    (op(P) = conj of a column-major buffer) and layouts without a unit stride are copied.
+    """
+    op = _lib.OP_N
+    if isinstance(B, Adjoint):
+        t, op = B.parent, (_lib.OP_T if _is_real(B.parent.dtype) else _lib.OP_C)
+    elif isinstance(B, Transpose):
+        t, op = B.parent, _lib.OP_T
+    else:
+        t = B
+    if not isinstance(t, torch.Tensor):
+        raise ArgumentError(f"dense operand must be a torch tensor, got {type(t).__name__}")
+    if t.is_conj():
+        t = t.resolve_conj()
+    if t.dim() == 1:
+        t = t.unsqueeze(1)  # an L-vector is the L x 1 parent
+    if t.dim() != 2:
+        raise ArgumentError("dense operands must be vectors or matrices")
+    r, c = t.shape
+    rows, cols = (r, c) if op == _lib.OP_N else (c, r)
+    if r <= 1 or t.stride(0) == 1:  # column-major parent
+        ld = t.stride(1) if c > 1 else max(r, 1)
+        return t, max(ld, r, 1), op, rows, cols
+    if c <= 1 or t.stride(1) == 1:  # row-major parent = transpose of a column-major buffer
+        ld = t.stride(0) if r > 1 else max(c, 1)
+        if op == _lib.OP_N:
+            return t, max(ld, c, 1), _lib.OP_T, rows, cols
+        if op == _lib.OP_T:
+            return t, max(ld, c, 1), _lib.OP_N, rows, cols
+    # copy op(B) into a column-major buffer
+    opb = t if op == _lib.OP_N else (t.t() if op == _lib.OP_T else t.conj().t())
+    buf = opb.resolve_conj().t().contiguous().t()
+    return buf, max(buf.shape[0], 1), _lib.OP_N, rows, cols
+
+
+def _scalar_buf(v, dtype: torch.dtype):
+    """alpha/beta as a host buffer of the element type; complex into a real C -> ArgumentError."""
+    npdt = _NP_OF[dtype]
+    if isinstance(v, bool):
+        v = int(v)
+    if isinstance(v, complex) and not np.issubdtype(npdt, np.complexfloating):
+        if v.imag != 0:
+            raise ArgumentError(
+                "element types of A, B, α, and β must be promotable to the element type of C")
+        v = v.real
+    if isinstance(v, float) and np.issubdtype(npdt, np.integer):
+        if v != int(v):
+            raise ArgumentError(
+                "element types of A, B, α, and β must be promotable to the element type of C")
+        v = int(v)
+    return np.array([v], dtype=npdt)
+
+
+def mul_(C: torch.Tensor, A, B, alpha=1, beta=0, algo: int = _lib.ALGO_AUTO,
+         workspace: Optional[torch.Tensor] = None) -> torch.Tensor:
+    """``mul!(C, A, B, α, β)``: ``C = β C + α op(A) op(B)`` on the GPU; returns ``C``.
+
+    Checks follow the reference's generated methods (src/matrix_csr/matrix_csr.jl:160-190):
+    three ``DimensionMismatch`` checks, the element-type check and the backend check, in that
+    order.  ``beta == 0`` never reads ``C``.  Asynchronous on the current torch stream.
+    """
+    Ap, opA = _unwrap_sparse(A)
+    if not isinstance(Ap, AbstractGenericSparseMatrix):
+        raise ArgumentError("A must be a GenericSparseMatrixCSR/CSC/COO or its transpose/adjoint")
+    Am, An = (Ap.m, Ap.n) if opA == _lib.OP_N else (Ap.n, Ap.m)
+    Bbuf, ldb, opB, Br, Bc = _dense_operand(B)
+    if not isinstance(C, torch.Tensor):
+        raise ArgumentError("C must be a torch tensor")
+    Cr, Cc = (C.shape[0], 1) if C.dim() == 1 else tuple(C.shape)
+    if An != Br:
+        raise DimensionMismatch(
+            f"second dimension of A, {An}, does not match the first dimension of B, {Br}")
+    if Am != Cr:
+        raise DimensionMismatch(
+            f"first dimension of A, {Am}, does not match the first dimension of C, {Cr}")
+    if Bc != Cc:
+        raise DimensionMismatch(
+            f"second dimension of B, {Bc}, does not match the second dimension of C, {Cc}")
+    dt = C.dtype
+    if dt not in _DTYPE:
+        raise ArgumentError(f"unsupported element type {dt}")
+    if Ap.dtype != dt or Bbuf.dtype != dt:
+        if (Ap.dtype.is_complex or Bbuf.dtype.is_complex) and not dt.is_complex:
+            raise ArgumentError(
+                "element types of A, B, α, and β must be promotable to the element type of C")
+        raise ArgumentError(
+            f"mixed element types (A {Ap.dtype}, B {Bbuf.dtype}, C {dt}) are not provided by the "
+            "GPU path; convert the operands to one type")
+    al, be = _scalar_buf(alpha, dt), _scalar_buf(beta, dt)
+    devs = {Ap.device, Bbuf.device, C.device}
+    if len(devs) != 1:
+        raise ArgumentError("All arrays must have the same backend")
+    dev = C.device
+    if dev.type != "cuda":
+        raise ArgumentError("mul! runs on the GPU only; adapt the operands to CUDA first")
+    # C must be column-major (unit row stride); otherwise compute into a column-major
+    # buffer and copy back.
+    C2 = C.unsqueeze(1) if C.dim() == 1 else C
+    direct = C2.shape[0] <= 1 or C2.stride(0) == 1
+    Cw = C2 if direct else C2.t().contiguous().t()
+    ldc = Cw.stride(1) if Cw.shape[1] > 1 else Cw.shape[0]
+    ldc = max(ldc, Cw.shape[0], 1)
+    lib = _lib.load()
+    k = Cc
+    stream = _stream_ptr(dev)
+    with torch.cuda.device(dev):
+        if isinstance(Ap, (GenericSparseMatrixCSR, GenericSparseMatrixCSC)):
+            csr = isinstance(Ap, GenericSparseMatrixCSR)
+            ptr, idx = (Ap.rowptr, Ap.colval) if csr else (Ap.colptr, Ap.rowval)
+            ws_bytes = lib.gsa_mul_workspace_size(0 if csr else 1, _DTYPE[dt], _ITYPE[Ap.itype],
+                                                  Ap.m, Ap.n, nnz(Ap), opA, k, algo)
+            if ws_bytes and (workspace is None or workspace.numel() < ws_bytes):
+                workspace = torch.empty(ws_bytes, dtype=torch.uint8, device=dev)
+            fn = lib.gsa_csr_mul if csr else lib.gsa_csc_mul
+            st = fn(stream, _DTYPE[dt], _ITYPE[Ap.itype], Ap.m, Ap.n, nnz(Ap), _ptr(ptr), _ptr(idx),
+                    _ptr(Ap.nzval), BASE, opA, k, _ptr(Bbuf), ldb, opB, _ptr(Cw), ldc,
+                    al.ctypes.data_as(ctypes.c_void_p), be.ctypes.data_as(ctypes.c_void_p), algo,
+                    _ptr(workspace) if ws_bytes else ctypes.c_void_p(0),
+                    workspace.numel() if ws_bytes else 0)
+        else:
+            st = lib.gsa_coo_mul(stream, _DTYPE[dt], _ITYPE[Ap.itype], Ap.m, Ap.n, nnz(Ap),
+                                 _ptr(Ap.rowind), _ptr(Ap.colind), _ptr(Ap.nzval), BASE, opA, k,
+                                 _ptr(Bbuf), ldb, opB, _ptr(Cw), ldc,
+                                 al.ctypes.data_as(ctypes.c_void_p),
+                                 be.ctypes.data_as(ctypes.c_void_p))
+    _lib.check(st)
+    if not direct:
+        C2.copy_(Cw)
+    return C
+
+
+def mul(A, B) -> torch.Tensor:
+    """``A * B`` for a sparse ``A`` (LinearAlgebra's generic ``*`` -> ``mul!``): a new
+    column-major result with ``β = 0``."""
+    Ap, opA = _unwrap_sparse(A)
+    Am = Ap.m if opA == _lib.OP_N else Ap.n
+    _, _, _, Br, Bc = _dense_operand(B)
+    Bt = B.parent if isinstance(B, Transpose) else B
+    vec = isinstance(Bt, torch.Tensor) and Bt.dim() == 1 and not isinstance(B, Transpose)
+    if vec:
+        C = torch.empty(Am, dtype=Ap.dtype, device=Ap.device)
+    else:
+        C = torch.empty((Bc, Am), dtype=Ap.dtype, device=Ap.device).t()
+    return mul_(C, A, B)
+
+
+# ---------------------------------------------------------------------------
+# Conversions (src/conversions/conversions.jl)
+
+def _require_cuda(A):
+    if A.device.type != "cuda":
+        raise ArgumentError("format conversion runs on the GPU only; adapt the matrix to CUDA first")
+
+
+def _coo_to_compressed(A: GenericSparseMatrixCOO, colmajor: bool):
+    _require_cuda(A)
+    lib = _lib.load()
+    dev = A.device
+    nz = nnz(A)
+    major_n = A.n if colmajor else A.m
+    ptr = torch.empty(major_n + 1, dtype=A.itype, device=dev)
+    idx = torch.empty(nz, dtype=A.itype, device=dev)
+    val = torch.empty(nz, dtype=A.dtype, device=dev)
+    with torch.cuda.device(dev):
+        ws_bytes = lib.gsa_coo_to_compressed_workspace_size(int(colmajor), _DTYPE[A.dtype],
+                                                            _ITYPE[A.itype], A.m, A.n, nz)
+        ws = torch.empty(max(ws_bytes, 1), dtype=torch.uint8, device=dev)
+        fn = lib.gsa_coo_to_csc if colmajor else lib.gsa_coo_to_csr
+        st = fn(_stream_ptr(dev), _DTYPE[A.dtype], _ITYPE[A.itype], A.m, A.n, nz, _ptr(A.rowind),
+                _ptr(A.colind), _ptr(A.nzval), BASE, _ptr(ptr), _ptr(idx), _ptr(val), _ptr(ws),
+                ws.numel())
+    _lib.check(st)
+    return ptr, idx, val
+
+
+def _compressed_to_coo(A, colmajor: bool):
+    _require_cuda(A)
+    lib = _lib.load()
+    dev = A.device
+    nz = nnz(A)
+    ptr, idx = (A.colptr, A.rowval) if colmajor else (A.rowptr, A.colval)
+    r = torch.empty(nz, dtype=A.itype, device=dev)
+    c = torch.empty(nz, dtype=A.itype, device=dev)
+    v = torch.empty(nz, dtype=A.dtype, device=dev)
+    with torch.cuda.device(dev):
+        fn = lib.gsa_csc_to_coo if colmajor else lib.gsa_csr_to_coo
+        st = fn(_stream_ptr(dev), _DTYPE[A.dtype], _ITYPE[A.itype], A.m, A.n, nz, _ptr(ptr),
+                _ptr(idx), _ptr(A.nzval), BASE, _ptr(r), _ptr(c), _ptr(v))
+    _lib.check(st)
+    return r, c, v
+
+
+def _from_scipy(cls, S):
+    import scipy.sparse as sp
+    m, n = S.shape
+    if cls is GenericSparseMatrixCSR:
+        X = sp.csr_matrix(S)
+        X.sort_indices()
+        it = np.int64 if X.indptr.dtype == np.int64 else np.int32
+        return GenericSparseMatrixCSR(m, n, X.indptr.astype(it) + 1, X.indices.astype(it) + 1, X.data)
+    if cls is GenericSparseMatrixCSC:
+        X = sp.csc_matrix(S)
+        X.sort_indices()
+        it = np.int64 if X.indptr.dtype == np.int64 else np.int32
+        return GenericSparseMatrixCSC(m, n, X.indptr.astype(it) + 1, X.indices.astype(it) + 1, X.data)
+    # COO from SparseMatrixCSC walks columns in order (src/matrix_coo/matrix_coo.jl:64-83)
+    X = sp.csc_matrix(S)
+    X.sort_indices()
+    it = np.int64 if X.indptr.dtype == np.int64 else np.int32
+    cols = np.repeat(np.arange(n, dtype=it), np.diff(X.indptr))
+    return GenericSparseMatrixCOO(m, n, X.indices.astype(it) + 1, cols + 1, X.data)
+
+
+def _convert_to(cls, A):
+    """One-argument constructors of src/conversions/conversions.jl."""
+    if isinstance(A, cls):
+        return _same_structure(A, A.nzval) if cls is not GenericSparseMatrixCOO else A
+    try:
+        import scipy.sparse as sp
+        if sp.issparse(A):
+            return _from_scipy(cls, A)
+    except ImportError:  # pragma: no cover
+        pass
+    if isinstance(A, Transpose):
+        P = A.parent
+        conj = isinstance(A, Adjoint) and P.dtype.is_complex
+        val = (lambda v: v.conj().resolve_conj()) if conj else (lambda v: v)
+        # conversions.jl:88-103,106-123: transpose(CSR) <-> CSC reuse the buffers
+        if cls is GenericSparseMatrixCSC and isinstance(P, GenericSparseMatrixCSR):
+            return GenericSparseMatrixCSC(P.n, P.m, P.rowptr, P.colval, val(P.nzval))
+        if cls is GenericSparseMatrixCSR and isinstance(P, GenericSparseMatrixCSC):
+            return GenericSparseMatrixCSR(P.n, P.m, P.colptr, P.rowval, val(P.nzval))
+        # conversions.jl:125-147,214-258,325-346: COO of a transpose swaps the index arrays
+        coo = P if isinstance(P, GenericSparseMatrixCOO) else GenericSparseMatrixCOO(P)
+        T = GenericSparseMatrixCOO(coo.n, coo.m, coo.colind, coo.rowind, val(coo.nzval))
+        return T if cls is GenericSparseMatrixCOO else cls(T)
+    if cls is GenericSparseMatrixCOO:
+        if isinstance(A, GenericSparseMatrixCSR):  # conversions.jl:264-280
+            r, c, v = _compressed_to_coo(A, colmajor=False)
+        elif isinstance(A, GenericSparseMatrixCSC):  # conversions.jl:153-169
+            r, c, v = _compressed_to_coo(A, colmajor=True)
+        else:
+            raise ArgumentError(f"cannot convert {type(A).__name__} to COO")
+        return GenericSparseMatrixCOO(A.m, A.n, r, c, v)
+    if isinstance(A, (GenericSparseMatrixCSR, GenericSparseMatrixCSC)):
+        # CSC <-> CSR through COO (conversions.jl:85-86,104-105)
+        return cls(GenericSparseMatrixCOO(A))
+    if isinstance(A, GenericSparseMatrixCOO):
+        colmajor = cls is GenericSparseMatrixCSC
+        ptr, idx, val = _coo_to_compressed(A, colmajor)  # conversions.jl:171-212 / 282-323
+        return cls(A.m, A.n, ptr, idx, val)
+    raise ArgumentError(f"cannot convert {type(A).__name__} to {cls.__name__}")
+
+
+# ---------------------------------------------------------------------------
+# Host views
+
+def SparseMatrixCSC(A):
+    """``SparseMatrixCSC(A)``: a scipy.sparse CSC matrix on the host (sums duplicates, as
+    ``sparse(I, J, V)`` does for COO in the reference)."""
+    import scipy.sparse as sp
+    if isinstance(A, Transpose):
+        S = SparseMatrixCSC(A.parent).T
+        if isinstance(A, Adjoint):
+            S = S.conj()
+        return sp.csc_matrix(S)
+    if isinstance(A, GenericSparseMatrixCSR):
+        p, i, v = (t.cpu().numpy() for t in (A.rowptr, A.colval, A.nzval))
+        return sp.csr_matrix((v, i - 1, p - 1), shape=A.shape).tocsc()
+    if isinstance(A, GenericSparseMatrixCSC):
+        p, i, v = (t.cpu().numpy() for t in (A.colptr, A.rowval, A.nzval))
+        return sp.csc_matrix((v, i - 1, p - 1), shape=A.shape)
+    if isinstance(A, GenericSparseMatrixCOO):
+        r, c, v = (t.cpu().numpy() for t in (A.rowind, A.colind, A.nzval))
+        return sp.coo_matrix((v, (r - 1, c - 1)), shape=A.shape).tocsc()
+    raise ArgumentError(f"cannot convert {type(A).__name__}")
+
+
+def collect(A) -> np.ndarray:
+    """Dense host copy (``collect(A)``)."""
+    if isinstance(A, torch.Tensor):
+        return A.cpu().numpy()
+    return SparseMatrixCSC(A).toarray()
+
+
+def validate(A) -> None:
+    """Device-side structure check (pointers monotone from 1 to nnz+1, indices in range);
+    raises ``ArgumentError`` on a malformed matrix.  Synchronizes the stream."""
+    if isinstance(A, GenericSparseMatrixCOO):
+        r, c = A.rowind.cpu(), A.colind.cpu()
+        if r.numel() and (int(r.min()) < 1 or int(r.max()) > A.m or int(c.min()) < 1 or
+                          int(c.max()) > A.n):
+            raise ArgumentError("COO index out of range")
+        return
+    _require_cuda(A)
+    csr = isinstance(A, GenericSparseMatrixCSR)
+    ptr, idx = (A.rowptr, A.colval) if csr else (A.colptr, A.rowval)
+    outer, inner = (A.m, A.n) if csr else (A.n, A.m)
+    lib = _lib.load()
+    with torch.cuda.device(A.device):
+        st = lib.gsa_validate_compressed(_stream_ptr(A.device), _ITYPE[A.itype], outer, inner,
+                                         nnz(A), _ptr(ptr), _ptr(idx), BASE)
+    _lib.check(st)

@@ -1,0 +1,170 @@
+/*
+ * gsa.h -- C ABI of libgsa, the GB300 (sm_103a) library behind the sparse x dense
+ * mul! path of GenericSparseArrays.jl and the COO -> CSR/CSC conversions that
+ * feed it.
+ *
+ * Every entry point takes plain device pointers and sizes, runs asynchronously on
+ * the caller's CUDA stream and returns a status code (GSA_OK == 0).  The library
+ * never frees caller buffers.  gsa_last_error_string() gives a message for the
+ * last failing call on the calling host thread.
+ *
+ * Conventions shared by all entry points
+ *   dtype   element type of values and dense operands (gsa_dtype)
+ *   itype   index type of pointer and index arrays (gsa_itype)
+ *   base    index base of every index/pointer array: 1 for Julia's 1-based
+ *           buffers (rowptr[0] == 1), 0 for C-style buffers
+ *   alpha, beta  HOST pointers to one value of type dtype (complex: re, im)
+ *   stream  a cudaStream_t (NULL = legacy default stream)
+ *   Buffers must be aligned to their element size (complex: 2 x the real size).
+ *
+ * Dense operands are column-major (Julia's layout).  op(B) is given by its
+ * parent buffer: opB == GSA_OP_N reads B(i, c) = B[i + c*ldb]; GSA_OP_T and
+ * GSA_OP_C read B(i, c) = B[c + i*ldb] (GSA_OP_C conjugated), i.e. the parent
+ * is the k x rows(op(B)) matrix that Julia's Transpose/Adjoint wraps.
+ *
+ * Workspace: entry points that need scratch take (workspace, workspace_bytes).
+ * Pass workspace == NULL to let the library take it from the stream-ordered
+ * pool (cudaMallocAsync / cudaFreeAsync on the same stream); otherwise pass at
+ * least the size the matching *_workspace_size function returns.  A caller
+ * workspace must not be used by another call that overlaps on the GPU.
+ */
+#ifndef GSA_H
+#define GSA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    GSA_OK = 0,
+    GSA_ERR_INVALID_ARG = 1,   /* bad pointer, size, enum or alignment: ArgumentError */
+    GSA_ERR_DIM = 2,           /* sizes of A, B, C do not agree: DimensionMismatch */
+    GSA_ERR_UNSUPPORTED = 3,   /* dtype/itype/format combination not provided */
+    GSA_ERR_CUDA = 4,          /* a CUDA launch or runtime call failed */
+    GSA_ERR_ALLOC = 5,         /* stream-ordered workspace allocation failed */
+    GSA_ERR_STRUCTURE = 6,     /* validator found a malformed matrix */
+    GSA_ERR_TIMEOUT = 7        /* a bounded device-side wait gave up */
+} gsa_status;
+
+typedef enum {
+    GSA_F32 = 0, GSA_F64 = 1, GSA_C32 = 2, GSA_C64 = 3, GSA_I32 = 4, GSA_I64 = 5
+} gsa_dtype;
+
+typedef enum { GSA_IDX32 = 0, GSA_IDX64 = 1 } gsa_itype;
+
+/* op(A) / op(B): identity, transpose, adjoint (conjugate transpose). */
+typedef enum { GSA_OP_N = 0, GSA_OP_T = 1, GSA_OP_C = 2 } gsa_op;
+
+/* Gather kernel selection for the row-gather paths (CSR N, CSC T). */
+typedef enum {
+    GSA_ALGO_AUTO = 0,     /* library choice */
+    GSA_ALGO_MERGE = 1,    /* nnz-balanced merge-path tiles (any row-length mix) */
+    GSA_ALGO_VECTOR = 2    /* a group of threads per row (short, even rows) */
+} gsa_algo;
+
+/* ---- library ------------------------------------------------------------ */
+
+/* Version as major*10000 + minor*100 + patch. */
+int gsa_version(void);
+
+/* Message for the last non-OK status returned on this host thread. */
+const char *gsa_last_error_string(void);
+
+/* Profiling hook (no counterpart in the reference, which has no tracing): when set, the
+ * library records `before` and `after` (cudaEvent_t) on the call's stream right around the
+ * main compute kernel of each following call from this host thread -- the merge-path or
+ * vector gather, the scatter, the COO kernel, or the whole sort of a conversion.  Pass
+ * NULL, NULL to switch it off. */
+void gsa_set_kernel_timer(void *before, void *after);
+
+/* ---- sparse x dense mul! --------------------------------------------------
+ * C = beta*C + alpha * op(A) * op(B), with C (rows(op(A)) x k, column-major,
+ * leading dimension ldc).  beta == 0 never reads C (NaN in C is overwritten),
+ * beta == 1 skips the scaling, as LinearAlgebra._rmul_or_fill! does before
+ * the reference's kernels.  m x n is the stored (parent) size of A, nnz the
+ * number of stored entries.  B and C must not overlap.
+ */
+
+/* Replaces the mul! methods generated at src/matrix_csr/matrix_csr.jl:145-211
+ * (kernels kernel_spmatmul_csr_N! / _T!, src/matrix_csr/matrix_csr_kernels.jl:1-45).
+ * opA == N gathers along rows; T/C scatter (CSR-T, atomics). */
+int gsa_csr_mul(void *stream, int dtype, int itype, int64_t m, int64_t n, int64_t nnz,
+                const void *rowptr, const void *colval, const void *nzval, int base, int opA,
+                int64_t k, const void *B, int64_t ldb, int opB, void *C, int64_t ldc,
+                const void *alpha, const void *beta, int algo, void *workspace,
+                size_t workspace_bytes);
+
+/* Replaces src/matrix_csc/matrix_csc.jl:144-213 (kernels kernel_spmatmul_csc_N! /
+ * _T!, src/matrix_csc/matrix_csc_kernels.jl:1-45).  opA == N scatters along
+ * columns; T/C gather (the CSR-N kernel on the stored structure). */
+int gsa_csc_mul(void *stream, int dtype, int itype, int64_t m, int64_t n, int64_t nnz,
+                const void *colptr, const void *rowval, const void *nzval, int base, int opA,
+                int64_t k, const void *B, int64_t ldb, int opB, void *C, int64_t ldc,
+                const void *alpha, const void *beta, int algo, void *workspace,
+                size_t workspace_bytes);
+
+/* Replaces src/matrix_coo/matrix_coo.jl:155-221 (kernels kernel_spmatmul_coo_N! /
+ * _T!, src/matrix_coo/matrix_coo_kernels.jl:1-43).  Any storage order and
+ * duplicates are accepted; runs of equal output rows are reduced in registers
+ * before the atomics.  Needs no workspace. */
+int gsa_coo_mul(void *stream, int dtype, int itype, int64_t m, int64_t n, int64_t nnz,
+                const void *rowind, const void *colind, const void *nzval, int base, int opA,
+                int64_t k, const void *B, int64_t ldb, int opB, void *C, int64_t ldc,
+                const void *alpha, const void *beta);
+
+/* Workspace bytes for gsa_csr_mul / gsa_csc_mul with these sizes (format:
+ * 0 CSR, 1 CSC).  0 means none is needed. */
+size_t gsa_mul_workspace_size(int format, int dtype, int itype, int64_t m, int64_t n,
+                              int64_t nnz, int opA, int64_t k, int algo);
+
+/* ---- format conversions ---------------------------------------------------- */
+
+/* GenericSparseMatrixCSR(::GenericSparseMatrixCOO), src/conversions/conversions.jl:282-323
+ * (keys src/conversions/conversion_kernels.jl:49-57): stable sort of the triplets by
+ * (row, col) -- duplicates kept in input order -- then rowptr (m+1 entries,
+ * rowptr[m] == nnz + base).  Outputs must not overlap inputs. */
+int gsa_coo_to_csr(void *stream, int dtype, int itype, int64_t m, int64_t n, int64_t nnz,
+                   const void *rowind, const void *colind, const void *nzval, int base,
+                   void *rowptr_out, void *colval_out, void *nzval_out, void *workspace,
+                   size_t workspace_bytes);
+
+/* GenericSparseMatrixCSC(::GenericSparseMatrixCOO), src/conversions/conversions.jl:171-212
+ * (keys src/conversions/conversion_kernels.jl:38-46): the same with (col, row) order. */
+int gsa_coo_to_csc(void *stream, int dtype, int itype, int64_t m, int64_t n, int64_t nnz,
+                   const void *rowind, const void *colind, const void *nzval, int base,
+                   void *colptr_out, void *rowval_out, void *nzval_out, void *workspace,
+                   size_t workspace_bytes);
+
+/* Workspace bytes for gsa_coo_to_csr (colmajor == 0) / gsa_coo_to_csc (1). */
+size_t gsa_coo_to_compressed_workspace_size(int colmajor, int dtype, int itype, int64_t m,
+                                            int64_t n, int64_t nnz);
+
+/* GenericSparseMatrixCOO(::GenericSparseMatrixCSR), src/conversions/conversions.jl:264-280
+ * (kernel_csr_to_coo!, src/conversions/conversion_kernels.jl:20-35). */
+int gsa_csr_to_coo(void *stream, int dtype, int itype, int64_t m, int64_t n, int64_t nnz,
+                   const void *rowptr, const void *colval, const void *nzval, int base,
+                   void *rowind_out, void *colind_out, void *nzval_out);
+
+/* GenericSparseMatrixCOO(::GenericSparseMatrixCSC), src/conversions/conversions.jl:153-169
+ * (kernel_csc_to_coo!, src/conversions/conversion_kernels.jl:2-17). */
+int gsa_csc_to_coo(void *stream, int dtype, int itype, int64_t m, int64_t n, int64_t nnz,
+                   const void *colptr, const void *rowval, const void *nzval, int base,
+                   void *rowind_out, void *colind_out, void *nzval_out);
+
+/* ---- structure check ------------------------------------------------------
+ * The reference constructors skip the structural check
+ * (src/matrix_csr/matrix_csr.jl:49, "TODO: this uses scalar indexing").
+ * This one runs on the device and synchronizes the stream: ptr[0] == base,
+ * ptr non-decreasing, ptr[outer_n] == nnz + base and every index in
+ * [base, inner_n + base).  Returns GSA_OK or GSA_ERR_STRUCTURE. */
+int gsa_validate_compressed(void *stream, int itype, int64_t outer_n, int64_t inner_n,
+                            int64_t nnz, const void *ptr, const void *idx, int base);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GSA_H */

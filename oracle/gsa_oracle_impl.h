@@ -1,0 +1,284 @@
+/*
+ * Type-generic body of the CPU oracle.  TEST INFRASTRUCTURE ONLY: this file is
+ * compiled into libgsa_oracle.so, which only tests/, __graft_entry__.smoke() and
+ * bench.py's CPU-baseline leg load.  The product path never links it.
+ *
+ * Included once per (value type, index type) pair by gsa_oracle.c with these
+ * macros defined:
+ *   V, I          value and index C types
+ *   SUFFIX        name suffix of the instantiation
+ *   V_ZERO        additive identity
+ *   V_ADD(a,b)    a + b in the reference's arithmetic (wrapping for integers)
+ *   V_MUL(a,b)    a * b in the reference's arithmetic (Julia's complex formula)
+ *   V_CONJ(a)     conj(a)
+ *   V_EQ_ONE(a)   a == one(a)
+ *   V_IS_ZERO(a)  iszero(a)
+ *   V_TO_C(a,re,im) widen to two doubles (error oracle)
+ */
+
+#define CAT_(a, b) a##_##b
+#define CAT(a, b) CAT_(a, b)
+#define FN(name) CAT(name, SUFFIX)
+
+/* B(i, c) of op(B) for a column-major parent with leading dimension ldb.
+ * opB: 0 = identity, 1 = transpose, 2 = adjoint; the TRANSB/CONJB index
+ * swap of src/matrix_csr/matrix_csr_kernels.jl:16-18. */
+static inline V FN(getB)(const V *B, int64_t ldb, int opB, int64_t i, int64_t c) {
+    V v = (opB == 0) ? B[i + c * ldb] : B[c + i * ldb];
+    return (opB == 2) ? V_CONJ(v) : v;
+}
+
+/* LinearAlgebra._rmul_or_fill!(C, beta) as called before every kernel
+ * (src/matrix_csr/matrix_csr.jl:192): beta == 1 leaves C alone, beta == 0
+ * fills zero without reading C, otherwise C .*= beta. */
+static void FN(rmul_or_fill)(V *C, int64_t rows, int64_t k, int64_t ldc, V beta) {
+    if (V_EQ_ONE(beta) || rows == 0 || k == 0) return;
+    for (int64_t c = 0; c < k; ++c)
+        for (int64_t r = 0; r < rows; ++r) {
+            if (V_IS_ZERO(beta)) C[r + c * ldc] = V_ZERO;
+            else C[r + c * ldc] = V_MUL(C[r + c * ldc], beta);
+        }
+}
+
+/* Gather over the compressed dimension: kernel_spmatmul_csr_N!
+ * (src/matrix_csr/matrix_csr_kernels.jl:1-22), identical in shape to
+ * kernel_spmatmul_csc_T! (src/matrix_csc/matrix_csc_kernels.jl:24-45).
+ * One work item per (c, outer): a serial walk of the outer's range, alpha
+ * applied once at the end (C[row,k] += tmp * alpha). */
+static void FN(gather)(int64_t outer_n, const I *ptr, const I *idx, const V *val, int base,
+                       int conjA, int64_t k, const V *B, int64_t ldb, int opB,
+                       V *C, int64_t ldc, V alpha, int nthreads) {
+    (void)nthreads;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static) num_threads(nthreads > 0 ? nthreads : 1) collapse(2)
+#endif
+    for (int64_t c = 0; c < k; ++c) {
+        for (int64_t o = 0; o < outer_n; ++o) {
+            V tmp = V_ZERO;
+            for (int64_t j = (int64_t)ptr[o] - base; j < (int64_t)ptr[o + 1] - base; ++j) {
+                V a = conjA ? V_CONJ(val[j]) : val[j];
+                V b = FN(getB)(B, ldb, opB, (int64_t)idx[j] - base, c);
+                tmp = V_ADD(tmp, V_MUL(a, b));
+            }
+            C[o + c * ldc] = V_ADD(C[o + c * ldc], V_MUL(tmp, alpha));
+        }
+    }
+}
+
+/* Scatter over the compressed dimension: kernel_spmatmul_csr_T!
+ * (src/matrix_csr/matrix_csr_kernels.jl:24-45) and kernel_spmatmul_csc_N!
+ * (src/matrix_csc/matrix_csc_kernels.jl:1-22).  axj = B(outer, c) * alpha,
+ * then C[idx_j, c] += a_j * axj for every stored entry.  The reference runs
+ * these adds as unordered atomics; the oracle runs them in storage order,
+ * which is one of the orders the reference may take. */
+static void FN(scatter)(int64_t outer_n, const I *ptr, const I *idx, const V *val, int base,
+                        int conjA, int64_t k, const V *B, int64_t ldb, int opB,
+                        V *C, int64_t ldc, V alpha) {
+    for (int64_t c = 0; c < k; ++c) {
+        for (int64_t o = 0; o < outer_n; ++o) {
+            V axj = V_MUL(FN(getB)(B, ldb, opB, o, c), alpha);
+            for (int64_t j = (int64_t)ptr[o] - base; j < (int64_t)ptr[o + 1] - base; ++j) {
+                V a = conjA ? V_CONJ(val[j]) : val[j];
+                int64_t r = (int64_t)idx[j] - base;
+                C[r + c * ldc] = V_ADD(C[r + c * ldc], V_MUL(a, axj));
+            }
+        }
+    }
+}
+
+/* COO: kernel_spmatmul_coo_N! / kernel_spmatmul_coo_T!
+ * (src/matrix_coo/matrix_coo_kernels.jl:1-43).  One contribution per stored
+ * entry, any storage order, no duplicate merging: C[out,c] += a*(B(in,c)*alpha). */
+static void FN(coo)(int64_t nnz, const I *rowind, const I *colind, const V *val, int base,
+                    int trans, int conjA, int64_t k, const V *B, int64_t ldb, int opB,
+                    V *C, int64_t ldc, V alpha) {
+    for (int64_t c = 0; c < k; ++c) {
+        for (int64_t i = 0; i < nnz; ++i) {
+            int64_t row = (int64_t)rowind[i] - base, col = (int64_t)colind[i] - base;
+            int64_t out = trans ? col : row, in = trans ? row : col;
+            V a = conjA ? V_CONJ(val[i]) : val[i];
+            V axj = V_MUL(FN(getB)(B, ldb, opB, in, c), alpha);
+            C[out + c * ldc] = V_ADD(C[out + c * ldc], V_MUL(a, axj));
+        }
+    }
+}
+
+/* mul!(C, op(A), op(B), alpha, beta) dispatch, following the method
+ * generators src/matrix_csr/matrix_csr.jl:145-211,
+ * src/matrix_csc/matrix_csc.jl:144-213 and src/matrix_coo/matrix_coo.jl:155-221:
+ * beta pass first, then the N (opA == 0) or T kernel with CONJA = (opA == 2).
+ * fmt: 0 CSR (p0 rowptr, p1 colval), 1 CSC (p0 colptr, p1 rowval),
+ *      2 COO (p0 rowind, p1 colind). */
+static int FN(mul)(int fmt, int opA, int64_t m, int64_t n, int64_t nnz,
+                   const void *p0v, const void *p1v, const void *valv, int base,
+                   int64_t k, const void *Bv, int64_t ldb, int opB,
+                   void *Cv, int64_t ldc, const void *alphav, const void *betav, int nthreads) {
+    const I *p0 = (const I *)p0v, *p1 = (const I *)p1v;
+    const V *val = (const V *)valv, *B = (const V *)Bv;
+    V *C = (V *)Cv;
+    V alpha = *(const V *)alphav, beta = *(const V *)betav;
+    int conjA = (opA == 2);
+    int64_t rows_out = (opA == 0) ? m : n;
+    FN(rmul_or_fill)(C, rows_out, k, ldc, beta);
+    if (fmt == 0) {
+        if (opA == 0) FN(gather)(m, p0, p1, val, base, conjA, k, B, ldb, opB, C, ldc, alpha, nthreads);
+        else FN(scatter)(m, p0, p1, val, base, conjA, k, B, ldb, opB, C, ldc, alpha);
+    } else if (fmt == 1) {
+        if (opA == 0) FN(scatter)(n, p0, p1, val, base, conjA, k, B, ldb, opB, C, ldc, alpha);
+        else FN(gather)(n, p0, p1, val, base, conjA, k, B, ldb, opB, C, ldc, alpha, nthreads);
+    } else if (fmt == 2) {
+        FN(coo)(nnz, p0, p1, val, base, opA != 0, conjA, k, B, ldb, opB, C, ldc, alpha);
+    } else {
+        return 1;
+    }
+    return 0;
+}
+
+/* Error oracle: the same product in double-double, with the per-output scale
+ * |alpha| * sum_j |a_j||b_j| + |beta||C0| that the tolerance is relative to.
+ * Outputs are doubles: yre/yim and scale, each rows_out x k column-major
+ * (yim is ignored for real types).  Contributions are format-agnostic: every
+ * stored entry adds a(out, in) * B(in, c) to output out. */
+static int FN(mul_exact)(int fmt, int opA, int64_t m, int64_t n, int64_t nnz,
+                         const void *p0v, const void *p1v, const void *valv, int base,
+                         int64_t k, const void *Bv, int64_t ldb, int opB,
+                         const void *C0v, int64_t ldc0, const void *alphav, const void *betav,
+                         double *yre, double *yim, double *scale) {
+    const I *p0 = (const I *)p0v, *p1 = (const I *)p1v;
+    const V *val = (const V *)valv, *B = (const V *)Bv;
+    const V *C0 = (const V *)C0v;
+    V alpha = *(const V *)alphav, beta = *(const V *)betav;
+    int conjA = (opA == 2), trans = (opA != 0);
+    int64_t rows_out = trans ? n : m;
+    int64_t tot = rows_out * k;
+    dd *are = (dd *)calloc((size_t)(tot > 0 ? tot : 1), sizeof(dd));
+    dd *aim = (dd *)calloc((size_t)(tot > 0 ? tot : 1), sizeof(dd));
+    double *abssum = (double *)calloc((size_t)(tot > 0 ? tot : 1), sizeof(double));
+    if (!are || !aim || !abssum) { free(are); free(aim); free(abssum); return 2; }
+    int64_t outer_n = (fmt == 0) ? m : n;
+    int64_t cnt = (fmt == 2) ? nnz : outer_n;
+    for (int64_t c = 0; c < k; ++c) {
+        for (int64_t o = 0; o < cnt; ++o) {
+            int64_t jlo = (fmt == 2) ? o : (int64_t)p0[o] - base;
+            int64_t jhi = (fmt == 2) ? o + 1 : (int64_t)p0[o + 1] - base;
+            for (int64_t j = jlo; j < jhi; ++j) {
+                int64_t row, col;
+                if (fmt == 0) { row = o; col = (int64_t)p1[j] - base; }
+                else if (fmt == 1) { row = (int64_t)p1[j] - base; col = o; }
+                else { row = (int64_t)p0[j] - base; col = (int64_t)p1[j] - base; }
+                int64_t out = trans ? col : row, in = trans ? row : col;
+                double ar, ai, br, bi;
+                V_TO_C(val[j], ar, ai);
+                if (conjA) ai = -ai;
+                V_TO_C(FN(getB)(B, ldb, opB, in, c), br, bi);
+                int64_t t = out + c * rows_out;
+                are[t] = dd_add_dd(are[t], two_prod(ar, br));
+                are[t] = dd_add_dd(are[t], two_prod(-ai, bi));
+                aim[t] = dd_add_dd(aim[t], two_prod(ar, bi));
+                aim[t] = dd_add_dd(aim[t], two_prod(ai, br));
+                abssum[t] += hypot(ar, ai) * hypot(br, bi);
+            }
+        }
+    }
+    double alr, ali, ber, bei;
+    V_TO_C(alpha, alr, ali);
+    V_TO_C(beta, ber, bei);
+    int beta_one = V_EQ_ONE(beta), beta_zero = V_IS_ZERO(beta);
+    for (int64_t c = 0; c < k; ++c) {
+        for (int64_t r = 0; r < rows_out; ++r) {
+            int64_t t = r + c * rows_out;
+            /* alpha * acc */
+            dd re = dd_add_dd(dd_mul_d(are[t], alr), dd_mul_d(aim[t], -ali));
+            dd im = dd_add_dd(dd_mul_d(are[t], ali), dd_mul_d(aim[t], alr));
+            double yr = 0.0, yi = 0.0, s = hypot(alr, ali) * abssum[t];
+            if (!beta_zero) {
+                V_TO_C(C0[r + c * ldc0], yr, yi);
+                if (!beta_one) {
+                    re = dd_add_dd(re, dd_add_dd(two_prod(yr, ber), two_prod(-yi, bei)));
+                    im = dd_add_dd(im, dd_add_dd(two_prod(yr, bei), two_prod(yi, ber)));
+                } else {
+                    re = dd_add(re, yr);
+                    im = dd_add(im, yi);
+                }
+                s += hypot(ber, bei) * hypot(yr, yi);
+            }
+            yre[t] = re.hi + re.lo;
+            if (yim) yim[t] = im.hi + im.lo;
+            scale[t] = s;
+        }
+    }
+    free(are); free(aim); free(abssum);
+    return 0;
+}
+
+/* COO -> compressed conversion, following src/conversions/conversions.jl:282-323
+ * (COO -> CSR) and :171-212 (COO -> CSC) with kernel_make_csr_keys! /
+ * kernel_make_csc_keys! (src/conversions/conversion_kernels.jl:38-57):
+ * key = major * minor_dim + minor, a stable sortperm of the keys, the three
+ * gathers by perm, ptr[r] = searchsortedfirst(major_sorted, r) and
+ * ptr[end] = nnz + 1 (in the index base).  Duplicates are kept, in input
+ * order.  Keys are unsigned 64-bit (the reference computes them in Ti, which
+ * wraps for Int32 once major_dim * minor_dim >= 2^31). */
+static int FN(coo_to_compressed)(int colmajor, int64_t m, int64_t n, int64_t nnz,
+                                 const void *rowindv, const void *colindv, const void *valv,
+                                 int base, void *ptr_outv, void *idx_outv, void *val_outv) {
+    const I *rowind = (const I *)rowindv, *colind = (const I *)colindv;
+    const V *val = (const V *)valv;
+    I *ptr_out = (I *)ptr_outv, *idx_out = (I *)idx_outv;
+    V *val_out = (V *)val_outv;
+    const I *major = colmajor ? colind : rowind;
+    const I *minor = colmajor ? rowind : colind;
+    int64_t major_n = colmajor ? n : m, minor_n = colmajor ? m : n;
+    if (nnz == 0) {
+        for (int64_t r = 0; r <= major_n; ++r) ptr_out[r] = (I)base;
+        return 0;
+    }
+    uint64_t *keys = (uint64_t *)malloc((size_t)nnz * sizeof(uint64_t));
+    int64_t *perm = (int64_t *)malloc((size_t)nnz * sizeof(int64_t));
+    int64_t *tmp = (int64_t *)malloc((size_t)nnz * sizeof(int64_t));
+    if (!keys || !perm || !tmp) { free(keys); free(perm); free(tmp); return 2; }
+    for (int64_t i = 0; i < nnz; ++i) {
+        keys[i] = (uint64_t)((int64_t)major[i] - base) * (uint64_t)minor_n +
+                  (uint64_t)((int64_t)minor[i] - base);
+        perm[i] = i;
+    }
+    stable_sortperm(keys, perm, tmp, nnz);
+    for (int64_t i = 0; i < nnz; ++i) {
+        idx_out[i] = minor[perm[i]];
+        val_out[i] = val[perm[i]];
+    }
+    /* searchsortedfirst over the sorted major indices, one query per major r */
+    int64_t pos = 0;
+    for (int64_t r = 0; r < major_n; ++r) {
+        while (pos < nnz && (int64_t)major[perm[pos]] - base < r) ++pos;
+        ptr_out[r] = (I)(pos + base);
+    }
+    ptr_out[major_n] = (I)(nnz + base);
+    free(keys); free(perm); free(tmp);
+    return 0;
+}
+
+/* Compressed -> COO expansion: kernel_csr_to_coo! / kernel_csc_to_coo!
+ * (src/conversions/conversion_kernels.jl:2-35).  Every stored entry of outer
+ * o gets major index o (in the index base); minor indices and values copy. */
+static int FN(compressed_to_coo)(int colmajor, int64_t m, int64_t n, int64_t nnz,
+                                 const void *ptrv, const void *idxv, const void *valv, int base,
+                                 void *rowind_outv, void *colind_outv, void *val_outv) {
+    const I *ptr = (const I *)ptrv, *idx = (const I *)idxv;
+    const V *val = (const V *)valv;
+    I *rowind_out = (I *)rowind_outv, *colind_out = (I *)colind_outv;
+    V *val_out = (V *)val_outv;
+    int64_t outer_n = colmajor ? n : m;
+    (void)nnz;
+    for (int64_t o = 0; o < outer_n; ++o) {
+        for (int64_t j = (int64_t)ptr[o] - base; j < (int64_t)ptr[o + 1] - base; ++j) {
+            I major = (I)(o + base);
+            if (colmajor) { rowind_out[j] = idx[j]; colind_out[j] = major; }
+            else { rowind_out[j] = major; colind_out[j] = idx[j]; }
+            val_out[j] = val[j];
+        }
+    }
+    return 0;
+}
+
+#undef FN

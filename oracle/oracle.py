@@ -1,0 +1,215 @@
+"""CPU oracle for the sparse x dense mul! path and the COO <-> CSR/CSC conversions.
+
+TEST INFRASTRUCTURE, NOT PRODUCT.  Only tests/, ``__graft_entry__.smoke()`` and the
+CPU-baseline leg of ``bench.py`` import this module, and only as the checker (or, for
+the baseline, as the timed CPU restatement of the reference).  The CUDA library and
+the ``genericsparsearrays_gb300`` package never import it.
+
+The arithmetic lives in ``gsa_oracle.c`` / ``gsa_oracle_impl.h`` (plain C, built by
+``build()`` below with ``-ffp-contract=off`` so that it rounds like Julia).  Each C
+function cites the reference file:line it restates:
+
+* ``mul``            -- ``LinearAlgebra.mul!`` for CSR/CSC/COO with identity, transpose
+  and adjoint on A and B (src/matrix_csr/matrix_csr.jl:145-211,
+  src/matrix_csc/matrix_csc.jl:144-213, src/matrix_coo/matrix_coo.jl:155-221 and the
+  kernels in src/matrix_*/matrix_*_kernels.jl:1-45).
+* ``mul_exact``      -- the same product in double-double plus the per-output scale
+  ``|alpha| sum|a||b| + |beta||C0|`` that the tolerance is relative to.
+* ``coo_to_csr`` / ``coo_to_csc`` -- src/conversions/conversions.jl:171-212,282-323.
+* ``csr_to_coo`` / ``csc_to_coo`` -- src/conversions/conversion_kernels.jl:2-35.
+
+Parity pin: Julia is absent on both machines of this build, so the restatement is
+pinned against the reference's known-answer fixtures (tests/golden/) and checked
+against scipy.sparse, which stands in for SparseArrays.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+import threading
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_BUILD = os.path.join(_HERE, "_build")
+_SO = os.path.join(_BUILD, "libgsa_oracle.so")
+_SRC = [os.path.join(_HERE, "gsa_oracle.c"), os.path.join(_HERE, "gsa_oracle_impl.h")]
+_lock = threading.Lock()
+_lib = None
+
+FMT = {"csr": 0, "csc": 1, "coo": 2}
+OP = {"N": 0, "T": 1, "C": 2}
+DTYPE = {np.dtype(np.float32): 0, np.dtype(np.float64): 1, np.dtype(np.complex64): 2,
+         np.dtype(np.complex128): 3, np.dtype(np.int32): 4, np.dtype(np.int64): 5}
+ITYPE = {np.dtype(np.int32): 0, np.dtype(np.int64): 1}
+
+
+def build(force: bool = False) -> str:
+    """Compile the C restatement into oracle/_build/libgsa_oracle.so (gcc, OpenMP)."""
+    os.makedirs(_BUILD, exist_ok=True)
+    newest = max(os.path.getmtime(p) for p in _SRC)
+    if force or not os.path.exists(_SO) or os.path.getmtime(_SO) < newest:
+        tmp = _SO + f".tmp{os.getpid()}"
+        cmd = ["gcc", "-O2", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared", "-std=c11",
+               "-o", tmp, _SRC[0], "-lm"]
+        subprocess.run(cmd, check=True)
+        os.replace(tmp, _SO)
+    return _SO
+
+
+def lib():
+    global _lib
+    with _lock:
+        if _lib is None:
+            build()
+            L = ctypes.CDLL(_SO)
+            i64, i32, vp = ctypes.c_int64, ctypes.c_int, ctypes.c_void_p
+            L.oracle_mul.argtypes = [i32, i32, i32, i32, i64, i64, i64, vp, vp, vp, i32,
+                                     i64, vp, i64, i32, vp, i64, vp, vp, i32]
+            L.oracle_mul_exact.argtypes = [i32, i32, i32, i32, i64, i64, i64, vp, vp, vp, i32,
+                                           i64, vp, i64, i32, vp, i64, vp, vp, vp, vp, vp]
+            L.oracle_coo_to_compressed.argtypes = [i32, i32, i32, i64, i64, i64, vp, vp, vp,
+                                                   i32, vp, vp, vp]
+            L.oracle_compressed_to_coo.argtypes = [i32, i32, i32, i64, i64, i64, vp, vp, vp,
+                                                   i32, vp, vp, vp]
+            for f in ("oracle_mul", "oracle_mul_exact", "oracle_coo_to_compressed",
+                      "oracle_compressed_to_coo", "oracle_max_threads"):
+                getattr(L, f).restype = ctypes.c_int
+            _lib = L
+    return _lib
+
+
+def max_threads() -> int:
+    return int(lib().oracle_max_threads())
+
+
+def _p(a):
+    return ctypes.c_void_p(a.ctypes.data) if a is not None and a.size else ctypes.c_void_p(0)
+
+
+def _scalar(v, dtype):
+    return np.array([v], dtype=dtype)
+
+
+def _dense_parts(B, opB):
+    """(array as Fortran-ordered 2-D view, ldb, rows_of_op(B), cols_of_op(B))."""
+    B2 = B.reshape(-1, 1) if B.ndim == 1 else B
+    B2 = np.asfortranarray(B2)
+    ld = max(B2.shape[0], 1)
+    if opB == "N":
+        return B2, ld, B2.shape[0], B2.shape[1]
+    return B2, ld, B2.shape[1], B2.shape[0]
+
+
+def mul(fmt, opA, m, n, p0, p1, val, base, B, C, alpha=1, beta=0, opB="N", nthreads=1):
+    """mul!(C, op(A), op(B), alpha, beta) on the CPU; C (1-D or Fortran 2-D) is updated in place.
+
+    ``p0, p1`` are (rowptr, colval) for CSR, (colptr, rowval) for CSC and (rowind, colind)
+    for COO, in index base ``base``.  Returns C.
+    """
+    val = np.ascontiguousarray(val)
+    dt = val.dtype
+    p0 = np.ascontiguousarray(p0)
+    p1 = np.ascontiguousarray(p1, dtype=p0.dtype)
+    B2, ldb, rb, k = _dense_parts(np.asarray(B, dtype=dt), opB)
+    C2 = C.reshape(-1, 1) if C.ndim == 1 else C
+    assert C2.flags.f_contiguous and C2.dtype == dt
+    rows_out = m if opA == "N" else n
+    assert C2.shape == (rows_out, k), (C2.shape, rows_out, k)
+    assert rb == (n if opA == "N" else m)
+    nnz = val.size
+    al, be = _scalar(alpha, dt), _scalar(beta, dt)  # kept alive across the call
+    rc = lib().oracle_mul(FMT[fmt], OP[opA], DTYPE[dt], ITYPE[p0.dtype], m, n, nnz,
+                          _p(p0), _p(p1), _p(val), base, k, _p(B2), ldb, OP[opB],
+                          _p(C2), max(C2.shape[0], 1), _p(al), _p(be), nthreads)
+    if rc != 0:
+        raise RuntimeError(f"oracle_mul failed: {rc}")
+    return C
+
+
+def mul_exact(fmt, opA, m, n, p0, p1, val, base, B, C0, alpha=1, beta=0, opB="N"):
+    """Double-double product; returns (y, scale) with y complex128 or float64 and scale
+    = |alpha| * sum|a||b| + |beta| * |C0| per output element (same shape as C0)."""
+    val = np.ascontiguousarray(val)
+    dt = val.dtype
+    p0 = np.ascontiguousarray(p0)
+    p1 = np.ascontiguousarray(p1, dtype=p0.dtype)
+    B2, ldb, rb, k = _dense_parts(np.asarray(B, dtype=dt), opB)
+    rows_out = m if opA == "N" else n
+    C02 = np.asfortranarray((C0.reshape(-1, 1) if C0.ndim == 1 else C0).astype(dt))
+    assert C02.shape == (rows_out, k)
+    yre = np.zeros((rows_out, k), dtype=np.float64, order="F")
+    yim = np.zeros((rows_out, k), dtype=np.float64, order="F")
+    sc = np.zeros((rows_out, k), dtype=np.float64, order="F")
+    al, be = _scalar(alpha, dt), _scalar(beta, dt)  # kept alive across the call
+    rc = lib().oracle_mul_exact(FMT[fmt], OP[opA], DTYPE[dt], ITYPE[p0.dtype], m, n, val.size,
+                                _p(p0), _p(p1), _p(val), base, k, _p(B2), ldb, OP[opB],
+                                _p(C02), max(rows_out, 1), _p(al), _p(be), _p(yre), _p(yim),
+                                _p(sc))
+    if rc != 0:
+        raise RuntimeError(f"oracle_mul_exact failed: {rc}")
+    y = yre + 1j * yim if np.iscomplexobj(val) else yre
+    if C0.ndim == 1:
+        return y[:, 0], sc[:, 0]
+    return y, sc
+
+
+def _coo_to(colmajor, m, n, rowind, colind, val, base):
+    rowind = np.ascontiguousarray(rowind)
+    colind = np.ascontiguousarray(colind, dtype=rowind.dtype)
+    val = np.ascontiguousarray(val)
+    nnz = val.size
+    major_n = n if colmajor else m
+    ptr = np.empty(major_n + 1, dtype=rowind.dtype)
+    idx = np.empty(nnz, dtype=rowind.dtype)
+    out = np.empty(nnz, dtype=val.dtype)
+    rc = lib().oracle_coo_to_compressed(colmajor, DTYPE[val.dtype], ITYPE[rowind.dtype], m, n,
+                                        nnz, _p(rowind), _p(colind), _p(val), base, _p(ptr),
+                                        _p(idx), _p(out))
+    if rc != 0:
+        raise RuntimeError(f"oracle_coo_to_compressed failed: {rc}")
+    return ptr, idx, out
+
+
+def coo_to_csr(m, n, rowind, colind, val, base=1):
+    """GenericSparseMatrixCSR(::GenericSparseMatrixCOO) -> (rowptr, colval, nzval)."""
+    return _coo_to(0, m, n, rowind, colind, val, base)
+
+
+def coo_to_csc(m, n, rowind, colind, val, base=1):
+    """GenericSparseMatrixCSC(::GenericSparseMatrixCOO) -> (colptr, rowval, nzval)."""
+    return _coo_to(1, m, n, rowind, colind, val, base)
+
+
+def _to_coo(colmajor, m, n, ptr, idx, val, base):
+    ptr = np.ascontiguousarray(ptr)
+    idx = np.ascontiguousarray(idx, dtype=ptr.dtype)
+    val = np.ascontiguousarray(val)
+    nnz = val.size
+    r = np.empty(nnz, dtype=ptr.dtype)
+    c = np.empty(nnz, dtype=ptr.dtype)
+    v = np.empty(nnz, dtype=val.dtype)
+    rc = lib().oracle_compressed_to_coo(colmajor, DTYPE[val.dtype], ITYPE[ptr.dtype], m, n, nnz,
+                                        _p(ptr), _p(idx), _p(val), base, _p(r), _p(c), _p(v))
+    if rc != 0:
+        raise RuntimeError(f"oracle_compressed_to_coo failed: {rc}")
+    return r, c, v
+
+
+def csr_to_coo(m, n, rowptr, colval, nzval, base=1):
+    """GenericSparseMatrixCOO(::GenericSparseMatrixCSR) -> (rowind, colind, nzval)."""
+    return _to_coo(0, m, n, rowptr, colval, nzval, base)
+
+
+def csc_to_coo(m, n, colptr, rowval, nzval, base=1):
+    """GenericSparseMatrixCOO(::GenericSparseMatrixCSC) -> (rowind, colind, nzval)."""
+    return _to_coo(1, m, n, colptr, rowval, nzval, base)
+
+
+def max_rel_error(y, y_exact, scale):
+    """max_i |y_i - y_exact_i| / scale_i (scale 0 -> absolute error)."""
+    y = np.asarray(y).astype(np.complex128 if np.iscomplexobj(y) else np.float64)
+    err = np.abs(y - y_exact)
+    s = np.where(scale > 0, scale, 1.0)
+    return float(np.max(err / s)) if err.size else 0.0

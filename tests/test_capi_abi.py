@@ -1,0 +1,75 @@
+"""libgsa.so loads, exports every symbol include/gsa.h declares, and rejects bad arguments
+before touching the GPU (CPU only: no compute call is made here)."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "gsa.h")
+
+
+def declared_functions():
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(gsa_[a-z0-9_]+)\s*\(", text)))
+
+
+@pytest.fixture(scope="module")
+def lib(gsa):
+    return gsa._lib.load()
+
+
+def test_every_declared_symbol_is_exported(lib, gsa):
+    names = declared_functions()
+    assert len(names) >= 12
+    for name in names:
+        assert hasattr(lib, name), f"{name} declared in gsa.h but not exported"
+        assert name in gsa._lib.SIGNATURES, f"{name} has no ctypes signature"
+
+
+def test_version_and_error_string(lib):
+    assert lib.gsa_version() == 100
+    assert isinstance(lib.gsa_last_error_string(), bytes)
+
+
+def _mul_call(lib, **kw):
+    a = dict(stream=None, dtype=1, itype=0, m=4, n=3, nnz=0, p0=None, p1=None, v=None, base=1,
+             opA=0, k=1, B=None, ldb=3, opB=0, C=None, ldc=4)
+    a.update(kw)
+    one = np.array([1.0])
+    zero = np.array([0.0])
+    return lib.gsa_csr_mul(a["stream"], a["dtype"], a["itype"], a["m"], a["n"], a["nnz"], a["p0"],
+                           a["p1"], a["v"], a["base"], a["opA"], a["k"], a["B"], a["ldb"], a["opB"],
+                           a["C"], a["ldc"], one.ctypes.data_as(ctypes.c_void_p),
+                           zero.ctypes.data_as(ctypes.c_void_p), 0, None, 0)
+
+
+def test_argument_checks_precede_gpu_work(lib, gsa):
+    L = gsa._lib
+    assert _mul_call(lib, dtype=99) == L.ERR_UNSUPPORTED
+    assert b"unsupported dtype" in lib.gsa_last_error_string()
+    assert _mul_call(lib, itype=7) == L.ERR_UNSUPPORTED
+    assert _mul_call(lib, opA=5) == L.ERR_INVALID_ARG
+    assert _mul_call(lib, m=-1) == L.ERR_INVALID_ARG
+    assert _mul_call(lib, ldb=2) == L.ERR_DIM  # op(A) is 4x3 -> B needs ldb >= 3
+    assert _mul_call(lib, ldc=3) == L.ERR_DIM  # C needs ldc >= 4
+    assert _mul_call(lib, opA=1, ldb=3) == L.ERR_DIM  # op(A) 3x4 -> B needs ldb >= 4
+    # misaligned dense operand (an odd address)
+    assert _mul_call(lib, B=ctypes.c_void_p(8 * 1000 + 4), C=ctypes.c_void_p(8 * 2000)) == L.ERR_INVALID_ARG
+    assert b"aligned" in lib.gsa_last_error_string()
+
+
+def test_workspace_size_queries(lib):
+    # gather (CSR, opA = N): tile coordinates + carries; scatter (CSR, opA = T): coordinates only
+    g = lib.gsa_mul_workspace_size(0, 1, 0, 1000, 1000, 5000, 0, 1, 0)
+    s = lib.gsa_mul_workspace_size(0, 1, 0, 1000, 1000, 5000, 1, 1, 0)
+    v = lib.gsa_mul_workspace_size(0, 1, 0, 1000, 1000, 5000, 0, 1, 2)
+    assert g > 0 and s > 0 and v == 0
+    assert lib.gsa_mul_workspace_size(0, 1, 0, 1000, 1000, 5000, 0, 16, 0) > g
+    assert lib.gsa_mul_workspace_size(0, 99, 0, 10, 10, 5, 0, 1, 0) == 0
+    w = lib.gsa_coo_to_compressed_workspace_size(0, 1, 0, 1000, 1000, 5000)
+    assert w >= 5000 * 24
+    assert lib.gsa_coo_to_compressed_workspace_size(0, 1, 0, 10, 10, 0) == 0

@@ -1,0 +1,125 @@
+"""COO -> CSR/CSC and CSR/CSC -> COO on the GPU: bit-exact against the oracle and the
+reference's known answers."""
+import json
+import os
+
+import numpy as np
+import pytest
+import torch
+
+from helpers import INDEX_TYPES, VALUE_TYPES, parts, rand_values, sprand
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "known_answers.json")))
+
+
+def coo(gsa, dev, m, n, r, c, v):
+    return gsa.adapt(dev, gsa.GenericSparseMatrixCOO(m, n, r, c, v))
+
+
+def np_(t):
+    return t.cpu().numpy()
+
+
+def test_structure_pin_2x2(gsa, cuda):
+    """test/shared/matrix_csr.jl:34-58 through the GPU COO -> CSR path."""
+    g = GOLDEN["csr_2x2_structure"]
+    A = coo(gsa, cuda, 2, 2, np.array(g["coo"]["rowind"]), np.array(g["coo"]["colind"]),
+            np.array(g["coo"]["nzval"]))
+    C = gsa.GenericSparseMatrixCSR(A)
+    assert C.rowptr.tolist() == g["expected_csr"]["rowptr"]
+    assert C.colval.tolist() == g["expected_csr"]["colval"]
+    assert C.nzval.tolist() == g["expected_csr"]["nzval"]
+    K = gsa.GenericSparseMatrixCSC(A)
+    assert K.colptr.tolist() == g["csc"]["colptr"] and K.rowval.tolist() == g["csc"]["rowval"]
+
+
+@pytest.mark.parametrize("name", ["single", "full_row", "full_col"])
+def test_edge_cases(gsa, cuda, name):
+    """test/shared/conversions.jl:128-152: CSC -> COO (nnz kept) and CSC -> CSR via COO."""
+    g = GOLDEN[f"conversion_edge_{name}"]
+    csc = gsa.adapt(cuda, gsa.GenericSparseMatrixCSC(3, 4, np.array(g["csc"]["colptr"]),
+                                                     np.array(g["csc"]["rowval"]),
+                                                     np.array(g["csc"]["nzval"])))
+    c = gsa.GenericSparseMatrixCOO(csc)
+    assert gsa.nnz(c) == len(g["coo"]["nzval"])
+    assert c.rowind.tolist() == g["coo"]["rowind"] and c.colind.tolist() == g["coo"]["colind"]
+    r = gsa.GenericSparseMatrixCSR(csc)
+    assert r.rowptr.tolist() == g["expected_csr"]["rowptr"]
+    assert r.colval.tolist() == g["expected_csr"]["colval"]
+    assert r.nzval.tolist() == g["expected_csr"]["nzval"]
+    assert np.array_equal(gsa.collect(r), np.array(g["dense"]))
+
+
+@pytest.mark.parametrize("m,n", [(0, 0), (5, 3), (0, 4)])
+def test_empty(gsa, cuda, m, n):
+    e = np.zeros(0, np.int64)
+    A = coo(gsa, cuda, m, n, e, e, np.zeros(0))
+    C = gsa.GenericSparseMatrixCSR(A)
+    assert C.rowptr.tolist() == [1] * (m + 1) and gsa.nnz(C) == 0
+    K = gsa.GenericSparseMatrixCSC(A)
+    assert K.colptr.tolist() == [1] * (n + 1)
+
+
+@pytest.mark.parametrize("it", INDEX_TYPES)
+@pytest.mark.parametrize("dt", VALUE_TYPES)
+def test_permuted_coo_bit_exact(gsa, oracle, cuda, it, dt):
+    """test/shared/conversions.jl shapes (100x200 at 0.05), triplets shuffled, with duplicate
+    (row, col) pairs: CSR and CSC structure and values equal the oracle's bit for bit."""
+    rng = np.random.default_rng(31)
+    S = sprand(rng, 100, 200, 0.05, dt)
+    r, c, v = parts(S, "coo", it, order="shuffle", rng=rng)
+    dup = rng.choice(v.size, 40, replace=False)
+    r = np.concatenate([r, r[dup]])
+    c = np.concatenate([c, c[dup]])
+    v = np.concatenate([v, rand_values(rng, 40, dt)])
+    p = rng.permutation(v.size)
+    r, c, v = r[p], c[p], v[p]
+    A = coo(gsa, cuda, 100, 200, r, c, v)
+    for cls, f in ((gsa.GenericSparseMatrixCSR, oracle.coo_to_csr), (gsa.GenericSparseMatrixCSC, oracle.coo_to_csc)):
+        B = cls(A)
+        ptr, idx = (B.rowptr, B.colval) if cls is gsa.GenericSparseMatrixCSR else (B.colptr, B.rowval)
+        e_ptr, e_idx, e_val = f(100, 200, r, c, v)
+        assert np.array_equal(np_(ptr), e_ptr)
+        assert np.array_equal(np_(idx), e_idx)
+        assert np.array_equal(np_(B.nzval), e_val)
+
+
+@pytest.mark.parametrize("it", INDEX_TYPES)
+def test_compressed_to_coo_and_round_trips(gsa, oracle, cuda, it):
+    rng = np.random.default_rng(8)
+    S = sprand(rng, 150, 90, 0.07, np.complex128)
+    p0, p1, v = parts(S, "csr", it)
+    A = gsa.adapt(cuda, gsa.GenericSparseMatrixCSR(150, 90, p0, p1, v))
+    C = gsa.GenericSparseMatrixCOO(A)
+    er, ec, ev = oracle.csr_to_coo(150, 90, p0, p1, v)
+    assert np.array_equal(np_(C.rowind), er) and np.array_equal(np_(C.colind), ec)
+    assert np.array_equal(np_(C.nzval), ev)
+    q0, q1, w = parts(S, "csc", it)
+    K = gsa.adapt(cuda, gsa.GenericSparseMatrixCSC(150, 90, q0, q1, w))
+    Ck = gsa.GenericSparseMatrixCOO(K)
+    er, ec, ev = oracle.csc_to_coo(150, 90, q0, q1, w)
+    assert np.array_equal(np_(Ck.rowind), er) and np.array_equal(np_(Ck.colind), ec)
+    # round trips CSR -> COO -> CSR, CSC -> CSR -> CSC, and transposes
+    R = gsa.GenericSparseMatrixCSR(gsa.GenericSparseMatrixCOO(A))
+    assert torch.equal(R.rowptr, A.rowptr) and torch.equal(R.colval, A.colval)
+    assert torch.equal(R.nzval, A.nzval)
+    K2 = gsa.GenericSparseMatrixCSC(gsa.GenericSparseMatrixCSR(K))
+    assert torch.equal(K2.colptr, K.colptr) and torch.equal(K2.rowval, K.rowval)
+    assert torch.equal(K2.nzval, K.nzval)
+    At = gsa.GenericSparseMatrixCSR(gsa.adjoint(K))
+    assert np.allclose(gsa.collect(At), S.toarray().conj().T)
+    Tc = gsa.GenericSparseMatrixCSC(gsa.transpose(C))
+    assert np.allclose(gsa.collect(Tc), S.toarray().T)
+
+
+def test_power_law_rows_conversion(gsa, oracle, cuda):
+    """Rows of up to 50,000 entries, shuffled triplets: bit-exact against the oracle."""
+    from genericsparsearrays_gb300 import workloads
+    m, n, rp, cv, nz = workloads.power_law(n=100_000, seed=4, itype=np.int64, dtype=np.float64)
+    _, _, r, c, v = workloads.permuted_coo(m, n, rp, cv, nz, seed=5)
+    A = coo(gsa, cuda, m, n, r, c, v)
+    B = gsa.GenericSparseMatrixCSR(A)
+    assert np.array_equal(np_(B.rowptr), rp) and np.array_equal(np_(B.colval), cv)
+    assert np.array_equal(np_(B.nzval), nz)

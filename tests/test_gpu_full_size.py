@@ -1,0 +1,105 @@
+"""Full-size benchmark workloads on the GPU against the oracle: the 2048x2048 Laplacian (SpMV
+and SpMM, CSR and CSC, F64 and F32, Int32 and Int64 indices, permuted-COO conversion), the
+n = 1e6 power-law ComplexF64 matrix (CSR and COO) and the n = 1e5 Poisson(10) matrix."""
+import numpy as np
+import pytest
+import scipy.sparse as sp
+import torch
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def wl(gsa):
+    from genericsparsearrays_gb300 import workloads
+    return workloads
+
+
+def rel_err_vs(y, ref, scale):
+    y = np.asarray(y)
+    return float(np.max(np.abs(y - ref) / np.where(scale > 0, scale, 1)))
+
+
+@pytest.mark.parametrize("it", [np.int32, np.int64])
+@pytest.mark.parametrize("dt", [np.float64, np.float32])
+def test_laplacian_spmv_csr_csc(gsa, oracle, cuda, wl, it, dt):
+    m, n, rp, cv, nz = wl.laplacian_2d(2048, itype=it, dtype=dt)
+    rng = np.random.default_rng(0)
+    x = rng.uniform(-1, 1, n).astype(dt)
+    S = sp.csr_matrix((nz.astype(np.float64), cv.astype(np.int64) - 1, rp.astype(np.int64) - 1), shape=(m, n))
+    ref = S @ x.astype(np.float64)
+    scale = abs(S) @ np.abs(x.astype(np.float64))
+    tol = 1e-12 if dt == np.float64 else 1e-5
+    A = gsa.adapt(cuda, gsa.GenericSparseMatrixCSR(m, n, rp, cv, nz))
+    xd = torch.from_numpy(x).to(cuda)
+    for algo in (gsa.ALGO_MERGE, gsa.ALGO_VECTOR):
+        y = torch.empty(m, dtype=xd.dtype, device=cuda)
+        gsa.mul_(y, A, xd, algo=algo)
+        assert rel_err_vs(y.cpu().numpy(), ref, scale) <= tol
+    _, _, cp, rv, cz = wl.csr_to_csc(m, n, rp, cv, nz)
+    K = gsa.adapt(cuda, gsa.GenericSparseMatrixCSC(m, n, cp, rv, cz))
+    y = K @ xd
+    assert rel_err_vs(y.cpu().numpy(), ref, scale) <= tol
+
+
+def test_laplacian_spmm_k16(gsa, oracle, cuda, wl):
+    m, n, rp, cv, nz = wl.laplacian_2d(2048, itype=np.int32, dtype=np.float64)
+    rng = np.random.default_rng(1)
+    X = np.asfortranarray(rng.uniform(-1, 1, (n, 16)))
+    Y = np.zeros((m, 16), order="F")
+    oracle.mul("csr", "N", m, n, rp, cv, nz, 1, X, Y, nthreads=oracle.max_threads())
+    S = sp.csr_matrix((nz, cv.astype(np.int64) - 1, rp.astype(np.int64) - 1), shape=(m, n))
+    scale = abs(S) @ np.abs(X)
+    A = gsa.adapt(cuda, gsa.GenericSparseMatrixCSR(m, n, rp, cv, nz))
+    Yd = A @ torch.from_numpy(X).to(cuda)
+    assert rel_err_vs(Yd.cpu().numpy(), Y, scale) <= 1e-12
+    _, _, cp, rv, cz = wl.csr_to_csc(m, n, rp, cv, nz)
+    K = gsa.adapt(cuda, gsa.GenericSparseMatrixCSC(m, n, cp, rv, cz))
+    Yk = K @ torch.from_numpy(X).to(cuda)
+    assert rel_err_vs(Yk.cpu().numpy(), Y, scale) <= 1e-12
+
+
+@pytest.mark.parametrize("it", [np.int32, np.int64])
+def test_laplacian_permuted_coo_conversion(gsa, cuda, wl, it):
+    """COO -> CSR and COO -> CSC of the randomly permuted Laplacian triplets are bit-exact
+    (keys need 44 bits: the reference's Int32 keys would wrap here)."""
+    m, n, rp, cv, nz = wl.laplacian_2d(2048, itype=it, dtype=np.float64)
+    _, _, r, c, v = wl.permuted_coo(m, n, rp, cv, nz, seed=7)
+    A = gsa.adapt(cuda, gsa.GenericSparseMatrixCOO(m, n, r, c, v))
+    B = gsa.GenericSparseMatrixCSR(A)
+    assert np.array_equal(B.rowptr.cpu().numpy(), rp)
+    assert np.array_equal(B.colval.cpu().numpy(), cv)
+    assert np.array_equal(B.nzval.cpu().numpy(), nz)
+    _, _, cp, rv, cz = wl.csr_to_csc(m, n, rp, cv, nz)
+    K = gsa.GenericSparseMatrixCSC(A)
+    assert np.array_equal(K.colptr.cpu().numpy(), cp)
+    assert np.array_equal(K.rowval.cpu().numpy(), rv)
+    assert np.array_equal(K.nzval.cpu().numpy(), cz)
+
+
+def test_power_law_complex_csr_coo(gsa, oracle, cuda, wl):
+    m, n, rp, cv, nz = wl.power_law(1_000_000, seed=0, itype=np.int64, dtype=np.complex128)
+    rng = np.random.default_rng(2)
+    x = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    ye, sc = oracle.mul_exact("csr", "N", m, n, rp, cv, nz, 1, x, np.zeros(m, np.complex128))
+    xd = torch.from_numpy(x).to(cuda)
+    A = gsa.adapt(cuda, gsa.GenericSparseMatrixCSR(m, n, rp, cv, nz))
+    assert oracle.max_rel_error((A @ xd).cpu().numpy(), ye, sc) <= 1e-12
+    rows = wl.csr_rows(rp)
+    C = gsa.adapt(cuda, gsa.GenericSparseMatrixCOO(m, n, rows, cv, nz))
+    assert oracle.max_rel_error((C @ xd).cpu().numpy(), ye, sc) <= 1e-12
+
+
+def test_random_poisson_three_formats(gsa, oracle, cuda, wl):
+    m, n, rp, cv, nz = wl.random_poisson(100_000, seed=0)
+    rng = np.random.default_rng(3)
+    x = rng.uniform(-1, 1, n)
+    ye, sc = oracle.mul_exact("csr", "N", m, n, rp, cv, nz, 1, x, np.zeros(m))
+    xd = torch.from_numpy(x).to(cuda)
+    A = gsa.adapt(cuda, gsa.GenericSparseMatrixCSR(m, n, rp, cv, nz))
+    assert oracle.max_rel_error((A @ xd).cpu().numpy(), ye, sc) <= 1e-12
+    _, _, cp, rv, cz = wl.csr_to_csc(m, n, rp, cv, nz)
+    K = gsa.adapt(cuda, gsa.GenericSparseMatrixCSC(m, n, cp, rv, cz))
+    assert oracle.max_rel_error((K @ xd).cpu().numpy(), ye, sc) <= 1e-12
+    C = gsa.adapt(cuda, gsa.GenericSparseMatrixCOO(K))  # column-major triplets
+    assert oracle.max_rel_error((C @ xd).cpu().numpy(), ye, sc) <= 1e-12

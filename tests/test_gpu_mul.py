@@ -1,0 +1,220 @@
+"""mul! on the GPU through the C ABI against the oracle (parity tests proper).
+
+Floating point: per-row error against the double-double oracle within 1e-12 (F64/C64) or 1e-5
+(F32/C32) of |alpha| sum|a||b| + |beta||C|.  Integers: bit-exact against the oracle's
+restatement of the reference kernels.
+"""
+import zlib
+
+import numpy as np
+import pytest
+import torch
+
+from helpers import (INDEX_TYPES, OPS, VALUE_TYPES, dense_parent, is_complex, is_int, op_apply,
+                     parts, rand_values, sprand, tol)
+
+pytestmark = pytest.mark.gpu
+
+CLS = {"csr": "GenericSparseMatrixCSR", "csc": "GenericSparseMatrixCSC", "coo": "GenericSparseMatrixCOO"}
+
+
+def make(gsa, fmt, m, n, p0, p1, v, dev):
+    return gsa.adapt(dev, getattr(gsa, CLS[fmt])(m, n, p0, p1, v))
+
+
+def wrap(gsa, X, op):
+    return X if op == "N" else (gsa.transpose(X) if op == "T" else gsa.adjoint(X))
+
+
+def check(oracle, fmt, opA, m, n, p0, p1, v, P, opB, C0, C_gpu, alpha, beta, dt):
+    C_gpu = C_gpu.cpu().numpy()
+    if is_int(dt):
+        C = np.asfortranarray(C0.copy())
+        oracle.mul(fmt, opA, m, n, p0, p1, v, 1, P, C, alpha=alpha, beta=beta, opB=opB)
+        assert np.array_equal(C_gpu, C), "integer product differs from the oracle"
+        return 0.0
+    ye, sc = oracle.mul_exact(fmt, opA, m, n, p0, p1, v, 1, P, C0, alpha=alpha, beta=beta, opB=opB)
+    err = oracle.max_rel_error(C_gpu, ye, sc)
+    assert err <= tol(dt), f"{fmt} op(A)={opA} op(B)={opB}: max rel error {err:.3e} > {tol(dt)}"
+    return err
+
+
+@pytest.mark.parametrize("fmt", ["csr", "csc", "coo"])
+@pytest.mark.parametrize("it", INDEX_TYPES)
+@pytest.mark.parametrize("dt", VALUE_TYPES)
+def test_shared_suite_parity(gsa, oracle, cuda, fmt, it, dt):
+    """test/shared/matrix_{csr,csc,coo}.jl mul! sections: 100x80 at density 0.1, b of 80, B of
+    80x50, all op(A) x op(B); plus alpha/beta (the reference never tests 5-arg mul!).  Complex
+    CSR-T, CSC-N and COO, skipped by the reference (KA @atomic), are covered here."""
+    rng = np.random.default_rng(zlib.crc32(f"{fmt}-{np.dtype(it)}-{np.dtype(dt)}".encode()))
+    scalars = [(1, 0), (2, 1), (3, 2)]
+    if is_complex(dt):
+        scalars.append((0.5 - 1j, 2 + 0.25j))
+    for opA in OPS:
+        m, n = (100, 80) if opA == "N" else (80, 100)
+        S = sprand(rng, m, n, 0.1, dt)
+        p0, p1, v = parts(S, fmt, it)
+        A = wrap(gsa, make(gsa, fmt, m, n, p0, p1, v, cuda), opA)
+        for opB in OPS:
+            for k in (1, 50):
+                P = dense_parent(rng, 80, k, opB, dt)
+                Pd = torch.from_numpy(P).to(cuda)
+                if k == 1 and opB == "N":
+                    P, Pd = P[:, 0].copy(), Pd[:, 0].contiguous()
+                B = wrap(gsa, Pd, opB)
+                for alpha, beta in scalars:
+                    C0 = rand_values(rng, (100,) if (k == 1 and opB == "N") else (100, k), dt)
+                    C0 = np.asfortranarray(C0)
+                    C = torch.from_numpy(C0).to(cuda)
+                    gsa.mul_(C, A, B, alpha, beta)
+                    check(oracle, fmt, opA, m, n, p0, p1, v, P, opB, C0, C, alpha, beta, dt)
+
+
+@pytest.mark.parametrize("fmt", ["csr", "csc", "coo"])
+def test_star_matches_mul(gsa, oracle, cuda, fmt):
+    """``A * b`` and 3-arg ``mul!`` (what the reference tests call) give the same answer."""
+    rng = np.random.default_rng(2)
+    S = sprand(rng, 100, 80, 0.1, np.float64)
+    p0, p1, v = parts(S, fmt, np.int64)
+    A = make(gsa, fmt, 100, 80, p0, p1, v, cuda)
+    b = torch.from_numpy(rng.uniform(-1, 1, 80)).to(cuda)
+    c1 = (A @ b).cpu().numpy()
+    c2 = torch.full((100,), float("nan"), dtype=torch.float64, device=cuda)
+    gsa.mul_(c2, A, b)
+    if fmt == "csr":  # the gather has no atomics: identical results
+        assert np.array_equal(c1, c2.cpu().numpy())
+    ye, sc = oracle.mul_exact(fmt, "N", 100, 80, p0, p1, v, 1, b.cpu().numpy(), np.zeros(100))
+    assert oracle.max_rel_error(c1, ye, sc) <= 1e-12
+    assert oracle.max_rel_error(c2.cpu().numpy(), ye, sc) <= 1e-12
+
+
+def test_docs_example(gsa, cuda):
+    """docs/src/index.md:47-58 on the GPU: CSC times [1,2,3] == [10, 3, 15] exactly."""
+    import json
+    import os
+    g = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "known_answers.json")))["docs_spmv_3x3"]
+    for fmt, keys in (("csc", ("colptr", "rowval")), ("csr", ("rowptr", "colval")), ("coo", ("rowind", "colind"))):
+        a = g[fmt]
+        A = make(gsa, fmt, 3, 3, np.array(a[keys[0]]), np.array(a[keys[1]]), np.array(a["nzval"]), cuda)
+        c = A @ torch.tensor(g["b"], dtype=torch.float64, device=cuda)
+        assert c.cpu().tolist() == g["c"]
+
+
+@pytest.mark.parametrize("fmt", ["csr", "csc", "coo"])
+def test_beta_zero_overwrites_nan(gsa, cuda, fmt):
+    rng = np.random.default_rng(9)
+    S = sprand(rng, 64, 48, 0.2, np.float64)
+    p0, p1, v = parts(S, fmt, np.int32)
+    A = make(gsa, fmt, 64, 48, p0, p1, v, cuda)
+    x = torch.from_numpy(rng.uniform(-1, 1, 48)).to(cuda)
+    C = torch.full((64,), float("nan"), dtype=torch.float64, device=cuda)
+    gsa.mul_(C, A, x, 1.0, 0.0)
+    assert torch.isfinite(C).all()
+
+
+@pytest.mark.parametrize("fmt", ["csr", "csc", "coo"])
+@pytest.mark.parametrize("algo", [0, 2])
+def test_edge_shapes(gsa, oracle, cuda, fmt, algo):
+    """Empty matrix, empty rows, k = 0, m = 0 and n = 0: beta still applies (or not)."""
+    rng = np.random.default_rng(4)
+    cases = [(0, 5), (5, 0), (7, 6), (1, 1)]
+    for m, n in cases:
+        for density in (0.0, 0.5):
+            S = sprand(rng, m, n, density, np.float64) if m and n else None
+            if S is None:
+                import scipy.sparse as sp
+                S = sp.csr_matrix((m, n))
+            p0, p1, v = parts(S, fmt, np.int64)
+            A = make(gsa, fmt, m, n, p0, p1, v, cuda)
+            for k in (0, 1, 3):
+                X = np.asfortranarray(rng.uniform(-1, 1, (n, k)))
+                C0 = np.asfortranarray(rng.uniform(-1, 1, (m, k)))
+                C = torch.from_numpy(C0).to(cuda)
+                if fmt == "coo":
+                    gsa.mul_(C, A, torch.from_numpy(X).to(cuda), 2.0, 0.5)
+                else:
+                    gsa.mul_(C, A, torch.from_numpy(X).to(cuda), 2.0, 0.5, algo=algo)
+                if m and k:
+                    ye, sc = oracle.mul_exact(fmt, "N", m, n, p0, p1, v, 1, X, C0, alpha=2.0, beta=0.5)
+                    assert oracle.max_rel_error(C.cpu().numpy(), ye, sc) <= 1e-12
+
+
+@pytest.mark.parametrize("dt", [np.float64, np.complex128, np.int64])
+@pytest.mark.parametrize("k", [1, 3])
+def test_long_rows_cross_tiles(gsa, oracle, cuda, dt, k):
+    """Rows of 0, 1, 5 000 and 60 000 entries mixed: merge-path tiles split long rows over
+    many CTAs; the open-row partials must come back in full (integers: bit-exact)."""
+    rng = np.random.default_rng(12)
+    n = 70_000
+    lengths = np.array([0, 60_000, 1, 0, 5_000, 3, 0, 0, 2, 60_000] + [4] * 500 + [0] * 40)
+    m = lengths.size
+    rowptr = np.concatenate([[0], np.cumsum(lengths)]).astype(np.int64) + 1
+    cols = np.concatenate([np.sort(rng.choice(n, size=l, replace=False)) for l in lengths]).astype(np.int64) + 1
+    vals = rand_values(rng, cols.size, dt)
+    for algo in (1, 2):
+        for fmt in ("csr", "csc_t"):
+            if fmt == "csr":
+                A = make(gsa, "csr", m, n, rowptr, cols, vals, cuda)
+                opA, f, mm, nn = "N", "csr", m, n
+            else:  # the same arrays as a CSC of the transpose; op(A) = T gathers
+                A = gsa.transpose(make(gsa, "csc", n, m, rowptr, cols, vals, cuda))
+                opA, f, mm, nn = "T", "csc", n, m
+            X = np.asfortranarray(rand_values(rng, (n, k), dt))
+            C0 = np.asfortranarray(rand_values(rng, (m, k), dt))
+            C = torch.from_numpy(C0).to(cuda)
+            gsa.mul_(C, A, torch.from_numpy(X).to(cuda), 3, 2, algo=algo)
+            check(oracle, f, opA, mm, nn, rowptr, cols, vals, X, "N", C0, C, 3, 2, dt)
+
+
+def test_gather_is_deterministic(gsa, cuda):
+    """The CSR gather uses no atomics: two runs are bit-identical."""
+    from genericsparsearrays_gb300 import workloads
+    m, n, rp, cv, nz = workloads.power_law(n=200_000, seed=3, itype=np.int64, dtype=np.float64)
+    A = make(gsa, "csr", m, n, rp, cv, nz, cuda)
+    x = torch.randn(n, dtype=torch.float64, device=cuda)
+    y1 = A @ x
+    y2 = A @ x
+    assert torch.equal(y1, y2)
+
+
+@pytest.mark.parametrize("order", ["rows", "storage", "shuffle"])
+def test_coo_orders_and_duplicates(gsa, oracle, cuda, order):
+    """COO in row order, column order (as built from SparseMatrixCSC) and random order, with
+    duplicated entries: every stored entry contributes (no merging), as in the reference."""
+    rng = np.random.default_rng(21)
+    S = sprand(rng, 300, 200, 0.05, np.complex128)
+    r, c, v = parts(S, "coo", np.int32, order=order, rng=rng)
+    r = np.concatenate([r, r[:50]])
+    c = np.concatenate([c, c[:50]])
+    v = np.concatenate([v, v[:50] * 2])
+    A = make(gsa, "coo", 300, 200, r, c, v, cuda)
+    for opA in OPS:
+        rows_out, inner = (300, 200) if opA == "N" else (200, 300)
+        X = np.asfortranarray(rand_values(rng, (inner, 4), np.complex128))
+        C0 = np.asfortranarray(rand_values(rng, (rows_out, 4), np.complex128))
+        C = torch.from_numpy(C0).to(cuda)
+        gsa.mul_(C, wrap(gsa, A, opA), torch.from_numpy(X).to(cuda), 1 + 1j, 0.5)
+        check(oracle, "coo", opA, 300, 200, r, c, v, X, "N", C0, C, 1 + 1j, 0.5, np.complex128)
+
+
+def test_row_major_dense_operands(gsa, oracle, cuda):
+    """Row-major torch tensors for B and C work in place of column-major ones."""
+    rng = np.random.default_rng(5)
+    S = sprand(rng, 120, 90, 0.1, np.float64)
+    p0, p1, v = parts(S, "csr", np.int32)
+    A = make(gsa, "csr", 120, 90, p0, p1, v, cuda)
+    X = rng.uniform(-1, 1, (90, 7))
+    Xd = torch.from_numpy(np.ascontiguousarray(X)).to(cuda)  # row-major
+    C = torch.zeros(120, 7, dtype=torch.float64, device=cuda)  # row-major
+    gsa.mul_(C, A, Xd)
+    ye, sc = oracle.mul_exact("csr", "N", 120, 90, p0, p1, v, 1, np.asfortranarray(X), np.zeros((120, 7)))
+    assert oracle.max_rel_error(C.cpu().numpy(), ye, sc) <= 1e-12
+
+
+def test_validate(gsa, cuda):
+    rowptr = np.array([1, 3, 2, 4], np.int64)  # decreasing
+    A = make(gsa, "csr", 3, 3, rowptr, np.array([1, 2, 3]), np.array([1.0, 2.0, 3.0]), cuda)
+    with pytest.raises(gsa.ArgumentError, match="decreasing"):
+        gsa.validate(A)
+    B = make(gsa, "csr", 3, 3, np.array([1, 2, 3, 4]), np.array([1, 2, 3]), np.array([1.0, 2.0, 3.0]), cuda)
+    gsa.validate(B)

@@ -1,0 +1,139 @@
+"""The CPU oracle against the reference's known answers and against scipy.sparse (CPU only)."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from helpers import INDEX_TYPES, OPS, VALUE_TYPES, dense_parent, is_int, op_apply, parts, sprand, tol
+
+GOLDEN = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "known_answers.json")))
+
+
+@pytest.mark.parametrize("fmt", ["csr", "csc", "coo"])
+def test_docs_example_spmv(oracle, fmt):
+    """docs/src/index.md:47-58: c = A * [1,2,3] == [10, 3, 15] (exact)."""
+    g = GOLDEN["docs_spmv_3x3"]
+    key = {"csr": ("rowptr", "colval"), "csc": ("colptr", "rowval"), "coo": ("rowind", "colind")}[fmt]
+    a = g[fmt]
+    p0, p1 = np.array(a[key[0]], np.int64), np.array(a[key[1]], np.int64)
+    c = np.full(3, np.nan)
+    oracle.mul(fmt, "N", 3, 3, p0, p1, np.array(a["nzval"]), 1, np.array(g["b"]), c)
+    assert c.tolist() == g["c"]
+
+
+def test_csr_structure_pin(oracle):
+    """test/shared/matrix_csr.jl:34-58: CSR arrays of the 2x2 fixture, bit for bit."""
+    g = GOLDEN["csr_2x2_structure"]
+    coo = g["coo"]
+    ptr, idx, val = oracle.coo_to_csr(2, 2, np.array(coo["rowind"], np.int64),
+                                      np.array(coo["colind"], np.int64), np.array(coo["nzval"]))
+    assert ptr.tolist() == g["expected_csr"]["rowptr"]
+    assert idx.tolist() == g["expected_csr"]["colval"]
+    assert val.tolist() == g["expected_csr"]["nzval"]
+    csc = g["csc"]
+    r, c, v = oracle.csc_to_coo(2, 2, np.array(csc["colptr"], np.int64),
+                                np.array(csc["rowval"], np.int64), np.array(csc["nzval"]))
+    assert r.tolist() == coo["rowind"] and c.tolist() == coo["colind"] and v.tolist() == coo["nzval"]
+
+
+@pytest.mark.parametrize("name", ["single", "full_row", "full_col"])
+@pytest.mark.parametrize("it", INDEX_TYPES)
+def test_conversion_edge_cases(oracle, name, it):
+    """test/shared/conversions.jl:128-152: CSC -> COO -> CSR for the three edge matrices."""
+    g = GOLDEN[f"conversion_edge_{name}"]
+    csc = g["csc"]
+    r, c, v = oracle.csc_to_coo(3, 4, np.array(csc["colptr"], it), np.array(csc["rowval"], it),
+                                np.array(csc["nzval"]))
+    assert r.tolist() == g["coo"]["rowind"] and c.tolist() == g["coo"]["colind"]
+    ptr, idx, val = oracle.coo_to_csr(3, 4, r, c, v)
+    assert ptr.tolist() == g["expected_csr"]["rowptr"]
+    assert idx.tolist() == g["expected_csr"]["colval"]
+    assert val.tolist() == g["expected_csr"]["nzval"]
+    ptr2, idx2, val2 = oracle.coo_to_csc(3, 4, r, c, v)
+    assert ptr2.tolist() == csc["colptr"] and idx2.tolist() == csc["rowval"]
+
+
+def test_empty_conversion(oracle):
+    g = GOLDEN["empty_0x0"]
+    e = np.zeros(0, np.int64)
+    ptr, idx, val = oracle.coo_to_csr(0, 0, e, e, np.zeros(0))
+    assert ptr.tolist() == g["expected_csr"]["rowptr"] and idx.size == 0 and val.size == 0
+    ptr, _, _ = oracle.coo_to_csr(5, 3, e, e, np.zeros(0))
+    assert ptr.tolist() == [1] * 6
+
+
+@pytest.mark.parametrize("dt", VALUE_TYPES)
+@pytest.mark.parametrize("it", INDEX_TYPES)
+@pytest.mark.parametrize("fmt", ["csr", "csc", "coo"])
+def test_mul_matches_scipy(oracle, dt, it, fmt):
+    """Shared-suite shapes (test/shared/matrix_csr.jl:281-327): 100x80 at 0.1, b of 80,
+    B of 80x50, every (op(A), op(B)) pair, alpha = 2, beta = 0 and beta = 0.5."""
+    rng = np.random.default_rng(7)
+    for opA in OPS:
+        dims = (100, 80) if opA == "N" else (80, 100)
+        S = sprand(rng, *dims, 0.1, dt)
+        p0, p1, v = parts(S, fmt, it)
+        Sop = op_apply(S, opA)
+        for opB in OPS:
+            for k in (1, 50):
+                P = dense_parent(rng, 80, k, opB, dt)
+                Bop = op_apply(P, opB) if opB != "N" else P
+                C0 = dense_parent(rng, 100, k, "N", dt)
+                for alpha, beta in ((2, 0), (1, 1), (3, 2)):
+                    C = C0.copy(order="F")
+                    oracle.mul(fmt, opA, *dims, p0, p1, v, 1, P, C, alpha=alpha, beta=beta, opB=opB)
+                    ref = alpha * (Sop @ Bop) + beta * C0
+                    if is_int(dt):
+                        assert np.array_equal(C, ref.astype(dt)), (fmt, opA, opB, k)
+                    else:
+                        scale = abs(alpha) * (abs(Sop) @ abs(Bop)) + abs(beta) * abs(C0)
+                        err = np.max(np.abs(C - ref) / np.where(scale > 0, scale, 1))
+                        assert err <= 4 * tol(dt), (fmt, opA, opB, k, err)
+
+
+def test_beta_zero_ignores_nan(oracle):
+    """_rmul_or_fill!: beta == 0 overwrites C without reading it (NaN does not propagate)."""
+    rng = np.random.default_rng(3)
+    S = sprand(rng, 30, 20, 0.2, np.float64)
+    p0, p1, v = parts(S, "csr", np.int64)
+    x = rng.uniform(-1, 1, 20)
+    for fmt in ("csr", "csc", "coo"):
+        q0, q1, w = parts(S, fmt, np.int64)
+        C = np.full(30, np.nan)
+        oracle.mul(fmt, "N", 30, 20, q0, q1, w, 1, x, C, alpha=1, beta=0)
+        assert np.all(np.isfinite(C))
+        assert np.allclose(C, S @ x, rtol=0, atol=1e-13)
+
+
+def test_error_oracle_is_tighter_than_plain(oracle):
+    """The double-double oracle agrees with the plain restatement within 1e-14 relative."""
+    rng = np.random.default_rng(11)
+    S = sprand(rng, 200, 150, 0.3, np.complex128)
+    p0, p1, v = parts(S, "csr", np.int32)
+    x = rng.standard_normal(150) + 1j * rng.standard_normal(150)
+    y = np.zeros(200, np.complex128)
+    oracle.mul("csr", "N", 200, 150, p0, p1, v, 1, x, y, alpha=1 - 2j, beta=0)
+    ye, sc = oracle.mul_exact("csr", "N", 200, 150, p0, p1, v, 1, x, np.zeros(200, np.complex128),
+                              alpha=1 - 2j, beta=0)
+    assert oracle.max_rel_error(y, ye, sc) < 1e-14
+
+
+@pytest.mark.parametrize("it", INDEX_TYPES)
+def test_conversion_matches_scipy_and_keeps_duplicates(oracle, it):
+    """COO -> CSR/CSC equals scipy's sorted structure; duplicates stay, in input order."""
+    rng = np.random.default_rng(5)
+    S = sprand(rng, 100, 200, 0.05, np.float64)
+    r, c, v = parts(S, "coo", it, order="shuffle", rng=rng)
+    for colmajor, fmt in ((False, "csr"), (True, "csc")):
+        f = oracle.coo_to_csc if colmajor else oracle.coo_to_csr
+        ptr, idx, val = f(100, 200, r, c, v)
+        e0, e1, ev = parts(S, fmt, it)
+        assert np.array_equal(ptr, e0) and np.array_equal(idx, e1) and np.array_equal(val, ev)
+    # duplicates: (2,3) twice with different values, in input order
+    r = np.array([2, 1, 2, 2], it)
+    c = np.array([3, 1, 3, 1], it)
+    v = np.array([10.0, 20.0, 30.0, 40.0])
+    ptr, idx, val = oracle.coo_to_csr(3, 3, r, c, v)
+    assert ptr.tolist() == [1, 2, 5, 5] and idx.tolist() == [1, 1, 3, 3]
+    assert val.tolist() == [20.0, 40.0, 10.0, 30.0]
