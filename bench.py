@@ -201,6 +201,9 @@ class DeviceTimer:
         ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
         kb = [torch.cuda.Event(enable_timing=True) for _ in range(steps)] if kernel_events else None
         ka = [torch.cuda.Event(enable_timing=True) for _ in range(steps)] if kernel_events else None
+        if kernel_events:  # torch creates the CUDA event on first record; the library re-records it
+            for e in kb + ka:
+                e.record()
         torch.cuda.synchronize()
         for i in range(steps):
             if flush:

@@ -43,6 +43,7 @@ SIGNATURES = {
     "gsa_csc_to_coo": ([_vp, _i32, _i32, _i64, _i64, _i64, _vp, _vp, _vp, _i32, _vp, _vp, _vp],
                        _i32),
     "gsa_validate_compressed": ([_vp, _i32, _i64, _i64, _i64, _vp, _vp, _i32], _i32),
+    "gsa_check_device_status": ([_vp], _i32),
 }
 
 _lock = threading.Lock()

@@ -365,6 +365,14 @@ int gsa_csc_to_coo(void *stream, int dtype, int itype, int64_t m, int64_t n, int
                              rowind_out, colind_out, nzval_out);
 }
 
+int gsa_check_device_status(void *stream) {
+    int flag = 0;
+    int rc = read_pipe_error((cudaStream_t)stream, &flag);
+    if (rc) return rc;
+    if (flag) return fail(GSA_ERR_TIMEOUT, "a bounded device-side wait gave up (error word %d)", flag);
+    return GSA_OK;
+}
+
 int gsa_validate_compressed(void *stream, int itype, int64_t outer_n, int64_t inner_n, int64_t nnz,
                             const void *ptr, const void *idx, int base) {
     size_t is = itype_size(itype);

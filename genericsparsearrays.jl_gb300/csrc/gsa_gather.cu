@@ -291,6 +291,7 @@ static int64_t gather_num_tiles(int64_t outer_n, int64_t nnz) {
 template <typename V, typename I>
 size_t gather_workspace_size(int64_t outer_n, int64_t nnz, int64_t k, int algo) {
     if (algo == GSA_ALGO_VECTOR || outer_n == 0 || k == 0) return 0;
+    if (k == 1 && algo == GSA_ALGO_AUTO) return spmv_pipe_workspace_size<V, I>(outer_n, nnz);
     int64_t T = gather_num_tiles<V, I>(outer_n, nnz);
     Carver cv(nullptr);
     cv.take<int64_t>(T + 1);
@@ -325,6 +326,7 @@ int launch_gather(cudaStream_t s, const CompressedArgs<V, I> &a, int64_t k, Dens
         if (avg <= 16) return launch_vector_g<V, I, 16>(s, a, k, B, C);
         return launch_vector_g<V, I, 32>(s, a, k, B, C);
     }
+    if (k == 1 && algo == GSA_ALGO_AUTO) return launch_spmv_pipe<V, I>(s, a, B, C, ws, ws_bytes);
     constexpr int TILE = GatherShape<V>::TILE;
     const int64_t T = gather_num_tiles<V, I>(a.outer_n, a.nnz);
     if (ws_bytes < gather_workspace_size<V, I>(a.outer_n, a.nnz, k, algo))

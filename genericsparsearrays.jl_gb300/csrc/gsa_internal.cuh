@@ -277,6 +277,14 @@ int launch_gather(cudaStream_t s, const CompressedArgs<V, I> &a, int64_t k, Dens
 template <typename V, typename I>
 size_t gather_workspace_size(int64_t outer_n, int64_t nnz, int64_t k, int algo);
 
+// Persistent TMA-pipelined SpMV (k = 1) behind launch_gather's default algorithm.
+template <typename V, typename I>
+int launch_spmv_pipe(cudaStream_t s, const CompressedArgs<V, I> &a, DenseIn<V> B, DenseOut<V> C,
+                     void *ws, size_t ws_bytes);
+template <typename V, typename I> size_t spmv_pipe_workspace_size(int64_t outer_n, int64_t nnz);
+// Reads and clears the device error word of bounded waits (synchronizes s).
+int read_pipe_error(cudaStream_t s, int *out);
+
 // Scatter: out[idx_j, c] += conj?(val_j) * (op(B)(o, c) * alpha), after the beta pass.
 template <typename V, typename I>
 int launch_scatter(cudaStream_t s, const CompressedArgs<V, I> &a, int64_t k, DenseIn<V> B,

@@ -143,7 +143,9 @@ int launch_scatter(cudaStream_t s, const CompressedArgs<V, I> &a, int64_t k, Den
 }
 
 // ---------------------------------------------------------------------------
-// COO: each warp covers CHUNK consecutive entries in groups of 32.
+// COO: each warp takes 32 consecutive entries at a time; a segmented scan over runs of
+// equal adjacent output indices leaves each run's sum in its last lane, which adds it
+// with one atomic.  Equal indices that are not adjacent form separate runs.
 template <typename V, typename I>
 __global__ void __launch_bounds__(256)
 coo_kernel(int64_t nnz, const I *__restrict__ out_idx, const I *__restrict__ in_idx,
@@ -167,15 +169,22 @@ coo_kernel(int64_t nnz, const I *__restrict__ out_idx, const I *__restrict__ in_
                 key = -1;
             }
         }
+        // runs of equal adjacent keys: a run starts where the previous lane's key differs
+        const int64_t prev_key = __shfl_up_sync(0xffffffffu, key, 1);
         const int64_t next_key = __shfl_down_sync(0xffffffffu, key, 1);
         const bool tail = valid && (lane == 31 || next_key != key);
+        int run_start = (lane == 0 || prev_key != key) ? lane : 0;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            int o = __shfl_up_sync(0xffffffffu, run_start, off);
+            if (lane >= off && o > run_start) run_start = o;
+        }
         for (int64_t c = 0; c < k; ++c) {
             V v = valid ? mul(av, mul(B.at(in, c), C.alpha)) : VT<V>::zero();
 #pragma unroll
             for (int off = 1; off < 32; off <<= 1) {
                 V ov = shfl_up(v, off);
-                int64_t ok = __shfl_up_sync(0xffffffffu, key, off);
-                if (lane >= off && ok == key) v = add(ov, v);
+                if (lane - off >= run_start) v = add(ov, v);
             }
             if (tail) atomic_add(C.p + key + c * C.ld, v);
         }

@@ -1,0 +1,456 @@
+// Persistent, TMA-pipelined row-gather SpMV (one right-hand side):
+//   y[o] = beta*y[o] + alpha * sum_j a_j * x[idx_j]
+// over the compressed outer dimension -- the work of kernel_spmatmul_csr_N!
+// (src/matrix_csr/matrix_csr_kernels.jl:1-22) and kernel_spmatmul_csc_T!
+// (src/matrix_csc/matrix_csc_kernels.jl:24-45) for a vector x.
+//
+// Work split: the merge path of the outer end offsets and the stored entries
+// (Merrill & Garland, SC'16) is cut into tiles of TILE items (an item is one
+// stored entry or one row end), and every CTA owns one contiguous run of tiles,
+// so CTAs get equal numbers of items whatever the row-length mix.
+//
+// Per CTA:
+//   * one cooperative 256-ary search of the pointer array finds the start of
+//     its run; after that each tile's end is found from a 512-row probe of the
+//     pointer array, with no separate partition pass
+//   * the index and value streams of the NEXT tile are copied into shared
+//     memory by the bulk-copy engine (cp.async.bulk + mbarrier, 16-byte
+//     aligned interior; the <16-byte head and tail by plain loads) while the
+//     current tile is reduced, so HBM streaming overlaps the x gathers
+//   * rows are reduced by size class: a thread per row portion of <= 32
+//     entries, a warp per portion of <= 1024, the whole CTA for a longer one;
+//     every order is fixed, so results are deterministic
+//   * the partial of a row that continues into the next tile is carried in
+//     shared memory; only the open row at the end of a CTA's run goes to the
+//     fixup pass (gather_fixup_kernel), in CTA order
+// Every mbarrier wait is bounded; a wait that gives up sets the device error
+// word (read by gsa_check_device_status) and the CTA returns.
+#include "gsa_internal.cuh"
+
+namespace gsa {
+
+__device__ int g_pipe_error = 0;
+
+constexpr int PIPE_THREADS = 256;
+constexpr int PIPE_WARPS = PIPE_THREADS / 32;
+constexpr int PIPE_PROBE = 2 * PIPE_THREADS;   // rows examined per probe
+constexpr int SHORT_ROW = 32;                  // thread-per-row limit
+constexpr int WARP_ROW = 1024;                 // warp-per-row limit
+constexpr uint32_t WAIT_LIMIT = 1u << 24;      // bounded mbarrier polls
+
+template <typename V> struct PipeShape {
+    static constexpr int TILE = sizeof(V) >= 16 ? 1024 : 2048;
+};
+
+// ---- PTX helpers ----------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_addr(const void *p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void fence_mbar_init() {
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void fence_proxy_async_smem() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(done)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return done != 0;
+}
+__device__ __forceinline__ void bulk_copy_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_addr(dst)),
+        "l"(src), "r"(bytes), "r"(smem_addr(bar))
+        : "memory");
+}
+
+// One array segment [a, b) of a stream, placed so that its 16-byte-aligned
+// interior lands on 16-byte-aligned shared memory.
+struct Segment {
+    uintptr_t ga, gb;      // global byte range
+    uintptr_t lo16, hi16;  // aligned interior (valid when hi16 > lo16)
+    __device__ __forceinline__ Segment(const void *base, int64_t a, int64_t b, int esize) {
+        ga = (uintptr_t)base + (uintptr_t)(a * esize);
+        gb = (uintptr_t)base + (uintptr_t)(b * esize);
+        lo16 = (ga + 15) & ~(uintptr_t)15;
+        hi16 = gb & ~(uintptr_t)15;
+    }
+    __device__ __forceinline__ bool has_interior() const { return hi16 > lo16; }
+    __device__ __forceinline__ uint32_t interior_bytes() const {
+        return has_interior() ? (uint32_t)(hi16 - lo16) : 0u;
+    }
+    // shared-memory address of global byte g for a stage buffer at sbuf
+    __device__ __forceinline__ unsigned char *map(unsigned char *sbuf, uintptr_t g) const {
+        return sbuf + (g - (ga & ~(uintptr_t)15));
+    }
+};
+
+template <typename V, typename I> struct PipeSmem {
+    static constexpr int TILE = PipeShape<V>::TILE;
+    alignas(16) unsigned char col[2][TILE * sizeof(I) + 16];
+    alignas(16) unsigned char val[2][TILE * sizeof(V) + 16];
+    int rowend[TILE];
+    V red[PIPE_WARPS];
+    V carry[2];
+    uint64_t bar[2];
+    int nlong;
+    int longrow[TILE / (SHORT_ROW + 1) + 2];
+    static constexpr int LONG_CAP = TILE / (SHORT_ROW + 1) + 2;
+    int huge;
+    int64_t bcast;
+};
+
+// First r in [lo, hi) with end(r) + r >= D (hi if none): a 256-ary search, one
+// pointer load per thread per round.  Uniform across the CTA.
+template <typename I>
+__device__ int64_t coop_search(const I *__restrict__ ptr, int base, int64_t lo, int64_t hi, int64_t D) {
+    while (lo < hi) {
+        const int64_t step = (hi - lo + PIPE_THREADS - 1) / PIPE_THREADS;
+        const int64_t p = lo + (int64_t)threadIdx.x * step;
+        const bool f = p < hi && ((int64_t)__ldg(ptr + p + 1) - base + p < D);
+        const int c = __syncthreads_count(f);
+        const int64_t nlo = c > 0 ? lo + (int64_t)(c - 1) * step + 1 : lo;
+        int64_t nhi = lo + (int64_t)c * step;
+        hi = nhi < hi ? nhi : hi;
+        lo = nlo;
+    }
+    return lo;
+}
+
+template <typename V, typename I, bool UNIT_B>
+__device__ __forceinline__ V load_x(const CompressedArgs<V, I> &a, const DenseIn<V> &B, I col) {
+    const int64_t ci = (int64_t)col - a.base;
+    if ((uint64_t)ci >= (uint64_t)a.inner_n) return VT<V>::zero();
+    const V xv = UNIT_B ? ldg(B.p + ci) : ldg(B.p + ci * B.rs);
+    return conj_if(xv, B.conj);
+}
+
+template <typename V, typename I, bool UNIT_B>
+__global__ void __launch_bounds__(PIPE_THREADS)
+spmv_pipe_kernel(CompressedArgs<V, I> a, DenseIn<V> B, DenseOut<V> C, int64_t tiles_per_cta,
+                 int64_t *__restrict__ carry_row, V *__restrict__ carry_val) {
+    using S_t = PipeSmem<V, I>;
+    constexpr int TILE = S_t::TILE;
+    constexpr int LONG_CAP = S_t::LONG_CAP;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    S_t &S = *reinterpret_cast<S_t *>(smem_raw);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int64_t total = a.outer_n + a.nnz;
+    const int64_t D0 = (int64_t)blockIdx.x * tiles_per_cta * TILE;
+    if (D0 >= total) {
+        if (tid == 0) carry_row[blockIdx.x] = -1;
+        return;
+    }
+    const int64_t Dend = D0 + tiles_per_cta * TILE < total ? D0 + tiles_per_cta * TILE : total;
+    if (tid == 0) {
+        mbar_init(&S.bar[0], 1);
+        mbar_init(&S.bar[1], 1);
+        fence_mbar_init();
+        S.carry[0] = VT<V>::zero();
+    }
+    // start of this CTA's run on diagonal D0
+    int64_t rs = coop_search(a.ptr, a.base, D0 - a.nnz > 0 ? D0 - a.nnz : 0,
+                             D0 < a.outer_n ? D0 : a.outer_n, D0);
+    int64_t js = D0 - rs;
+
+    // issue the copies of [js, min(js + TILE, nnz)) into stage st
+    auto issue = [&](int st, int64_t j0) {
+        j0 = j0 < 0 ? 0 : (j0 > a.nnz ? a.nnz : j0);
+        const int64_t j1 = j0 + TILE < a.nnz ? j0 + TILE : a.nnz;
+        const Segment sc(a.idx, j0, j1, sizeof(I)), sv(a.val, j0, j1, sizeof(V));
+        if (tid == 0) {
+            fence_proxy_async_smem();
+            mbar_arrive_expect_tx(&S.bar[st], sc.interior_bytes() + sv.interior_bytes());
+            if (sc.has_interior())
+                bulk_copy_g2s(sc.map(S.col[st], sc.lo16), (const void *)sc.lo16, sc.interior_bytes(), &S.bar[st]);
+            if (sv.has_interior())
+                bulk_copy_g2s(sv.map(S.val[st], sv.lo16), (const void *)sv.lo16, sv.interior_bytes(), &S.bar[st]);
+        }
+        // head and tail (fewer than 16 bytes each) by plain loads
+        if (tid < 32) {
+            const bool col_side = tid < 16;
+            const Segment &sg = col_side ? sc : sv;
+            const int es = col_side ? (int)sizeof(I) : (int)sizeof(V);
+            const int k = tid & 15;  // element slot: 0..3 head, 4..7 tail (at most 3 + 3)
+            uintptr_t g = 0;
+            bool ok = false;
+            if (sg.has_interior()) {
+                if (k < 4) { g = sg.ga + (uintptr_t)k * es; ok = g < sg.lo16; }
+                else if (k < 8) { g = sg.hi16 + (uintptr_t)(k - 4) * es; ok = g < sg.gb; }
+            } else {
+                g = sg.ga + (uintptr_t)k * es;
+                ok = k < 8 && g < sg.gb;
+            }
+            if (ok) {
+                unsigned char *d = sg.map(col_side ? S.col[st] : S.val[st], g);
+                if (col_side) *reinterpret_cast<I *>(d) = ld_stream(reinterpret_cast<const I *>(g));
+                else *reinterpret_cast<V *>(d) = ld_stream(reinterpret_cast<const V *>(g));
+            }
+        }
+    };
+    // probe: end offsets of rows rs + tid and rs + 256 + tid
+    auto probe = [&](int64_t r0, int64_t &e0, int64_t &e1) {
+        const int64_t r_a = r0 + tid, r_b = r0 + PIPE_THREADS + tid;
+        e0 = r_a < a.outer_n ? (int64_t)__ldg(a.ptr + r_a + 1) - a.base : INT64_MAX / 2;
+        e1 = r_b < a.outer_n ? (int64_t)__ldg(a.ptr + r_b + 1) - a.base : INT64_MAX / 2;
+    };
+
+    int64_t pe0, pe1;
+    probe(rs, pe0, pe1);
+    issue(0, js);
+    uint32_t parity = 0u;  // bit st: phase parity of stage st
+    bool failed = false;
+    int64_t d0 = D0;
+    int64_t re = rs;
+    int it = 0;
+    for (; d0 < Dend; ++it) {
+        const int st = it & 1;
+        const int64_t d1 = d0 + TILE < Dend ? d0 + TILE : Dend;
+        // ---- end coordinate of this tile
+        const bool f0 = pe0 + (rs + tid) < d1;
+        const bool f1 = pe1 + (rs + PIPE_THREADS + tid) < d1;
+        int cnt = __syncthreads_count(f0);
+        if (cnt == PIPE_THREADS) cnt += __syncthreads_count(f1);
+        if (cnt == PIPE_PROBE) {
+            const int64_t lo = rs + PIPE_PROBE > d1 - a.nnz ? rs + PIPE_PROBE : d1 - a.nnz;
+            re = coop_search(a.ptr, a.base, lo, d1 < a.outer_n ? d1 : a.outer_n, d1);
+        } else {
+            re = rs + cnt;
+        }
+        re = re < rs ? rs : (re > a.outer_n ? a.outer_n : re);
+        const int64_t je = d1 - re;
+        // a malformed pointer array can only make a tile wrong, never out of bounds
+        int tile_rows = (int)(re - rs), tile_nnz = (int)(je - js);
+        if (tile_rows > TILE || tile_nnz < 0 || tile_nnz > TILE || js < 0 || je > a.nnz)
+            tile_rows = tile_nnz = 0;
+        // row ends of the tile, local to js
+        auto local_end = [&](int64_t end) {
+            int64_t v = end - js;
+            return (int)(v < 0 ? 0 : (v > tile_nnz ? tile_nnz : v));
+        };
+        if (tid < tile_rows) S.rowend[tid] = local_end(pe0);
+        if (PIPE_THREADS + tid < tile_rows) S.rowend[PIPE_THREADS + tid] = local_end(pe1);
+        for (int e = PIPE_PROBE + tid; e < tile_rows; e += PIPE_THREADS)
+            S.rowend[e] = local_end((int64_t)__ldg(a.ptr + rs + 1 + e) - a.base);
+        if (tid == 0) { S.nlong = 0; S.huge = -1; }
+        // ---- prefetch the next tile
+        const bool more = d1 < Dend;
+        if (more) {
+            probe(re, pe0, pe1);
+            issue(st ^ 1, je);
+        }
+        // ---- wait for this tile's streams
+        bool ok = false;
+        for (uint32_t w = 0; w < WAIT_LIMIT; ++w)
+            if ((ok = mbar_try_wait(&S.bar[st], (parity >> st) & 1u))) break;
+        if (ok) parity ^= 1u << st;
+        if (__syncthreads_or(!ok)) { failed = true; break; }
+
+        const Segment sc(a.idx, js, js, sizeof(I)), sv(a.val, js, js, sizeof(V));
+        const I *tcol = reinterpret_cast<const I *>(sc.map(S.col[st], sc.ga));
+        const V *tval = reinterpret_cast<const V *>(sv.map(S.val[st], sv.ga));
+        const V carry_in = S.carry[st];
+        const bool open_row = re < a.outer_n;
+        const int last = open_row && tile_nnz >= 0 ? tile_rows : tile_rows - 1;
+        // ---- short rows: a thread each; longer ones are queued
+        for (int e = tid; e <= last; e += PIPE_THREADS) {
+            const int b0 = e == 0 ? 0 : S.rowend[e - 1];
+            const int b1 = e < tile_rows ? S.rowend[e] : tile_nnz;
+            const int len = b1 - b0;
+            if (len > WARP_ROW) { S.huge = e; continue; }
+            if (len > SHORT_ROW) {
+                const int q = atomicAdd(&S.nlong, 1);
+                if (q < LONG_CAP) S.longrow[q] = e;
+                continue;
+            }
+            V acc = VT<V>::zero();
+            if (len <= 8) {  // all gathers of the row in flight at once
+                V av[8], xv[8];
+#pragma unroll
+                for (int u = 0; u < 8; ++u)
+                    if (u < len) {
+                        av[u] = conj_if(tval[b0 + u], a.conjA);
+                        xv[u] = load_x<V, I, UNIT_B>(a, B, tcol[b0 + u]);
+                    }
+#pragma unroll
+                for (int u = 0; u < 8; ++u)
+                    if (u < len) acc = add(acc, mul(av[u], xv[u]));
+            } else {
+#pragma unroll 4
+                for (int j = b0; j < b1; ++j)
+                    acc = add(acc, mul(conj_if(tval[j], a.conjA), load_x<V, I, UNIT_B>(a, B, tcol[j])));
+            }
+            if (e == 0) acc = add(carry_in, acc);
+            if (e < tile_rows) C.store(rs + e, 0, acc);
+            else S.carry[st ^ 1] = acc;
+        }
+        __syncthreads();
+        // ---- row portions of 33..1024 entries: a warp each
+        const int nlong = S.nlong < LONG_CAP ? S.nlong : LONG_CAP;
+        for (int q = warp; q < nlong; q += PIPE_WARPS) {
+            const int e = S.longrow[q];
+            const int b0 = e == 0 ? 0 : S.rowend[e - 1];
+            const int b1 = e < tile_rows ? S.rowend[e] : tile_nnz;
+            V acc = VT<V>::zero();
+            for (int j = b0 + lane; j < b1; j += 32)
+                acc = add(acc, mul(conj_if(tval[j], a.conjA), load_x<V, I, UNIT_B>(a, B, tcol[j])));
+#pragma unroll
+            for (int m = 16; m > 0; m >>= 1) acc = add(acc, shfl_xor(acc, m));
+            if (lane == 0) {
+                if (e == 0) acc = add(carry_in, acc);
+                if (e < tile_rows) C.store(rs + e, 0, acc);
+                else S.carry[st ^ 1] = acc;
+            }
+        }
+        // ---- one portion of more than 1024 entries: the whole CTA
+        const int huge = S.huge;
+        if (huge >= 0) {
+            const int e = huge;
+            const int b0 = e == 0 ? 0 : S.rowend[e - 1];
+            const int b1 = e < tile_rows ? S.rowend[e] : tile_nnz;
+            V acc = VT<V>::zero();
+            for (int j = b0 + tid; j < b1; j += PIPE_THREADS)
+                acc = add(acc, mul(conj_if(tval[j], a.conjA), load_x<V, I, UNIT_B>(a, B, tcol[j])));
+#pragma unroll
+            for (int m = 16; m > 0; m >>= 1) acc = add(acc, shfl_xor(acc, m));
+            if (lane == 0) S.red[warp] = acc;
+            __syncthreads();
+            if (tid == 0) {
+                V t = S.red[0];
+                for (int w = 1; w < PIPE_WARPS; ++w) t = add(t, S.red[w]);
+                if (e == 0) t = add(carry_in, t);
+                if (e < tile_rows) C.store(rs + e, 0, t);
+                else S.carry[st ^ 1] = t;
+            }
+        }
+        __syncthreads();
+        rs = re;
+        js = je;
+        d0 = d1;
+    }
+    if (failed) {
+        // let copies still in flight land before the CTA's shared memory goes away
+        if (tid == 0) {
+            atomicOr(&g_pipe_error, 1);
+            for (int st = 0; st < 2; ++st)
+                for (uint32_t w = 0; w < WAIT_LIMIT / 16; ++w)
+                    if (mbar_try_wait(&S.bar[st], (parity >> st) & 1u)) break;
+            carry_row[blockIdx.x] = -1;
+        }
+        return;
+    }
+    if (tid == 0) {
+        // the row left open at the end of the run (completed by a later CTA)
+        const bool open = re < a.outer_n;
+        carry_row[blockIdx.x] = open ? re : -1;
+        carry_val[blockIdx.x] = open ? S.carry[it & 1] : VT<V>::zero();
+    }
+}
+
+// Same as gather_fixup_kernel (k = 1): one entry per CTA, runs of CTAs carrying
+// one row summed in CTA order.
+template <typename V>
+__global__ void pipe_fixup_kernel(int64_t n, const int64_t *__restrict__ carry_row,
+                                  const V *__restrict__ carry_val, DenseOut<V> C) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const int64_t r = carry_row[t];
+    if (r < 0 || (t > 0 && carry_row[t - 1] == r)) return;
+    V sum = carry_val[t];
+    for (int64_t t2 = t + 1; t2 < n && carry_row[t2] == r; ++t2) sum = add(sum, carry_val[t2]);
+    C.accumulate(r, 0, mul(sum, C.alpha));
+}
+
+template <typename V, typename I>
+size_t spmv_pipe_workspace_size(int64_t outer_n, int64_t nnz) {
+    const int64_t T = ceil_div(outer_n + nnz, PipeShape<V>::TILE);
+    Carver cv(nullptr);
+    cv.take<int64_t>(T);
+    cv.take<V>(T);
+    return align_up(cv.off, 256);
+}
+
+template <typename V, typename I, bool UNIT_B>
+static int launch_pipe_impl(cudaStream_t s, const CompressedArgs<V, I> &a, DenseIn<V> B,
+                            DenseOut<V> C, void *ws, size_t ws_bytes) {
+    constexpr int TILE = PipeShape<V>::TILE;
+    const size_t smem = sizeof(PipeSmem<V, I>);
+    auto kern = spmv_pipe_kernel<V, I, UNIT_B>;
+    int rc = check_cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                        "spmv_pipe smem attribute");
+    if (rc) return rc;
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    rc = check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, PIPE_THREADS, smem),
+                    "spmv_pipe occupancy");
+    if (rc) return rc;
+    if (per_sm < 1) per_sm = 1;
+    const int64_t T = ceil_div(a.outer_n + a.nnz, TILE);
+    int64_t G = (int64_t)sms * per_sm;
+    if (G > T) G = T;
+    const int64_t Q = ceil_div(T, G);
+    G = ceil_div(T, Q);
+    if (ws_bytes < spmv_pipe_workspace_size<V, I>(a.outer_n, a.nnz))
+        return fail(GSA_ERR_INVALID_ARG, "spmv workspace too small");
+    Carver cv(ws);
+    int64_t *carry_row = cv.take<int64_t>(T);
+    V *carry_val = cv.take<V>(T);
+    timer_before(s);
+    kern<<<(unsigned)G, PIPE_THREADS, smem, s>>>(a, B, C, Q, carry_row, carry_val);
+    timer_after(s);
+    rc = check_cuda(cudaGetLastError(), "spmv_pipe_kernel");
+    if (rc) return rc;
+    pipe_fixup_kernel<V><<<(unsigned)ceil_div(G, 256), 256, 0, s>>>(G, carry_row, carry_val, C);
+    return check_cuda(cudaGetLastError(), "pipe_fixup_kernel");
+}
+
+template <typename V, typename I>
+int launch_spmv_pipe(cudaStream_t s, const CompressedArgs<V, I> &a, DenseIn<V> B, DenseOut<V> C,
+                     void *ws, size_t ws_bytes) {
+    if (a.outer_n == 0) return GSA_OK;
+    if (B.rs == 1) return launch_pipe_impl<V, I, true>(s, a, B, C, ws, ws_bytes);
+    return launch_pipe_impl<V, I, false>(s, a, B, C, ws, ws_bytes);
+}
+
+int read_pipe_error(cudaStream_t s, int *out) {
+    int rc = check_cuda(cudaStreamSynchronize(s), "device status sync");
+    if (rc) return rc;
+    int zero = 0;
+    rc = check_cuda(cudaMemcpyFromSymbol(out, g_pipe_error, sizeof(int)), "device status read");
+    if (rc) return rc;
+    return check_cuda(cudaMemcpyToSymbol(g_pipe_error, &zero, sizeof(int)), "device status clear");
+}
+
+#define GSA_INST_PIPE(V, I)                                                                     \
+    template int launch_spmv_pipe<V, I>(cudaStream_t, const CompressedArgs<V, I> &, DenseIn<V>, \
+                                        DenseOut<V>, void *, size_t);                           \
+    template size_t spmv_pipe_workspace_size<V, I>(int64_t, int64_t);
+GSA_INST_PIPE(float, int32_t)
+GSA_INST_PIPE(float, int64_t)
+GSA_INST_PIPE(double, int32_t)
+GSA_INST_PIPE(double, int64_t)
+GSA_INST_PIPE(cf32, int32_t)
+GSA_INST_PIPE(cf32, int64_t)
+GSA_INST_PIPE(cf64, int32_t)
+GSA_INST_PIPE(cf64, int64_t)
+GSA_INST_PIPE(int32_t, int32_t)
+GSA_INST_PIPE(int32_t, int64_t)
+GSA_INST_PIPE(int64_t, int32_t)
+GSA_INST_PIPE(int64_t, int64_t)
+
+}  // namespace gsa

@@ -1,0 +1,151 @@
+# GenericSparseArraysCUDAExt -- CUDA package extension of GenericSparseArrays.jl that sends
+# sparse x dense mul! and COO -> CSR/CSC conversion on CuArray-backed matrices to libgsa
+# (include/gsa.h).  It adds methods that are more specific than the package's generated
+# KernelAbstractions methods (src/matrix_csr/matrix_csr.jl:145-211,
+# src/matrix_csc/matrix_csc.jl:144-213, src/matrix_coo/matrix_coo.jl:155-221,
+# src/conversions/conversions.jl:171-212,282-323) for element types Float32, Float64,
+# ComplexF32, ComplexF64, Int32, Int64 and index types Int32, Int64 when A, B and C share one
+# element type; every other combination keeps the package's own methods.
+#
+# Loading: weak dependency CUDA (see the [weakdeps]/[extensions] entries in INTEGRATION.md);
+# the library path comes from ENV["GSA_LIBRARY"] or deps/libgsa.so next to the package.
+module GenericSparseArraysCUDAExt
+
+using CUDA
+using LinearAlgebra
+using GenericSparseArrays
+using GenericSparseArrays: GenericSparseMatrixCSR, GenericSparseMatrixCSC, GenericSparseMatrixCOO
+
+const libgsa = get(ENV, "GSA_LIBRARY", joinpath(@__DIR__, "..", "deps", "libgsa.so"))
+
+const GSAValue = Union{Float32, Float64, ComplexF32, ComplexF64, Int32, Int64}
+const GSAIndex = Union{Int32, Int64}
+
+gsa_dtype(::Type{Float32}) = Cint(0)
+gsa_dtype(::Type{Float64}) = Cint(1)
+gsa_dtype(::Type{ComplexF32}) = Cint(2)
+gsa_dtype(::Type{ComplexF64}) = Cint(3)
+gsa_dtype(::Type{Int32}) = Cint(4)
+gsa_dtype(::Type{Int64}) = Cint(5)
+gsa_itype(::Type{Int32}) = Cint(0)
+gsa_itype(::Type{Int64}) = Cint(1)
+
+const CSRCu{T, Ti} = GenericSparseMatrixCSR{T, Ti, <:CuVector{Ti}, <:CuVector{Ti}, <:CuVector{T}}
+const CSCCu{T, Ti} = GenericSparseMatrixCSC{T, Ti, <:CuVector{Ti}, <:CuVector{Ti}, <:CuVector{T}}
+const COOCu{T, Ti} = GenericSparseMatrixCOO{T, Ti, <:CuVector{Ti}, <:CuVector{Ti}, <:CuVector{T}}
+
+function gsa_check(status::Cint)
+    status == 0 && return nothing
+    msg = unsafe_string(ccall((:gsa_last_error_string, libgsa), Cstring, ()))
+    status == 2 && throw(DimensionMismatch(msg))
+    status in (1, 3, 6) && throw(ArgumentError(msg))
+    return error("libgsa status $status: $msg")
+end
+
+# op(A) code and parent, following trans_adj_wrappers (src/core.jl:102-113)
+_opA(A) = (A, Cint(0))
+_opA(A::Transpose) = (parent(A), Cint(1))
+_opA(A::Adjoint{<:Real}) = (parent(A), Cint(1))
+_opA(A::Adjoint) = (parent(A), Cint(2))
+
+# op(B) as (parent, ld, code): the parent is column-major, ld = stride(parent, 2)
+_ld(P::CuVector) = max(length(P), 1)
+_ld(P::CuMatrix) = max(stride(P, 2), size(P, 1), 1)
+_opB(B::CuVecOrMat) = (B, _ld(B), Cint(0))
+_opB(B::Transpose{<:Any, <:CuVecOrMat}) = (parent(B), _ld(parent(B)), Cint(1))
+_opB(B::Adjoint{<:Real, <:CuVecOrMat}) = (parent(B), _ld(parent(B)), Cint(1))
+_opB(B::Adjoint{<:Any, <:CuVecOrMat}) = (parent(B), _ld(parent(B)), Cint(2))
+
+_ptrs(A::GenericSparseMatrixCSR) = (A.rowptr, A.colval)
+_ptrs(A::GenericSparseMatrixCSC) = (A.colptr, A.rowval)
+_ptrs(A::GenericSparseMatrixCOO) = (A.rowind, A.colind)
+_entry(::GenericSparseMatrixCSR) = :gsa_csr_mul
+_entry(::GenericSparseMatrixCSC) = :gsa_csc_mul
+
+function _gsa_mul!(C::CuVecOrMat{T}, A, B, α::Number, β::Number) where {T}
+    _A, opA = _opA(A)
+    P, ldb, opB = _opB(B)
+    # checks in the order of the generated methods (src/matrix_csr/matrix_csr.jl:160-190)
+    size(A, 2) == size(B, 1) || throw(DimensionMismatch(
+        "second dimension of A, $(size(A, 2)), does not match the first dimension of B, $(size(B, 1))"))
+    size(A, 1) == size(C, 1) || throw(DimensionMismatch(
+        "first dimension of A, $(size(A, 1)), does not match the first dimension of C, $(size(C, 1))"))
+    size(B, 2) == size(C, 2) || throw(DimensionMismatch(
+        "second dimension of B, $(size(B, 2)), does not match the second dimension of C, $(size(C, 2))"))
+    promote_type(eltype(A), eltype(B), typeof(α), typeof(β)) <: T || throw(ArgumentError(
+        "element types of A, B, α, and β must be promotable to the element type of C"))
+    Ti = eltype(_ptrs(_A)[1])
+    p0, p1 = _ptrs(_A)
+    a, b = Ref{T}(T(α)), Ref{T}(T(β))
+    k = size(C, 2)
+    ldc = C isa CuVector ? max(length(C), 1) : max(stride(C, 2), size(C, 1), 1)
+    stream = CUDA.stream()
+    if _A isa GenericSparseMatrixCOO
+        st = ccall((:gsa_coo_mul, libgsa), Cint,
+            (CUstream, Cint, Cint, Int64, Int64, Int64, CuPtr{Ti}, CuPtr{Ti}, CuPtr{T}, Cint, Cint,
+             Int64, CuPtr{T}, Int64, Cint, CuPtr{T}, Int64, Ref{T}, Ref{T}),
+            stream, gsa_dtype(T), gsa_itype(Ti), _A.m, _A.n, length(_A.nzval), p0, p1, _A.nzval,
+            Cint(1), opA, k, P, ldb, opB, C, ldc, a, b)
+    else
+        # NULL workspace: libgsa takes it from the stream-ordered pool on `stream`
+        st = ccall((_entry(_A), libgsa), Cint,
+            (CUstream, Cint, Cint, Int64, Int64, Int64, CuPtr{Ti}, CuPtr{Ti}, CuPtr{T}, Cint, Cint,
+             Int64, CuPtr{T}, Int64, Cint, CuPtr{T}, Int64, Ref{T}, Ref{T}, Cint, Ptr{Cvoid}, Csize_t),
+            stream, gsa_dtype(T), gsa_itype(Ti), _A.m, _A.n, length(_A.nzval), p0, p1, _A.nzval,
+            Cint(1), opA, k, P, ldb, opB, C, ldc, a, b, Cint(0), C_NULL, Csize_t(0))
+    end
+    gsa_check(st)
+    return C  # asynchronous, like the package's kernels
+end
+
+const DenseCu{T} = Union{CuVecOrMat{T}, Transpose{T, <:CuVecOrMat{T}}, Adjoint{T, <:CuVecOrMat{T}}}
+
+for Fmt in (:CSRCu, :CSCCu, :COOCu)
+    for TA in ((Fmt), :(Transpose{T, <:$Fmt{T, Ti}}), :(Adjoint{T, <:$Fmt{T, Ti}}))
+        SA = TA == Fmt ? :($Fmt{T, Ti}) : TA
+        @eval function LinearAlgebra.mul!(C::CuVecOrMat{T}, A::$SA, B::DenseCu{T}, α::Number,
+                                          β::Number) where {T <: GSAValue, Ti <: GSAIndex}
+            return _gsa_mul!(C, A, B, α, β)
+        end
+    end
+end
+
+# COO -> CSR / CSC (src/conversions/conversions.jl:171-212, 282-323)
+for (Out, entry, colmajor) in ((:GenericSparseMatrixCSR, :gsa_coo_to_csr, 0),
+                               (:GenericSparseMatrixCSC, :gsa_coo_to_csc, 1))
+    @eval function GenericSparseArrays.$Out(A::COOCu{T, Ti}) where {T <: GSAValue, Ti <: GSAIndex}
+        m, n = size(A)
+        nz = length(A.nzval)
+        major = $colmajor == 1 ? n : m
+        ptr = CuVector{Ti}(undef, major + 1)
+        idx = CuVector{Ti}(undef, nz)
+        val = CuVector{T}(undef, nz)
+        st = ccall(($(QuoteNode(entry)), libgsa), Cint,
+            (CUstream, Cint, Cint, Int64, Int64, Int64, CuPtr{Ti}, CuPtr{Ti}, CuPtr{T}, Cint,
+             CuPtr{Ti}, CuPtr{Ti}, CuPtr{T}, Ptr{Cvoid}, Csize_t),
+            CUDA.stream(), gsa_dtype(T), gsa_itype(Ti), m, n, nz, A.rowind, A.colind, A.nzval,
+            Cint(1), ptr, idx, val, C_NULL, Csize_t(0))
+        gsa_check(st)
+        return $Out(m, n, ptr, idx, val)
+    end
+end
+
+# CSR / CSC -> COO (src/conversions/conversions.jl:153-169, 264-280)
+for (In, entry) in ((:CSRCu, :gsa_csr_to_coo), (:CSCCu, :gsa_csc_to_coo))
+    @eval function GenericSparseArrays.GenericSparseMatrixCOO(A::$In{T, Ti}) where {T <: GSAValue, Ti <: GSAIndex}
+        m, n = size(A)
+        nz = length(A.nzval)
+        p0, p1 = _ptrs(A)
+        r = CuVector{Ti}(undef, nz)
+        c = CuVector{Ti}(undef, nz)
+        v = CuVector{T}(undef, nz)
+        st = ccall(($(QuoteNode(entry)), libgsa), Cint,
+            (CUstream, Cint, Cint, Int64, Int64, Int64, CuPtr{Ti}, CuPtr{Ti}, CuPtr{T}, Cint,
+             CuPtr{Ti}, CuPtr{Ti}, CuPtr{T}),
+            CUDA.stream(), gsa_dtype(T), gsa_itype(Ti), m, n, nz, p0, p1, A.nzval, Cint(1), r, c, v)
+        gsa_check(st)
+        return GenericSparseMatrixCOO(m, n, r, c, v)
+    end
+end
+
+end # module

@@ -60,8 +60,9 @@ typedef enum { GSA_OP_N = 0, GSA_OP_T = 1, GSA_OP_C = 2 } gsa_op;
 
 /* Gather kernel selection for the row-gather paths (CSR N, CSC T). */
 typedef enum {
-    GSA_ALGO_AUTO = 0,     /* library choice */
-    GSA_ALGO_MERGE = 1,    /* nnz-balanced merge-path tiles (any row-length mix) */
+    GSA_ALGO_AUTO = 0,     /* library choice: for one right-hand side the persistent
+                              bulk-copy pipelined merge-path kernel */
+    GSA_ALGO_MERGE = 1,    /* one CTA per merge-path tile (any row-length mix) */
     GSA_ALGO_VECTOR = 2    /* a group of threads per row (short, even rows) */
 } gsa_algo;
 
@@ -153,6 +154,12 @@ int gsa_csr_to_coo(void *stream, int dtype, int itype, int64_t m, int64_t n, int
 int gsa_csc_to_coo(void *stream, int dtype, int itype, int64_t m, int64_t n, int64_t nnz,
                    const void *colptr, const void *rowval, const void *nzval, int base,
                    void *rowind_out, void *colind_out, void *nzval_out);
+
+/* Synchronizes the stream, then reads and clears the device error word that
+ * bounded device-side waits set when they give up (no counterpart in the
+ * reference).  GSA_OK, or GSA_ERR_TIMEOUT if any wait gave up since the last
+ * check; the results of the call that timed out are not valid. */
+int gsa_check_device_status(void *stream);
 
 /* ---- structure check ------------------------------------------------------
  * The reference constructors skip the structural check

@@ -32,3 +32,20 @@ def cuda():
     if not torch.cuda.is_available():
         pytest.fail("a test marked gpu ran without a CUDA device")
     return torch.device("cuda:0")
+
+
+@pytest.fixture(autouse=True)
+def _device_status_after_gpu_tests(request):
+    """After every gpu test: no bounded device-side wait gave up (gsa_check_device_status)."""
+    yield
+    if request.node.get_closest_marker("gpu") is None:
+        return
+    import torch
+    if not torch.cuda.is_available():
+        return
+    import __graft_entry__
+    gsa = __graft_entry__.load_package()
+    lib = gsa._lib.load()
+    import ctypes
+    st = lib.gsa_check_device_status(ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+    assert st == 0, f"device status {st}: {gsa._lib.last_error()}"

@@ -32,7 +32,7 @@ def test_laplacian_spmv_csr_csc(gsa, oracle, cuda, wl, it, dt):
     tol = 1e-12 if dt == np.float64 else 1e-5
     A = gsa.adapt(cuda, gsa.GenericSparseMatrixCSR(m, n, rp, cv, nz))
     xd = torch.from_numpy(x).to(cuda)
-    for algo in (gsa.ALGO_MERGE, gsa.ALGO_VECTOR):
+    for algo in (gsa.ALGO_AUTO, gsa.ALGO_MERGE, gsa.ALGO_VECTOR):
         y = torch.empty(m, dtype=xd.dtype, device=cuda)
         gsa.mul_(y, A, xd, algo=algo)
         assert rel_err_vs(y.cpu().numpy(), ref, scale) <= tol

@@ -151,7 +151,7 @@ def test_long_rows_cross_tiles(gsa, oracle, cuda, dt, k):
     rowptr = np.concatenate([[0], np.cumsum(lengths)]).astype(np.int64) + 1
     cols = np.concatenate([np.sort(rng.choice(n, size=l, replace=False)) for l in lengths]).astype(np.int64) + 1
     vals = rand_values(rng, cols.size, dt)
-    for algo in (1, 2):
+    for algo in (0, 1, 2):
         for fmt in ("csr", "csc_t"):
             if fmt == "csr":
                 A = make(gsa, "csr", m, n, rowptr, cols, vals, cuda)
@@ -218,3 +218,25 @@ def test_validate(gsa, cuda):
         gsa.validate(A)
     B = make(gsa, "csr", 3, 3, np.array([1, 2, 3, 4]), np.array([1, 2, 3]), np.array([1.0, 2.0, 3.0]), cuda)
     gsa.validate(B)
+
+
+@pytest.mark.parametrize("dt", [np.float64, np.complex64, np.int32])
+def test_sparse_rows_span_many_tiles(gsa, oracle, cuda, dt):
+    """Mostly empty rows: one merge-path tile spans thousands of rows, beyond the 512-row
+    probe, so tile ends come from the pointer search; beta keeps the empty rows' scaling."""
+    rng = np.random.default_rng(44)
+    m, n = 200_000, 3_000
+    lengths = np.zeros(m, np.int64)
+    hot = rng.choice(m, 700, replace=False)
+    lengths[hot] = rng.integers(1, 40, 700)
+    lengths[m // 2] = 2_500  # one long row among them
+    rowptr = np.concatenate([[0], np.cumsum(lengths)]).astype(np.int32) + 1
+    cols = np.concatenate([np.sort(rng.choice(n, size=int(l), replace=False)) for l in lengths]).astype(np.int32) + 1
+    vals = rand_values(rng, cols.size, dt)
+    A = make(gsa, "csr", m, n, rowptr, cols, vals, cuda)
+    x = rand_values(rng, n, dt)
+    C0 = rand_values(rng, m, dt)
+    for algo in (0, 1, 2):
+        C = torch.from_numpy(C0.copy()).to(cuda)
+        gsa.mul_(C, A, torch.from_numpy(x).to(cuda), 2, 3, algo=algo)
+        check(oracle, "csr", "N", m, n, rowptr, cols, vals, x, "N", C0, C, 2, 3, dt)
