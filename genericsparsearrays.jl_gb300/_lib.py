@@ -20,6 +20,7 @@ IDX32, IDX64 = 0, 1
 # op codes (gsa_op) and algorithms (gsa_algo)
 OP_N, OP_T, OP_C = 0, 1, 2
 ALGO_AUTO, ALGO_MERGE, ALGO_VECTOR = 0, 1, 2
+TUNE_PIPE_THREADS = 1
 
 # Every exported symbol of include/gsa.h with its ctypes signature.
 _i32, _i64, _vp, _sz = ctypes.c_int, ctypes.c_int64, ctypes.c_void_p, ctypes.c_size_t
@@ -29,6 +30,8 @@ SIGNATURES = {
     "gsa_version": ([], _i32),
     "gsa_last_error_string": ([], ctypes.c_char_p),
     "gsa_set_kernel_timer": ([_vp, _vp], None),
+    "gsa_set_tuning": ([_i32, _i32], _i32),
+    "gsa_get_tuning": ([_i32], _i32),
     "gsa_csr_mul": (_MUL + [_i32, _vp, _sz], _i32),
     "gsa_csc_mul": (_MUL + [_i32, _vp, _sz], _i32),
     "gsa_coo_mul": (_MUL, _i32),

@@ -365,6 +365,20 @@ int gsa_csc_to_coo(void *stream, int dtype, int itype, int64_t m, int64_t n, int
                              rowind_out, colind_out, nzval_out);
 }
 
+int gsa_set_tuning(int key, int value) {
+    if (key == GSA_TUNE_PIPE_THREADS) {
+        if (value != 256 && value != 512) return fail(GSA_ERR_INVALID_ARG, "threads must be 256 or 512");
+        set_pipe_threads(value);
+        return GSA_OK;
+    }
+    return fail(GSA_ERR_INVALID_ARG, "unknown tuning key %d", key);
+}
+
+int gsa_get_tuning(int key) {
+    if (key == GSA_TUNE_PIPE_THREADS) return get_pipe_threads();
+    return -1;
+}
+
 int gsa_check_device_status(void *stream) {
     int flag = 0;
     int rc = read_pipe_error((cudaStream_t)stream, &flag);

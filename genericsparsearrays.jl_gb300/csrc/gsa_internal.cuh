@@ -284,6 +284,8 @@ int launch_spmv_pipe(cudaStream_t s, const CompressedArgs<V, I> &a, DenseIn<V> B
 template <typename V, typename I> size_t spmv_pipe_workspace_size(int64_t outer_n, int64_t nnz);
 // Reads and clears the device error word of bounded waits (synchronizes s).
 int read_pipe_error(cudaStream_t s, int *out);
+void set_pipe_threads(int t);
+int get_pipe_threads();
 
 // Scatter: out[idx_j, c] += conj?(val_j) * (op(B)(o, c) * alpha), after the beta pass.
 template <typename V, typename I>

@@ -1,4 +1,4 @@
-// Persistent, TMA-pipelined row-gather SpMV (one right-hand side):
+// Persistent, bulk-copy-pipelined row-gather SpMV (one right-hand side):
 //   y[o] = beta*y[o] + alpha * sum_j a_j * x[idx_j]
 // over the compressed outer dimension -- the work of kernel_spmatmul_csr_N!
 // (src/matrix_csr/matrix_csr_kernels.jl:1-22) and kernel_spmatmul_csc_T!
@@ -10,19 +10,22 @@
 // so CTAs get equal numbers of items whatever the row-length mix.
 //
 // Per CTA:
-//   * one cooperative 256-ary search of the pointer array finds the start of
-//     its run; after that each tile's end is found from a 512-row probe of the
-//     pointer array, with no separate partition pass
+//   * one cooperative search of the pointer array (THREADS-ary) finds the start
+//     of its run; after that each tile's end comes from a 2*THREADS-row probe of
+//     the pointer array, with no separate partition pass
 //   * the index and value streams of the NEXT tile are copied into shared
-//     memory by the bulk-copy engine (cp.async.bulk + mbarrier, 16-byte
-//     aligned interior; the <16-byte head and tail by plain loads) while the
-//     current tile is reduced, so HBM streaming overlaps the x gathers
-//   * rows are reduced by size class: a thread per row portion of <= 32
-//     entries, a warp per portion of <= 1024, the whole CTA for a longer one;
-//     every order is fixed, so results are deterministic
+//     memory by the bulk-copy engine (cp.async.bulk + mbarrier, 16-byte aligned
+//     interior; the <16-byte head and tail by plain loads) while the current
+//     tile is reduced, so HBM streaming overlaps the x gathers
+//   * phase 1 (balanced over entries): every thread forms the products
+//     a_j * x[idx_j] of TILE/THREADS entries, all gathers in flight together,
+//     and writes them over the staged values
+//   * phase 2 (over rows): a thread sums a row portion of <= 32 products, a
+//     warp one of <= 1024, the whole CTA a longer one; every order is fixed, so
+//     results are deterministic
 //   * the partial of a row that continues into the next tile is carried in
 //     shared memory; only the open row at the end of a CTA's run goes to the
-//     fixup pass (gather_fixup_kernel), in CTA order
+//     fixup pass, in CTA order (no atomics)
 // Every mbarrier wait is bounded; a wait that gives up sets the device error
 // word (read by gsa_check_device_status) and the CTA returns.
 #include "gsa_internal.cuh"
@@ -31,12 +34,9 @@ namespace gsa {
 
 __device__ int g_pipe_error = 0;
 
-constexpr int PIPE_THREADS = 256;
-constexpr int PIPE_WARPS = PIPE_THREADS / 32;
-constexpr int PIPE_PROBE = 2 * PIPE_THREADS;   // rows examined per probe
-constexpr int SHORT_ROW = 32;                  // thread-per-row limit
-constexpr int WARP_ROW = 1024;                 // warp-per-row limit
-constexpr uint32_t WAIT_LIMIT = 1u << 24;      // bounded mbarrier polls
+constexpr int SHORT_ROW = 32;               // thread-per-row limit
+constexpr int WARP_ROW = 1024;              // warp-per-row limit
+constexpr uint32_t WAIT_LIMIT = 1u << 24;   // bounded mbarrier polls
 
 template <typename V> struct PipeShape {
     static constexpr int TILE = sizeof(V) >= 16 ? 1024 : 2048;
@@ -99,53 +99,63 @@ struct Segment {
     }
 };
 
-template <typename V, typename I> struct PipeSmem {
+template <typename V, typename I, int THREADS> struct PipeSmem {
     static constexpr int TILE = PipeShape<V>::TILE;
+    static constexpr int WARPS = THREADS / 32;
+    static constexpr int LONG_CAP = TILE / (SHORT_ROW + 1) + 2;
     alignas(16) unsigned char col[2][TILE * sizeof(I) + 16];
     alignas(16) unsigned char val[2][TILE * sizeof(V) + 16];
     int rowend[TILE];
-    V red[PIPE_WARPS];
+    V red[WARPS];
     V carry[2];
     uint64_t bar[2];
     int nlong;
-    int longrow[TILE / (SHORT_ROW + 1) + 2];
-    static constexpr int LONG_CAP = TILE / (SHORT_ROW + 1) + 2;
     int huge;
-    int64_t bcast;
+    int longrow[LONG_CAP];
 };
 
-// First r in [lo, hi) with end(r) + r >= D (hi if none): a 256-ary search, one
-// pointer load per thread per round.  Uniform across the CTA.
-template <typename I>
+// First r in [lo, hi) with end(r) + r >= D (hi if none): a THREADS-ary search,
+// one pointer load per thread per round.  Uniform across the CTA.
+template <typename I, int THREADS>
 __device__ int64_t coop_search(const I *__restrict__ ptr, int base, int64_t lo, int64_t hi, int64_t D) {
     while (lo < hi) {
-        const int64_t step = (hi - lo + PIPE_THREADS - 1) / PIPE_THREADS;
+        const int64_t step = (hi - lo + THREADS - 1) / THREADS;
         const int64_t p = lo + (int64_t)threadIdx.x * step;
         const bool f = p < hi && ((int64_t)__ldg(ptr + p + 1) - base + p < D);
         const int c = __syncthreads_count(f);
         const int64_t nlo = c > 0 ? lo + (int64_t)(c - 1) * step + 1 : lo;
-        int64_t nhi = lo + (int64_t)c * step;
+        const int64_t nhi = lo + (int64_t)c * step;
         hi = nhi < hi ? nhi : hi;
         lo = nlo;
     }
     return lo;
 }
 
-template <typename V, typename I, bool UNIT_B>
+// x[col] (conjugated if op(B) is an adjoint); indices outside [0, inner_n) read nothing.
+template <typename V, typename I>
 __device__ __forceinline__ V load_x(const CompressedArgs<V, I> &a, const DenseIn<V> &B, I col) {
+    if (sizeof(I) == 4) {  // Int32 indices: inner_n < 2^31, 32-bit index math
+        const int ci = (int)col - a.base;
+        if ((unsigned)ci >= (unsigned)a.inner_n) return VT<V>::zero();
+        return conj_if(ldg(B.p + (int64_t)ci * B.rs), B.conj);
+    }
     const int64_t ci = (int64_t)col - a.base;
     if ((uint64_t)ci >= (uint64_t)a.inner_n) return VT<V>::zero();
-    const V xv = UNIT_B ? ldg(B.p + ci) : ldg(B.p + ci * B.rs);
-    return conj_if(xv, B.conj);
+    return conj_if(ldg(B.p + ci * B.rs), B.conj);
 }
 
-template <typename V, typename I, bool UNIT_B>
-__global__ void __launch_bounds__(PIPE_THREADS)
+// Resident CTAs per SM the register cap is sized for: three 256-thread CTAs
+// (their shared memory fits three times), or two 512-thread CTAs.
+template <typename V, typename I, int THREADS>
+__global__ void __launch_bounds__(THREADS, THREADS >= 512 ? 2 : 3)
 spmv_pipe_kernel(CompressedArgs<V, I> a, DenseIn<V> B, DenseOut<V> C, int64_t tiles_per_cta,
                  int64_t *__restrict__ carry_row, V *__restrict__ carry_val) {
-    using S_t = PipeSmem<V, I>;
+    using S_t = PipeSmem<V, I, THREADS>;
     constexpr int TILE = S_t::TILE;
+    constexpr int WARPS = S_t::WARPS;
     constexpr int LONG_CAP = S_t::LONG_CAP;
+    constexpr int PROBE = 2 * THREADS;
+    constexpr int U = TILE / THREADS;  // entries per thread in phase 1
     extern __shared__ __align__(16) unsigned char smem_raw[];
     S_t &S = *reinterpret_cast<S_t *>(smem_raw);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -163,11 +173,11 @@ spmv_pipe_kernel(CompressedArgs<V, I> a, DenseIn<V> B, DenseOut<V> C, int64_t ti
         S.carry[0] = VT<V>::zero();
     }
     // start of this CTA's run on diagonal D0
-    int64_t rs = coop_search(a.ptr, a.base, D0 - a.nnz > 0 ? D0 - a.nnz : 0,
-                             D0 < a.outer_n ? D0 : a.outer_n, D0);
+    int64_t rs = coop_search<I, THREADS>(a.ptr, a.base, D0 - a.nnz > 0 ? D0 - a.nnz : 0,
+                                         D0 < a.outer_n ? D0 : a.outer_n, D0);
     int64_t js = D0 - rs;
 
-    // issue the copies of [js, min(js + TILE, nnz)) into stage st
+    // copies of [j0, min(j0 + TILE, nnz)) into stage st
     auto issue = [&](int st, int64_t j0) {
         j0 = j0 < 0 ? 0 : (j0 > a.nnz ? a.nnz : j0);
         const int64_t j1 = j0 + TILE < a.nnz ? j0 + TILE : a.nnz;
@@ -179,13 +189,12 @@ spmv_pipe_kernel(CompressedArgs<V, I> a, DenseIn<V> B, DenseOut<V> C, int64_t ti
                 bulk_copy_g2s(sc.map(S.col[st], sc.lo16), (const void *)sc.lo16, sc.interior_bytes(), &S.bar[st]);
             if (sv.has_interior())
                 bulk_copy_g2s(sv.map(S.val[st], sv.lo16), (const void *)sv.lo16, sv.interior_bytes(), &S.bar[st]);
-        }
-        // head and tail (fewer than 16 bytes each) by plain loads
-        if (tid < 32) {
-            const bool col_side = tid < 16;
+        } else if (tid >= 32 && tid < 64) {
+            // head and tail (fewer than 16 bytes each) by plain loads
+            const bool col_side = tid < 48;
             const Segment &sg = col_side ? sc : sv;
             const int es = col_side ? (int)sizeof(I) : (int)sizeof(V);
-            const int k = tid & 15;  // element slot: 0..3 head, 4..7 tail (at most 3 + 3)
+            const int k = tid & 15;  // element slot: 0..3 head, 4..7 tail
             uintptr_t g = 0;
             bool ok = false;
             if (sg.has_interior()) {
@@ -202,15 +211,16 @@ spmv_pipe_kernel(CompressedArgs<V, I> a, DenseIn<V> B, DenseOut<V> C, int64_t ti
             }
         }
     };
-    // probe: end offsets of rows rs + tid and rs + 256 + tid
-    auto probe = [&](int64_t r0, int64_t &e0, int64_t &e1) {
-        const int64_t r_a = r0 + tid, r_b = r0 + PIPE_THREADS + tid;
-        e0 = r_a < a.outer_n ? (int64_t)__ldg(a.ptr + r_a + 1) - a.base : INT64_MAX / 2;
-        e1 = r_b < a.outer_n ? (int64_t)__ldg(a.ptr + r_b + 1) - a.base : INT64_MAX / 2;
+
+    // probe: end offsets of rows r0 + tid and r0 + THREADS + tid
+    int64_t pe0, pe1;
+    auto probe = [&](int64_t r0) {
+        const int64_t r_a = r0 + tid, r_b = r0 + THREADS + tid;
+        pe0 = r_a < a.outer_n ? (int64_t)__ldg(a.ptr + r_a + 1) - a.base : INT64_MAX / 2;
+        pe1 = r_b < a.outer_n ? (int64_t)__ldg(a.ptr + r_b + 1) - a.base : INT64_MAX / 2;
     };
 
-    int64_t pe0, pe1;
-    probe(rs, pe0, pe1);
+    probe(rs);
     issue(0, js);
     uint32_t parity = 0u;  // bit st: phase parity of stage st
     bool failed = false;
@@ -222,12 +232,12 @@ spmv_pipe_kernel(CompressedArgs<V, I> a, DenseIn<V> B, DenseOut<V> C, int64_t ti
         const int64_t d1 = d0 + TILE < Dend ? d0 + TILE : Dend;
         // ---- end coordinate of this tile
         const bool f0 = pe0 + (rs + tid) < d1;
-        const bool f1 = pe1 + (rs + PIPE_THREADS + tid) < d1;
+        const bool f1 = pe1 + (rs + THREADS + tid) < d1;
         int cnt = __syncthreads_count(f0);
-        if (cnt == PIPE_THREADS) cnt += __syncthreads_count(f1);
-        if (cnt == PIPE_PROBE) {
-            const int64_t lo = rs + PIPE_PROBE > d1 - a.nnz ? rs + PIPE_PROBE : d1 - a.nnz;
-            re = coop_search(a.ptr, a.base, lo, d1 < a.outer_n ? d1 : a.outer_n, d1);
+        if (cnt == THREADS) cnt += __syncthreads_count(f1);
+        if (cnt == PROBE) {
+            const int64_t lo = rs + PROBE > d1 - a.nnz ? rs + PROBE : d1 - a.nnz;
+            re = coop_search<I, THREADS>(a.ptr, a.base, lo, d1 < a.outer_n ? d1 : a.outer_n, d1);
         } else {
             re = rs + cnt;
         }
@@ -237,20 +247,18 @@ spmv_pipe_kernel(CompressedArgs<V, I> a, DenseIn<V> B, DenseOut<V> C, int64_t ti
         int tile_rows = (int)(re - rs), tile_nnz = (int)(je - js);
         if (tile_rows > TILE || tile_nnz < 0 || tile_nnz > TILE || js < 0 || je > a.nnz)
             tile_rows = tile_nnz = 0;
-        // row ends of the tile, local to js
         auto local_end = [&](int64_t end) {
-            int64_t v = end - js;
+            const int64_t v = end - js;
             return (int)(v < 0 ? 0 : (v > tile_nnz ? tile_nnz : v));
         };
         if (tid < tile_rows) S.rowend[tid] = local_end(pe0);
-        if (PIPE_THREADS + tid < tile_rows) S.rowend[PIPE_THREADS + tid] = local_end(pe1);
-        for (int e = PIPE_PROBE + tid; e < tile_rows; e += PIPE_THREADS)
+        if (THREADS + tid < tile_rows) S.rowend[THREADS + tid] = local_end(pe1);
+        for (int e = PROBE + tid; e < tile_rows; e += THREADS)
             S.rowend[e] = local_end((int64_t)__ldg(a.ptr + rs + 1 + e) - a.base);
         if (tid == 0) { S.nlong = 0; S.huge = -1; }
         // ---- prefetch the next tile
-        const bool more = d1 < Dend;
-        if (more) {
-            probe(re, pe0, pe1);
+        if (d1 < Dend) {
+            probe(re);
             issue(st ^ 1, je);
         }
         // ---- wait for this tile's streams
@@ -262,12 +270,32 @@ spmv_pipe_kernel(CompressedArgs<V, I> a, DenseIn<V> B, DenseOut<V> C, int64_t ti
 
         const Segment sc(a.idx, js, js, sizeof(I)), sv(a.val, js, js, sizeof(V));
         const I *tcol = reinterpret_cast<const I *>(sc.map(S.col[st], sc.ga));
-        const V *tval = reinterpret_cast<const V *>(sv.map(S.val[st], sv.ga));
+        V *tv = reinterpret_cast<V *>(sv.map(S.val[st], sv.ga));
+
+        // ---- phase 1: products of all entries, gathers in flight together
+        {
+            I cj[U];
+            V av[U], xv[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const int e = tid + u * THREADS;
+                if (e < tile_nnz) { cj[u] = tcol[e]; av[u] = tv[e]; }
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u)
+                if (tid + u * THREADS < tile_nnz) xv[u] = load_x<V, I>(a, B, cj[u]);
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const int e = tid + u * THREADS;
+                if (e < tile_nnz) tv[e] = mul(conj_if(av[u], a.conjA), xv[u]);
+            }
+        }
+        __syncthreads();
+
+        // ---- phase 2: row sums over the products
         const V carry_in = S.carry[st];
-        const bool open_row = re < a.outer_n;
-        const int last = open_row && tile_nnz >= 0 ? tile_rows : tile_rows - 1;
-        // ---- short rows: a thread each; longer ones are queued
-        for (int e = tid; e <= last; e += PIPE_THREADS) {
+        const int last = re < a.outer_n ? tile_rows : tile_rows - 1;  // the open row too
+        for (int e = tid; e <= last; e += THREADS) {
             const int b0 = e == 0 ? 0 : S.rowend[e - 1];
             const int b1 = e < tile_rows ? S.rowend[e] : tile_nnz;
             const int len = b1 - b0;
@@ -278,36 +306,20 @@ spmv_pipe_kernel(CompressedArgs<V, I> a, DenseIn<V> B, DenseOut<V> C, int64_t ti
                 continue;
             }
             V acc = VT<V>::zero();
-            if (len <= 8) {  // all gathers of the row in flight at once
-                V av[8], xv[8];
-#pragma unroll
-                for (int u = 0; u < 8; ++u)
-                    if (u < len) {
-                        av[u] = conj_if(tval[b0 + u], a.conjA);
-                        xv[u] = load_x<V, I, UNIT_B>(a, B, tcol[b0 + u]);
-                    }
-#pragma unroll
-                for (int u = 0; u < 8; ++u)
-                    if (u < len) acc = add(acc, mul(av[u], xv[u]));
-            } else {
-#pragma unroll 4
-                for (int j = b0; j < b1; ++j)
-                    acc = add(acc, mul(conj_if(tval[j], a.conjA), load_x<V, I, UNIT_B>(a, B, tcol[j])));
-            }
+            for (int j = b0; j < b1; ++j) acc = add(acc, tv[j]);
             if (e == 0) acc = add(carry_in, acc);
             if (e < tile_rows) C.store(rs + e, 0, acc);
             else S.carry[st ^ 1] = acc;
         }
         __syncthreads();
-        // ---- row portions of 33..1024 entries: a warp each
+        // portions of 33..1024 entries: a warp each
         const int nlong = S.nlong < LONG_CAP ? S.nlong : LONG_CAP;
-        for (int q = warp; q < nlong; q += PIPE_WARPS) {
+        for (int q = warp; q < nlong; q += WARPS) {
             const int e = S.longrow[q];
             const int b0 = e == 0 ? 0 : S.rowend[e - 1];
             const int b1 = e < tile_rows ? S.rowend[e] : tile_nnz;
             V acc = VT<V>::zero();
-            for (int j = b0 + lane; j < b1; j += 32)
-                acc = add(acc, mul(conj_if(tval[j], a.conjA), load_x<V, I, UNIT_B>(a, B, tcol[j])));
+            for (int j = b0 + lane; j < b1; j += 32) acc = add(acc, tv[j]);
 #pragma unroll
             for (int m = 16; m > 0; m >>= 1) acc = add(acc, shfl_xor(acc, m));
             if (lane == 0) {
@@ -316,22 +328,21 @@ spmv_pipe_kernel(CompressedArgs<V, I> a, DenseIn<V> B, DenseOut<V> C, int64_t ti
                 else S.carry[st ^ 1] = acc;
             }
         }
-        // ---- one portion of more than 1024 entries: the whole CTA
+        // one portion of more than 1024 entries: the whole CTA
         const int huge = S.huge;
         if (huge >= 0) {
             const int e = huge;
             const int b0 = e == 0 ? 0 : S.rowend[e - 1];
             const int b1 = e < tile_rows ? S.rowend[e] : tile_nnz;
             V acc = VT<V>::zero();
-            for (int j = b0 + tid; j < b1; j += PIPE_THREADS)
-                acc = add(acc, mul(conj_if(tval[j], a.conjA), load_x<V, I, UNIT_B>(a, B, tcol[j])));
+            for (int j = b0 + tid; j < b1; j += THREADS) acc = add(acc, tv[j]);
 #pragma unroll
             for (int m = 16; m > 0; m >>= 1) acc = add(acc, shfl_xor(acc, m));
             if (lane == 0) S.red[warp] = acc;
             __syncthreads();
             if (tid == 0) {
                 V t = S.red[0];
-                for (int w = 1; w < PIPE_WARPS; ++w) t = add(t, S.red[w]);
+                for (int w = 1; w < WARPS; ++w) t = add(t, S.red[w]);
                 if (e == 0) t = add(carry_in, t);
                 if (e < tile_rows) C.store(rs + e, 0, t);
                 else S.carry[st ^ 1] = t;
@@ -361,8 +372,7 @@ spmv_pipe_kernel(CompressedArgs<V, I> a, DenseIn<V> B, DenseOut<V> C, int64_t ti
     }
 }
 
-// Same as gather_fixup_kernel (k = 1): one entry per CTA, runs of CTAs carrying
-// one row summed in CTA order.
+// One entry per CTA; runs of CTAs carrying one row are summed in CTA order.
 template <typename V>
 __global__ void pipe_fixup_kernel(int64_t n, const int64_t *__restrict__ carry_row,
                                   const V *__restrict__ carry_val, DenseOut<V> C) {
@@ -375,6 +385,11 @@ __global__ void pipe_fixup_kernel(int64_t n, const int64_t *__restrict__ carry_r
     C.accumulate(r, 0, mul(sum, C.alpha));
 }
 
+// Threads per CTA of the pipelined kernel (256 or 512); settable for tuning.
+static int g_pipe_threads = 512;
+void set_pipe_threads(int t) { g_pipe_threads = (t == 256) ? 256 : 512; }
+int get_pipe_threads() { return g_pipe_threads; }
+
 template <typename V, typename I>
 size_t spmv_pipe_workspace_size(int64_t outer_n, int64_t nnz) {
     const int64_t T = ceil_div(outer_n + nnz, PipeShape<V>::TILE);
@@ -384,19 +399,19 @@ size_t spmv_pipe_workspace_size(int64_t outer_n, int64_t nnz) {
     return align_up(cv.off, 256);
 }
 
-template <typename V, typename I, bool UNIT_B>
+template <typename V, typename I, int THREADS>
 static int launch_pipe_impl(cudaStream_t s, const CompressedArgs<V, I> &a, DenseIn<V> B,
                             DenseOut<V> C, void *ws, size_t ws_bytes) {
     constexpr int TILE = PipeShape<V>::TILE;
-    const size_t smem = sizeof(PipeSmem<V, I>);
-    auto kern = spmv_pipe_kernel<V, I, UNIT_B>;
+    const size_t smem = sizeof(PipeSmem<V, I, THREADS>);
+    auto kern = spmv_pipe_kernel<V, I, THREADS>;
     int rc = check_cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                         "spmv_pipe smem attribute");
     if (rc) return rc;
     int dev = 0, sms = 0, per_sm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    rc = check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, PIPE_THREADS, smem),
+    rc = check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, THREADS, smem),
                     "spmv_pipe occupancy");
     if (rc) return rc;
     if (per_sm < 1) per_sm = 1;
@@ -411,7 +426,7 @@ static int launch_pipe_impl(cudaStream_t s, const CompressedArgs<V, I> &a, Dense
     int64_t *carry_row = cv.take<int64_t>(T);
     V *carry_val = cv.take<V>(T);
     timer_before(s);
-    kern<<<(unsigned)G, PIPE_THREADS, smem, s>>>(a, B, C, Q, carry_row, carry_val);
+    kern<<<(unsigned)G, THREADS, smem, s>>>(a, B, C, Q, carry_row, carry_val);
     timer_after(s);
     rc = check_cuda(cudaGetLastError(), "spmv_pipe_kernel");
     if (rc) return rc;
@@ -423,8 +438,8 @@ template <typename V, typename I>
 int launch_spmv_pipe(cudaStream_t s, const CompressedArgs<V, I> &a, DenseIn<V> B, DenseOut<V> C,
                      void *ws, size_t ws_bytes) {
     if (a.outer_n == 0) return GSA_OK;
-    if (B.rs == 1) return launch_pipe_impl<V, I, true>(s, a, B, C, ws, ws_bytes);
-    return launch_pipe_impl<V, I, false>(s, a, B, C, ws, ws_bytes);
+    if (g_pipe_threads == 256) return launch_pipe_impl<V, I, 256>(s, a, B, C, ws, ws_bytes);
+    return launch_pipe_impl<V, I, 512>(s, a, B, C, ws, ws_bytes);
 }
 
 int read_pipe_error(cudaStream_t s, int *out) {

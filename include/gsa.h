@@ -66,6 +66,11 @@ typedef enum {
     GSA_ALGO_VECTOR = 2    /* a group of threads per row (short, even rows) */
 } gsa_algo;
 
+/* Tuning keys for gsa_set_tuning / gsa_get_tuning. */
+typedef enum {
+    GSA_TUNE_PIPE_THREADS = 1  /* threads per CTA of the pipelined SpMV: 256 or 512 */
+} gsa_tune_key;
+
 /* ---- library ------------------------------------------------------------ */
 
 /* Version as major*10000 + minor*100 + patch. */
@@ -73,6 +78,12 @@ int gsa_version(void);
 
 /* Message for the last non-OK status returned on this host thread. */
 const char *gsa_last_error_string(void);
+
+/* Process-wide kernel tuning (no counterpart in the reference): set a key to a
+ * value (GSA_ERR_INVALID_ARG if either is unknown), or read it back (-1 for an
+ * unknown key).  Affects calls issued afterwards. */
+int gsa_set_tuning(int key, int value);
+int gsa_get_tuning(int key);
 
 /* Profiling hook (no counterpart in the reference, which has no tracing): when set, the
  * library records `before` and `after` (cudaEvent_t) on the call's stream right around the
