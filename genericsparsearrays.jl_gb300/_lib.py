@@ -35,6 +35,8 @@ SIGNATURES = {
     "gsa_csr_mul": (_MUL + [_i32, _vp, _sz], _i32),
     "gsa_csc_mul": (_MUL + [_i32, _vp, _sz], _i32),
     "gsa_coo_mul": (_MUL, _i32),
+    "gsa_csr_spmv_noalloc": ([_vp, _i32, _i32, _i64, _i64, _i64, _vp, _vp, _vp, _i32, _vp, _vp,
+                              _vp, _vp], _i32),
     "gsa_mul_workspace_size": ([_i32, _i32, _i32, _i64, _i64, _i64, _i32, _i64, _i32], _sz),
     "gsa_coo_to_csr": ([_vp, _i32, _i32, _i64, _i64, _i64, _vp, _vp, _vp, _i32, _vp, _vp, _vp, _vp,
                         _sz], _i32),

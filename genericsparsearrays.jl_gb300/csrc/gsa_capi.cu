@@ -185,6 +185,20 @@ struct CooToCompressedBody {
     }
 };
 
+struct NoallocSpmvBody {
+    cudaStream_t s; int64_t m, n, nnz; const void *ptr, *idx, *val, *x, *alpha, *beta; void *y;
+    int base;
+    template <typename V, typename I> int operator()() {
+        CompressedArgs<V, I> a;
+        a.outer_n = m; a.inner_n = n; a.nnz = nnz;
+        a.ptr = (const I *)ptr; a.idx = (const I *)idx; a.val = (const V *)val;
+        a.base = base; a.conjA = false;
+        DenseIn<V> Bv = make_in<V>(x, n > 1 ? n : 1, GSA_OP_N);
+        DenseOut<V> Cv = make_out<V>(y, m > 1 ? m : 1, alpha, beta);
+        return launch_spmv_noalloc<V, I>(s, a, Bv, Cv);
+    }
+};
+
 struct CooToCompressedWsBody {
     bool colmajor; int64_t m, n, nnz; size_t out;
     template <typename V, typename I> int operator()() {
@@ -363,6 +377,20 @@ int gsa_csc_to_coo(void *stream, int dtype, int itype, int64_t m, int64_t n, int
                    void *rowind_out, void *colind_out, void *nzval_out) {
     return compressed_to_coo(true, stream, dtype, itype, m, n, nnz, colptr, rowval, nzval, base,
                              rowind_out, colind_out, nzval_out);
+}
+
+int gsa_csr_spmv_noalloc(void *stream, int dtype, int itype, int64_t m, int64_t n, int64_t nnz,
+                         const void *rowptr, const void *colval, const void *nzval, int base,
+                         const void *x, void *y, const void *alpha, const void *beta) {
+    const void *arrs[3] = {rowptr, colval, nzval};
+    int rc = check_mul_args(dtype, itype, m, n, nnz, GSA_OP_N, 1, n > 1 ? n : 1, GSA_OP_N,
+                            m > 1 ? m : 1, alpha, beta, x, y, arrs, 3);
+    if (rc) return rc;
+    if (!rowptr) return fail(GSA_ERR_INVALID_ARG, "rowptr is NULL");
+    if (nnz > 0 && (!colval || !nzval)) return fail(GSA_ERR_INVALID_ARG, "colval/nzval are NULL");
+    if (m == 0) return GSA_OK;
+    NoallocSpmvBody body{(cudaStream_t)stream, m, n, nnz, rowptr, colval, nzval, x, alpha, beta, y, base};
+    return dispatch_vi(dtype, itype, body);
 }
 
 int gsa_set_tuning(int key, int value) {

@@ -282,6 +282,9 @@ template <typename V, typename I>
 int launch_spmv_pipe(cudaStream_t s, const CompressedArgs<V, I> &a, DenseIn<V> B, DenseOut<V> C,
                      void *ws, size_t ws_bytes);
 template <typename V, typename I> size_t spmv_pipe_workspace_size(int64_t outer_n, int64_t nnz);
+// The same product with its carry slots in a static device array (no allocation).
+template <typename V, typename I>
+int launch_spmv_noalloc(cudaStream_t s, const CompressedArgs<V, I> &a, DenseIn<V> B, DenseOut<V> C);
 // Reads and clears the device error word of bounded waits (synchronizes s).
 int read_pipe_error(cudaStream_t s, int *out);
 void set_pipe_threads(int t);

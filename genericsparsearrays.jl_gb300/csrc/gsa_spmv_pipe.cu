@@ -28,6 +28,8 @@
 //     fixup pass, in CTA order (no atomics)
 // Every mbarrier wait is bounded; a wait that gives up sets the device error
 // word (read by gsa_check_device_status) and the CTA returns.
+#include <mutex>
+
 #include "gsa_internal.cuh"
 
 namespace gsa {
@@ -442,6 +444,86 @@ int launch_spmv_pipe(cudaStream_t s, const CompressedArgs<V, I> &a, DenseIn<V> B
     return launch_pipe_impl<V, I, 512>(s, a, B, C, ws, ws_bytes);
 }
 
+// ---------------------------------------------------------------------------
+// SpMV without any allocation (gsa_csr_spmv_noalloc).
+//
+// Some callers cannot allocate device memory at the moment they need a
+// product: a process whose device memory is already owned by another pool (so
+// cudaMalloc fails), or code that must not let an allocation synchronize the
+// device or, in Julia, run the garbage collector and its finalizers.  For them
+// the carry slots of the pipelined kernel -- its only scratch -- live in this
+// file-scope device array instead of a workspace.  The array is part of the
+// library's device image: every GPU that loads the library's kernels holds it
+// (NOALLOC_MAX_RUNS * 24 bytes = 192 KiB) until the process exits.  It is shared
+// by every call, so calls that overlap on the GPU race on it.  No slot has to
+// start at zero: each slot the fixup reads is written earlier in the same call.
+constexpr int64_t NOALLOC_MAX_RUNS = 8192;  // CTA runs (= carry slots) per call
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_MAX_RUNS * (8 + 16)];
+
+// Device address of g_noalloc_scratch on the current device, looked up once per
+// device (the first call on a device does this set-up).
+static int noalloc_scratch(unsigned char **out) {
+    static std::mutex mu;
+    static void *addr[128] = {};
+    int dev = 0;
+    int rc = check_cuda(cudaGetDevice(&dev), "noalloc: current device");
+    if (rc) return rc;
+    if (dev < 0 || dev >= 128) return fail(GSA_ERR_UNSUPPORTED, "noalloc: device ordinal %d", dev);
+    std::lock_guard<std::mutex> lock(mu);
+    if (!addr[dev]) {
+        void *p = nullptr;
+        rc = check_cuda(cudaGetSymbolAddress(&p, g_noalloc_scratch), "noalloc: scratch address");
+        if (rc) return rc;
+        addr[dev] = p;
+    }
+    *out = (unsigned char *)addr[dev];
+    return GSA_OK;
+}
+
+template <typename V, typename I, int THREADS>
+static int launch_noalloc_impl(cudaStream_t s, const CompressedArgs<V, I> &a, DenseIn<V> B,
+                               DenseOut<V> C) {
+    constexpr int TILE = PipeShape<V>::TILE;
+    const size_t smem = sizeof(PipeSmem<V, I, THREADS>);
+    auto kern = spmv_pipe_kernel<V, I, THREADS>;
+    int rc = check_cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                        "spmv_pipe smem attribute");
+    if (rc) return rc;
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    rc = check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, THREADS, smem),
+                    "spmv_pipe occupancy");
+    if (rc) return rc;
+    if (per_sm < 1) per_sm = 1;
+    const int64_t T = ceil_div(a.outer_n + a.nnz, TILE);
+    int64_t G = (int64_t)sms * per_sm;
+    if (G > T) G = T;
+    const int64_t Q = ceil_div(T, G);
+    G = ceil_div(T, Q);
+    if (G > NOALLOC_MAX_RUNS)
+        return fail(GSA_ERR_INVALID_ARG,
+                    "noalloc SpMV needs %lld carry slots, more than the %lld of its static scratch",
+                    (long long)G, (long long)NOALLOC_MAX_RUNS);
+    unsigned char *scratch = nullptr;
+    rc = noalloc_scratch(&scratch);
+    if (rc) return rc;
+    int64_t *carry_row = reinterpret_cast<int64_t *>(scratch);
+    V *carry_val = reinterpret_cast<V *>(scratch + NOALLOC_MAX_RUNS * 8);
+    kern<<<(unsigned)G, THREADS, smem, s>>>(a, B, C, Q, carry_row, carry_val);
+    rc = check_cuda(cudaGetLastError(), "spmv_pipe_kernel (noalloc)");
+    if (rc) return rc;
+    pipe_fixup_kernel<V><<<(unsigned)ceil_div(G, 256), 256, 0, s>>>(G, carry_row, carry_val, C);
+    return check_cuda(cudaGetLastError(), "pipe_fixup_kernel (noalloc)");
+}
+
+template <typename V, typename I>
+int launch_spmv_noalloc(cudaStream_t s, const CompressedArgs<V, I> &a, DenseIn<V> B, DenseOut<V> C) {
+    if (a.outer_n == 0) return GSA_OK;
+    if (g_pipe_threads == 256) return launch_noalloc_impl<V, I, 256>(s, a, B, C);
+    return launch_noalloc_impl<V, I, 512>(s, a, B, C);
+}
+
 int read_pipe_error(cudaStream_t s, int *out) {
     int rc = check_cuda(cudaStreamSynchronize(s), "device status sync");
     if (rc) return rc;
@@ -454,7 +536,9 @@ int read_pipe_error(cudaStream_t s, int *out) {
 #define GSA_INST_PIPE(V, I)                                                                     \
     template int launch_spmv_pipe<V, I>(cudaStream_t, const CompressedArgs<V, I> &, DenseIn<V>, \
                                         DenseOut<V>, void *, size_t);                           \
-    template size_t spmv_pipe_workspace_size<V, I>(int64_t, int64_t);
+    template size_t spmv_pipe_workspace_size<V, I>(int64_t, int64_t);                           \
+    template int launch_spmv_noalloc<V, I>(cudaStream_t, const CompressedArgs<V, I> &,          \
+                                           DenseIn<V>, DenseOut<V>);
 GSA_INST_PIPE(float, int32_t)
 GSA_INST_PIPE(float, int64_t)
 GSA_INST_PIPE(double, int32_t)

@@ -127,6 +127,23 @@ int gsa_coo_mul(void *stream, int dtype, int itype, int64_t m, int64_t n, int64_
                 int64_t k, const void *B, int64_t ldb, int opB, void *C, int64_t ldc,
                 const void *alpha, const void *beta);
 
+/* y = beta*y + alpha*A*x for a CSR matrix and vectors x (n) and y (m), like
+ * gsa_csr_mul with opA = opB = N and k = 1, but allocating nothing: no
+ * cudaMalloc, no stream-ordered pool, no workspace argument.  No counterpart in
+ * the reference.  It is for callers that cannot allocate device memory when they
+ * need the product -- a process whose device memory is owned by another pool,
+ * or code that must not let an allocation synchronize the device or (in Julia)
+ * run the garbage collector.  The kernel's carry slots live in a static device
+ * array of 8192 slots (192 KiB, held on every GPU that loads the library until
+ * the process exits); a call that would need more slots returns
+ * GSA_ERR_INVALID_ARG.  The first call on a device looks up the array's device
+ * address, so make it before any stream capture.  All calls share the array:
+ * calls that overlap on the GPU race on it.  Same tolerance and determinism as
+ * gsa_csr_mul. */
+int gsa_csr_spmv_noalloc(void *stream, int dtype, int itype, int64_t m, int64_t n, int64_t nnz,
+                         const void *rowptr, const void *colval, const void *nzval, int base,
+                         const void *x, void *y, const void *alpha, const void *beta);
+
 /* Workspace bytes for gsa_csr_mul / gsa_csc_mul with these sizes (format:
  * 0 CSR, 1 CSC).  0 means none is needed. */
 size_t gsa_mul_workspace_size(int format, int dtype, int itype, int64_t m, int64_t n,
