@@ -26,11 +26,12 @@ from .sparse import (
     validate,
 )
 
-ALGO_AUTO, ALGO_MERGE, ALGO_VECTOR = _lib.ALGO_AUTO, _lib.ALGO_MERGE, _lib.ALGO_VECTOR
+ALGO_AUTO, ALGO_MERGE, ALGO_VECTOR, ALGO_PIPE = (_lib.ALGO_AUTO, _lib.ALGO_MERGE, _lib.ALGO_VECTOR,
+                                                 _lib.ALGO_PIPE)
 
 __all__ = [
     "AbstractGenericSparseMatrix", "Adjoint", "ArgumentError", "DimensionMismatch",
     "GenericSparseMatrixCOO", "GenericSparseMatrixCSC", "GenericSparseMatrixCSR",
     "SparseMatrixCSC", "Transpose", "adapt", "adjoint", "collect", "mul", "mul_", "nnz", "size",
-    "transpose", "validate", "ALGO_AUTO", "ALGO_MERGE", "ALGO_VECTOR",
+    "transpose", "validate", "ALGO_AUTO", "ALGO_MERGE", "ALGO_VECTOR", "ALGO_PIPE",
 ]

@@ -19,7 +19,7 @@ F32, F64, C32, C64, I32, I64 = range(6)
 IDX32, IDX64 = 0, 1
 # op codes (gsa_op) and algorithms (gsa_algo)
 OP_N, OP_T, OP_C = 0, 1, 2
-ALGO_AUTO, ALGO_MERGE, ALGO_VECTOR = 0, 1, 2
+ALGO_AUTO, ALGO_MERGE, ALGO_VECTOR, ALGO_PIPE = 0, 1, 2, 3
 TUNE_PIPE_THREADS = 1
 
 # Every exported symbol of include/gsa.h with its ctypes signature.

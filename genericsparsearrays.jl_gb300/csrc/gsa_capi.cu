@@ -219,7 +219,7 @@ static int compressed_mul(bool csr, void *stream, int dtype, int itype, int64_t 
     if (rc) return rc;
     if (!ptr) return fail(GSA_ERR_INVALID_ARG, "pointer array is NULL");
     if (nnz > 0 && (!idx || !val)) return fail(GSA_ERR_INVALID_ARG, "index/value arrays are NULL");
-    if (algo < 0 || algo > 2) return fail(GSA_ERR_INVALID_ARG, "unknown algo %d", algo);
+    if (algo < 0 || algo > 3) return fail(GSA_ERR_INVALID_ARG, "unknown algo %d", algo);
     cudaStream_t s = (cudaStream_t)stream;
     const bool gather = csr ? (opA == GSA_OP_N) : (opA != GSA_OP_N);
     const int64_t outer_n = csr ? m : n, inner_n = csr ? n : m;

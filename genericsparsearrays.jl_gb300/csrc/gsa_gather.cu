@@ -290,8 +290,8 @@ static int64_t gather_num_tiles(int64_t outer_n, int64_t nnz) {
 
 template <typename V, typename I>
 size_t gather_workspace_size(int64_t outer_n, int64_t nnz, int64_t k, int algo) {
-    if (algo == GSA_ALGO_VECTOR || outer_n == 0 || k == 0) return 0;
-    if (k == 1 && algo == GSA_ALGO_AUTO) return spmv_pipe_workspace_size<V, I>(outer_n, nnz);
+    if (algo == GSA_ALGO_VECTOR || algo == GSA_ALGO_AUTO || outer_n == 0 || k == 0) return 0;
+    if (algo == GSA_ALGO_PIPE) return k == 1 ? spmv_pipe_workspace_size<V, I>(outer_n, nnz) : 0;
     int64_t T = gather_num_tiles<V, I>(outer_n, nnz);
     Carver cv(nullptr);
     cv.take<int64_t>(T + 1);
@@ -326,7 +326,11 @@ int launch_gather(cudaStream_t s, const CompressedArgs<V, I> &a, int64_t k, Dens
         if (avg <= 16) return launch_vector_g<V, I, 16>(s, a, k, B, C);
         return launch_vector_g<V, I, 32>(s, a, k, B, C);
     }
-    if (k == 1 && algo == GSA_ALGO_AUTO) return launch_spmv_pipe<V, I>(s, a, B, C, ws, ws_bytes);
+    if (algo == GSA_ALGO_AUTO) return launch_rowblock<V, I>(s, a, k, B, C);
+    if (algo == GSA_ALGO_PIPE) {
+        if (k != 1) return fail(GSA_ERR_UNSUPPORTED, "GSA_ALGO_PIPE takes one right-hand side");
+        return launch_spmv_pipe<V, I>(s, a, B, C, ws, ws_bytes);
+    }
     constexpr int TILE = GatherShape<V>::TILE;
     const int64_t T = gather_num_tiles<V, I>(a.outer_n, a.nnz);
     if (ws_bytes < gather_workspace_size<V, I>(a.outer_n, a.nnz, k, algo))

@@ -277,7 +277,11 @@ int launch_gather(cudaStream_t s, const CompressedArgs<V, I> &a, int64_t k, Dens
 template <typename V, typename I>
 size_t gather_workspace_size(int64_t outer_n, int64_t nnz, int64_t k, int algo);
 
-// Persistent TMA-pipelined SpMV (k = 1) behind launch_gather's default algorithm.
+// Row-block gather (thread / warp / CTA per row by length): launch_gather's default.
+template <typename V, typename I>
+int launch_rowblock(cudaStream_t s, const CompressedArgs<V, I> &a, int64_t k, DenseIn<V> B,
+                    DenseOut<V> C);
+// Persistent bulk-copy pipelined merge-path SpMV (k = 1): GSA_ALGO_PIPE.
 template <typename V, typename I>
 int launch_spmv_pipe(cudaStream_t s, const CompressedArgs<V, I> &a, DenseIn<V> B, DenseOut<V> C,
                      void *ws, size_t ws_bytes);

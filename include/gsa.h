@@ -60,10 +60,12 @@ typedef enum { GSA_OP_N = 0, GSA_OP_T = 1, GSA_OP_C = 2 } gsa_op;
 
 /* Gather kernel selection for the row-gather paths (CSR N, CSC T). */
 typedef enum {
-    GSA_ALGO_AUTO = 0,     /* library choice: for one right-hand side the persistent
-                              bulk-copy pipelined merge-path kernel */
+    GSA_ALGO_AUTO = 0,     /* library choice: row blocks -- a thread per short row, a warp
+                              per long row, a CTA per very long row; no workspace */
     GSA_ALGO_MERGE = 1,    /* one CTA per merge-path tile (any row-length mix) */
-    GSA_ALGO_VECTOR = 2    /* a group of threads per row (short, even rows) */
+    GSA_ALGO_VECTOR = 2,   /* a group of threads per row (short, even rows) */
+    GSA_ALGO_PIPE = 3      /* persistent merge-path runs with bulk-copy double buffering
+                              (one right-hand side) */
 } gsa_algo;
 
 /* Tuning keys for gsa_set_tuning / gsa_get_tuning. */

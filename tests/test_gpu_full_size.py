@@ -32,7 +32,7 @@ def test_laplacian_spmv_csr_csc(gsa, oracle, cuda, wl, it, dt):
     tol = 1e-12 if dt == np.float64 else 1e-5
     A = gsa.adapt(cuda, gsa.GenericSparseMatrixCSR(m, n, rp, cv, nz))
     xd = torch.from_numpy(x).to(cuda)
-    for algo in (gsa.ALGO_AUTO, gsa.ALGO_MERGE, gsa.ALGO_VECTOR):
+    for algo in (gsa.ALGO_AUTO, gsa.ALGO_MERGE, gsa.ALGO_VECTOR, gsa.ALGO_PIPE):
         y = torch.empty(m, dtype=xd.dtype, device=cuda)
         gsa.mul_(y, A, xd, algo=algo)
         assert rel_err_vs(y.cpu().numpy(), ref, scale) <= tol
@@ -84,7 +84,10 @@ def test_power_law_complex_csr_coo(gsa, oracle, cuda, wl):
     ye, sc = oracle.mul_exact("csr", "N", m, n, rp, cv, nz, 1, x, np.zeros(m, np.complex128))
     xd = torch.from_numpy(x).to(cuda)
     A = gsa.adapt(cuda, gsa.GenericSparseMatrixCSR(m, n, rp, cv, nz))
-    assert oracle.max_rel_error((A @ xd).cpu().numpy(), ye, sc) <= 1e-12
+    for algo in (gsa.ALGO_AUTO, gsa.ALGO_MERGE, gsa.ALGO_PIPE):
+        y = torch.empty(m, dtype=torch.complex128, device=cuda)
+        gsa.mul_(y, A, xd, algo=algo)
+        assert oracle.max_rel_error(y.cpu().numpy(), ye, sc) <= 1e-12
     rows = wl.csr_rows(rp)
     C = gsa.adapt(cuda, gsa.GenericSparseMatrixCOO(m, n, rows, cv, nz))
     assert oracle.max_rel_error((C @ xd).cpu().numpy(), ye, sc) <= 1e-12
