@@ -20,7 +20,7 @@ IDX32, IDX64 = 0, 1
 # op codes (gsa_op) and algorithms (gsa_algo)
 OP_N, OP_T, OP_C = 0, 1, 2
 ALGO_AUTO, ALGO_MERGE, ALGO_VECTOR, ALGO_PIPE = 0, 1, 2, 3
-TUNE_PIPE_THREADS = 1
+TUNE_PIPE_THREADS, TUNE_SPMM_COLUMNS = 1, 2
 
 # Every exported symbol of include/gsa.h with its ctypes signature.
 _i32, _i64, _vp, _sz = ctypes.c_int, ctypes.c_int64, ctypes.c_void_p, ctypes.c_size_t
@@ -35,6 +35,12 @@ SIGNATURES = {
     "gsa_csr_mul": (_MUL + [_i32, _vp, _sz], _i32),
     "gsa_csc_mul": (_MUL + [_i32, _vp, _sz], _i32),
     "gsa_coo_mul": (_MUL, _i32),
+    "gsa_plan_create": ([_vp, _i32, _i64, _i64, _vp, _i32, ctypes.POINTER(_vp)], _i32),
+    "gsa_plan_destroy": ([_vp], _i32),
+    "gsa_plan_info": ([_vp, ctypes.POINTER(_i64), ctypes.POINTER(_i64), ctypes.POINTER(_i64)], _i32),
+    "gsa_plan_workspace_size": ([_vp, _i32, _i64], _sz),
+    "gsa_csr_mul_planned": (_MUL + [_vp, _vp, _sz], _i32),
+    "gsa_csc_mul_planned": (_MUL + [_vp, _vp, _sz], _i32),
     "gsa_csr_spmv_noalloc": ([_vp, _i32, _i32, _i64, _i64, _i64, _vp, _vp, _vp, _i32, _vp, _vp,
                               _vp, _vp], _i32),
     "gsa_mul_workspace_size": ([_i32, _i32, _i32, _i64, _i64, _i64, _i32, _i64, _i32], _sz),

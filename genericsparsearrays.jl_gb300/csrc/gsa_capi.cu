@@ -1,6 +1,7 @@
 // extern "C" entry points of libgsa (declared in include/gsa.h): argument and
 // dimension checks in the order the reference's mul! methods make them,
 // dispatch to the kernels, stream-ordered workspace, error strings.
+#include <new>
 #include <stdarg.h>
 #include <stdio.h>
 #include <string.h>
@@ -129,7 +130,7 @@ static DenseOut<V> make_out(void *C, int64_t ldc, const void *alpha, const void 
 struct CompressedMulBody {
     cudaStream_t s; bool gather; int64_t outer_n, inner_n, nnz, k, rows_out;
     const void *ptr, *idx, *val, *B, *alpha, *beta; void *C; int base, opA, opB, algo;
-    int64_t ldb, ldc; void *ws; size_t ws_bytes;
+    int64_t ldb, ldc; void *ws; size_t ws_bytes; const Plan *plan;
     template <typename V, typename I> int operator()() {
         CompressedArgs<V, I> a;
         a.outer_n = outer_n; a.inner_n = inner_n; a.nnz = nnz;
@@ -139,11 +140,11 @@ struct CompressedMulBody {
         DenseOut<V> Cv = make_out<V>(C, ldc, alpha, beta);
         if (rows_out == 0 || k == 0) return GSA_OK;
         Workspace w;
-        size_t need = gather ? gather_workspace_size<V, I>(outer_n, nnz, k, algo)
+        size_t need = gather ? gather_workspace_size<V, I>(outer_n, nnz, k, algo, plan)
                              : scatter_workspace_size<V, I>(outer_n, nnz, k);
         int rc = w.acquire(s, ws, ws_bytes, need);
         if (rc) return rc;
-        if (gather) return launch_gather<V, I>(s, a, k, Bv, Cv, algo, w.p, w.bytes);
+        if (gather) return launch_gather<V, I>(s, a, k, Bv, Cv, algo, plan, w.p, w.bytes);
         return launch_scatter<V, I>(s, a, k, Bv, Cv, rows_out, w.p, w.bytes);
     }
 };
@@ -164,9 +165,9 @@ struct CooMulBody {
 };
 
 struct MulWsBody {
-    bool gather; int64_t outer_n, nnz, k; int algo; size_t out;
+    bool gather; int64_t outer_n, nnz, k; int algo; size_t out; const Plan *plan;
     template <typename V, typename I> int operator()() {
-        out = gather ? gather_workspace_size<V, I>(outer_n, nnz, k, algo)
+        out = gather ? gather_workspace_size<V, I>(outer_n, nnz, k, algo, plan)
                      : scatter_workspace_size<V, I>(outer_n, nnz, k);
         return 0;
     }
@@ -213,19 +214,21 @@ static int compressed_mul(bool csr, void *stream, int dtype, int itype, int64_t 
                           int64_t nnz, const void *ptr, const void *idx, const void *val, int base,
                           int opA, int64_t k, const void *B, int64_t ldb, int opB, void *C,
                           int64_t ldc, const void *alpha, const void *beta, int algo, void *ws,
-                          size_t ws_bytes) {
+                          size_t ws_bytes, const Plan *plan = nullptr) {
     const void *arrs[3] = {ptr, idx, val};
     int rc = check_mul_args(dtype, itype, m, n, nnz, opA, k, ldb, opB, ldc, alpha, beta, B, C, arrs, 3);
     if (rc) return rc;
     if (!ptr) return fail(GSA_ERR_INVALID_ARG, "pointer array is NULL");
     if (nnz > 0 && (!idx || !val)) return fail(GSA_ERR_INVALID_ARG, "index/value arrays are NULL");
     if (algo < 0 || algo > 3) return fail(GSA_ERR_INVALID_ARG, "unknown algo %d", algo);
+    if (plan && (plan->outer_n != (csr ? m : n) || plan->nnz != nnz))
+        return fail(GSA_ERR_INVALID_ARG, "plan was made for another structure");
     cudaStream_t s = (cudaStream_t)stream;
     const bool gather = csr ? (opA == GSA_OP_N) : (opA != GSA_OP_N);
     const int64_t outer_n = csr ? m : n, inner_n = csr ? n : m;
     const int64_t rows_out = opA == GSA_OP_N ? m : n;
     CompressedMulBody body{s, gather, outer_n, inner_n, nnz, k, rows_out, ptr, idx, val, B, alpha,
-                           beta, C, base, opA, opB, algo, ldb, ldc, ws, ws_bytes};
+                           beta, C, base, opA, opB, algo, ldb, ldc, ws, ws_bytes, plan};
     return dispatch_vi(dtype, itype, body);
 }
 
@@ -262,6 +265,67 @@ int gsa_csc_mul(void *stream, int dtype, int itype, int64_t m, int64_t n, int64_
                           k, B, ldb, opB, C, ldc, alpha, beta, algo, workspace, workspace_bytes);
 }
 
+int gsa_plan_create(void *stream, int itype, int64_t outer_n, int64_t nnz, const void *ptr, int base,
+                    gsa_plan **out) {
+    if (!out) return fail(GSA_ERR_INVALID_ARG, "out is NULL");
+    *out = nullptr;
+    if (!itype_size(itype)) return fail(GSA_ERR_UNSUPPORTED, "unsupported itype %d", itype);
+    if (outer_n < 0 || nnz < 0) return fail(GSA_ERR_INVALID_ARG, "negative size");
+    if (!ptr) return fail(GSA_ERR_INVALID_ARG, "pointer array is NULL");
+    Plan *p = new (std::nothrow) Plan();
+    if (!p) return fail(GSA_ERR_ALLOC, "plan: host memory");
+    int rc = plan_create((cudaStream_t)stream, itype, outer_n, nnz, ptr, base, p);
+    if (rc) {
+        if (p->mem) cudaFree(p->mem);
+        delete p;
+        return rc;
+    }
+    *out = p;
+    return GSA_OK;
+}
+
+int gsa_plan_destroy(gsa_plan *plan) {
+    if (!plan) return GSA_OK;
+    int rc = GSA_OK;
+    if (plan->mem) rc = check_cuda(cudaFree(plan->mem), "plan: free");
+    delete plan;
+    return rc;
+}
+
+int gsa_plan_info(const gsa_plan *plan, int64_t *max_len, int64_t *nlong, int64_t *nchunks) {
+    if (!plan) return fail(GSA_ERR_INVALID_ARG, "plan is NULL");
+    if (max_len) *max_len = plan->max_len;
+    if (nlong) *nlong = plan->nlong;
+    if (nchunks) *nchunks = plan->nchunks;
+    return GSA_OK;
+}
+
+int gsa_csr_mul_planned(void *stream, int dtype, int itype, int64_t m, int64_t n, int64_t nnz,
+                        const void *rowptr, const void *colval, const void *nzval, int base, int opA,
+                        int64_t k, const void *B, int64_t ldb, int opB, void *C, int64_t ldc,
+                        const void *alpha, const void *beta, const gsa_plan *plan, void *workspace,
+                        size_t workspace_bytes) {
+    if (opA != GSA_OP_N) plan = nullptr;  // the plan covers the row gather only
+    return compressed_mul(true, stream, dtype, itype, m, n, nnz, rowptr, colval, nzval, base, opA,
+                          k, B, ldb, opB, C, ldc, alpha, beta, GSA_ALGO_AUTO, workspace,
+                          workspace_bytes, plan);
+}
+
+int gsa_csc_mul_planned(void *stream, int dtype, int itype, int64_t m, int64_t n, int64_t nnz,
+                        const void *colptr, const void *rowval, const void *nzval, int base, int opA,
+                        int64_t k, const void *B, int64_t ldb, int opB, void *C, int64_t ldc,
+                        const void *alpha, const void *beta, const gsa_plan *plan, void *workspace,
+                        size_t workspace_bytes) {
+    if (opA == GSA_OP_N) plan = nullptr;  // the plan covers the column gather (op T / C) only
+    return compressed_mul(false, stream, dtype, itype, m, n, nnz, colptr, rowval, nzval, base, opA,
+                          k, B, ldb, opB, C, ldc, alpha, beta, GSA_ALGO_AUTO, workspace,
+                          workspace_bytes, plan);
+}
+
+size_t gsa_plan_workspace_size(const gsa_plan *plan, int dtype, int64_t k) {
+    return rowblock_workspace_size(plan, dtype_size(dtype), k);
+}
+
 int gsa_coo_mul(void *stream, int dtype, int itype, int64_t m, int64_t n, int64_t nnz,
                 const void *rowind, const void *colind, const void *nzval, int base, int opA,
                 int64_t k, const void *B, int64_t ldb, int opB, void *C, int64_t ldc,
@@ -285,7 +349,7 @@ size_t gsa_mul_workspace_size(int format, int dtype, int itype, int64_t m, int64
     const bool csr = format == 0;
     const bool gather = csr ? (opA == GSA_OP_N) : (opA != GSA_OP_N);
     const int64_t outer_n = csr ? m : n;
-    MulWsBody body{gather, outer_n, nnz, k, algo, 0};
+    MulWsBody body{gather, outer_n, nnz, k, algo, 0, nullptr};
     if (dispatch_vi(dtype, itype, body)) return 0;
     return body.out;
 }
@@ -399,11 +463,18 @@ int gsa_set_tuning(int key, int value) {
         set_pipe_threads(value);
         return GSA_OK;
     }
+    if (key == GSA_TUNE_SPMM_COLUMNS) {
+        if (value != 0 && value != 1 && value != 2 && value != 4 && value != 8)
+            return fail(GSA_ERR_INVALID_ARG, "columns per thread must be 0, 1, 2, 4 or 8");
+        set_spmm_columns(value);
+        return GSA_OK;
+    }
     return fail(GSA_ERR_INVALID_ARG, "unknown tuning key %d", key);
 }
 
 int gsa_get_tuning(int key) {
     if (key == GSA_TUNE_PIPE_THREADS) return get_pipe_threads();
+    if (key == GSA_TUNE_SPMM_COLUMNS) return get_spmm_columns();
     return -1;
 }
 

@@ -289,8 +289,9 @@ static int64_t gather_num_tiles(int64_t outer_n, int64_t nnz) {
 }
 
 template <typename V, typename I>
-size_t gather_workspace_size(int64_t outer_n, int64_t nnz, int64_t k, int algo) {
-    if (algo == GSA_ALGO_VECTOR || algo == GSA_ALGO_AUTO || outer_n == 0 || k == 0) return 0;
+size_t gather_workspace_size(int64_t outer_n, int64_t nnz, int64_t k, int algo, const Plan *plan) {
+    if (algo == GSA_ALGO_AUTO) return rowblock_workspace_size(plan, sizeof(V), k);
+    if (algo == GSA_ALGO_VECTOR || outer_n == 0 || k == 0) return 0;
     if (algo == GSA_ALGO_PIPE) return k == 1 ? spmv_pipe_workspace_size<V, I>(outer_n, nnz) : 0;
     int64_t T = gather_num_tiles<V, I>(outer_n, nnz);
     Carver cv(nullptr);
@@ -316,7 +317,7 @@ static int launch_vector_g(cudaStream_t s, const CompressedArgs<V, I> &a, int64_
 
 template <typename V, typename I>
 int launch_gather(cudaStream_t s, const CompressedArgs<V, I> &a, int64_t k, DenseIn<V> B,
-                  DenseOut<V> C, int algo, void *ws, size_t ws_bytes) {
+                  DenseOut<V> C, int algo, const Plan *plan, void *ws, size_t ws_bytes) {
     if (a.outer_n == 0 || k == 0) return GSA_OK;
     if (algo == GSA_ALGO_VECTOR) {
         double avg = a.outer_n ? (double)a.nnz / (double)a.outer_n : 0.0;
@@ -326,14 +327,14 @@ int launch_gather(cudaStream_t s, const CompressedArgs<V, I> &a, int64_t k, Dens
         if (avg <= 16) return launch_vector_g<V, I, 16>(s, a, k, B, C);
         return launch_vector_g<V, I, 32>(s, a, k, B, C);
     }
-    if (algo == GSA_ALGO_AUTO) return launch_rowblock<V, I>(s, a, k, B, C);
+    if (algo == GSA_ALGO_AUTO) return launch_rowblock<V, I>(s, a, k, B, C, plan, ws, ws_bytes);
     if (algo == GSA_ALGO_PIPE) {
         if (k != 1) return fail(GSA_ERR_UNSUPPORTED, "GSA_ALGO_PIPE takes one right-hand side");
         return launch_spmv_pipe<V, I>(s, a, B, C, ws, ws_bytes);
     }
     constexpr int TILE = GatherShape<V>::TILE;
     const int64_t T = gather_num_tiles<V, I>(a.outer_n, a.nnz);
-    if (ws_bytes < gather_workspace_size<V, I>(a.outer_n, a.nnz, k, algo))
+    if (ws_bytes < gather_workspace_size<V, I>(a.outer_n, a.nnz, k, algo, nullptr))
         return fail(GSA_ERR_INVALID_ARG, "gather workspace too small");
     Carver cv(ws);
     int64_t *coords = cv.take<int64_t>(T + 1);
@@ -362,8 +363,8 @@ int launch_gather(cudaStream_t s, const CompressedArgs<V, I> &a, int64_t k, Dens
 
 #define GSA_INST_GATHER(V, I)                                                                   \
     template int launch_gather<V, I>(cudaStream_t, const CompressedArgs<V, I> &, int64_t,       \
-                                     DenseIn<V>, DenseOut<V>, int, void *, size_t);             \
-    template size_t gather_workspace_size<V, I>(int64_t, int64_t, int64_t, int);
+                                     DenseIn<V>, DenseOut<V>, int, const Plan *, void *, size_t); \
+    template size_t gather_workspace_size<V, I>(int64_t, int64_t, int64_t, int, const Plan *);
 GSA_INST_GATHER(float, int32_t)
 GSA_INST_GATHER(float, int64_t)
 GSA_INST_GATHER(double, int32_t)

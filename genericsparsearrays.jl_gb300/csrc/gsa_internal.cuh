@@ -9,6 +9,17 @@
 
 #include "../../include/gsa.h"
 
+// A plan (gsa_plan_create): the outer entries of one compressed structure that have more
+// than 512 stored entries, each cut into chunks of 512 entries (device arrays).
+struct gsa_plan {
+    int64_t outer_n = 0, nnz = 0, max_len = 0, nlong = 0, nchunks = 0;
+    const int64_t *row = nullptr;         // outer index of each long entry
+    const int32_t *first = nullptr;       // its first chunk
+    const int32_t *count = nullptr;       // its number of chunks
+    const int32_t *chunk_slot = nullptr;  // the long entry a chunk belongs to
+    void *mem = nullptr;                  // one device allocation holding the arrays
+};
+
 namespace gsa {
 
 // ---------------------------------------------------------------------------
@@ -94,6 +105,17 @@ template <> __device__ __forceinline__ cf32 ldg(const cf32 *p) {
 }
 template <> __device__ __forceinline__ cf64 ldg(const cf64 *p) {
     double2 v = __ldg(reinterpret_cast<const double2 *>(p));
+    return cf64{v.x, v.y};
+}
+
+// Loads that bypass L1 (L2 is coherent across SMs): data other CTAs wrote during the kernel.
+template <typename T> __device__ __forceinline__ T ld_coherent(const T *p) { return __ldcg(p); }
+template <> __device__ __forceinline__ cf32 ld_coherent(const cf32 *p) {
+    float2 v = __ldcg(reinterpret_cast<const float2 *>(p));
+    return cf32{v.x, v.y};
+}
+template <> __device__ __forceinline__ cf64 ld_coherent(const cf64 *p) {
+    double2 v = __ldcg(reinterpret_cast<const double2 *>(p));
     return cf64{v.x, v.y};
 }
 
@@ -273,14 +295,18 @@ template <typename V, typename I> struct CompressedArgs {
 // Gather: out[o, c] = beta*out[o, c] + alpha * sum_j conj?(val_j) * op(B)(idx_j, c)
 template <typename V, typename I>
 int launch_gather(cudaStream_t s, const CompressedArgs<V, I> &a, int64_t k, DenseIn<V> B,
-                  DenseOut<V> C, int algo, void *ws, size_t ws_bytes);
+                  DenseOut<V> C, int algo, const ::gsa_plan *plan, void *ws, size_t ws_bytes);
 template <typename V, typename I>
-size_t gather_workspace_size(int64_t outer_n, int64_t nnz, int64_t k, int algo);
+size_t gather_workspace_size(int64_t outer_n, int64_t nnz, int64_t k, int algo, const ::gsa_plan *plan);
 
-// Row-block gather (thread / warp / CTA per row by length): launch_gather's default.
+using Plan = ::gsa_plan;
+int plan_create(cudaStream_t s, int itype, int64_t outer_n, int64_t nnz, const void *ptr, int base, Plan *p);
+
+// Row-block gather (thread per short row; long rows by warp, or by plan chunks): the default.
 template <typename V, typename I>
 int launch_rowblock(cudaStream_t s, const CompressedArgs<V, I> &a, int64_t k, DenseIn<V> B,
-                    DenseOut<V> C);
+                    DenseOut<V> C, const Plan *plan, void *ws, size_t ws_bytes);
+size_t rowblock_workspace_size(const Plan *plan, size_t vsize, int64_t k);
 // Persistent bulk-copy pipelined merge-path SpMV (k = 1): GSA_ALGO_PIPE.
 template <typename V, typename I>
 int launch_spmv_pipe(cudaStream_t s, const CompressedArgs<V, I> &a, DenseIn<V> B, DenseOut<V> C,
@@ -293,6 +319,8 @@ int launch_spmv_noalloc(cudaStream_t s, const CompressedArgs<V, I> &a, DenseIn<V
 int read_pipe_error(cudaStream_t s, int *out);
 void set_pipe_threads(int t);
 int get_pipe_threads();
+void set_spmm_columns(int c);   // 0 (by value size), 1, 2, 4 or 8
+int get_spmm_columns();
 
 // Scatter: out[idx_j, c] += conj?(val_j) * (op(B)(o, c) * alpha), after the beta pass.
 template <typename V, typename I>

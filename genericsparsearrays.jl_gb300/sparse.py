@@ -396,6 +396,45 @@ def _scalar_buf(v, dtype: torch.dtype):
     return np.array([v], dtype=npdt)
 
 
+class _PlanHandle:
+    """Owns a gsa_plan (long outer entries of one structure, cut into chunks)."""
+
+    def __init__(self, handle: int, nlong: int, nchunks: int, max_len: int):
+        self.handle, self.nlong, self.nchunks, self.max_len = handle, nlong, nchunks, max_len
+
+    def __del__(self):
+        try:
+            _lib.load().gsa_plan_destroy(ctypes.c_void_p(self.handle))
+        except Exception:  # interpreter shutdown
+            pass
+
+
+def _gather_plan(A) -> Optional[_PlanHandle]:
+    """The plan of A's compressed structure, made on first use and kept on the matrix
+    (None when no outer entry is longer than 512, so plain calls are as good).  Making it
+    synchronizes the stream once; the structure must not be changed in place afterwards."""
+    cached = A.__dict__.get("_plan", False)
+    if cached is not False:
+        return cached
+    csr = isinstance(A, GenericSparseMatrixCSR)
+    ptr = A.rowptr if csr else A.colptr
+    outer = A.m if csr else A.n
+    lib = _lib.load()
+    h = ctypes.c_void_p(0)
+    with torch.cuda.device(A.device):
+        st = lib.gsa_plan_create(_stream_ptr(A.device), _ITYPE[A.itype], outer, nnz(A), _ptr(ptr),
+                                 BASE, ctypes.byref(h))
+    _lib.check(st)
+    ml, nl, nc = ctypes.c_int64(0), ctypes.c_int64(0), ctypes.c_int64(0)
+    lib.gsa_plan_info(h, ctypes.byref(ml), ctypes.byref(nl), ctypes.byref(nc))
+    if nl.value == 0:
+        lib.gsa_plan_destroy(h)
+        A._plan = None
+    else:
+        A._plan = _PlanHandle(h.value, nl.value, nc.value, ml.value)
+    return A._plan
+
+
 def mul_(C: torch.Tensor, A, B, alpha=1, beta=0, algo: int = _lib.ALGO_AUTO,
          workspace: Optional[torch.Tensor] = None) -> torch.Tensor:
     """``mul!(C, A, B, α, β)``: ``C = β C + α op(A) op(B)`` on the GPU; returns ``C``.
@@ -452,6 +491,20 @@ def mul_(C: torch.Tensor, A, B, alpha=1, beta=0, algo: int = _lib.ALGO_AUTO,
         if isinstance(Ap, (GenericSparseMatrixCSR, GenericSparseMatrixCSC)):
             csr = isinstance(Ap, GenericSparseMatrixCSR)
             ptr, idx = (Ap.rowptr, Ap.colval) if csr else (Ap.colptr, Ap.rowval)
+            gather = (opA == _lib.OP_N) == csr
+            plan = _gather_plan(Ap) if (gather and algo == _lib.ALGO_AUTO) else None
+        if isinstance(Ap, (GenericSparseMatrixCSR, GenericSparseMatrixCSC)) and plan is not None:
+            ws_bytes = lib.gsa_plan_workspace_size(ctypes.c_void_p(plan.handle), _DTYPE[dt], k)
+            if ws_bytes and (workspace is None or workspace.numel() < ws_bytes):
+                workspace = torch.empty(ws_bytes, dtype=torch.uint8, device=dev)
+            fn = lib.gsa_csr_mul_planned if csr else lib.gsa_csc_mul_planned
+            st = fn(stream, _DTYPE[dt], _ITYPE[Ap.itype], Ap.m, Ap.n, nnz(Ap), _ptr(ptr), _ptr(idx),
+                    _ptr(Ap.nzval), BASE, opA, k, _ptr(Bbuf), ldb, opB, _ptr(Cw), ldc,
+                    al.ctypes.data_as(ctypes.c_void_p), be.ctypes.data_as(ctypes.c_void_p),
+                    ctypes.c_void_p(plan.handle),
+                    _ptr(workspace) if ws_bytes else ctypes.c_void_p(0),
+                    workspace.numel() if ws_bytes else 0)
+        elif isinstance(Ap, (GenericSparseMatrixCSR, GenericSparseMatrixCSC)):
             ws_bytes = lib.gsa_mul_workspace_size(0 if csr else 1, _DTYPE[dt], _ITYPE[Ap.itype],
                                                   Ap.m, Ap.n, nnz(Ap), opA, k, algo)
             if ws_bytes and (workspace is None or workspace.numel() < ws_bytes):

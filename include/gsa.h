@@ -60,8 +60,8 @@ typedef enum { GSA_OP_N = 0, GSA_OP_T = 1, GSA_OP_C = 2 } gsa_op;
 
 /* Gather kernel selection for the row-gather paths (CSR N, CSC T). */
 typedef enum {
-    GSA_ALGO_AUTO = 0,     /* library choice: row blocks -- a thread per short row, a warp
-                              per long row, a CTA per very long row; no workspace */
+    GSA_ALGO_AUTO = 0,     /* library choice: row blocks -- per warp of 32 rows, 1..32
+                              lanes per row from the rows' average length; no workspace */
     GSA_ALGO_MERGE = 1,    /* one CTA per merge-path tile (any row-length mix) */
     GSA_ALGO_VECTOR = 2,   /* a group of threads per row (short, even rows) */
     GSA_ALGO_PIPE = 3      /* persistent merge-path runs with bulk-copy double buffering
@@ -70,7 +70,9 @@ typedef enum {
 
 /* Tuning keys for gsa_set_tuning / gsa_get_tuning. */
 typedef enum {
-    GSA_TUNE_PIPE_THREADS = 1  /* threads per CTA of the pipelined SpMV: 256 or 512 */
+    GSA_TUNE_PIPE_THREADS = 1, /* threads per CTA of the pipelined SpMV: 256 or 512 */
+    GSA_TUNE_SPMM_COLUMNS = 2  /* right-hand-side columns a thread accumulates in the default
+                                  gather with k > 1: 0 (by value size), 1, 2, 4 or 8 */
 } gsa_tune_key;
 
 /* ---- library ------------------------------------------------------------ */
@@ -145,6 +147,39 @@ int gsa_coo_mul(void *stream, int dtype, int itype, int64_t m, int64_t n, int64_
 int gsa_csr_spmv_noalloc(void *stream, int dtype, int itype, int64_t m, int64_t n, int64_t nnz,
                          const void *rowptr, const void *colval, const void *nzval, int base,
                          const void *x, void *y, const void *alpha, const void *beta);
+
+/* ---- plans ----------------------------------------------------------------
+ * A plan records which outer entries of one compressed structure (rows of a CSR
+ * pointer array, columns of a CSC one) hold more than 512 stored entries, cut into
+ * chunks of 512 entries.  With a plan, the row gather (CSR opA = N, CSC opA = T/C)
+ * sums such long entries chunk by chunk across the whole GPU instead of one warp
+ * per long entry -- what power-law row lengths need; without long entries a plan
+ * changes nothing.  Creating one copies the pointer array to the host once and
+ * synchronizes the stream; the plan holds one device allocation until destroyed.
+ * The structure must not change while its plan is in use.  No counterpart in the
+ * reference (its kernels take one work item per row). */
+typedef struct gsa_plan gsa_plan;
+int gsa_plan_create(void *stream, int itype, int64_t outer_n, int64_t nnz, const void *ptr,
+                    int base, gsa_plan **out);
+int gsa_plan_destroy(gsa_plan *plan);
+/* Longest outer entry, number of long entries and of their chunks. */
+int gsa_plan_info(const gsa_plan *plan, int64_t *max_len, int64_t *nlong, int64_t *nchunks);
+/* Workspace bytes of a planned call with k right-hand sides (0 without long entries). */
+size_t gsa_plan_workspace_size(const gsa_plan *plan, int dtype, int64_t k);
+
+/* gsa_csr_mul / gsa_csc_mul with a plan of the same structure (replace the same
+ * reference methods).  The plan applies to the gather directions (CSR opA = N,
+ * CSC opA = T/C); other directions ignore it.  NULL plan = plain call. */
+int gsa_csr_mul_planned(void *stream, int dtype, int itype, int64_t m, int64_t n, int64_t nnz,
+                        const void *rowptr, const void *colval, const void *nzval, int base, int opA,
+                        int64_t k, const void *B, int64_t ldb, int opB, void *C, int64_t ldc,
+                        const void *alpha, const void *beta, const gsa_plan *plan, void *workspace,
+                        size_t workspace_bytes);
+int gsa_csc_mul_planned(void *stream, int dtype, int itype, int64_t m, int64_t n, int64_t nnz,
+                        const void *colptr, const void *rowval, const void *nzval, int base, int opA,
+                        int64_t k, const void *B, int64_t ldb, int opB, void *C, int64_t ldc,
+                        const void *alpha, const void *beta, const gsa_plan *plan, void *workspace,
+                        size_t workspace_bytes);
 
 /* Workspace bytes for gsa_csr_mul / gsa_csc_mul with these sizes (format:
  * 0 CSR, 1 CSC).  0 means none is needed. */
