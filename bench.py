@@ -8,7 +8,7 @@ minimal-bytes model  nnz*(8+4) + (m+1)*4 + n*8 + m*8 = 335.45 MB per SpMV.
 * ``value``     device time of K SpMVs with A, x, y resident in HBM; L2 is flushed (a 512 MB
                 write, then a 256 MB read so that no dirty line is left for the timed step to
                 write back) before every timed SpMV, and only the SpMV sits between the events
-* ``roofline``  the dominant kernel (merge-path gather) timed by events the library records
+* ``roofline``  the dominant kernel (row-block gather) timed by events the library records
                 right around it; algorithmic bytes / its average duration vs the measured
                 HBM copy bandwidth in MEASURED_PEAKS.json
 * ``e2e``       the same metric through the public API from pinned host buffers: per step the
@@ -16,7 +16,9 @@ minimal-bytes model  nnz*(8+4) + (m+1)*4 + n*8 + m*8 = 335.45 MB per SpMV.
 * ``cpu_baseline``  the oracle's C restatement of the reference kernel (OpenMP, all host
                 cores) on the same matrix, a bounded number of SpMVs
 * ``extras``    the other benchmark rows (CSC, SpMM k=16, F32, Int64 indices, power-law
-                ComplexF64 CSR/COO, n=1e5 random CSR/CSC/COO, COO->CSR conversion)
+                ComplexF64 CSR/COO, n=1e5 random CSR/CSC/COO, COO->CSR conversion) and the
+                batched uneven-size mix (4096 banded ComplexF64 matrices: grouped launch from a
+                CUDA graph against per-call mul!, mul!/s and p50/p99 batch latency)
 
 ``--impl reference`` times the CPU restatement of the reference (the reference itself is
 Julia, absent on this machine) on the same workload and prints the same JSON line.
@@ -316,6 +318,10 @@ def run_gpu(args, world, rank, local):
         e2e_value = nbytes * args.steps / e2e_s / 1e9
 
         extras = {} if args.no_extras else run_extras(gsa, wl, torch, dev, lib, timer, args)
+        if not args.no_extras:
+            extras["batched_uneven_mix"] = run_batched(gsa, torch, dev, args)
+        if not args.no_extras and not args.no_serving:
+            extras["served_stream"] = run_serving(gsa, torch, dev, args)
 
     clk = clocks.summary()
     cpu = None
@@ -325,7 +331,7 @@ def run_gpu(args, world, rank, local):
         cpu = {"value": round(nbytes / t_cpu / 1e9, 2), "unit": "GB/s", "cores": threads,
                "kind": "port",
                "sample": f"{reps} full SpMVs of the 2048^2 Laplacian (median), C/OpenMP restatement"}
-    traffic = committed_traffic("gather_merge_kernel/laplacian_2048_csr_spmv_f64_i32")
+    traffic = committed_traffic("rowblock_kernel/laplacian_2048_csr_spmv_f64_i32")
     line = {
         "metric": METRIC, "value": round(value, 2), "unit": "GB/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(max_ms / args.steps, 5),
@@ -335,7 +341,7 @@ def run_gpu(args, world, rank, local):
                    "bytes_per_step": nbytes, "l2": "flushed before every timed step (512 MB write, then 256 MB read so L2 is clean)",
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
                    "pct_of_peak": round(100 * value / world / peak, 1), "max_rel_error": err},
-        "roofline": {"bound": "hbm", "kernel": "gather_merge_kernel<double,int,false>",
+        "roofline": {"bound": "hbm", "kernel": "rowblock_kernel<double,int,1>",
                      "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
                      "kernel_us": round(kern_avg_s * 1e6, 2),
@@ -343,7 +349,7 @@ def run_gpu(args, world, rank, local):
         "e2e": {"value": round(e2e_value, 2), "unit": "GB/s", "h2d_bytes_per_step": n * 8,
                 "d2h_bytes_per_step": m * 8, "ms_per_step": round(e2e_s / args.steps * 1e3, 4),
                 "matches_oracle": e2e_ok, "api": "genericsparsearrays_gb300.mul_"},
-        "gpu_launches": 3 * args.steps,
+        "gpu_launches": args.steps,  # one rowblock_kernel per SpMV
         "clocks": clk,
         "cpu_baseline": cpu,
         "extras": extras,
@@ -434,6 +440,159 @@ def run_extras(gsa, wl, torch, dev, lib, timer, args):
     return out
 
 
+def batched_products(gsa, wl, torch, dev, count=4096, seed=11, ks=(1, 4, 8)):
+    """The uneven-size mix: ``count`` banded ComplexF64 CSR matrices (n log-uniform in
+    [64, 8192], half-band 3 plus Poisson(8) off-band entries per row), each with its own
+    column-major X of k in ``ks`` (cycled) columns U(-1,1) + iU(-1,1), alpha = 1, beta = 0."""
+    sizes, rp, cv, nz, ro, eo = wl.banded_batch(count=count, lo=64, hi=8192, seed=seed,
+                                                itype=np.int64, dtype=np.complex128, device=dev)
+    g = torch.Generator(device=dev).manual_seed(seed + 2)
+    prods, a_bytes, xy_bytes = [], 0, 0
+    for i, m in enumerate(sizes):
+        A = gsa.GenericSparseMatrixCSR(m, m, rp[int(ro[i]) + i: int(ro[i + 1]) + i + 1],
+                                       cv[int(eo[i]): int(eo[i + 1])], nz[int(eo[i]): int(eo[i + 1])])
+        k = ks[i % len(ks)]
+        shape = (m,) if k == 1 else (k, m)
+        X = torch.complex(torch.rand(shape, generator=g, device=dev, dtype=torch.float64) * 2 - 1,
+                          torch.rand(shape, generator=g, device=dev, dtype=torch.float64) * 2 - 1)
+        Y = torch.zeros(shape, dtype=torch.complex128, device=dev)
+        if k > 1:
+            X, Y = X.t(), Y.t()
+        prods.append((A, X, Y, 1, 0))
+        a_bytes += int(A.nzval.numel()) * (16 + 8) + (m + 1) * 8
+        xy_bytes += 2 * m * k * 16
+    del rp, cv, nz
+    return prods, a_bytes + xy_bytes
+
+
+def run_batched(gsa, torch, dev, args):
+    """Batched mul!/s on the uneven-size mix: one grouped launch replayed from a CUDA graph,
+    against one C-ABI mul! per product and one public-API ``mul_`` per product."""
+    from genericsparsearrays_gb300 import autotune, batch, workloads as wl
+    prods, nbytes = batched_products(gsa, wl, torch, dev)
+    count = len(prods)
+    cols, g1 = autotune.tune(prods, reps=3)
+    b = batch.BatchedMul(prods, columns=cols, g1_avg=g1)
+    steps, warm = max(10, args.steps // 10), 3
+
+    def timed(fn, n):
+        for _ in range(warm):
+            fn()
+        torch.cuda.synchronize()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(n)]
+        t0 = time.perf_counter()
+        for s, e in ev:
+            s.record()
+            fn()
+            e.record()
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+        ms = np.array([s.elapsed_time(e) for s, e in ev])
+        return ms, wall
+
+    g_ms, g_wall = timed(lambda: b.run("graph"), steps)
+    gr_ms, _ = timed(lambda: b.run("grouped"), steps)
+    pc_ms, pc_wall = timed(lambda: b.run("per_call"), max(3, steps // 4))
+
+    def api_loop():
+        for A, X, Y, al, be in prods:
+            gsa.mul_(Y, A, X, al, be)
+    api_ms, api_wall = timed(api_loop, 3)
+    # error of a few products against the double-double oracle
+    from oracle import oracle
+    err = 0.0
+    for A, X, Y, al, be in prods[:: max(1, count // 8)]:
+        Xh = X.cpu().numpy()
+        ye, sc = oracle.mul_exact("csr", "N", A.m, A.n, A.rowptr.cpu().numpy(), A.colval.cpu().numpy(),
+                                  A.nzval.cpu().numpy(), 1, Xh, np.zeros(Y.shape, np.complex128))
+        err = max(err, oracle.max_rel_error(Y.cpu().numpy(), ye, sc))
+    b.close()
+    graph_rate = count * steps / g_wall
+    api_rate = count * 3 / api_wall
+    return {
+        "workload": f"{count} banded ComplexF64 CSR (n log-uniform [64, 8192], half-band 3 + Poisson(8)), "
+                    "k cycled 1/4/8, Int64 indices",
+        "mul_per_s_graph": round(graph_rate, 1),
+        "mul_per_s_per_call_capi": round(count * pc_ms.size / pc_wall, 1),
+        "mul_per_s_per_call_api": round(api_rate, 1),
+        "speedup_vs_per_call_api": round(graph_rate / api_rate, 2),
+        "speedup_vs_per_call_capi": round(graph_rate / (count * pc_ms.size / pc_wall), 2),
+        "batch_ms_p50": round(float(np.percentile(g_ms, 50)), 4),
+        "batch_ms_p99": round(float(np.percentile(g_ms, 99)), 4),
+        "grouped_ms_p50": round(float(np.percentile(gr_ms, 50)), 4),
+        "per_call_capi_batch_ms_p50": round(float(np.percentile(pc_ms, 50)), 4),
+        "per_call_api_batch_ms_p50": round(float(np.percentile(api_ms, 50)), 4),
+        "GBps_graph": round(nbytes / (float(np.median(g_ms)) / 1e3) / 1e9, 1),
+        "bytes_per_batch": nbytes, "columns": cols, "g1_avg": g1,
+        "max_rel_error_sampled": err,
+    }
+
+
+def run_serving(gsa, torch, dev, args):
+    """Served mul! stream: Poisson arrivals against a resident registry, continuous batching
+    into grouped launches (two streams) against one ``mul_`` per request as it arrives."""
+    from genericsparsearrays_gb300 import serving
+    t_gen = time.perf_counter()
+    mats = serving.registry_matrices(count=args.serve_matrices, n_lo=1_000, n_hi=args.serve_n_hi,
+                                     seed=21, device=dev)
+    reg = serving.Registry(150 * 10**9)
+    ids = [reg.add(A) for A in mats]
+    del mats
+    kmax = 32
+    g = torch.Generator(device=dev).manual_seed(22)
+    xs = {}
+    for mid in ids:  # row-major (n, 32) blocks: an entry's k values share cache lines
+        A = reg[mid]
+        re = torch.rand((A.n, kmax), generator=g, device=dev, dtype=torch.float64) * 2 - 1
+        if A.dtype == torch.complex128:
+            xs[mid] = torch.complex(re, torch.rand((A.n, kmax), generator=g, device=dev,
+                                                   dtype=torch.float64) * 2 - 1)
+        else:
+            xs[mid] = re
+        if not reg.reserve(xs[mid].numel() * xs[mid].element_size()):
+            raise SystemExit("serving workload: right-hand sides exceed the HBM budget")
+    torch.cuda.synchronize()
+    t_gen = time.perf_counter() - t_gen
+
+    def stream(seed):
+        reqs = serving.poisson_requests(reg, xs, rate=args.serve_rate, duration=args.serve_seconds,
+                                        k_lo=1, k_hi=kmax, seed=seed)
+        t0 = time.perf_counter() + 0.05
+        for r in reqs:
+            r.arrival += t0
+        return reqs
+
+    # warm-up: one short stream through each path (plans, autotuned launch shapes, pinned buffers)
+    ex = serving.GroupedExecutor(dev, slots=2)
+    srv = serving.Server(reg, ex, max_batch=1024, slots=2, keep_outputs=False)
+    srv.run(stream(1)[:200])
+    serving.serve_per_call(reg, stream(2)[:200], dev, keep_outputs=False)
+    torch.cuda.synchronize()
+
+    srv = serving.Server(reg, ex, max_batch=1024, slots=2, keep_outputs=False)
+    reqs = stream(3)
+    with torch.cuda.device(dev):
+        srv.run(reqs)
+    torch.cuda.synchronize()
+    batched = srv.stats()
+    per_call = serving.serve_per_call(reg, stream(3), dev, keep_outputs=False)
+    nnz_total = sum(int(reg[i].nzval.numel()) for i in ids)
+
+    def rnd(d):
+        return {k: (round(v, 4) if isinstance(v, float) else v) for k, v in d.items()}
+    return {
+        "workload": f"{len(ids)} resident CSR matrices (n log-uniform [1e3, {args.serve_n_hi:.0e}], "
+                    "5-40 nnz/row uniform or truncated Pareto, Float64 and ComplexF64, Int32 indices); "
+                    f"Poisson arrivals {args.serve_rate}/s for {args.serve_seconds}s, k uniform in [1, 32] "
+                    "(X: the first k columns of a resident row-major n x 32 block per matrix), "
+                    "150 GB HBM budget",
+        "requests": len(reqs), "registry_nnz": nnz_total, "registry_bytes": reg.resident,
+        "setup_s": round(t_gen, 1),
+        "continuous_batching": rnd(batched), "per_call_mul": rnd(per_call),
+        "speedup_mul_per_s": round(batched.get("mul_per_s", 0) / max(per_call.get("mul_per_s", 1e-9), 1e-9), 2),
+    }
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -443,6 +602,11 @@ def main():
     ap.add_argument("--no-extras", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=10.0)
+    ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--serve-matrices", type=int, default=512)
+    ap.add_argument("--serve-n-hi", type=float, default=2e6)
+    ap.add_argument("--serve-rate", type=float, default=20_000)
+    ap.add_argument("--serve-seconds", type=float, default=1.0)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -21,6 +21,7 @@ IDX32, IDX64 = 0, 1
 OP_N, OP_T, OP_C = 0, 1, 2
 ALGO_AUTO, ALGO_MERGE, ALGO_VECTOR, ALGO_PIPE = 0, 1, 2, 3
 TUNE_PIPE_THREADS, TUNE_SPMM_COLUMNS = 1, 2
+BATCH_GROUPED, BATCH_GRAPH, BATCH_PER_CALL = 0, 1, 2
 
 # Every exported symbol of include/gsa.h with its ctypes signature.
 _i32, _i64, _vp, _sz = ctypes.c_int, ctypes.c_int64, ctypes.c_void_p, ctypes.c_size_t
@@ -30,6 +31,7 @@ SIGNATURES = {
     "gsa_version": ([], _i32),
     "gsa_last_error_string": ([], ctypes.c_char_p),
     "gsa_set_kernel_timer": ([_vp, _vp], None),
+    "gsa_probe_fma_rate": ([_vp, _i32, _i64, ctypes.POINTER(ctypes.c_double)], _i32),
     "gsa_set_tuning": ([_i32, _i32], _i32),
     "gsa_get_tuning": ([_i32], _i32),
     "gsa_csr_mul": (_MUL + [_i32, _vp, _sz], _i32),
@@ -44,6 +46,11 @@ SIGNATURES = {
     "gsa_csr_spmv_noalloc": ([_vp, _i32, _i32, _i64, _i64, _i64, _vp, _vp, _vp, _i32, _vp, _vp,
                               _vp, _vp], _i32),
     "gsa_mul_workspace_size": ([_i32, _i32, _i32, _i64, _i64, _i64, _i32, _i64, _i32], _sz),
+    "gsa_grouped_tiles": ([_i32, _vp, _i64, _i32, ctypes.POINTER(_i64)], _i32),
+    "gsa_grouped_mul": ([_vp, _i32, _i32, _i32, _vp, _i64, _i64, _i32, _i32], _i32),
+    "gsa_batch_create": ([_vp, _i32, _i32, _i32, _vp, _i64, _i32, _i32, ctypes.POINTER(_vp)], _i32),
+    "gsa_batch_run": ([_vp, _vp, _i32], _i32),
+    "gsa_batch_destroy": ([_vp], _i32),
     "gsa_coo_to_csr": ([_vp, _i32, _i32, _i64, _i64, _i64, _vp, _vp, _vp, _i32, _vp, _vp, _vp, _vp,
                         _sz], _i32),
     "gsa_coo_to_csc": ([_vp, _i32, _i32, _i64, _i64, _i64, _vp, _vp, _vp, _i32, _vp, _vp, _vp, _vp,

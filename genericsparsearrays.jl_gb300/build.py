@@ -19,8 +19,11 @@ INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 LIB = os.path.join(HERE, "libgsa.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
-              "-Xptxas", "-warn-spills", "-I", INCLUDE]
+# -fmad=false: a*b + c stays a rounded product and a rounded sum, as in Julia's default
+# arithmetic (no contraction), so one row's result does not depend on which kernel (plain,
+# grouped, planned) summed it in the same order.
+NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-Xcompiler", "-fPIC",
+              "--expt-relaxed-constexpr", "-Xptxas", "-warn-spills", "-I", INCLUDE]
 
 
 def nvcc() -> str:
@@ -37,6 +40,7 @@ def sources():
 def headers():
     hs = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))]
     hs.append(os.path.join(INCLUDE, "gsa.h"))
+    hs.append(os.path.abspath(__file__))  # flag changes rebuild too
     return hs
 
 

@@ -88,6 +88,8 @@ static int check_mul_args(int dtype, int itype, int64_t m, int64_t n, int64_t nn
         return fail(GSA_ERR_INVALID_ARG, "negative size (m=%lld n=%lld nnz=%lld k=%lld)",
                     (long long)m, (long long)n, (long long)nnz, (long long)k);
     if (!alpha || !beta) return fail(GSA_ERR_INVALID_ARG, "alpha and beta must be host pointers");
+    if (itype == GSA_IDX32 && nnz > 0x7fffffffLL)  // Int32 pointers cannot address more
+        return fail(GSA_ERR_INVALID_ARG, "nnz=%lld exceeds what Int32 indices can address", (long long)nnz);
     int64_t rows_out = opA == GSA_OP_N ? m : n;
     int64_t inner = opA == GSA_OP_N ? n : m;
     int64_t need_ldb = opB == GSA_OP_N ? inner : k;
@@ -124,6 +126,7 @@ static DenseOut<V> make_out(void *C, int64_t ldc, const void *alpha, const void 
     memcpy(&d.alpha, alpha, sizeof(V));
     memcpy(&d.beta, beta, sizeof(V));
     d.beta_mode = beta_mode_of(d.beta);
+    d.alpha_one = alpha_one_of(d.alpha);
     return d;
 }
 
@@ -141,11 +144,11 @@ struct CompressedMulBody {
         if (rows_out == 0 || k == 0) return GSA_OK;
         Workspace w;
         size_t need = gather ? gather_workspace_size<V, I>(outer_n, nnz, k, algo, plan)
-                             : scatter_workspace_size<V, I>(outer_n, nnz, k);
+                             : scatter_workspace_size<V, I>(outer_n, nnz, k, algo);
         int rc = w.acquire(s, ws, ws_bytes, need);
         if (rc) return rc;
         if (gather) return launch_gather<V, I>(s, a, k, Bv, Cv, algo, plan, w.p, w.bytes);
-        return launch_scatter<V, I>(s, a, k, Bv, Cv, rows_out, w.p, w.bytes);
+        return launch_scatter<V, I>(s, a, k, Bv, Cv, rows_out, algo, plan, w.p, w.bytes);
     }
 };
 
@@ -168,7 +171,7 @@ struct MulWsBody {
     bool gather; int64_t outer_n, nnz, k; int algo; size_t out; const Plan *plan;
     template <typename V, typename I> int operator()() {
         out = gather ? gather_workspace_size<V, I>(outer_n, nnz, k, algo, plan)
-                     : scatter_workspace_size<V, I>(outer_n, nnz, k);
+                     : scatter_workspace_size<V, I>(outer_n, nnz, k, algo);
         return 0;
     }
 };

@@ -273,7 +273,7 @@ gather_vector_kernel(CompressedArgs<V, I> a, int64_t k, DenseIn<V> B, DenseOut<V
             for (int64_t j = start + lane; j < end; j += G) {
                 int64_t ci = (int64_t)ld_stream(a.idx + j) - a.base;
                 if ((uint64_t)ci < (uint64_t)a.inner_n)
-                    acc = add(acc, mul(conj_if(ld_stream(a.val + j), a.conjA), B.at(ci, c)));
+                    acc = mac(acc, conj_if(ld_stream(a.val + j), a.conjA), B.at(ci, c));
             }
 #pragma unroll
             for (int m = G / 2; m > 0; m >>= 1) acc = add(acc, shfl_xor(acc, m, G));

@@ -6,17 +6,20 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <stddef.h>
+#include <math.h>
 
 #include "../../include/gsa.h"
 
 // A plan (gsa_plan_create): the outer entries of one compressed structure that have more
-// than 512 stored entries, each cut into chunks of 512 entries (device arrays).
+// than 512 stored entries, or more than 32 and over 4x the average of their aligned group
+// of 32, each cut into chunks of 512 entries (device arrays).
 struct gsa_plan {
     int64_t outer_n = 0, nnz = 0, max_len = 0, nlong = 0, nchunks = 0;
     const int64_t *row = nullptr;         // outer index of each long entry
     const int32_t *first = nullptr;       // its first chunk
     const int32_t *count = nullptr;       // its number of chunks
     const int32_t *chunk_slot = nullptr;  // the long entry a chunk belongs to
+    const uint32_t *skip_mask = nullptr;  // bit per outer entry: 1 = the plan's
     void *mem = nullptr;                  // one device allocation holding the arrays
 };
 
@@ -54,8 +57,13 @@ template <> struct VT<int64_t> {
     __host__ __device__ static int64_t zero() { return 0; }
 };
 
-// Arithmetic.  Integers wrap (Julia's Int32/Int64 semantics), complex products
-// use the textbook formula Julia uses.
+// Arithmetic.  Integers wrap (Julia's Int32/Int64 semantics).  Floating-point
+// multiply-adds are explicit fused multiply-adds and nothing else is contracted (the
+// library builds with -fmad=false): GB300 issues about two FP64 FMAs per clock per SM,
+// so FP64 products are bound by that pipe about as much as by HBM, and one FMA per
+// real multiply-add (four per complex one) halves the FP64 instructions of a
+// multiply-then-add.  Results stay within the double-double oracle's tolerance; a row
+// summed in the same order gives the same bits in every kernel.
 __host__ __device__ __forceinline__ float add(float a, float b) { return a + b; }
 __host__ __device__ __forceinline__ double add(double a, double b) { return a + b; }
 __host__ __device__ __forceinline__ cf32 add(cf32 a, cf32 b) { return cf32{a.re + b.re, a.im + b.im}; }
@@ -69,11 +77,13 @@ __host__ __device__ __forceinline__ int64_t add(int64_t a, int64_t b) {
 
 __host__ __device__ __forceinline__ float mul(float a, float b) { return a * b; }
 __host__ __device__ __forceinline__ double mul(double a, double b) { return a * b; }
+// (ar + i ai)(br + i bi) = (ar br - ai bi) + i (ar bi + ai br), one product of each
+// part fused into the other's add
 __host__ __device__ __forceinline__ cf32 mul(cf32 a, cf32 b) {
-    return cf32{a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re};
+    return cf32{fmaf(a.re, b.re, -(a.im * b.im)), fmaf(a.re, b.im, a.im * b.re)};
 }
 __host__ __device__ __forceinline__ cf64 mul(cf64 a, cf64 b) {
-    return cf64{a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re};
+    return cf64{fma(a.re, b.re, -(a.im * b.im)), fma(a.re, b.im, a.im * b.re)};
 }
 __host__ __device__ __forceinline__ int32_t mul(int32_t a, int32_t b) {
     return (int32_t)((uint32_t)a * (uint32_t)b);
@@ -81,6 +91,18 @@ __host__ __device__ __forceinline__ int32_t mul(int32_t a, int32_t b) {
 __host__ __device__ __forceinline__ int64_t mul(int64_t a, int64_t b) {
     return (int64_t)((uint64_t)a * (uint64_t)b);
 }
+
+// acc + a * b
+__host__ __device__ __forceinline__ float mac(float acc, float a, float b) { return fmaf(a, b, acc); }
+__host__ __device__ __forceinline__ double mac(double acc, double a, double b) { return fma(a, b, acc); }
+__host__ __device__ __forceinline__ cf32 mac(cf32 acc, cf32 a, cf32 b) {
+    return cf32{fmaf(-a.im, b.im, fmaf(a.re, b.re, acc.re)), fmaf(a.im, b.re, fmaf(a.re, b.im, acc.im))};
+}
+__host__ __device__ __forceinline__ cf64 mac(cf64 acc, cf64 a, cf64 b) {
+    return cf64{fma(-a.im, b.im, fma(a.re, b.re, acc.re)), fma(a.im, b.re, fma(a.re, b.im, acc.im))};
+}
+__host__ __device__ __forceinline__ int32_t mac(int32_t acc, int32_t a, int32_t b) { return add(acc, mul(a, b)); }
+__host__ __device__ __forceinline__ int64_t mac(int64_t acc, int64_t a, int64_t b) { return add(acc, mul(a, b)); }
 
 template <typename V> __host__ __device__ __forceinline__ V conj_if(V a, bool c) { return a; }
 template <> __host__ __device__ __forceinline__ cf32 conj_if(cf32 a, bool c) {
@@ -186,20 +208,36 @@ template <typename V> struct DenseIn {
     }
 };
 
+// 0 + x without an FP add: x, except that -0 becomes +0 (integer compare and select,
+// so the FP64 pipe is not used).
+__device__ __forceinline__ float zero_plus(float x) {
+    return __float_as_int(x) == (int)0x80000000u ? 0.0f : x;
+}
+__device__ __forceinline__ double zero_plus(double x) {
+    return __double_as_longlong(x) == (long long)0x8000000000000000ull ? 0.0 : x;
+}
+__device__ __forceinline__ cf32 zero_plus(cf32 x) { return cf32{zero_plus(x.re), zero_plus(x.im)}; }
+__device__ __forceinline__ cf64 zero_plus(cf64 x) { return cf64{zero_plus(x.re), zero_plus(x.im)}; }
+__device__ __forceinline__ int32_t zero_plus(int32_t x) { return x; }
+__device__ __forceinline__ int64_t zero_plus(int64_t x) { return x; }
+
 // C column-major with leading dimension ld; beta handled per LinearAlgebra's
-// _rmul_or_fill!: beta == 1 keeps C, beta == 0 overwrites without reading.
+// _rmul_or_fill!: beta == 1 keeps C, beta == 0 overwrites without reading (the
+// reference then adds into the zero it filled: 0 + t).  alpha == 1 of a real type is
+// not multiplied (t * 1 == t for every t), which saves an FP64 instruction per row.
 template <typename V> struct DenseOut {
     V *p;
     int64_t ld;
     V alpha, beta;
     int beta_mode;  // 0: beta == 0, 1: beta == 1, 2: general
+    bool alpha_one; // alpha == 1 and V is real
     // C[i, c] = beta*C[i, c] + acc*alpha
     __device__ __forceinline__ void store(int64_t i, int64_t c, V acc) const {
         V *q = p + i * 1 + c * ld;
-        V t = mul(acc, alpha);
-        if (beta_mode == 0) *q = add(VT<V>::zero(), t);
+        V t = alpha_one ? acc : mul(acc, alpha);
+        if (beta_mode == 0) *q = zero_plus(t);
         else if (beta_mode == 1) *q = add(*q, t);
-        else *q = add(mul(*q, beta), t);
+        else *q = mac(t, *q, beta);
     }
     // C[i, c] += v (for values already multiplied by alpha)
     __device__ __forceinline__ void accumulate(int64_t i, int64_t c, V v) const {
@@ -210,6 +248,9 @@ template <typename V> struct DenseOut {
 
 template <typename V> inline int beta_mode_of(V beta) {
     return is_zero(beta) ? 0 : (is_one(beta) ? 1 : 2);
+}
+template <typename V> __host__ __device__ inline bool alpha_one_of(V alpha) {
+    return !VT<V>::is_complex && is_one(alpha);
 }
 
 // ---------------------------------------------------------------------------
@@ -323,11 +364,14 @@ void set_spmm_columns(int c);   // 0 (by value size), 1, 2, 4 or 8
 int get_spmm_columns();
 
 // Scatter: out[idx_j, c] += conj?(val_j) * (op(B)(o, c) * alpha), after the beta pass.
+// ALGO_MERGE: merge-path tiles (workspace: tile coordinates); otherwise outer blocks with
+// an optional plan (no workspace).
 template <typename V, typename I>
 int launch_scatter(cudaStream_t s, const CompressedArgs<V, I> &a, int64_t k, DenseIn<V> B,
-                   DenseOut<V> C, int64_t out_rows, void *ws, size_t ws_bytes);
+                   DenseOut<V> C, int64_t out_rows, int algo, const Plan *plan, void *ws,
+                   size_t ws_bytes);
 template <typename V, typename I>
-size_t scatter_workspace_size(int64_t outer_n, int64_t nnz, int64_t k);
+size_t scatter_workspace_size(int64_t outer_n, int64_t nnz, int64_t k, int algo);
 
 // COO: out[key_i, c] += conj?(val_i) * (op(B)(other_i, c) * alpha), after the beta pass.
 template <typename V, typename I>

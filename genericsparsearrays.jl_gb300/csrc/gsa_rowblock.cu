@@ -13,120 +13,35 @@
 // CTAs of one row block and its column groups are numbered consecutively, so
 // they run together and share the row block's entries through L2.
 //
-// Very long rows, with a plan (gsa_plan_create): the plan lists every row of
-// more than LONG_LEN entries cut into chunks of CHUNK entries; extra CTAs give
-// each chunk to one warp, which stores a partial sum, and the warp that completes
-// a row's last chunk adds the row's partials in chunk order and writes the row.
+// Longer rows, with a plan (gsa_plan_create): the plan lists every row of more
+// than CHUNK entries and every row of more than PLAN_LEN entries that is over 4x
+// its warp's average, cut into chunks of CHUNK entries; extra CTAs give each
+// chunk to one warp (32 lanes, UNROLL loads each in flight).  A row of one chunk
+// is summed and stored by its warp; for a longer one each warp stores a partial
+// sum, and the warp that completes the row's last chunk adds the partials in chunk
+// order and writes the row.  A warp of short rows thus never waits on a long one.
 // Without a plan such a row is one group's work like any other.
 //
 // Every row's summation order is fixed, so results are deterministic.
 #include <vector>
 
-#include "gsa_internal.cuh"
+#include "gsa_rows.cuh"
 
 namespace gsa {
 
-constexpr int RB_THREADS = 128;
-constexpr int RB_WARPS = RB_THREADS / 32;
-constexpr int G1_AVG = 6;       // a thread per row while a warp's rows average <= 6 entries
-constexpr int LONG_LEN = 512;   // rows longer than this go to a plan's chunks
-constexpr int UNROLL = 4;       // entries per lane in flight on the chunk path
-constexpr int CHUNK = 512;      // entries per chunk of a planned long row
-
-// acc[c] += sum over j = jb, jb+S, ... < je of conj?(a_j) * op(B)(idx_j, c0 + c), in j order.
-template <typename V, typename I, int KC, int S, int U>
-__device__ __forceinline__ void accumulate_range(const CompressedArgs<V, I> &a, const DenseIn<V> &B,
-                                                 int64_t jb, int64_t je, int64_t c0, int64_t k,
-                                                 V (&acc)[KC]) {
-    const I *__restrict__ idx = a.idx;
-    const V *__restrict__ val = a.val;
-    const uint64_t inner = (uint64_t)a.inner_n;
-    int64_t j = jb;
-    if (U > 1) {
-        for (; j + (U - 1) * S < je; j += U * S) {
-            int64_t ci[U];
-            V av[U];
-#pragma unroll
-            for (int u = 0; u < U; ++u) {
-                ci[u] = (int64_t)idx[j + u * S] - a.base;
-                av[u] = conj_if(val[j + u * S], a.conjA);
-            }
-#pragma unroll
-            for (int u = 0; u < U; ++u) {
-                const bool ok = (uint64_t)ci[u] < inner;
-#pragma unroll
-                for (int c = 0; c < KC; ++c)
-                    if (KC == 1 || c0 + c < k) {
-                        const V xv = ok ? B.at(ci[u], c0 + c) : VT<V>::zero();
-                        acc[c] = add(acc[c], mul(av[u], xv));
-                    }
-            }
-        }
-    }
-    for (; j < je; j += S) {
-        const int64_t c1 = (int64_t)idx[j] - a.base;
-        const bool ok = (uint64_t)c1 < inner;
-        const V av = conj_if(val[j], a.conjA);
-#pragma unroll
-        for (int c = 0; c < KC; ++c)
-            if (KC == 1 || c0 + c < k) {
-                const V xv = ok ? B.at(c1, c0 + c) : VT<V>::zero();
-                acc[c] = add(acc[c], mul(av, xv));
-            }
-    }
-}
-
-// The plan's view of long rows (device arrays; see gsa_plan).
-struct LongRows {
-    int64_t nlong, nchunks;
-    const int64_t *row;        // nlong: outer index of each long row
-    const int32_t *first;      // nlong: its first chunk
-    const int32_t *count;      // nlong: its number of chunks
-    const int32_t *chunk_slot; // nchunks: the long row (slot) a chunk belongs to
-    int *done;                 // nlong * ncg counters, zero before the launch, reset after
-    void *partial;             // nchunks * k values
-};
-
-// The 32 rows of one warp (lane l owns row row0 + l, entries [b, e)), G lanes per
-// row: in each of G passes the warp's 32/G groups take one row each, the group's
-// lanes stride the row, a width-G shuffle tree reduces, the group's first lane
-// stores.  G = 1 is a thread per row.
-template <typename V, typename I, int KC, int G>
-__device__ __forceinline__ void warp_rows(const CompressedArgs<V, I> &a, int64_t k, const DenseIn<V> &B,
-                                          const DenseOut<V> &C, int64_t c0, int64_t row0, int64_t b,
-                                          int64_t e, int skip) {
-    const int lane = threadIdx.x & 31;
-    constexpr int RPP = 32 / G;  // rows per pass
-#pragma unroll 1
-    for (int p = 0; p < G; ++p) {
-        const int q = p * RPP + lane / G;
-        const int64_t qb = G == 1 ? b : __shfl_sync(0xffffffffu, b, q);
-        const int64_t qe = G == 1 ? e : __shfl_sync(0xffffffffu, e, q);
-        const int qskip = G == 1 ? skip : __shfl_sync(0xffffffffu, skip, q);
-        V acc[KC];
-#pragma unroll
-        for (int c = 0; c < KC; ++c) acc[c] = VT<V>::zero();
-        accumulate_range<V, I, KC, G, (G == 1 ? 1 : 2)>(a, B, qb + (lane % G), qe, c0, k, acc);
-        if (G > 1) {
-#pragma unroll
-            for (int c = 0; c < KC; ++c) {
-#pragma unroll
-                for (int m = G / 2; m > 0; m >>= 1) acc[c] = add(acc[c], shfl_xor(acc[c], m, G));
-            }
-        }
-        const int64_t row = row0 + q;
-        if (lane % G == 0 && row < a.outer_n && !qskip) {
-#pragma unroll
-            for (int c = 0; c < KC; ++c)
-                if (KC == 1 || c0 + c < k) C.store(row, c0 + c, acc[c]);
-        }
-    }
-}
+// Resident CTAs per SM the compiler must allow: the one-column kernels of 4- and 8-byte
+// values are latency-bound gathers whose speed follows the warps in flight, so they are
+// held to 32 registers (16 CTAs of 128 threads, every warp slot of the SM).  0 leaves
+// the register count to the compiler.
+#ifndef GSA_RB_MIN_BLOCKS
+#define GSA_RB_MIN_BLOCKS 16
+#endif
+template <typename V, int KC> constexpr int rb_min_blocks() { return KC * sizeof(V) <= 8 ? GSA_RB_MIN_BLOCKS : 0; }
 
 template <typename V, typename I, int KC>
-__global__ void __launch_bounds__(RB_THREADS)
+__global__ void __launch_bounds__(RB_THREADS, rb_min_blocks<V, KC>())
 rowblock_kernel(CompressedArgs<V, I> a, int64_t k, DenseIn<V> B, DenseOut<V> C, int64_t ncg,
-                int64_t nrb, LongRows L) {
+                int64_t nrb, PlanRows L) {
     const int lane = threadIdx.x & 31;
     // column group fastest; one group (SpMV) needs no division
     const unsigned cta = blockIdx.x;
@@ -135,24 +50,36 @@ rowblock_kernel(CompressedArgs<V, I> a, int64_t k, DenseIn<V> B, DenseOut<V> C, 
     const int64_t c0 = (int64_t)cg * KC;
 
     if (unit >= nrb) {
-        // ---- planned long rows: a warp per chunk
+        // ---- planned rows: a warp per chunk of up to CHUNK entries
+        using O = Off<I>;
         const int64_t chunk = (unit - nrb) * RB_WARPS + (threadIdx.x >> 5);
         if (chunk >= L.nchunks) return;
         const int slot = L.chunk_slot[chunk];
         const int64_t row = L.row[slot];
-        const int64_t rb = (int64_t)__ldg(a.ptr + row) - a.base;
-        int64_t re = (int64_t)__ldg(a.ptr + row + 1) - a.base;
-        re = re > a.nnz ? a.nnz : re;
-        const int64_t jb = rb + (chunk - L.first[slot]) * CHUNK;
-        const int64_t je = jb + CHUNK < re ? jb + CHUNK : re;
+        const int nch = L.count[slot];
+        const O nz = (O)a.nnz, base = (O)a.base;
+        O rb = (O)__ldg(a.ptr + row) - base;
+        O re = (O)__ldg(a.ptr + row + 1) - base;
+        rb = rb < nz ? rb : nz;
+        re = re < nz ? re : nz;
+        const O jb = rb + (O)(chunk - L.first[slot]) * (O)CHUNK;
+        const O je = jb < re && re - jb > (O)CHUNK ? jb + (O)CHUNK : re;
         V acc[KC];
 #pragma unroll
         for (int c = 0; c < KC; ++c) acc[c] = VT<V>::zero();
-        accumulate_range<V, I, KC, 32, UNROLL>(a, B, (jb < 0 ? 0 : jb) + lane, je, c0, k, acc);
+        if (jb < je) accumulate_range<V, I, KC, 32, UNROLL>(a, B, jb + (O)lane, je, c0, k, acc);
 #pragma unroll
         for (int c = 0; c < KC; ++c) {
 #pragma unroll
             for (int m = 16; m > 0; m >>= 1) acc[c] = add(acc[c], shfl_xor(acc[c], m));
+        }
+        if (nch == 1) {  // the whole row: store it
+            if (lane == 0) {
+#pragma unroll
+                for (int c = 0; c < KC; ++c)
+                    if (c0 + c < k) C.store(row, c0 + c, acc[c]);
+            }
+            return;
         }
         V *part = reinterpret_cast<V *>(L.partial);
         int last = 0;
@@ -162,19 +89,19 @@ rowblock_kernel(CompressedArgs<V, I> a, int64_t k, DenseIn<V> B, DenseOut<V> C, 
                 if (c0 + c < k) part[chunk * k + c0 + c] = acc[c];
             __threadfence();
             const int prev = atomicAdd(&L.done[slot * ncg + cg], 1);
-            last = prev == L.count[slot] - 1;
+            last = prev == nch - 1;
         }
         last = __shfl_sync(0xffffffffu, last, 0);
         if (!last) return;
         // the row's last chunk: add the partials in chunk order
         __threadfence();
         if (lane == 0) {
-            const int f = L.first[slot], n = L.count[slot];
+            const int f = L.first[slot];
 #pragma unroll
             for (int c = 0; c < KC; ++c) {
                 if (c0 + c >= k) continue;
                 V t = VT<V>::zero();
-                for (int q = 0; q < n; ++q) t = add(t, ld_coherent(part + (int64_t)(f + q) * k + c0 + c));
+                for (int q = 0; q < nch; ++q) t = add(t, ld_coherent(part + (int64_t)(f + q) * k + c0 + c));
                 C.store(row, c0 + c, t);
             }
             L.done[slot * ncg + cg] = 0;
@@ -182,29 +109,8 @@ rowblock_kernel(CompressedArgs<V, I> a, int64_t k, DenseIn<V> B, DenseOut<V> C, 
         return;
     }
 
-    // ---- this warp's 32 rows, G lanes per row (G from the rows' average length)
-    const int64_t row0 = unit * RB_THREADS + (threadIdx.x & ~31);
-    const int64_t r = row0 + lane;
-    int64_t b = 0, e = 0;
-    if (r < a.outer_n) {
-        b = (int64_t)__ldg(a.ptr + r) - a.base;
-        e = (int64_t)__ldg(a.ptr + r + 1) - a.base;
-        b = b < 0 ? 0 : (b > a.nnz ? a.nnz : b);
-        e = e < b ? b : (e > a.nnz ? a.nnz : e);
-    }
-    int skip = 0;
-    if (L.nlong > 0 && e - b > LONG_LEN) {  // the plan's chunk CTAs take it
-        e = b;
-        skip = 1;
-    }
-    const int64_t total = __shfl_sync(0xffffffffu, e, 31) - __shfl_sync(0xffffffffu, b, 0);
-    const int64_t avg = total >> 5;
-    if (avg <= G1_AVG) warp_rows<V, I, KC, 1>(a, k, B, C, c0, row0, b, e, skip);
-    else if (avg <= 2 * G1_AVG) warp_rows<V, I, KC, 2>(a, k, B, C, c0, row0, b, e, skip);
-    else if (avg <= 4 * G1_AVG) warp_rows<V, I, KC, 4>(a, k, B, C, c0, row0, b, e, skip);
-    else if (avg <= 8 * G1_AVG) warp_rows<V, I, KC, 8>(a, k, B, C, c0, row0, b, e, skip);
-    else if (avg <= 16 * G1_AVG) warp_rows<V, I, KC, 16>(a, k, B, C, c0, row0, b, e, skip);
-    else warp_rows<V, I, KC, 32>(a, k, B, C, c0, row0, b, e, skip);
+    // ---- this warp's 32 rows
+    warp_unit<V, I, KC>(a, k, B, C, c0, unit * RB_THREADS + (threadIdx.x & ~31), L.skip_mask);
 }
 
 // ---------------------------------------------------------------------------
@@ -222,7 +128,7 @@ int launch_rowblock(cudaStream_t s, const CompressedArgs<V, I> &a, int64_t k, De
     if (k == 1) KC = 1;
     if (KC > k) KC = k <= 1 ? 1 : (k <= 2 ? 2 : (k <= 4 ? 4 : 8));
     const int64_t ncg = ceil_div(k, KC);
-    LongRows L{};
+    PlanRows L{};
     int64_t units = nrb;
     if (plan && plan->nlong > 0) {
         if (plan->outer_n != a.outer_n || plan->nnz != a.nnz)
@@ -234,8 +140,8 @@ int launch_rowblock(cudaStream_t s, const CompressedArgs<V, I> &a, int64_t k, De
         void *partial = cv.take<V>((size_t)(plan->nchunks * k));
         int rc = check_cuda(cudaMemsetAsync(done, 0, sizeof(int) * plan->nlong * ncg, s), "plan counters");
         if (rc) return rc;
-        L = LongRows{plan->nlong, plan->nchunks, plan->row, plan->first, plan->count, plan->chunk_slot,
-                     done, partial};
+        L = PlanRows{plan->nlong, plan->nchunks, plan->row, plan->first, plan->count, plan->chunk_slot,
+                     plan->skip_mask, done, partial};
         units += ceil_div(plan->nchunks, RB_WARPS);
     }
     const int64_t blocks = units * ncg;
@@ -270,23 +176,36 @@ static int build_plan(cudaStream_t s, int64_t outer_n, int64_t nnz, const I *ptr
     if (rc) return rc;
     rc = check_cuda(cudaStreamSynchronize(s), "plan: sync");
     if (rc) return rc;
-    std::vector<int64_t> row;
-    std::vector<int32_t> first, count, slot;
+    std::vector<int64_t> len((size_t)outer_n);
     int64_t maxlen = 0;
     for (int64_t r = 0; r < outer_n; ++r) {
         int64_t b = (int64_t)h[r] - base, e = (int64_t)h[r + 1] - base;
         b = b < 0 ? 0 : (b > nnz ? nnz : b);
         e = e < b ? b : (e > nnz ? nnz : e);
-        const int64_t len = e - b;
-        maxlen = len > maxlen ? len : maxlen;
-        if (len <= LONG_LEN) continue;
-        const int64_t nch = ceil_div(len, CHUNK);
-        if ((int64_t)slot.size() + nch > 0x7fffffffLL)
-            return fail(GSA_ERR_UNSUPPORTED, "plan: too many chunks");
-        row.push_back(r);
-        first.push_back((int32_t)slot.size());
-        count.push_back((int32_t)nch);
-        for (int64_t q = 0; q < nch; ++q) slot.push_back((int32_t)(row.size() - 1));
+        len[r] = e - b;
+        maxlen = len[r] > maxlen ? len[r] : maxlen;
+    }
+    // A row goes to the plan when it is longer than CHUNK, or longer than PLAN_LEN and
+    // more than 4x the average of its warp's 32 rows (it would hold the warp's other
+    // rows back).  Rows of even length stay in their warps, G lanes per row.
+    std::vector<int64_t> row;
+    std::vector<int32_t> first, count, slot;
+    std::vector<uint32_t> mask((size_t)ceil_div(outer_n, 32), 0u);
+    for (int64_t w0 = 0; w0 < outer_n; w0 += 32) {
+        const int64_t w1 = w0 + 32 < outer_n ? w0 + 32 : outer_n;
+        int64_t sum = 0;
+        for (int64_t r = w0; r < w1; ++r) sum += len[r];
+        for (int64_t r = w0; r < w1; ++r) {
+            if (len[r] <= PLAN_LEN || (len[r] <= CHUNK && 8 * len[r] <= sum)) continue;
+            const int64_t nch = ceil_div(len[r], CHUNK);
+            if ((int64_t)slot.size() + nch > 0x7fffffffLL)
+                return fail(GSA_ERR_UNSUPPORTED, "plan: too many chunks");
+            mask[(size_t)(w0 >> 5)] |= 1u << (r - w0);
+            row.push_back(r);
+            first.push_back((int32_t)slot.size());
+            count.push_back((int32_t)nch);
+            for (int64_t q = 0; q < nch; ++q) slot.push_back((int32_t)(row.size() - 1));
+        }
     }
     p->outer_n = outer_n;
     p->nnz = nnz;
@@ -295,7 +214,8 @@ static int build_plan(cudaStream_t s, int64_t outer_n, int64_t nnz, const I *ptr
     p->nchunks = (int64_t)slot.size();
     if (p->nlong == 0) return GSA_OK;
     size_t bytes = align_up(row.size() * 8, 256) + align_up(first.size() * 4, 256) +
-                   align_up(count.size() * 4, 256) + align_up(slot.size() * 4, 256);
+                   align_up(count.size() * 4, 256) + align_up(slot.size() * 4, 256) +
+                   align_up(mask.size() * 4, 256);
     rc = check_cuda(cudaMalloc(&p->mem, bytes), "plan: device memory");
     if (rc) return rc;
     Carver cv(p->mem);
@@ -303,15 +223,18 @@ static int build_plan(cudaStream_t s, int64_t outer_n, int64_t nnz, const I *ptr
     int32_t *d_first = cv.take<int32_t>(first.size());
     int32_t *d_count = cv.take<int32_t>(count.size());
     int32_t *d_slot = cv.take<int32_t>(slot.size());
+    uint32_t *d_mask = cv.take<uint32_t>(mask.size());
     rc = check_cuda(cudaMemcpy(d_row, row.data(), row.size() * 8, cudaMemcpyHostToDevice), "plan: rows");
     if (!rc) rc = check_cuda(cudaMemcpy(d_first, first.data(), first.size() * 4, cudaMemcpyHostToDevice), "plan: first");
     if (!rc) rc = check_cuda(cudaMemcpy(d_count, count.data(), count.size() * 4, cudaMemcpyHostToDevice), "plan: count");
     if (!rc) rc = check_cuda(cudaMemcpy(d_slot, slot.data(), slot.size() * 4, cudaMemcpyHostToDevice), "plan: chunks");
+    if (!rc) rc = check_cuda(cudaMemcpy(d_mask, mask.data(), mask.size() * 4, cudaMemcpyHostToDevice), "plan: mask");
     if (rc) return rc;
     p->row = d_row;
     p->first = d_first;
     p->count = d_count;
     p->chunk_slot = d_slot;
+    p->skip_mask = d_mask;
     return GSA_OK;
 }
 

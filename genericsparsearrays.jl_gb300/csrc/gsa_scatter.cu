@@ -4,10 +4,13 @@
 //   stored entry j of outer o -- kernel_spmatmul_csr_T!
 //   (src/matrix_csr/matrix_csr_kernels.jl:24-45) and kernel_spmatmul_csc_N!
 //   (src/matrix_csc/matrix_csc_kernels.jl:1-22).  Those give one work item per
-//   outer entry, so one long column serialises a thread.  Here the entries are
-//   cut into the same nnz-balanced merge-path tiles as the gather; a tile
-//   first labels each of its entries with its outer index (shared memory),
-//   then streams the entries coalesced and adds them with atomics.
+//   outer entry, so one long column serialises a thread.  The default here is the
+//   outer-block form of the row-block gather: a warp owns 32 outer entries and gives
+//   each G lanes (G from their average length), a lane reads op(B)(o, c) * alpha once
+//   per outer entry and adds its entries' products with atomics; with a plan, long
+//   outer entries go to warps of their own, chunk by chunk.  ALGO_MERGE cuts the
+//   entries into nnz-balanced merge-path tiles instead; a tile first labels each of
+//   its entries with its outer index (shared memory), then streams them coalesced.
 // * COO: kernel_spmatmul_coo_N! / _T! (src/matrix_coo/matrix_coo_kernels.jl:1-43),
 //   one atomic per entry there.  Here each warp takes 32 consecutive entries,
 //   reduces runs of equal output rows with a segmented shuffle scan and issues
@@ -17,7 +20,7 @@
 //
 // Complex values use one atomic per component (the reference's KA @atomic
 // cannot do Complex, so its CSR-T / CSC-N / COO products skip Complex).
-#include "gsa_internal.cuh"
+#include "gsa_rows.cuh"
 
 namespace gsa {
 
@@ -115,8 +118,129 @@ scatter_merge_kernel(CompressedArgs<V, I> a, int64_t k, DenseIn<V> B, DenseOut<V
     }
 }
 
+// ---------------------------------------------------------------------------
+// Outer-block scatter (the default).
+
+// C[idx_j, c0 + c] += conj?(a_j) * xa[c] for j = jb, jb+S, ... < je; entries whose index
+// falls outside C's rows are skipped.
+template <typename V, typename I, int KC, int S>
+__device__ __forceinline__ void scatter_range(const CompressedArgs<V, I> &a, const DenseOut<V> &C,
+                                              Off<I> j, Off<I> je, int64_t c0, int64_t k,
+                                              const V (&xa)[KC]) {
+    using O = Off<I>;
+    const O inner = sizeof(O) == 8 ? (O)a.inner_n
+                                   : (O)(a.inner_n < 0xffffffffLL ? a.inner_n : 0xffffffffLL);
+    const O base = (O)a.base;
+    for (; j < je; j += S) {
+        const O r = (O)ld_stream(a.idx + j) - base;
+        const V av = conj_if(ld_stream(a.val + j), a.conjA);
+        if (r >= inner) continue;
+#pragma unroll
+        for (int c = 0; c < KC; ++c)
+            if (KC == 1 || c0 + c < k) atomic_add(C.p + (int64_t)r + (c0 + c) * C.ld, mul(av, xa[c]));
+    }
+}
+
+// The 32 outer entries of one warp, G lanes each (as warp_rows, scattering).
+template <typename V, typename I, int KC, int G>
+__device__ __forceinline__ void scatter_rows(const CompressedArgs<V, I> &a, int64_t k, const DenseIn<V> &B,
+                                             const DenseOut<V> &C, int64_t c0, int64_t row0, Off<I> b,
+                                             Off<I> e) {
+    using O = Off<I>;
+    const int lane = threadIdx.x & 31;
+    constexpr int RPP = 32 / G;
+#pragma unroll 1
+    for (int p = 0; p < G; ++p) {
+        const int q = p * RPP + lane / G;
+        const O qb = G == 1 ? b : (O)__shfl_sync(0xffffffffu, b, q);
+        const O qe = G == 1 ? e : (O)__shfl_sync(0xffffffffu, e, q);
+        if (qb >= qe) continue;  // empty, planned, or past the last outer entry
+        const int64_t o = row0 + q;
+        V xa[KC];
+#pragma unroll
+        for (int c = 0; c < KC; ++c)
+            xa[c] = (KC == 1 || c0 + c < k) ? mul(B.at(o, c0 + c), C.alpha) : VT<V>::zero();
+        scatter_range<V, I, KC, G>(a, C, qb + (O)(lane % G), qe, c0, k, xa);
+    }
+}
+
+template <typename V, typename I, int KC>
+__global__ void __launch_bounds__(RB_THREADS)
+scatter_block_kernel(CompressedArgs<V, I> a, int64_t k, DenseIn<V> B, DenseOut<V> C, int64_t ncg,
+                     int64_t nrb, PlanRows P) {
+    using O = Off<I>;
+    const int lane = threadIdx.x & 31;
+    const unsigned cta = blockIdx.x;
+    const unsigned cg = ncg == 1 ? 0u : cta % (unsigned)ncg;
+    const int64_t unit = ncg == 1 ? (int64_t)cta : (int64_t)(cta / (unsigned)ncg);
+    const int64_t c0 = (int64_t)cg * KC;
+    if (unit >= nrb) {
+        // planned outer entries: a warp per chunk, straight to the atomics
+        const int64_t chunk = (unit - nrb) * RB_WARPS + (threadIdx.x >> 5);
+        if (chunk >= P.nchunks) return;
+        const int slot = P.chunk_slot[chunk];
+        const int64_t o = P.row[slot];
+        const O nz = (O)a.nnz, base = (O)a.base;
+        O rb = (O)__ldg(a.ptr + o) - base;
+        O re = (O)__ldg(a.ptr + o + 1) - base;
+        rb = rb < nz ? rb : nz;
+        re = re < nz ? re : nz;
+        const O jb = rb + (O)(chunk - P.first[slot]) * (O)CHUNK;
+        const O je = jb < re && re - jb > (O)CHUNK ? jb + (O)CHUNK : re;
+        if (jb >= je) return;
+        V xa[KC];
+#pragma unroll
+        for (int c = 0; c < KC; ++c)
+            xa[c] = (KC == 1 || c0 + c < k) ? mul(B.at(o, c0 + c), C.alpha) : VT<V>::zero();
+        scatter_range<V, I, KC, 32>(a, C, jb + (O)lane, je, c0, k, xa);
+        return;
+    }
+    const int64_t row0 = unit * RB_THREADS + (threadIdx.x & ~31);
+    Off<I> b, e;
+    int skip;
+    const int64_t avg = warp_extent(a, row0, P.skip_mask, b, e, skip);
+    dispatch_lanes(avg, G1_AVG, [&](auto g) {
+        scatter_rows<V, I, KC, decltype(g)::value>(a, k, B, C, c0, row0, b, e);
+    });
+}
+
 template <typename V, typename I>
-size_t scatter_workspace_size(int64_t outer_n, int64_t nnz, int64_t k) {
+int launch_scatter_block(cudaStream_t s, const CompressedArgs<V, I> &a, int64_t k, DenseIn<V> B,
+                         DenseOut<V> C, const Plan *plan) {
+    const int64_t nrb = ceil_div(a.outer_n, RB_THREADS);
+    int KC = get_spmm_columns();
+    if (KC == 0) KC = sizeof(V) >= 16 ? 2 : 4;
+    if (k == 1) KC = 1;
+    if (KC > k) KC = k <= 2 ? 2 : (k <= 4 ? 4 : 8);
+    const int64_t ncg = ceil_div(k, KC);
+    PlanRows P{};
+    int64_t units = nrb;
+    if (plan && plan->nlong > 0) {
+        if (plan->outer_n != a.outer_n || plan->nnz != a.nnz)
+            return fail(GSA_ERR_INVALID_ARG, "plan was made for another structure");
+        P.nlong = plan->nlong;
+        P.nchunks = plan->nchunks;
+        P.row = plan->row;
+        P.first = plan->first;
+        P.count = plan->count;
+        P.chunk_slot = plan->chunk_slot;
+        P.skip_mask = plan->skip_mask;
+        units += ceil_div(plan->nchunks, RB_WARPS);
+    }
+    const int64_t blocks = units * ncg;
+    if (blocks > 0x7fffffffLL) return fail(GSA_ERR_UNSUPPORTED, "too many outer entries");
+    timer_before(s);
+    if (KC == 1) scatter_block_kernel<V, I, 1><<<(unsigned)blocks, RB_THREADS, 0, s>>>(a, k, B, C, ncg, nrb, P);
+    else if (KC == 2) scatter_block_kernel<V, I, 2><<<(unsigned)blocks, RB_THREADS, 0, s>>>(a, k, B, C, ncg, nrb, P);
+    else if (KC == 4) scatter_block_kernel<V, I, 4><<<(unsigned)blocks, RB_THREADS, 0, s>>>(a, k, B, C, ncg, nrb, P);
+    else scatter_block_kernel<V, I, 8><<<(unsigned)blocks, RB_THREADS, 0, s>>>(a, k, B, C, ncg, nrb, P);
+    timer_after(s);
+    return check_cuda(cudaGetLastError(), "scatter_block_kernel");
+}
+
+template <typename V, typename I>
+size_t scatter_workspace_size(int64_t outer_n, int64_t nnz, int64_t k, int algo) {
+    if (algo != GSA_ALGO_MERGE) return 0;
     if (outer_n == 0 || nnz == 0 || k == 0) return 0;
     int64_t T = ceil_div(outer_n + nnz, ScatterShape<V>::TILE);
     return align_up((size_t)(T + 1) * sizeof(int64_t), 256);
@@ -124,13 +248,15 @@ size_t scatter_workspace_size(int64_t outer_n, int64_t nnz, int64_t k) {
 
 template <typename V, typename I>
 int launch_scatter(cudaStream_t s, const CompressedArgs<V, I> &a, int64_t k, DenseIn<V> B,
-                   DenseOut<V> C, int64_t out_rows, void *ws, size_t ws_bytes) {
+                   DenseOut<V> C, int64_t out_rows, int algo, const Plan *plan, void *ws,
+                   size_t ws_bytes) {
     int rc = launch_rmul_or_fill<V>(s, C, out_rows, k);
     if (rc) return rc;
     if (a.outer_n == 0 || a.nnz == 0 || k == 0) return GSA_OK;
+    if (algo != GSA_ALGO_MERGE) return launch_scatter_block<V, I>(s, a, k, B, C, plan);
     constexpr int TILE = ScatterShape<V>::TILE;
     const int64_t T = ceil_div(a.outer_n + a.nnz, TILE);
-    if (ws_bytes < scatter_workspace_size<V, I>(a.outer_n, a.nnz, k))
+    if (ws_bytes < scatter_workspace_size<V, I>(a.outer_n, a.nnz, k, algo))
         return fail(GSA_ERR_INVALID_ARG, "scatter workspace too small");
     if (T > 0x7fffffffLL) return fail(GSA_ERR_UNSUPPORTED, "too many tiles");
     int64_t *coords = (int64_t *)ws;
@@ -210,8 +336,9 @@ int launch_coo(cudaStream_t s, int64_t nnz, const I *out_idx, const I *in_idx, c
 
 #define GSA_INST_SCATTER(V, I)                                                                  \
     template int launch_scatter<V, I>(cudaStream_t, const CompressedArgs<V, I> &, int64_t,      \
-                                      DenseIn<V>, DenseOut<V>, int64_t, void *, size_t);        \
-    template size_t scatter_workspace_size<V, I>(int64_t, int64_t, int64_t);                    \
+                                      DenseIn<V>, DenseOut<V>, int64_t, int, const Plan *,      \
+                                      void *, size_t);                                          \
+    template size_t scatter_workspace_size<V, I>(int64_t, int64_t, int64_t, int);               \
     template int launch_coo<V, I>(cudaStream_t, int64_t, const I *, const I *, const V *, int, \
                                   bool, int64_t, DenseIn<V>, DenseOut<V>, int64_t, int64_t);
 GSA_INST_SCATTER(float, int32_t)

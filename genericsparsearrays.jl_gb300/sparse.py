@@ -397,7 +397,7 @@ def _scalar_buf(v, dtype: torch.dtype):
 
 
 class _PlanHandle:
-    """Owns a gsa_plan (long outer entries of one structure, cut into chunks)."""
+    """Owns a gsa_plan (the outer entries of one structure longer than 32, cut into chunks)."""
 
     def __init__(self, handle: int, nlong: int, nchunks: int, max_len: int):
         self.handle, self.nlong, self.nchunks, self.max_len = handle, nlong, nchunks, max_len
@@ -411,7 +411,7 @@ class _PlanHandle:
 
 def _gather_plan(A) -> Optional[_PlanHandle]:
     """The plan of A's compressed structure, made on first use and kept on the matrix
-    (None when no outer entry is longer than 512, so plain calls are as good).  Making it
+    (None when no outer entry is longer than 32, so plain calls are as good).  Making it
     synchronizes the stream once; the structure must not be changed in place afterwards."""
     cached = A.__dict__.get("_plan", False)
     if cached is not False:
@@ -492,7 +492,7 @@ def mul_(C: torch.Tensor, A, B, alpha=1, beta=0, algo: int = _lib.ALGO_AUTO,
             csr = isinstance(Ap, GenericSparseMatrixCSR)
             ptr, idx = (Ap.rowptr, Ap.colval) if csr else (Ap.colptr, Ap.rowval)
             gather = (opA == _lib.OP_N) == csr
-            plan = _gather_plan(Ap) if (gather and algo == _lib.ALGO_AUTO) else None
+            plan = _gather_plan(Ap) if algo == _lib.ALGO_AUTO else None
         if isinstance(Ap, (GenericSparseMatrixCSR, GenericSparseMatrixCSC)) and plan is not None:
             ws_bytes = lib.gsa_plan_workspace_size(ctypes.c_void_p(plan.handle), _DTYPE[dt], k)
             if ws_bytes and (workspace is None or workspace.numel() < ws_bytes):

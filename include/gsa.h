@@ -60,12 +60,15 @@ typedef enum { GSA_OP_N = 0, GSA_OP_T = 1, GSA_OP_C = 2 } gsa_op;
 
 /* Gather kernel selection for the row-gather paths (CSR N, CSC T). */
 typedef enum {
-    GSA_ALGO_AUTO = 0,     /* library choice: row blocks -- per warp of 32 rows, 1..32
-                              lanes per row from the rows' average length; no workspace */
-    GSA_ALGO_MERGE = 1,    /* one CTA per merge-path tile (any row-length mix) */
-    GSA_ALGO_VECTOR = 2,   /* a group of threads per row (short, even rows) */
-    GSA_ALGO_PIPE = 3      /* persistent merge-path runs with bulk-copy double buffering
-                              (one right-hand side) */
+    GSA_ALGO_AUTO = 0,     /* library choice: row blocks -- per warp of 32 rows (columns
+                              for the scatter directions), 1..32 lanes per row from the
+                              rows' average length; no workspace */
+    GSA_ALGO_MERGE = 1,    /* one CTA per merge-path tile (any row-length mix); gather and
+                              scatter */
+    GSA_ALGO_VECTOR = 2,   /* gather: a group of threads per row (short, even rows);
+                              scatter: as AUTO */
+    GSA_ALGO_PIPE = 3      /* gather: persistent merge-path runs with bulk-copy double
+                              buffering (one right-hand side); scatter: as AUTO */
 } gsa_algo;
 
 /* Tuning keys for gsa_set_tuning / gsa_get_tuning. */
@@ -91,10 +94,17 @@ int gsa_get_tuning(int key);
 
 /* Profiling hook (no counterpart in the reference, which has no tracing): when set, the
  * library records `before` and `after` (cudaEvent_t) on the call's stream right around the
- * main compute kernel of each following call from this host thread -- the merge-path or
- * vector gather, the scatter, the COO kernel, or the whole sort of a conversion.  Pass
+ * main compute kernel of each following call from this host thread -- the row-block,
+ * merge-path, vector or pipelined gather, the scatter, the COO kernel, the grouped kernel,
+ * or the whole sort of a conversion.  Pass
  * NULL, NULL to switch it off. */
 void gsa_set_kernel_timer(void *before, void *after);
+
+/* Fused multiply-adds per second the GPU retires for dtype GSA_F32 or GSA_F64 (8
+ * independent chains per thread, 2048 threads per SM, `iters` steps each; synchronizes
+ * the stream): the arithmetic roofline beside HBM for the product kernels, which do one
+ * FMA per real multiply-add.  No counterpart in the reference. */
+int gsa_probe_fma_rate(void *stream, int dtype, int64_t iters, double *fma_per_s);
 
 /* ---- sparse x dense mul! --------------------------------------------------
  * C = beta*C + alpha * op(A) * op(B), with C (rows(op(A)) x k, column-major,
@@ -150,26 +160,28 @@ int gsa_csr_spmv_noalloc(void *stream, int dtype, int itype, int64_t m, int64_t 
 
 /* ---- plans ----------------------------------------------------------------
  * A plan records which outer entries of one compressed structure (rows of a CSR
- * pointer array, columns of a CSC one) hold more than 512 stored entries, cut into
+ * pointer array, columns of a CSC one) hold more than 32 stored entries, cut into
  * chunks of 512 entries.  With a plan, the row gather (CSR opA = N, CSC opA = T/C)
- * sums such long entries chunk by chunk across the whole GPU instead of one warp
- * per long entry -- what power-law row lengths need; without long entries a plan
- * changes nothing.  Creating one copies the pointer array to the host once and
- * synchronizes the stream; the plan holds one device allocation until destroyed.
- * The structure must not change while its plan is in use.  No counterpart in the
- * reference (its kernels take one work item per row). */
+ * gives each chunk a warp of its own (a long entry is summed chunk by chunk across
+ * the whole GPU) and keeps such entries out of the warps of short ones -- what
+ * power-law row lengths need; without such entries a plan changes nothing.
+ * Creating one copies the pointer array to the host once and synchronizes the
+ * stream; the plan holds one device allocation until destroyed.  The structure
+ * must not change while its plan is in use.  No counterpart in the reference (its
+ * kernels take one work item per row). */
 typedef struct gsa_plan gsa_plan;
 int gsa_plan_create(void *stream, int itype, int64_t outer_n, int64_t nnz, const void *ptr,
                     int base, gsa_plan **out);
 int gsa_plan_destroy(gsa_plan *plan);
-/* Longest outer entry, number of long entries and of their chunks. */
+/* Longest outer entry, number of planned (longer than 32) entries and of their chunks. */
 int gsa_plan_info(const gsa_plan *plan, int64_t *max_len, int64_t *nlong, int64_t *nchunks);
-/* Workspace bytes of a planned call with k right-hand sides (0 without long entries). */
+/* Workspace bytes of a planned call with k right-hand sides (0 without planned entries). */
 size_t gsa_plan_workspace_size(const gsa_plan *plan, int dtype, int64_t k);
 
 /* gsa_csr_mul / gsa_csc_mul with a plan of the same structure (replace the same
- * reference methods).  The plan applies to the gather directions (CSR opA = N,
- * CSC opA = T/C); other directions ignore it.  NULL plan = plain call. */
+ * reference methods).  The plan applies to both directions under GSA_ALGO_AUTO: the
+ * gather (CSR opA = N, CSC opA = T/C) and the outer-block scatter (CSR opA = T/C,
+ * CSC opA = N) give planned entries warps of their own.  NULL plan = plain call. */
 int gsa_csr_mul_planned(void *stream, int dtype, int itype, int64_t m, int64_t n, int64_t nnz,
                         const void *rowptr, const void *colval, const void *nzval, int base, int opA,
                         int64_t k, const void *B, int64_t ldb, int opB, void *C, int64_t ldc,
@@ -185,6 +197,51 @@ int gsa_csc_mul_planned(void *stream, int dtype, int itype, int64_t m, int64_t n
  * 0 CSR, 1 CSC).  0 means none is needed. */
 size_t gsa_mul_workspace_size(int format, int dtype, int itype, int64_t m, int64_t n,
                               int64_t nnz, int opA, int64_t k, int algo);
+
+/* ---- grouped products -------------------------------------------------------
+ * Many CSR products C_i = beta_i*C_i + alpha_i*A_i*B_i (A_i m x n with nnz entries,
+ * B_i n x k column-major with leading dimension ldb, C_i m x k with ldc) in ONE
+ * persistent launch that walks (item, row block, column group) tiles -- instead of
+ * one launch per product, which is what dominates the time of thousands of small
+ * products.  alpha/beta hold the bytes of one value of the call's dtype (a double,
+ * or re then im).  No counterpart in the reference (one KA launch per mul!). */
+typedef struct {
+    const void *rowptr, *colval, *nzval;
+    const void *B;
+    void *C;                   /* m x k, column-major, leading dimension ldc */
+    int64_t m, n, nnz, ldb, ldc;
+    int32_t k;                 /* right-hand sides */
+    int32_t b_rowmajor;        /* 0: B(i, c) at B[i + c*ldb] (ldb >= n); 1: at B[i*ldb + c]
+                                  (ldb >= k) -- one entry's k values then share cache lines */
+    int64_t first_tile;        /* filled by gsa_grouped_tiles */
+    unsigned char alpha[16];
+    unsigned char beta[16];
+} gsa_group_item;
+
+/* Checks the items (host memory), fills first_tile and returns the tile count.
+ * columns: right-hand-side columns a thread accumulates (0 = by dtype, 1, 2, 4, 8);
+ * the launch must use the same value. */
+int gsa_grouped_tiles(int dtype, gsa_group_item *items, int64_t count, int columns, int64_t *ntiles);
+
+/* One grouped launch over a DEVICE array of items prepared by gsa_grouped_tiles.
+ * g1_avg: a warp sums one row per thread while its rows average at most g1_avg
+ * entries and doubles the lanes per row for every doubling beyond (0 = 6). */
+int gsa_grouped_mul(void *stream, int dtype, int itype, int base, const gsa_group_item *d_items,
+                    int64_t count, int64_t ntiles, int columns, int g1_avg);
+
+/* A batch: the items copied to the device once (one allocation, synchronizes the
+ * stream), run many times with new contents of the same B and C buffers. */
+typedef struct gsa_batch gsa_batch;
+typedef enum {
+    GSA_BATCH_GROUPED = 0,   /* one grouped launch */
+    GSA_BATCH_GRAPH = 1,     /* the grouped launch captured into a CUDA graph on first use,
+                                replayed afterwards */
+    GSA_BATCH_PER_CALL = 2   /* one gsa_csr_mul per item (the per-call baseline) */
+} gsa_batch_mode;
+int gsa_batch_create(void *stream, int dtype, int itype, int base, const gsa_group_item *items,
+                     int64_t count, int columns, int g1_avg, gsa_batch **out);
+int gsa_batch_run(gsa_batch *batch, void *stream, int mode);
+int gsa_batch_destroy(gsa_batch *batch);
 
 /* ---- format conversions ---------------------------------------------------- */
 

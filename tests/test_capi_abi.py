@@ -65,13 +65,14 @@ def test_argument_checks_precede_gpu_work(lib, gsa):
 def test_workspace_size_queries(lib):
     # gather (CSR, opA = N): the default row-block kernel and the vector kernel need none,
     # merge-path tiles need coordinates + carries, the pipelined kernel carries per CTA run;
-    # scatter (CSR, opA = T): tile coordinates only
+    # scatter (CSR, opA = T): none for the default outer blocks, tile coordinates for merge
     auto = lib.gsa_mul_workspace_size(0, 1, 0, 1000, 1000, 5000, 0, 1, 0)
     g = lib.gsa_mul_workspace_size(0, 1, 0, 1000, 1000, 5000, 0, 1, 1)
     p = lib.gsa_mul_workspace_size(0, 1, 0, 1000, 1000, 5000, 0, 1, 3)
     s = lib.gsa_mul_workspace_size(0, 1, 0, 1000, 1000, 5000, 1, 1, 0)
+    sm = lib.gsa_mul_workspace_size(0, 1, 0, 1000, 1000, 5000, 1, 1, 1)
     v = lib.gsa_mul_workspace_size(0, 1, 0, 1000, 1000, 5000, 0, 1, 2)
-    assert auto == 0 and v == 0 and g > 0 and p > 0 and s > 0
+    assert auto == 0 and v == 0 and g > 0 and p > 0 and s == 0 and sm > 0
     assert lib.gsa_mul_workspace_size(0, 1, 0, 1000, 1000, 5000, 0, 16, 1) > g
     assert lib.gsa_mul_workspace_size(0, 99, 0, 10, 10, 5, 0, 1, 0) == 0
     w = lib.gsa_coo_to_compressed_workspace_size(0, 1, 0, 1000, 1000, 5000)

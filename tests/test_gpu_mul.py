@@ -168,6 +168,34 @@ def test_long_rows_cross_tiles(gsa, oracle, cuda, dt, k):
             check(oracle, f, opA, mm, nn, rowptr, cols, vals, X, "N", C0, C, 3, 2, dt)
 
 
+@pytest.mark.parametrize("dt", [np.float64, np.complex128, np.int64])
+@pytest.mark.parametrize("k", [1, 3])
+def test_long_columns_scatter(gsa, oracle, cuda, dt, k):
+    """The scatter directions (CSC N, CSR T) over outer entries of 0 to 60 000 entries: the
+    default outer blocks with and without a plan (long entries chunked over warps) and the
+    merge-path tiles; integers bit-exact."""
+    rng = np.random.default_rng(13)
+    m = 70_000
+    lengths = np.array([0, 60_000, 1, 0, 5_000, 3, 0, 0, 2, 60_000, 40] + [4] * 500 + [0] * 40)
+    n = lengths.size
+    colptr = np.concatenate([[0], np.cumsum(lengths)]).astype(np.int64) + 1
+    rows = np.concatenate([np.sort(rng.choice(m, size=l, replace=False)) for l in lengths]).astype(np.int64) + 1
+    vals = rand_values(rng, rows.size, dt)
+    for algo in (0, 1, 2):
+        for fmt in ("csc", "csr_t"):
+            if fmt == "csc":
+                A = make(gsa, "csc", m, n, colptr, rows, vals, cuda)
+                opA, f, mm, nn = "N", "csc", m, n
+            else:  # the same arrays as a CSR of the transpose; op(A) = T scatters
+                A = gsa.transpose(make(gsa, "csr", n, m, colptr, rows, vals, cuda))
+                opA, f, mm, nn = "T", "csr", n, m
+            X = np.asfortranarray(rand_values(rng, (n, k), dt))
+            C0 = np.asfortranarray(rand_values(rng, (m, k), dt))
+            C = torch.from_numpy(C0).to(cuda)
+            gsa.mul_(C, A, torch.from_numpy(X).to(cuda), 3, 2, algo=algo)
+            check(oracle, f, opA, mm, nn, colptr, rows, vals, X, "N", C0, C, 3, 2, dt)
+
+
 def test_gather_is_deterministic(gsa, cuda):
     """The CSR gather uses no atomics: two runs are bit-identical."""
     from genericsparsearrays_gb300 import workloads
