@@ -323,6 +323,12 @@ def run_gpu(args, world, rank, local):
         if not args.no_extras and not args.no_serving:
             extras["served_stream"] = run_serving(gsa, torch, dev, args)
 
+    # arithmetic roofline: FP64 FMAs the SMs retire per second (the row-block kernel does
+    # one FMA per stored entry; alpha = 1 adds no multiply)
+    fma_rate = ctypes.c_double(0.0)
+    _lib.check(lib.gsa_probe_fma_rate(ctypes.c_void_p(torch.cuda.current_stream().cuda_stream),
+                                      _lib.F64, 1 << 14, ctypes.byref(fma_rate)))
+    fp64_ops = nnz
     clk = clocks.summary()
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -345,7 +351,12 @@ def run_gpu(args, world, rank, local):
                      "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
                      "kernel_us": round(kern_avg_s * 1e6, 2),
-                     "traffic": traffic},
+                     "traffic": traffic,
+                     "fp64": {"fma_per_launch": fp64_ops,
+                              "achieved_gfma_s": round(fp64_ops / kern_avg_s / 1e9, 1),
+                              "peak_gfma_s": round(fma_rate.value / 1e9, 1),
+                              "frac": round(fp64_ops / kern_avg_s / fma_rate.value, 4),
+                              "peak_kind": "measured by gsa_probe_fma_rate in this run"}},
         "e2e": {"value": round(e2e_value, 2), "unit": "GB/s", "h2d_bytes_per_step": n * 8,
                 "d2h_bytes_per_step": m * 8, "ms_per_step": round(e2e_s / args.steps * 1e3, 4),
                 "matches_oracle": e2e_ok, "api": "genericsparsearrays_gb300.mul_"},
@@ -424,6 +435,20 @@ def run_extras(gsa, wl, torch, dev, lib, timer, args):
     t, tk = time_call(lambda: gsa.mul_(y, Cp, x))
     out["powerlaw_coo_spmv_c64_i64"] = {"GBps": round(bq / t / 1e9, 1), "kernel_GBps": round(bq / tk / 1e9, 1),
                                          "us": round(t * 1e6, 2)}
+    # three-argument dot(x, A, y) on the same matrix (the call returns the scalar to the host)
+    xh = torch.from_numpy(rng.standard_normal(m) + 1j * rng.standard_normal(m)).to(dev)
+    gsa.dot(xh, A, x)
+    torch.cuda.synchronize()
+    ts = []
+    for _ in range(max(5, steps)):
+        timer.flush()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        gsa.dot(xh, A, x)
+        ts.append(time.perf_counter() - t0)
+    td = float(np.median(ts))
+    out["powerlaw_csr_dot_c64_i64"] = {"GBps": round(bp / td / 1e9, 1), "us": round(td * 1e6, 2),
+                                       "note": "wall time of gsa.dot incl. the scalar's copy to the host"}
     del A, Cp
     # n = 1e5 Poisson(10): CSR / CSC / COO (18 MB: L2-resident unless flushed; flushed here)
     m, n, rp, cv, nz = wl.random_poisson(100_000, seed=0)

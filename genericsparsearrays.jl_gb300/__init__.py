@@ -18,6 +18,7 @@ from .sparse import (
     adapt,
     adjoint,
     collect,
+    dot,
     mul,
     mul_,
     nnz,
@@ -33,5 +34,5 @@ __all__ = [
     "AbstractGenericSparseMatrix", "Adjoint", "ArgumentError", "DimensionMismatch",
     "GenericSparseMatrixCOO", "GenericSparseMatrixCSC", "GenericSparseMatrixCSR",
     "SparseMatrixCSC", "Transpose", "adapt", "adjoint", "collect", "mul", "mul_", "nnz", "size",
-    "transpose", "validate", "ALGO_AUTO", "ALGO_MERGE", "ALGO_VECTOR", "ALGO_PIPE",
+    "transpose", "validate", "dot", "ALGO_AUTO", "ALGO_MERGE", "ALGO_VECTOR", "ALGO_PIPE",
 ]

@@ -20,7 +20,7 @@ IDX32, IDX64 = 0, 1
 # op codes (gsa_op) and algorithms (gsa_algo)
 OP_N, OP_T, OP_C = 0, 1, 2
 ALGO_AUTO, ALGO_MERGE, ALGO_VECTOR, ALGO_PIPE = 0, 1, 2, 3
-TUNE_PIPE_THREADS, TUNE_SPMM_COLUMNS = 1, 2
+TUNE_PIPE_THREADS, TUNE_SPMM_COLUMNS, TUNE_PLAN_ORDER = 1, 2, 3
 BATCH_GROUPED, BATCH_GRAPH, BATCH_PER_CALL = 0, 1, 2
 
 # Every exported symbol of include/gsa.h with its ctypes signature.
@@ -43,6 +43,13 @@ SIGNATURES = {
     "gsa_plan_workspace_size": ([_vp, _i32, _i64], _sz),
     "gsa_csr_mul_planned": (_MUL + [_vp, _vp, _sz], _i32),
     "gsa_csc_mul_planned": (_MUL + [_vp, _vp, _sz], _i32),
+    "gsa_csr_dot": ([_vp, _i32, _i32, _i64, _i64, _i64, _vp, _vp, _vp, _i32, _i32, _vp, _vp, _vp, _vp,
+                     _vp, _sz], _i32),
+    "gsa_csc_dot": ([_vp, _i32, _i32, _i64, _i64, _i64, _vp, _vp, _vp, _i32, _i32, _vp, _vp, _vp, _vp,
+                     _vp, _sz], _i32),
+    "gsa_coo_dot": ([_vp, _i32, _i32, _i64, _i64, _i64, _vp, _vp, _vp, _i32, _i32, _vp, _vp, _vp,
+                     _vp, _sz], _i32),
+    "gsa_dot_workspace_size": ([_i32, _i32, _i32, _i64, _i64, _vp], _sz),
     "gsa_csr_spmv_noalloc": ([_vp, _i32, _i32, _i64, _i64, _i64, _vp, _vp, _vp, _i32, _vp, _vp,
                               _vp, _vp], _i32),
     "gsa_mul_workspace_size": ([_i32, _i32, _i32, _i64, _i64, _i64, _i32, _i64, _i32], _sz),

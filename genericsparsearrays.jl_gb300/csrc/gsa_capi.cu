@@ -42,36 +42,6 @@ int check_cuda(cudaError_t e, const char *what) {
 
 // Workspace: the caller's, or a stream-ordered allocation released on the
 // same stream once the enqueued work is done with it.
-struct Workspace {
-    void *p = nullptr;
-    size_t bytes = 0;
-    bool owned = false;
-    cudaStream_t s = nullptr;
-    int acquire(cudaStream_t stream, void *user, size_t user_bytes, size_t need) {
-        s = stream;
-        if (need == 0) { p = user; bytes = user_bytes; return GSA_OK; }
-        if (user) {
-            if (user_bytes < need)
-                return fail(GSA_ERR_INVALID_ARG, "workspace of %zu bytes is smaller than the %zu needed",
-                            user_bytes, need);
-            p = user;
-            bytes = user_bytes;
-            return GSA_OK;
-        }
-        cudaError_t e = cudaMallocAsync(&p, need, stream);
-        if (e != cudaSuccess) {
-            cudaGetLastError();
-            return fail(GSA_ERR_ALLOC, "stream-ordered workspace allocation of %zu bytes failed: %s",
-                        need, cudaGetErrorString(e));
-        }
-        owned = true;
-        bytes = need;
-        return GSA_OK;
-    }
-    ~Workspace() {
-        if (owned && p) cudaFreeAsync(p, s);
-    }
-};
 
 static bool misaligned(const void *p, size_t a) { return a && ((uintptr_t)p % a) != 0; }
 
@@ -298,8 +268,8 @@ int gsa_plan_destroy(gsa_plan *plan) {
 int gsa_plan_info(const gsa_plan *plan, int64_t *max_len, int64_t *nlong, int64_t *nchunks) {
     if (!plan) return fail(GSA_ERR_INVALID_ARG, "plan is NULL");
     if (max_len) *max_len = plan->max_len;
-    if (nlong) *nlong = plan->nlong;
-    if (nchunks) *nchunks = plan->nchunks;
+    if (nlong) *nlong = plan->nplanned;
+    if (nchunks) *nchunks = plan->nbin_warps > 0 ? plan->bin.nchunks : plan->nat.nchunks;
     return GSA_OK;
 }
 
@@ -344,6 +314,83 @@ int gsa_coo_mul(void *stream, int dtype, int itype, int64_t m, int64_t n, int64_
     CooMulBody body{s, trans, nnz, k, rows_out, in_rows, rowind, colind, nzval, B, alpha, beta, C,
                     base, opA, opB, ldb, ldc};
     return dispatch_vi(dtype, itype, body);
+}
+
+}  // extern "C"
+
+namespace gsa {
+struct DotBody {
+    cudaStream_t s; int fmt, opA; int64_t m, n, nnz; const void *p0, *p1, *val, *x, *y; int base;
+    const Plan *plan; void *ws; size_t ws_bytes; void *result;
+    template <typename V, typename I> int operator()() {
+        Workspace w;
+        int rc = w.acquire(s, ws, ws_bytes, dot_workspace_size<V, I>(fmt, fmt == 0 ? m : n, plan));
+        if (rc) return rc;
+        return launch_dot<V, I>(s, fmt, opA, m, n, nnz, (const I *)p0, (const I *)p1, (const V *)val, base,
+                                (const V *)x, (const V *)y, plan, w.p, w.bytes, result);
+    }
+};
+struct DotWsBody {
+    int fmt; int64_t outer_n; const Plan *plan; size_t out;
+    template <typename V, typename I> int operator()() {
+        out = dot_workspace_size<V, I>(fmt, outer_n, plan);
+        return 0;
+    }
+};
+
+static int dot_call(int fmt, void *stream, int dtype, int itype, int64_t m, int64_t n, int64_t nnz,
+                    const void *p0, const void *p1, const void *val, int base, int opA, const void *x,
+                    const void *y, void *result, const gsa_plan *plan, void *ws, size_t ws_bytes) {
+    size_t vs = dtype_size(dtype), is = itype_size(itype);
+    if (!vs || !is) return fail(GSA_ERR_UNSUPPORTED, "unsupported dtype %d / itype %d", dtype, itype);
+    if (opA < 0 || opA > 2) return fail(GSA_ERR_INVALID_ARG, "op must be 0 (N), 1 (T) or 2 (C)");
+    if (m < 0 || n < 0 || nnz < 0) return fail(GSA_ERR_INVALID_ARG, "negative size");
+    if (itype == GSA_IDX32 && nnz > 0x7fffffffLL)
+        return fail(GSA_ERR_INVALID_ARG, "nnz=%lld exceeds what Int32 indices can address", (long long)nnz);
+    if (!result) return fail(GSA_ERR_INVALID_ARG, "result must be a host pointer");
+    const int64_t xlen = opA == GSA_OP_N ? m : n, ylen = opA == GSA_OP_N ? n : m;
+    if ((xlen > 0 && !x) || (ylen > 0 && !y)) return fail(GSA_ERR_INVALID_ARG, "x or y is NULL");
+    if (fmt != 2 && !p0) return fail(GSA_ERR_INVALID_ARG, "pointer array is NULL");
+    if (nnz > 0 && (!p0 || !p1 || !val)) return fail(GSA_ERR_INVALID_ARG, "sparse arrays are NULL");
+    if (misaligned(p0, is) || misaligned(p1, is) || misaligned(val, vs) || misaligned(x, vs) ||
+        misaligned(y, vs))
+        return fail(GSA_ERR_INVALID_ARG, "arrays must be aligned to their element size");
+    if (plan && fmt != 2 && (plan->outer_n != (fmt == 0 ? m : n) || plan->nnz != nnz))
+        return fail(GSA_ERR_INVALID_ARG, "plan was made for another structure");
+    DotBody body{(cudaStream_t)stream, fmt, opA, m, n, nnz, p0, p1, val, x, y, base,
+                 fmt == 2 ? nullptr : plan, ws, ws_bytes, result};
+    return dispatch_vi(dtype, itype, body);
+}
+}  // namespace gsa
+
+extern "C" {
+
+int gsa_csr_dot(void *stream, int dtype, int itype, int64_t m, int64_t n, int64_t nnz, const void *rowptr,
+                const void *colval, const void *nzval, int base, int opA, const void *x, const void *y,
+                void *result, const gsa_plan *plan, void *workspace, size_t workspace_bytes) {
+    return dot_call(0, stream, dtype, itype, m, n, nnz, rowptr, colval, nzval, base, opA, x, y, result,
+                    plan, workspace, workspace_bytes);
+}
+
+int gsa_csc_dot(void *stream, int dtype, int itype, int64_t m, int64_t n, int64_t nnz, const void *colptr,
+                const void *rowval, const void *nzval, int base, int opA, const void *x, const void *y,
+                void *result, const gsa_plan *plan, void *workspace, size_t workspace_bytes) {
+    return dot_call(1, stream, dtype, itype, m, n, nnz, colptr, rowval, nzval, base, opA, x, y, result,
+                    plan, workspace, workspace_bytes);
+}
+
+int gsa_coo_dot(void *stream, int dtype, int itype, int64_t m, int64_t n, int64_t nnz, const void *rowind,
+                const void *colind, const void *nzval, int base, int opA, const void *x, const void *y,
+                void *result, void *workspace, size_t workspace_bytes) {
+    return dot_call(2, stream, dtype, itype, m, n, nnz, rowind, colind, nzval, base, opA, x, y, result,
+                    nullptr, workspace, workspace_bytes);
+}
+
+size_t gsa_dot_workspace_size(int format, int dtype, int itype, int64_t m, int64_t n, const gsa_plan *plan) {
+    if (format < 0 || format > 2) return 0;
+    DotWsBody body{format, format == 0 ? m : n, format == 2 ? nullptr : plan, 0};
+    if (dispatch_vi(dtype, itype, body)) return 0;
+    return body.out;
 }
 
 size_t gsa_mul_workspace_size(int format, int dtype, int itype, int64_t m, int64_t n, int64_t nnz,
@@ -472,12 +519,18 @@ int gsa_set_tuning(int key, int value) {
         set_spmm_columns(value);
         return GSA_OK;
     }
+    if (key == GSA_TUNE_PLAN_ORDER) {
+        if (value != 0 && value != 1) return fail(GSA_ERR_INVALID_ARG, "plan order must be 0 or 1");
+        set_plan_natural(value);
+        return GSA_OK;
+    }
     return fail(GSA_ERR_INVALID_ARG, "unknown tuning key %d", key);
 }
 
 int gsa_get_tuning(int key) {
     if (key == GSA_TUNE_PIPE_THREADS) return get_pipe_threads();
     if (key == GSA_TUNE_SPMM_COLUMNS) return get_spmm_columns();
+    if (key == GSA_TUNE_PLAN_ORDER) return get_plan_natural();
     return -1;
 }
 

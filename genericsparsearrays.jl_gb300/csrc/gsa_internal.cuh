@@ -10,17 +10,33 @@
 
 #include "../../include/gsa.h"
 
-// A plan (gsa_plan_create): the outer entries of one compressed structure that have more
-// than 512 stored entries, or more than 32 and over 4x the average of their aligned group
-// of 32, each cut into chunks of 512 entries (device arrays).
-struct gsa_plan {
-    int64_t outer_n = 0, nnz = 0, max_len = 0, nlong = 0, nchunks = 0;
-    const int64_t *row = nullptr;         // outer index of each long entry
+// A plan (gsa_plan_create), device arrays in one allocation.  In the natural order of row
+// blocks, outer entries of more than 512 stored entries, and those of more than 32 that
+// are over 4x the average of their aligned group of 32, are cut into chunks of 512 (the
+// `nat` set, marked in its skip_mask).  When lengths vary so much inside groups of 32
+// that lanes would idle, the plan also has a bin order: the entries of at most 512
+// grouped by length (exactly up to 32, then by powers of two), each bin with its lanes
+// per entry, so that the lanes of a warp do equal work; longer ones are chunked (`bin`).
+struct gsa_chunk_set {
+    int64_t nlong = 0, nchunks = 0;       // chunked entries and their chunks
+    const int64_t *row = nullptr;         // outer index of each chunked entry
     const int32_t *first = nullptr;       // its first chunk
     const int32_t *count = nullptr;       // its number of chunks
-    const int32_t *chunk_slot = nullptr;  // the long entry a chunk belongs to
-    const uint32_t *skip_mask = nullptr;  // bit per outer entry: 1 = the plan's
-    void *mem = nullptr;                  // one device allocation holding the arrays
+    const int32_t *chunk_slot = nullptr;  // the chunked entry a chunk belongs to
+    const uint32_t *skip_mask = nullptr;  // bit per outer entry, 1 = chunked
+};
+struct gsa_plan {
+    int64_t outer_n = 0, nnz = 0, max_len = 0;
+    int64_t nplanned = 0;                 // entries the plan takes out of the natural order
+    gsa_chunk_set nat;                    // natural order: > 512, or > 32 and over 4x the group
+    gsa_chunk_set bin;                    // bin order: > 512 only
+    // bin order (nbin_warps > 0)
+    int64_t nbin_warps = 0;
+    const int64_t *perm = nullptr;        // outer entries of at most 512 entries, bin by bin
+    const int64_t *seg = nullptr;         // [begin, end) of each, 0-based
+    const uint8_t *warp_bin = nullptr;    // bin of each warp of the bin order
+    const int64_t *bins = nullptr;        // per bin: first warp, first position, end, lanes
+    void *mem = nullptr;
 };
 
 namespace gsa {
@@ -104,12 +120,28 @@ __host__ __device__ __forceinline__ cf64 mac(cf64 acc, cf64 a, cf64 b) {
 __host__ __device__ __forceinline__ int32_t mac(int32_t acc, int32_t a, int32_t b) { return add(acc, mul(a, b)); }
 __host__ __device__ __forceinline__ int64_t mac(int64_t acc, int64_t a, int64_t b) { return add(acc, mul(a, b)); }
 
+// Conjugation flips the sign bit of the imaginary part with an integer XOR: the same
+// bits as negation, without an FP add (a negated double would take the FP64 pipe).
+__host__ __device__ __forceinline__ float flip_sign_if(float x, bool c) {
+#ifdef __CUDA_ARCH__
+    return __int_as_float(__float_as_int(x) ^ ((int)c << 31));
+#else
+    return c ? -x : x;
+#endif
+}
+__host__ __device__ __forceinline__ double flip_sign_if(double x, bool c) {
+#ifdef __CUDA_ARCH__
+    return __longlong_as_double(__double_as_longlong(x) ^ ((long long)c << 63));
+#else
+    return c ? -x : x;
+#endif
+}
 template <typename V> __host__ __device__ __forceinline__ V conj_if(V a, bool c) { return a; }
 template <> __host__ __device__ __forceinline__ cf32 conj_if(cf32 a, bool c) {
-    return c ? cf32{a.re, -a.im} : a;
+    return cf32{a.re, flip_sign_if(a.im, c)};
 }
 template <> __host__ __device__ __forceinline__ cf64 conj_if(cf64 a, bool c) {
-    return c ? cf64{a.re, -a.im} : a;
+    return cf64{a.re, flip_sign_if(a.im, c)};
 }
 
 template <typename V> __host__ __device__ __forceinline__ bool is_zero(V a) { return a == V(0); }
@@ -265,6 +297,40 @@ void timer_before(cudaStream_t s);
 void timer_after(cudaStream_t s);
 
 inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
+
+// Scratch of one call: the caller's buffer, or a stream-ordered allocation freed on the
+// same stream when the call returns.
+struct Workspace {
+    void *p = nullptr;
+    size_t bytes = 0;
+    bool owned = false;
+    cudaStream_t s = nullptr;
+    int acquire(cudaStream_t stream, void *user, size_t user_bytes, size_t need) {
+        s = stream;
+        if (need == 0) { p = user; bytes = user_bytes; return GSA_OK; }
+        if (user) {
+            if (user_bytes < need)
+                return fail(GSA_ERR_INVALID_ARG, "workspace of %zu bytes is smaller than the %zu needed",
+                            user_bytes, need);
+            p = user;
+            bytes = user_bytes;
+            return GSA_OK;
+        }
+        cudaError_t e = cudaMallocAsync(&p, need, stream);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return fail(GSA_ERR_ALLOC, "stream-ordered workspace allocation of %zu bytes failed: %s",
+                        need, cudaGetErrorString(e));
+        }
+        owned = true;
+        bytes = need;
+        return GSA_OK;
+    }
+    ~Workspace() {
+        if (owned && p) cudaFreeAsync(p, s);
+    }
+};
+
 inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
 // Splits one workspace into aligned sub-buffers.
@@ -362,6 +428,8 @@ void set_pipe_threads(int t);
 int get_pipe_threads();
 void set_spmm_columns(int c);   // 0 (by value size), 1, 2, 4 or 8
 int get_spmm_columns();
+void set_plan_natural(int v);   // 1: row blocks in natural order even where a plan bins them
+int get_plan_natural();
 
 // Scatter: out[idx_j, c] += conj?(val_j) * (op(B)(o, c) * alpha), after the beta pass.
 // ALGO_MERGE: merge-path tiles (workspace: tile coordinates); otherwise outer blocks with
@@ -372,6 +440,15 @@ int launch_scatter(cudaStream_t s, const CompressedArgs<V, I> &a, int64_t k, Den
                    size_t ws_bytes);
 template <typename V, typename I>
 size_t scatter_workspace_size(int64_t outer_n, int64_t nnz, int64_t k, int algo);
+
+// dot(x, op(A), y) for fmt 0 CSR, 1 CSC (optional plan), 2 COO; the scalar is copied to
+// result_host and the stream synchronized.
+template <typename V, typename I>
+size_t dot_workspace_size(int fmt, int64_t outer_n, const Plan *plan);
+template <typename V, typename I>
+int launch_dot(cudaStream_t s, int fmt, int opA, int64_t m, int64_t n, int64_t nnz, const I *p0,
+               const I *p1, const V *val, int base, const V *x, const V *y, const Plan *plan,
+               void *ws, size_t ws_bytes, void *result_host);
 
 // COO: out[key_i, c] += conj?(val_i) * (op(B)(other_i, c) * alpha), after the beta pass.
 template <typename V, typename I>

@@ -38,83 +38,163 @@ namespace gsa {
 #endif
 template <typename V, int KC> constexpr int rb_min_blocks() { return KC * sizeof(V) <= 8 ? GSA_RB_MIN_BLOCKS : 0; }
 
+template <typename V> constexpr bool bins_pay() { return std::is_same<V, cf64>::value; }
+
+// One warp sums chunk `chunk` of a chunked row (entries [jb, je), 32 lanes, UNROLL loads
+// each in flight).  A row of one chunk is stored at once; otherwise the warp stores its
+// partial sum, and the warp that completes the row's last chunk adds the partials in
+// chunk order and writes the row.
+template <typename V, typename I, int KC>
+__device__ __forceinline__ void chunk_unit(const CompressedArgs<V, I> &a, int64_t k, const DenseIn<V> &B,
+                                           const DenseOut<V> &C, int64_t c0, unsigned cg, int64_t ncg,
+                                           int64_t chunk, const PlanRows &L) {
+    using O = Off<I>;
+    const int lane = threadIdx.x & 31;
+    if (chunk >= L.nchunks) return;
+    const int slot = L.chunk_slot[chunk];
+    const int64_t row = L.row[slot];
+    const int nch = L.count[slot];
+    const O nz = (O)a.nnz, base = (O)a.base;
+    O rb = (O)__ldg(a.ptr + row) - base;
+    O re = (O)__ldg(a.ptr + row + 1) - base;
+    rb = rb < nz ? rb : nz;
+    re = re < nz ? re : nz;
+    const O jb = rb + (O)(chunk - L.first[slot]) * (O)CHUNK;
+    const O je = jb < re && re - jb > (O)CHUNK ? jb + (O)CHUNK : re;
+    V acc[KC];
+#pragma unroll
+    for (int c = 0; c < KC; ++c) acc[c] = VT<V>::zero();
+    if (jb < je) accumulate_range<V, I, KC, 32, UNROLL>(a, B, jb + (O)lane, je, c0, k, acc);
+#pragma unroll
+    for (int c = 0; c < KC; ++c) {
+#pragma unroll
+        for (int m = 16; m > 0; m >>= 1) acc[c] = add(acc[c], shfl_xor(acc[c], m));
+    }
+    if (nch == 1) {  // the whole row: store it
+        if (lane == 0) {
+#pragma unroll
+            for (int c = 0; c < KC; ++c)
+                if (c0 + c < k) C.store(row, c0 + c, acc[c]);
+        }
+        return;
+    }
+    V *part = reinterpret_cast<V *>(L.partial);
+    int last = 0;
+    if (lane == 0) {
+#pragma unroll
+        for (int c = 0; c < KC; ++c)
+            if (c0 + c < k) part[chunk * k + c0 + c] = acc[c];
+        __threadfence();
+        const int prev = atomicAdd(&L.done[slot * ncg + cg], 1);
+        last = prev == nch - 1;
+    }
+    last = __shfl_sync(0xffffffffu, last, 0);
+    if (!last) return;
+    // the row's last chunk: add the partials in chunk order
+    __threadfence();
+    if (lane == 0) {
+        const int f = L.first[slot];
+#pragma unroll
+        for (int c = 0; c < KC; ++c) {
+            if (c0 + c >= k) continue;
+            V t = VT<V>::zero();
+            for (int q = 0; q < nch; ++q) t = add(t, ld_coherent(part + (int64_t)(f + q) * k + c0 + c));
+            C.store(row, c0 + c, t);
+        }
+        L.done[slot * ncg + cg] = 0;
+    }
+}
+
 template <typename V, typename I, int KC>
 __global__ void __launch_bounds__(RB_THREADS, rb_min_blocks<V, KC>())
 rowblock_kernel(CompressedArgs<V, I> a, int64_t k, DenseIn<V> B, DenseOut<V> C, int64_t ncg,
                 int64_t nrb, PlanRows L) {
-    const int lane = threadIdx.x & 31;
     // column group fastest; one group (SpMV) needs no division
     const unsigned cta = blockIdx.x;
     const unsigned cg = ncg == 1 ? 0u : cta % (unsigned)ncg;
     const int64_t unit = ncg == 1 ? (int64_t)cta : (int64_t)(cta / (unsigned)ncg);
     const int64_t c0 = (int64_t)cg * KC;
-
-    if (unit >= nrb) {
-        // ---- planned rows: a warp per chunk of up to CHUNK entries
-        using O = Off<I>;
-        const int64_t chunk = (unit - nrb) * RB_WARPS + (threadIdx.x >> 5);
-        if (chunk >= L.nchunks) return;
-        const int slot = L.chunk_slot[chunk];
-        const int64_t row = L.row[slot];
-        const int nch = L.count[slot];
-        const O nz = (O)a.nnz, base = (O)a.base;
-        O rb = (O)__ldg(a.ptr + row) - base;
-        O re = (O)__ldg(a.ptr + row + 1) - base;
-        rb = rb < nz ? rb : nz;
-        re = re < nz ? re : nz;
-        const O jb = rb + (O)(chunk - L.first[slot]) * (O)CHUNK;
-        const O je = jb < re && re - jb > (O)CHUNK ? jb + (O)CHUNK : re;
-        V acc[KC];
-#pragma unroll
-        for (int c = 0; c < KC; ++c) acc[c] = VT<V>::zero();
-        if (jb < je) accumulate_range<V, I, KC, 32, UNROLL>(a, B, jb + (O)lane, je, c0, k, acc);
-#pragma unroll
-        for (int c = 0; c < KC; ++c) {
-#pragma unroll
-            for (int m = 16; m > 0; m >>= 1) acc[c] = add(acc[c], shfl_xor(acc[c], m));
-        }
-        if (nch == 1) {  // the whole row: store it
-            if (lane == 0) {
-#pragma unroll
-                for (int c = 0; c < KC; ++c)
-                    if (c0 + c < k) C.store(row, c0 + c, acc[c]);
-            }
-            return;
-        }
-        V *part = reinterpret_cast<V *>(L.partial);
-        int last = 0;
-        if (lane == 0) {
-#pragma unroll
-            for (int c = 0; c < KC; ++c)
-                if (c0 + c < k) part[chunk * k + c0 + c] = acc[c];
-            __threadfence();
-            const int prev = atomicAdd(&L.done[slot * ncg + cg], 1);
-            last = prev == nch - 1;
-        }
-        last = __shfl_sync(0xffffffffu, last, 0);
-        if (!last) return;
-        // the row's last chunk: add the partials in chunk order
-        __threadfence();
-        if (lane == 0) {
-            const int f = L.first[slot];
-#pragma unroll
-            for (int c = 0; c < KC; ++c) {
-                if (c0 + c >= k) continue;
-                V t = VT<V>::zero();
-                for (int q = 0; q < nch; ++q) t = add(t, ld_coherent(part + (int64_t)(f + q) * k + c0 + c));
-                C.store(row, c0 + c, t);
-            }
-            L.done[slot * ncg + cg] = 0;
-        }
+    if (unit >= nrb) {  // chunked rows: a warp per chunk
+        chunk_unit<V, I, KC>(a, k, B, C, c0, cg, ncg, (unit - nrb) * RB_WARPS + (threadIdx.x >> 5), L);
         return;
     }
-
     // ---- this warp's 32 rows
     warp_unit<V, I, KC>(a, k, B, C, c0, unit * RB_THREADS + (threadIdx.x & ~31), L.skip_mask);
 }
 
 // ---------------------------------------------------------------------------
-// Plans: which outer entries are long, cut into chunks.
+// Bin order: the plan lists the rows bin by bin (rows of equal length up to 32, then of
+// lengths within a power of two), each bin with its lanes per row; warp w of the order
+// takes 32 / G consecutive rows of its bin.  All lanes of a warp then do about the same
+// number of multiply-adds: FP64 products on GB300 are bound by the FP64 pipe, which
+// counts a warp instruction whole however few of its lanes are active.
+
+struct BinView {
+    int64_t nwarps;
+    const int64_t *perm, *seg;
+    const uint8_t *warp_bin;
+    const int64_t *bins;  // per bin: first warp, first position, end position, lanes per row
+};
+
+template <typename V, typename I, int KC, int G>
+__device__ __forceinline__ void binned_rows(const CompressedArgs<V, I> &a, int64_t k, const DenseIn<V> &B,
+                                            const DenseOut<V> &C, int64_t c0, int64_t pos0, int64_t pend,
+                                            const BinView &bv) {
+    using O = Off<I>;
+    const int lane = threadIdx.x & 31;
+    const int64_t i = pos0 + lane / G;
+    const bool valid = i < pend;
+    int64_t row = 0;
+    O b = 0, e = 0;
+    if (valid) {
+        row = __ldg(bv.perm + i);
+        const O nz = (O)a.nnz;
+        b = (O)__ldg(bv.seg + 2 * i);
+        e = (O)__ldg(bv.seg + 2 * i + 1);
+        b = b < nz ? b : nz;
+        e = e < nz ? e : nz;
+        e = e < b ? b : e;
+    }
+    V acc[KC];
+#pragma unroll
+    for (int c = 0; c < KC; ++c) acc[c] = VT<V>::zero();
+    accumulate_range<V, I, KC, G, (G == 1 ? 1 : 2)>(a, B, b + (O)(lane % G), e, c0, k, acc);
+    if (G > 1) {
+#pragma unroll
+        for (int c = 0; c < KC; ++c) {
+#pragma unroll
+            for (int m = G / 2; m > 0; m >>= 1) acc[c] = add(acc[c], shfl_xor(acc[c], m, G));
+        }
+    }
+    if (lane % G == 0 && valid && row < a.outer_n) {
+#pragma unroll
+        for (int c = 0; c < KC; ++c)
+            if (KC == 1 || c0 + c < k) C.store(row, c0 + c, acc[c]);
+    }
+}
+
+template <typename V, typename I, int KC>
+__global__ void __launch_bounds__(RB_THREADS, rb_min_blocks<V, KC>())
+binned_kernel(CompressedArgs<V, I> a, int64_t k, DenseIn<V> B, DenseOut<V> C, int64_t ncg, BinView bv,
+              PlanRows L) {
+    const unsigned cta = blockIdx.x;
+    const unsigned cg = ncg == 1 ? 0u : cta % (unsigned)ncg;
+    const int64_t unit = ncg == 1 ? (int64_t)cta : (int64_t)(cta / (unsigned)ncg);
+    const int64_t c0 = (int64_t)cg * KC;
+    const int64_t w = unit * RB_WARPS + (threadIdx.x >> 5);
+    if (w >= bv.nwarps) {  // chunked rows
+        chunk_unit<V, I, KC>(a, k, B, C, c0, cg, ncg, w - bv.nwarps, L);
+        return;
+    }
+    const int bi = __ldg(bv.warp_bin + w);
+    const int64_t first_warp = __ldg(bv.bins + 4 * bi), pos = __ldg(bv.bins + 4 * bi + 1);
+    const int64_t pend = __ldg(bv.bins + 4 * bi + 2);
+    const int G = (int)__ldg(bv.bins + 4 * bi + 3);
+    const int64_t pos0 = pos + (w - first_warp) * (32 / G);
+    dispatch_lanes(G, 1, [&](auto g) {  // G is a power of two: picks exactly G lanes
+        binned_rows<V, I, KC, decltype(g)::value>(a, k, B, C, c0, pos0, pend, bv);
+    });
+}
 
 template <typename V, typename I>
 int launch_rowblock(cudaStream_t s, const CompressedArgs<V, I> &a, int64_t k, DenseIn<V> B,
@@ -128,25 +208,41 @@ int launch_rowblock(cudaStream_t s, const CompressedArgs<V, I> &a, int64_t k, De
     if (k == 1) KC = 1;
     if (KC > k) KC = k <= 1 ? 1 : (k <= 2 ? 2 : (k <= 4 ? 4 : 8));
     const int64_t ncg = ceil_div(k, KC);
+    if (plan && (plan->outer_n != a.outer_n || plan->nnz != a.nnz))
+        return fail(GSA_ERR_INVALID_ARG, "plan was made for another structure");
+    // the bin order pays where the FP64 pipe binds (ComplexF64: four FMAs per entry);
+    // elsewhere its scattered rows cost more memory traffic than idle lanes cost time
+    const bool binned = plan && plan->nbin_warps > 0 && !get_plan_natural() && bins_pay<V>();
     PlanRows L{};
-    int64_t units = nrb;
-    if (plan && plan->nlong > 0) {
-        if (plan->outer_n != a.outer_n || plan->nnz != a.nnz)
-            return fail(GSA_ERR_INVALID_ARG, "plan was made for another structure");
+    int64_t chunk_warps = 0;
+    const gsa_chunk_set *cs = plan ? (binned ? &plan->bin : &plan->nat) : nullptr;
+    if (cs && cs->nlong > 0) {
         const size_t need = rowblock_workspace_size(plan, sizeof(V), k);
         if (ws_bytes < need) return fail(GSA_ERR_INVALID_ARG, "rowblock workspace too small");
         Carver cv(ws);
-        int *done = cv.take<int>((size_t)(plan->nlong * ncg));
-        void *partial = cv.take<V>((size_t)(plan->nchunks * k));
-        int rc = check_cuda(cudaMemsetAsync(done, 0, sizeof(int) * plan->nlong * ncg, s), "plan counters");
+        int *done = cv.take<int>((size_t)(cs->nlong * ncg));
+        void *partial = cv.take<V>((size_t)(cs->nchunks * k));
+        int rc = check_cuda(cudaMemsetAsync(done, 0, sizeof(int) * cs->nlong * ncg, s), "plan counters");
         if (rc) return rc;
-        L = PlanRows{plan->nlong, plan->nchunks, plan->row, plan->first, plan->count, plan->chunk_slot,
-                     plan->skip_mask, done, partial};
-        units += ceil_div(plan->nchunks, RB_WARPS);
+        L = plan_rows(*cs);
+        L.done = done;
+        L.partial = partial;
+        chunk_warps = cs->nchunks;
     }
+    const int64_t units = binned ? ceil_div(plan->nbin_warps + chunk_warps, RB_WARPS)
+                                 : nrb + ceil_div(chunk_warps, RB_WARPS);
     const int64_t blocks = units * ncg;
     if (blocks > 0x7fffffffLL) return fail(GSA_ERR_UNSUPPORTED, "too many rows");
     timer_before(s);
+    if (binned) {
+        const BinView bv{plan->nbin_warps, plan->perm, plan->seg, plan->warp_bin, plan->bins};
+        if (KC == 1) binned_kernel<V, I, 1><<<(unsigned)blocks, RB_THREADS, 0, s>>>(a, k, B, C, ncg, bv, L);
+        else if (KC == 2) binned_kernel<V, I, 2><<<(unsigned)blocks, RB_THREADS, 0, s>>>(a, k, B, C, ncg, bv, L);
+        else if (KC == 4) binned_kernel<V, I, 4><<<(unsigned)blocks, RB_THREADS, 0, s>>>(a, k, B, C, ncg, bv, L);
+        else binned_kernel<V, I, 8><<<(unsigned)blocks, RB_THREADS, 0, s>>>(a, k, B, C, ncg, bv, L);
+        timer_after(s);
+        return check_cuda(cudaGetLastError(), "binned_kernel");
+    }
     if (KC == 1) rowblock_kernel<V, I, 1><<<(unsigned)blocks, RB_THREADS, 0, s>>>(a, k, B, C, ncg, nrb, L);
     else if (KC == 2) rowblock_kernel<V, I, 2><<<(unsigned)blocks, RB_THREADS, 0, s>>>(a, k, B, C, ncg, nrb, L);
     else if (KC == 4) rowblock_kernel<V, I, 4><<<(unsigned)blocks, RB_THREADS, 0, s>>>(a, k, B, C, ncg, nrb, L);
@@ -158,14 +254,65 @@ int launch_rowblock(cudaStream_t s, const CompressedArgs<V, I> &a, int64_t k, De
 static int g_spmm_columns = 0;  // 0: by value size
 void set_spmm_columns(int c) { g_spmm_columns = c; }
 int get_spmm_columns() { return g_spmm_columns; }
+static int g_plan_order = 0;    // 0: the plan's choice, 1: natural order always
+void set_plan_natural(int v) { g_plan_order = v; }
+int get_plan_natural() { return g_plan_order; }
 
 size_t rowblock_workspace_size(const Plan *plan, size_t vsize, int64_t k) {
-    if (!plan || plan->nlong == 0 || k == 0) return 0;
-    const int64_t ncg = k;  // an upper bound on the column groups of any KC
+    if (!plan || k == 0) return 0;
+    // enough for either chunk set; ncg <= k for any KC
+    const int64_t nlong = plan->nat.nlong > plan->bin.nlong ? plan->nat.nlong : plan->bin.nlong;
+    const int64_t nchunks = plan->nat.nchunks > plan->bin.nchunks ? plan->nat.nchunks : plan->bin.nchunks;
+    if (nlong == 0) return 0;
     Carver cv(nullptr);
-    cv.take<int>((size_t)(plan->nlong * ncg));
-    cv.take<unsigned char>((size_t)(plan->nchunks * k) * vsize + 16);
+    cv.take<int>((size_t)(nlong * k));
+    cv.take<unsigned char>((size_t)(nchunks * k) * vsize + 16);
     return align_up(cv.off, 256);
+}
+
+// ---------------------------------------------------------------------------
+// Plans.
+
+// Bin of a row of len <= CHUNK entries and its lanes per row: rows of equal length up to
+// 32 (a lane each), then (32, 64], (64, 128], (128, 256], (256, 512] with 2, 4, 8, 16
+// lanes -- every lane sums 16 to 32 entries before the width-G reduction.
+constexpr int NBINS = 37;
+static int bin_of(int64_t len) {
+    if (len <= 32) return (int)len;
+    if (len <= 64) return 33;
+    if (len <= 128) return 34;
+    if (len <= 256) return 35;
+    return 36;
+}
+static int bin_lanes(int b) { return b <= 32 ? 1 : 1 << (b - 32); }
+
+// Lane utilisation of the natural order: the fraction of lane-iterations that do a
+// multiply-add when a warp of 32 rows runs G lanes per row (G from the rows' average, as
+// warp_extent and dispatch_lanes pick it) and each pass lasts as long as its longest row.
+static double natural_utilisation(const std::vector<int64_t> &len, const std::vector<uint32_t> &mask) {
+    double busy = 0, held = 0;
+    const int64_t n = (int64_t)len.size();
+    for (int64_t w0 = 0; w0 < n; w0 += 32) {
+        const int64_t w1 = w0 + 32 < n ? w0 + 32 : n;
+        int64_t l[32] = {0};
+        int64_t total = 0;
+        for (int64_t r = w0; r < w1; ++r) {
+            const bool skip = (mask[(size_t)(w0 >> 5)] >> (r - w0)) & 1u;
+            l[r - w0] = skip ? 0 : len[r];
+            total += l[r - w0];
+        }
+        const int64_t avg = total >> 5;
+        int G = 1;
+        while (G < 32 && avg > (int64_t)G * G1_AVG) G <<= 1;
+        for (int p = 0; p < G; ++p) {
+            int64_t longest = 0;
+            for (int q = p * (32 / G); q < (p + 1) * (32 / G); ++q)
+                longest = l[q] > longest ? l[q] : longest;
+            held += 32.0 * (double)ceil_div(longest, G);
+        }
+        busy += (double)total;
+    }
+    return held > 0 ? busy / held : 1.0;
 }
 
 template <typename I>
@@ -176,65 +323,136 @@ static int build_plan(cudaStream_t s, int64_t outer_n, int64_t nnz, const I *ptr
     if (rc) return rc;
     rc = check_cuda(cudaStreamSynchronize(s), "plan: sync");
     if (rc) return rc;
-    std::vector<int64_t> len((size_t)outer_n);
+    std::vector<int64_t> beg((size_t)outer_n), len((size_t)outer_n);
     int64_t maxlen = 0;
     for (int64_t r = 0; r < outer_n; ++r) {
         int64_t b = (int64_t)h[r] - base, e = (int64_t)h[r + 1] - base;
         b = b < 0 ? 0 : (b > nnz ? nnz : b);
         e = e < b ? b : (e > nnz ? nnz : e);
+        beg[r] = b;
         len[r] = e - b;
         maxlen = len[r] > maxlen ? len[r] : maxlen;
     }
-    // A row goes to the plan when it is longer than CHUNK, or longer than PLAN_LEN and
-    // more than 4x the average of its warp's 32 rows (it would hold the warp's other
-    // rows back).  Rows of even length stay in their warps, G lanes per row.
-    std::vector<int64_t> row;
-    std::vector<int32_t> first, count, slot;
-    std::vector<uint32_t> mask((size_t)ceil_div(outer_n, 32), 0u);
+    // Natural order: a row goes to chunks when it is longer than CHUNK, or longer than
+    // PLAN_LEN and more than 4x the average of its warp's 32 rows (it would hold the
+    // warp's other rows back).  Bin order: only rows longer than CHUNK are chunked.
+    std::vector<uint32_t> mask_nat((size_t)ceil_div(outer_n, 32), 0u), mask_bin(mask_nat.size(), 0u);
     for (int64_t w0 = 0; w0 < outer_n; w0 += 32) {
         const int64_t w1 = w0 + 32 < outer_n ? w0 + 32 : outer_n;
         int64_t sum = 0;
         for (int64_t r = w0; r < w1; ++r) sum += len[r];
         for (int64_t r = w0; r < w1; ++r) {
-            if (len[r] <= PLAN_LEN || (len[r] <= CHUNK && 8 * len[r] <= sum)) continue;
+            if (len[r] > CHUNK) mask_bin[(size_t)(w0 >> 5)] |= 1u << (r - w0);
+            if (len[r] > CHUNK || (len[r] > PLAN_LEN && 8 * len[r] > sum))
+                mask_nat[(size_t)(w0 >> 5)] |= 1u << (r - w0);
+        }
+    }
+    // bin order when the natural one would leave over a quarter of the lanes idle
+    const bool binned = outer_n >= 4096 && natural_utilisation(len, mask_nat) < 0.75;
+    struct HostSet {
+        std::vector<int64_t> row;
+        std::vector<int32_t> first, count, slot;
+    } hs[2];
+    for (int t = 0; t < (binned ? 2 : 1); ++t) {
+        const std::vector<uint32_t> &mask = t == 0 ? mask_nat : mask_bin;
+        HostSet &h2 = hs[t];
+        for (int64_t r = 0; r < outer_n; ++r) {
+            if (!((mask[(size_t)(r >> 5)] >> (r & 31)) & 1u)) continue;
             const int64_t nch = ceil_div(len[r], CHUNK);
-            if ((int64_t)slot.size() + nch > 0x7fffffffLL)
+            if ((int64_t)h2.slot.size() + nch > 0x7fffffffLL)
                 return fail(GSA_ERR_UNSUPPORTED, "plan: too many chunks");
-            mask[(size_t)(w0 >> 5)] |= 1u << (r - w0);
-            row.push_back(r);
-            first.push_back((int32_t)slot.size());
-            count.push_back((int32_t)nch);
-            for (int64_t q = 0; q < nch; ++q) slot.push_back((int32_t)(row.size() - 1));
+            h2.row.push_back(r);
+            h2.first.push_back((int32_t)h2.slot.size());
+            h2.count.push_back((int32_t)nch);
+            for (int64_t q = 0; q < nch; ++q) h2.slot.push_back((int32_t)(h2.row.size() - 1));
+        }
+    }
+    std::vector<int64_t> perm, seg, bins;
+    std::vector<uint8_t> warp_bin;
+    if (binned) {  // counting sort of the unchunked rows by bin, stable
+        std::vector<int64_t> cnt(NBINS + 1, 0);
+        for (int64_t r = 0; r < outer_n; ++r)
+            if (len[r] <= CHUNK) ++cnt[(size_t)bin_of(len[r]) + 1];
+        for (int b = 0; b < NBINS; ++b) cnt[(size_t)b + 1] += cnt[(size_t)b];
+        perm.resize((size_t)cnt[NBINS]);
+        seg.resize(perm.size() * 2);
+        std::vector<int64_t> at(cnt.begin(), cnt.end() - 1);
+        for (int64_t r = 0; r < outer_n; ++r) {
+            if (len[r] > CHUNK) continue;
+            const int64_t i = at[(size_t)bin_of(len[r])]++;
+            perm[(size_t)i] = r;
+            seg[(size_t)(2 * i)] = beg[r];
+            seg[(size_t)(2 * i + 1)] = beg[r] + len[r];
+        }
+        bins.assign(4 * NBINS, 0);
+        int64_t w = 0;
+        for (int b = 0; b < NBINS; ++b) {
+            const int G = bin_lanes(b);
+            const int64_t nrows = cnt[(size_t)b + 1] - cnt[(size_t)b];
+            const int64_t nw = ceil_div(nrows, 32 / G);
+            bins[4 * b] = w;
+            bins[4 * b + 1] = cnt[(size_t)b];
+            bins[4 * b + 2] = cnt[(size_t)b + 1];
+            bins[4 * b + 3] = G;
+            for (int64_t q = 0; q < nw; ++q) warp_bin.push_back((uint8_t)b);
+            w += nw;
         }
     }
     p->outer_n = outer_n;
     p->nnz = nnz;
     p->max_len = maxlen;
-    p->nlong = (int64_t)row.size();
-    p->nchunks = (int64_t)slot.size();
-    if (p->nlong == 0) return GSA_OK;
-    size_t bytes = align_up(row.size() * 8, 256) + align_up(first.size() * 4, 256) +
-                   align_up(count.size() * 4, 256) + align_up(slot.size() * 4, 256) +
-                   align_up(mask.size() * 4, 256);
+    p->nbin_warps = (int64_t)warp_bin.size();
+    p->nplanned = binned ? outer_n : (int64_t)hs[0].row.size();
+    if (p->nplanned == 0) return GSA_OK;
+    size_t bytes = align_up(perm.size() * 8, 256) + align_up(seg.size() * 8, 256) +
+                   align_up(warp_bin.size(), 256) + align_up(bins.size() * 8, 256);
+    for (int t = 0; t < 2; ++t)
+        bytes += align_up(hs[t].row.size() * 8, 256) + align_up(hs[t].first.size() * 4, 256) +
+                 align_up(hs[t].count.size() * 4, 256) + align_up(hs[t].slot.size() * 4, 256) +
+                 align_up(mask_nat.size() * 4, 256);
     rc = check_cuda(cudaMalloc(&p->mem, bytes), "plan: device memory");
     if (rc) return rc;
     Carver cv(p->mem);
-    int64_t *d_row = cv.take<int64_t>(row.size());
-    int32_t *d_first = cv.take<int32_t>(first.size());
-    int32_t *d_count = cv.take<int32_t>(count.size());
-    int32_t *d_slot = cv.take<int32_t>(slot.size());
-    uint32_t *d_mask = cv.take<uint32_t>(mask.size());
-    rc = check_cuda(cudaMemcpy(d_row, row.data(), row.size() * 8, cudaMemcpyHostToDevice), "plan: rows");
-    if (!rc) rc = check_cuda(cudaMemcpy(d_first, first.data(), first.size() * 4, cudaMemcpyHostToDevice), "plan: first");
-    if (!rc) rc = check_cuda(cudaMemcpy(d_count, count.data(), count.size() * 4, cudaMemcpyHostToDevice), "plan: count");
-    if (!rc) rc = check_cuda(cudaMemcpy(d_slot, slot.data(), slot.size() * 4, cudaMemcpyHostToDevice), "plan: chunks");
-    if (!rc) rc = check_cuda(cudaMemcpy(d_mask, mask.data(), mask.size() * 4, cudaMemcpyHostToDevice), "plan: mask");
+    auto up = [&](void *dst, const void *src, size_t n, const char *what) {
+        if (!rc && n) rc = check_cuda(cudaMemcpy(dst, src, n, cudaMemcpyHostToDevice), what);
+    };
+    for (int t = 0; t < 2; ++t) {
+        gsa_chunk_set &c = t == 0 ? p->nat : p->bin;
+        const std::vector<uint32_t> &mask = t == 0 ? mask_nat : mask_bin;
+        const HostSet &h2 = hs[t];
+        int64_t *d_row = cv.take<int64_t>(h2.row.size());
+        int32_t *d_first = cv.take<int32_t>(h2.first.size());
+        int32_t *d_count = cv.take<int32_t>(h2.count.size());
+        int32_t *d_slot = cv.take<int32_t>(h2.slot.size());
+        uint32_t *d_mask = cv.take<uint32_t>(mask.size());
+        up(d_row, h2.row.data(), h2.row.size() * 8, "plan: rows");
+        up(d_first, h2.first.data(), h2.first.size() * 4, "plan: first");
+        up(d_count, h2.count.data(), h2.count.size() * 4, "plan: count");
+        up(d_slot, h2.slot.data(), h2.slot.size() * 4, "plan: chunks");
+        up(d_mask, mask.data(), mask.size() * 4, "plan: mask");
+        c.nlong = (int64_t)h2.row.size();
+        c.nchunks = (int64_t)h2.slot.size();
+        c.row = d_row;
+        c.first = d_first;
+        c.count = d_count;
+        c.chunk_slot = d_slot;
+        c.skip_mask = d_mask;
+    }
+    int64_t *d_perm = cv.take<int64_t>(perm.size());
+    int64_t *d_seg = cv.take<int64_t>(seg.size());
+    uint8_t *d_wb = cv.take<uint8_t>(warp_bin.size());
+    int64_t *d_bins = cv.take<int64_t>(bins.size());
+    up(d_perm, perm.data(), perm.size() * 8, "plan: order");
+    up(d_seg, seg.data(), seg.size() * 8, "plan: extents");
+    up(d_wb, warp_bin.data(), warp_bin.size(), "plan: warp bins");
+    up(d_bins, bins.data(), bins.size() * 8, "plan: bins");
     if (rc) return rc;
-    p->row = d_row;
-    p->first = d_first;
-    p->count = d_count;
-    p->chunk_slot = d_slot;
-    p->skip_mask = d_mask;
+    if (binned) {
+        p->perm = d_perm;
+        p->seg = d_seg;
+        p->warp_bin = d_wb;
+        p->bins = d_bins;
+    }
     return GSA_OK;
 }
 

@@ -119,6 +119,19 @@ struct PlanRows {
     void *partial;             // nchunks * k values
 };
 
+// The device view of one chunk set of a plan (no counters or partials yet).
+inline PlanRows plan_rows(const gsa_chunk_set &c) {
+    PlanRows L{};
+    L.nlong = c.nlong;
+    L.nchunks = c.nchunks;
+    L.row = c.row;
+    L.first = c.first;
+    L.count = c.count;
+    L.chunk_slot = c.chunk_slot;
+    L.skip_mask = c.skip_mask;
+    return L;
+}
+
 // The extents [b, e) of one warp's 32 outer entries starting at row0 (a multiple of 32),
 // clamped to [0, nnz] (a malformed pointer never leads outside idx/val); entries the plan
 // takes (bit l of skip_mask[row0 / 32]) get an empty extent and skip = 1.  Returns the

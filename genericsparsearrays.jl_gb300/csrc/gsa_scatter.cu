@@ -121,6 +121,12 @@ scatter_merge_kernel(CompressedArgs<V, I> a, int64_t k, DenseIn<V> B, DenseOut<V
 // ---------------------------------------------------------------------------
 // Outer-block scatter (the default).
 
+// op(B)(o, c) * alpha, without the multiply when alpha == 1 of a real type (exact).
+template <typename V>
+__device__ __forceinline__ V alpha_times(const DenseOut<V> &C, V b) {
+    return C.alpha_one ? b : mul(b, C.alpha);
+}
+
 // C[idx_j, c0 + c] += conj?(a_j) * xa[c] for j = jb, jb+S, ... < je; entries whose index
 // falls outside C's rows are skipped.
 template <typename V, typename I, int KC, int S>
@@ -159,7 +165,7 @@ __device__ __forceinline__ void scatter_rows(const CompressedArgs<V, I> &a, int6
         V xa[KC];
 #pragma unroll
         for (int c = 0; c < KC; ++c)
-            xa[c] = (KC == 1 || c0 + c < k) ? mul(B.at(o, c0 + c), C.alpha) : VT<V>::zero();
+            xa[c] = (KC == 1 || c0 + c < k) ? alpha_times(C, B.at(o, c0 + c)) : VT<V>::zero();
         scatter_range<V, I, KC, G>(a, C, qb + (O)(lane % G), qe, c0, k, xa);
     }
 }
@@ -191,7 +197,7 @@ scatter_block_kernel(CompressedArgs<V, I> a, int64_t k, DenseIn<V> B, DenseOut<V
         V xa[KC];
 #pragma unroll
         for (int c = 0; c < KC; ++c)
-            xa[c] = (KC == 1 || c0 + c < k) ? mul(B.at(o, c0 + c), C.alpha) : VT<V>::zero();
+            xa[c] = (KC == 1 || c0 + c < k) ? alpha_times(C, B.at(o, c0 + c)) : VT<V>::zero();
         scatter_range<V, I, KC, 32>(a, C, jb + (O)lane, je, c0, k, xa);
         return;
     }
@@ -215,17 +221,11 @@ int launch_scatter_block(cudaStream_t s, const CompressedArgs<V, I> &a, int64_t 
     const int64_t ncg = ceil_div(k, KC);
     PlanRows P{};
     int64_t units = nrb;
-    if (plan && plan->nlong > 0) {
+    if (plan && plan->nat.nlong > 0) {  // natural order: the natural chunk set
         if (plan->outer_n != a.outer_n || plan->nnz != a.nnz)
             return fail(GSA_ERR_INVALID_ARG, "plan was made for another structure");
-        P.nlong = plan->nlong;
-        P.nchunks = plan->nchunks;
-        P.row = plan->row;
-        P.first = plan->first;
-        P.count = plan->count;
-        P.chunk_slot = plan->chunk_slot;
-        P.skip_mask = plan->skip_mask;
-        units += ceil_div(plan->nchunks, RB_WARPS);
+        P = plan_rows(plan->nat);
+        units += ceil_div(plan->nat.nchunks, RB_WARPS);
     }
     const int64_t blocks = units * ncg;
     if (blocks > 0x7fffffffLL) return fail(GSA_ERR_UNSUPPORTED, "too many outer entries");

@@ -542,6 +542,56 @@ def mul(A, B) -> torch.Tensor:
     return mul_(C, A, B)
 
 
+def dot(x: torch.Tensor, A, y: torch.Tensor):
+    """Three-argument ``dot(x, A, y) = x' A y`` (LinearAlgebra.dot; the reference's methods at
+    src/matrix_csr/matrix_csr.jl:213-277, src/matrix_csc/matrix_csc.jl:219,
+    src/matrix_coo/matrix_coo.jl:227): the sum over stored entries of conj(x_l) a y_r.
+
+    Same checks and messages as the reference (two ``DimensionMismatch``, then the backend
+    ``ArgumentError``); the element type is the promotion of the three, as there.  Returns a
+    numpy scalar; synchronizes the current stream (the reference returns the scalar to the
+    host as well).
+    """
+    Ap, opA = _unwrap_sparse(A)
+    if not isinstance(Ap, AbstractGenericSparseMatrix):
+        raise ArgumentError("A must be a GenericSparseMatrixCSR/CSC/COO or its transpose/adjoint")
+    if not isinstance(x, torch.Tensor) or not isinstance(y, torch.Tensor) or x.dim() != 1 or y.dim() != 1:
+        raise ArgumentError("x and y must be torch vectors")
+    Am, An = (Ap.m, Ap.n) if opA == _lib.OP_N else (Ap.n, Ap.m)
+    if Am != x.shape[0]:
+        raise DimensionMismatch(f"first dimension of A, {Am}, does not match the length of x, {x.shape[0]}")
+    if An != y.shape[0]:
+        raise DimensionMismatch(f"second dimension of A, {An}, does not match the length of y, {y.shape[0]}")
+    if not (x.device == Ap.device == y.device):
+        raise ArgumentError("All arrays must have the same backend")
+    if Ap.device.type != "cuda":
+        raise ArgumentError("dot runs on the GPU only; adapt the arrays to CUDA first")
+    dt = torch.promote_types(torch.promote_types(Ap.dtype, x.dtype), y.dtype)
+    if dt not in _DTYPE:
+        raise ArgumentError(f"unsupported element type {dt}")
+    val = Ap.nzval if Ap.dtype == dt else Ap.nzval.to(dt)
+    xv = x.to(dt).contiguous()
+    yv = y.to(dt).contiguous()
+    lib = _lib.load()
+    out = np.zeros(1, dtype=_NP_OF[dt])
+    stream = _stream_ptr(Ap.device)
+    with torch.cuda.device(Ap.device):
+        if isinstance(Ap, GenericSparseMatrixCOO):
+            st = lib.gsa_coo_dot(stream, _DTYPE[dt], _ITYPE[Ap.itype], Ap.m, Ap.n, nnz(Ap), _ptr(Ap.rowind),
+                                 _ptr(Ap.colind), _ptr(val), BASE, opA, _ptr(xv), _ptr(yv),
+                                 out.ctypes.data_as(ctypes.c_void_p), None, 0)
+        else:
+            csr = isinstance(Ap, GenericSparseMatrixCSR)
+            ptr, idx = (Ap.rowptr, Ap.colval) if csr else (Ap.colptr, Ap.rowval)
+            plan = _gather_plan(Ap)
+            fn = lib.gsa_csr_dot if csr else lib.gsa_csc_dot
+            st = fn(stream, _DTYPE[dt], _ITYPE[Ap.itype], Ap.m, Ap.n, nnz(Ap), _ptr(ptr), _ptr(idx), _ptr(val),
+                    BASE, opA, _ptr(xv), _ptr(yv), out.ctypes.data_as(ctypes.c_void_p),
+                    ctypes.c_void_p(plan.handle) if plan is not None else None, None, 0)
+    _lib.check(st)
+    return out[0]
+
+
 # ---------------------------------------------------------------------------
 # Conversions (src/conversions/conversions.jl)
 

@@ -74,8 +74,10 @@ typedef enum {
 /* Tuning keys for gsa_set_tuning / gsa_get_tuning. */
 typedef enum {
     GSA_TUNE_PIPE_THREADS = 1, /* threads per CTA of the pipelined SpMV: 256 or 512 */
-    GSA_TUNE_SPMM_COLUMNS = 2  /* right-hand-side columns a thread accumulates in the default
+    GSA_TUNE_SPMM_COLUMNS = 2, /* right-hand-side columns a thread accumulates in the default
                                   gather with k > 1: 0 (by value size), 1, 2, 4 or 8 */
+    GSA_TUNE_PLAN_ORDER = 3    /* 0: a planned gather runs in the plan's order (bin order
+                                  where the plan chose it); 1: always in natural row order */
 } gsa_tune_key;
 
 /* ---- library ------------------------------------------------------------ */
@@ -192,6 +194,32 @@ int gsa_csc_mul_planned(void *stream, int dtype, int itype, int64_t m, int64_t n
                         int64_t k, const void *B, int64_t ldb, int opB, void *C, int64_t ldc,
                         const void *alpha, const void *beta, const gsa_plan *plan, void *workspace,
                         size_t workspace_bytes);
+
+/* ---- three-argument dot ---------------------------------------------------
+ * *result = dot(x, op(A), y) = sum over stored entries of conj(x_l) * a * y_r (l = row,
+ * r = col for opA = N, swapped for T/C, a conjugated for C); x has rows(op(A)) entries,
+ * y cols(op(A)).  result is a HOST pointer to one value of dtype; the call synchronizes
+ * the stream (the reference returns the scalar to the host too).  The sum is taken in a
+ * fixed order (deterministic).  Replace LinearAlgebra.dot methods generated at
+ * src/matrix_csr/matrix_csr.jl:213-277, src/matrix_csc/matrix_csc.jl:219 and
+ * src/matrix_coo/matrix_coo.jl:227 (kernels kernel_workgroup_dot_*_N! / _T!).  plan:
+ * optional (NULL), a plan of the compressed structure for long outer entries.
+ * workspace: NULL (stream-ordered allocation) or gsa_dot_workspace_size bytes. */
+int gsa_csr_dot(void *stream, int dtype, int itype, int64_t m, int64_t n, int64_t nnz,
+                const void *rowptr, const void *colval, const void *nzval, int base, int opA,
+                const void *x, const void *y, void *result, const gsa_plan *plan,
+                void *workspace, size_t workspace_bytes);
+int gsa_csc_dot(void *stream, int dtype, int itype, int64_t m, int64_t n, int64_t nnz,
+                const void *colptr, const void *rowval, const void *nzval, int base, int opA,
+                const void *x, const void *y, void *result, const gsa_plan *plan,
+                void *workspace, size_t workspace_bytes);
+int gsa_coo_dot(void *stream, int dtype, int itype, int64_t m, int64_t n, int64_t nnz,
+                const void *rowind, const void *colind, const void *nzval, int base, int opA,
+                const void *x, const void *y, void *result, void *workspace,
+                size_t workspace_bytes);
+/* format: 0 CSR, 1 CSC, 2 COO (plan ignored for COO). */
+size_t gsa_dot_workspace_size(int format, int dtype, int itype, int64_t m, int64_t n,
+                              const gsa_plan *plan);
 
 /* Workspace bytes for gsa_csr_mul / gsa_csc_mul with these sizes (format:
  * 0 CSR, 1 CSC).  0 means none is needed. */

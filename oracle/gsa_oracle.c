@@ -285,6 +285,13 @@ int oracle_mul_exact(int fmt, int opA, int dtype, int itype, int64_t m, int64_t 
              alpha, beta, yre, yim, scale)
 }
 
+int oracle_dot(int fmt, int opA, int dtype, int itype, int64_t m, int64_t n, int64_t nnz,
+               const void *p0, const void *p1, const void *val, int base, const void *x,
+               const void *y, void *out, double *out_re, double *out_im, double *out_scale) {
+    if (dtype < 0 || dtype > 5 || itype < 0 || itype > 1) return 3;
+    DISPATCH(dot, fmt, opA, m, n, nnz, p0, p1, val, base, x, y, out, out_re, out_im, out_scale)
+}
+
 int oracle_coo_to_compressed(int colmajor, int dtype, int itype, int64_t m, int64_t n,
                              int64_t nnz, const void *rowind, const void *colind,
                              const void *val, int base, void *ptr_out, void *idx_out,

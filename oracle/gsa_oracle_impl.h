@@ -211,6 +211,56 @@ static int FN(mul_exact)(int fmt, int opA, int64_t m, int64_t n, int64_t nnz,
     return 0;
 }
 
+/* Three-argument dot(x, op(A), y) = sum over stored entries of conj(x_l) * a * y_r,
+ * following kernel_workgroup_dot_{csr,csc,coo}_{N,T}! (src/matrix_csr/matrix_csr_kernels.jl:47-131,
+ * src/matrix_csc/matrix_csc_kernels.jl:47-131, src/matrix_coo/matrix_coo_kernels.jl:45-130)
+ * and LinearAlgebra's dot(x::Number, a::Number, y::Number) = conj(x) * a * y: for an
+ * entry (row, col), l = row and r = col for op = N, swapped for T/C (a conjugated for C).
+ * *out gets the sum in the reference's arithmetic, terms in storage order (one of the
+ * orders the reference's work items may take; exact for integers); out_re/out_im the
+ * sum in double-double and out_scale sum |x_l||a||y_r|. */
+static int FN(dot)(int fmt, int opA, int64_t m, int64_t n, int64_t nnz,
+                   const void *p0v, const void *p1v, const void *valv, int base,
+                   const void *xv, const void *yv, void *outv,
+                   double *out_re, double *out_im, double *out_scale) {
+    const I *p0 = (const I *)p0v, *p1 = (const I *)p1v;
+    const V *val = (const V *)valv, *x = (const V *)xv, *y = (const V *)yv;
+    int conjA = (opA == 2), trans = (opA != 0);
+    int64_t outer_n = (fmt == 0) ? m : n;
+    int64_t cnt = (fmt == 2) ? nnz : outer_n;
+    V sum = V_ZERO;
+    dd sre = {0.0, 0.0}, sim = {0.0, 0.0};
+    double scale = 0.0;
+    for (int64_t o = 0; o < cnt; ++o) {
+        int64_t jlo = (fmt == 2) ? o : (int64_t)p0[o] - base;
+        int64_t jhi = (fmt == 2) ? o + 1 : (int64_t)p0[o + 1] - base;
+        for (int64_t j = jlo; j < jhi; ++j) {
+            int64_t row, col;
+            if (fmt == 0) { row = o; col = (int64_t)p1[j] - base; }
+            else if (fmt == 1) { row = (int64_t)p1[j] - base; col = o; }
+            else { row = (int64_t)p0[j] - base; col = (int64_t)p1[j] - base; }
+            int64_t l = trans ? col : row, r = trans ? row : col;
+            V a = conjA ? V_CONJ(val[j]) : val[j];
+            sum = V_ADD(sum, V_MUL(V_MUL(V_CONJ(x[l]), a), y[r]));
+            double xr, xi, ar, ai, yr, yi;
+            V_TO_C(x[l], xr, xi);
+            V_TO_C(a, ar, ai);
+            V_TO_C(y[r], yr, yi);
+            /* p = conj(x) a, exactly as double-double parts; then p * y */
+            dd pr = dd_add_dd(two_prod(xr, ar), two_prod(xi, ai));
+            dd pi = dd_add_dd(two_prod(xr, ai), two_prod(-xi, ar));
+            sre = dd_add_dd(sre, dd_add_dd(dd_mul_d(pr, yr), dd_mul_d(pi, -yi)));
+            sim = dd_add_dd(sim, dd_add_dd(dd_mul_d(pr, yi), dd_mul_d(pi, yr)));
+            scale += hypot(xr, xi) * hypot(ar, ai) * hypot(yr, yi);
+        }
+    }
+    *(V *)outv = sum;
+    *out_re = sre.hi + sre.lo;
+    *out_im = sim.hi + sim.lo;
+    *out_scale = scale;
+    return 0;
+}
+
 /* COO -> compressed conversion, following src/conversions/conversions.jl:282-323
  * (COO -> CSR) and :171-212 (COO -> CSC) with kernel_make_csr_keys! /
  * kernel_make_csc_keys! (src/conversions/conversion_kernels.jl:38-57):

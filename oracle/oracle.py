@@ -73,8 +73,10 @@ def lib():
                                                    i32, vp, vp, vp]
             L.oracle_compressed_to_coo.argtypes = [i32, i32, i32, i64, i64, i64, vp, vp, vp,
                                                    i32, vp, vp, vp]
+            L.oracle_dot.argtypes = [i32, i32, i32, i32, i64, i64, i64, vp, vp, vp, i32,
+                                     vp, vp, vp, vp, vp, vp]
             for f in ("oracle_mul", "oracle_mul_exact", "oracle_coo_to_compressed",
-                      "oracle_compressed_to_coo", "oracle_max_threads"):
+                      "oracle_compressed_to_coo", "oracle_max_threads", "oracle_dot"):
                 getattr(L, f).restype = ctypes.c_int
             _lib = L
     return _lib
@@ -153,6 +155,26 @@ def mul_exact(fmt, opA, m, n, p0, p1, val, base, B, C0, alpha=1, beta=0, opB="N"
     if C0.ndim == 1:
         return y[:, 0], sc[:, 0]
     return y, sc
+
+
+def dot(fmt, opA, m, n, p0, p1, val, base, x, y):
+    """dot(x, op(A), y): returns (value in the reference's arithmetic with terms in storage
+    order, double-double value as complex128/float64, scale sum|x||a||y|)."""
+    val = np.ascontiguousarray(val)
+    dt = val.dtype
+    p0 = np.ascontiguousarray(p0)
+    p1 = np.ascontiguousarray(p1, dtype=p0.dtype)
+    x = np.ascontiguousarray(x, dtype=dt)
+    y = np.ascontiguousarray(y, dtype=dt)
+    out = np.zeros(1, dtype=dt)
+    re, im, sc = (ctypes.c_double(0.0) for _ in range(3))
+    rc = lib().oracle_dot(FMT[fmt], OP[opA], DTYPE[dt], ITYPE[p0.dtype], m, n, val.size, _p(p0),
+                          _p(p1), _p(val), base, _p(x), _p(y), _p(out), ctypes.byref(re),
+                          ctypes.byref(im), ctypes.byref(sc))
+    if rc != 0:
+        raise RuntimeError(f"oracle_dot failed: {rc}")
+    exact = complex(re.value, im.value) if np.iscomplexobj(val) else re.value
+    return out[0], exact, sc.value
 
 
 def _coo_to(colmajor, m, n, rowind, colind, val, base):

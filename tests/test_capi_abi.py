@@ -78,3 +78,28 @@ def test_workspace_size_queries(lib):
     w = lib.gsa_coo_to_compressed_workspace_size(0, 1, 0, 1000, 1000, 5000)
     assert w >= 5000 * 24
     assert lib.gsa_coo_to_compressed_workspace_size(0, 1, 0, 10, 10, 0) == 0
+
+
+def test_dot_argument_checks(lib, gsa):
+    L = gsa._lib
+    out = np.zeros(1)
+    res = out.ctypes.data_as(ctypes.c_void_p)
+    fake = ctypes.c_void_p(8 * 4096)  # never dereferenced: the checks fail first
+    # NULL result
+    assert lib.gsa_csr_dot(None, 1, 0, 4, 3, 0, fake, None, None, 1, 0, fake, fake, None, None, None, 0) \
+        == L.ERR_INVALID_ARG
+    # bad op, bad dtype, negative size, NULL vectors
+    assert lib.gsa_csr_dot(None, 1, 0, 4, 3, 0, fake, None, None, 1, 7, fake, fake, res, None, None, 0) \
+        == L.ERR_INVALID_ARG
+    assert lib.gsa_coo_dot(None, 99, 0, 4, 3, 0, None, None, None, 1, 0, fake, fake, res, None, 0) \
+        == L.ERR_UNSUPPORTED
+    assert lib.gsa_csc_dot(None, 1, 0, -1, 3, 0, fake, None, None, 1, 0, fake, fake, res, None, None, 0) \
+        == L.ERR_INVALID_ARG
+    assert lib.gsa_csr_dot(None, 1, 0, 4, 3, 0, fake, None, None, 1, 0, None, fake, res, None, None, 0) \
+        == L.ERR_INVALID_ARG
+    # Int32 structures hold at most 2^31 - 1 entries
+    assert lib.gsa_csr_dot(None, 1, 0, 4, 3, 2**31, fake, fake, fake, 1, 0, fake, fake, res, None, None, 0) \
+        == L.ERR_INVALID_ARG
+    assert lib.gsa_dot_workspace_size(2, 1, 0, 10, 10, None) > 0
+    assert lib.gsa_dot_workspace_size(0, 3, 1, 1000, 10, None) >= (1000 // 128 + 1) * 4 * 16
+    assert lib.gsa_dot_workspace_size(5, 1, 0, 10, 10, None) == 0

@@ -273,3 +273,37 @@ def test_sparse_rows_span_many_tiles(gsa, oracle, cuda, dt):
         C = torch.from_numpy(C0.copy()).to(cuda)
         gsa.mul_(C, A, torch.from_numpy(x).to(cuda), 2, 3, algo=algo)
         check(oracle, "csr", "N", m, n, rowptr, cols, vals, x, "N", C0, C, 2, 3, dt)
+
+
+@pytest.mark.parametrize("dt", [np.float64, np.complex128, np.int64])
+@pytest.mark.parametrize("k", [1, 3])
+def test_plan_orders(gsa, oracle, cuda, dt, k):
+    """Power-law rows: the plan puts them in bin order (rows grouped by length) and chunks
+    rows over 512; the natural order (GSA_TUNE_PLAN_ORDER = 1) with the same plan, and both
+    for CSR N and the same arrays as a transposed CSC, match the oracle."""
+    from genericsparsearrays_gb300 import _lib, workloads
+    lib = _lib.load()
+    m, n, rp, cv, nz = workloads.power_law(n=60_000, cap=5_000, seed=5, itype=np.int64, dtype=np.float64)
+    rng = np.random.default_rng(3)
+    vals = rand_values(rng, cv.size, dt)
+    X = np.asfortranarray(rand_values(rng, (n, k), dt))
+    C0 = np.asfortranarray(rand_values(rng, (m, k), dt))
+    try:
+        for natural in (0, 1):
+            assert lib.gsa_set_tuning(_lib.TUNE_PLAN_ORDER, natural) == 0
+            for fmt in ("csr", "csc_t"):
+                if fmt == "csr":
+                    A = make(gsa, "csr", m, n, rp, cv, vals, cuda)
+                    opA, f = "N", "csr"
+                else:
+                    A = gsa.transpose(make(gsa, "csc", n, m, rp, cv, vals, cuda))
+                    opA, f = "T", "csc"
+                C = torch.from_numpy(C0).to(cuda)
+                beta = 3 if is_int(dt) else 0.5
+                gsa.mul_(C, A, torch.from_numpy(X).to(cuda), 2, beta)
+                plan = (A.parent if fmt == "csc_t" else A)._plan
+                assert plan is not None and plan.nlong == m  # bin order takes every row
+                mm, nn = (m, n) if fmt == "csr" else (n, m)
+                check(oracle, f, opA, mm, nn, rp, cv, vals, X, "N", C0, C, 2, beta, dt)
+    finally:
+        lib.gsa_set_tuning(_lib.TUNE_PLAN_ORDER, 0)

@@ -143,3 +143,18 @@ def test_vector_operands(gsa):
     buf, ld, op, rows, cols = _dense_operand(gsa.transpose(v))
     assert (rows, cols) == (1, 5)
     assert torch.equal(_materialise(buf, ld, op, rows, cols), v.unsqueeze(0))
+
+
+def test_dot_checks_match_reference_order(gsa):
+    """dot(x, A, y): first-dimension, then second-dimension DimensionMismatch, then the
+    backend ArgumentError (src/matrix_csr/matrix_csr.jl:223-240); the GPU-only check last."""
+    A, S = small_csr(gsa)  # 6 x 5, host tensors
+    x, y = torch.zeros(6, dtype=torch.float64), torch.zeros(5, dtype=torch.float64)
+    with pytest.raises(gsa.DimensionMismatch, match="first dimension of A, 6, does not match the length of x, 5"):
+        gsa.dot(torch.zeros(5, dtype=torch.float64), A, y)
+    with pytest.raises(gsa.DimensionMismatch, match="second dimension of A, 5, does not match the length of y, 6"):
+        gsa.dot(x, A, torch.zeros(6, dtype=torch.float64))
+    with pytest.raises(gsa.DimensionMismatch, match="first dimension of A, 5"):
+        gsa.dot(x, gsa.transpose(A), y)  # op(A) is 5 x 6
+    with pytest.raises(gsa.ArgumentError, match="GPU only"):
+        gsa.dot(x, A, y)
