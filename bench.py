@@ -594,13 +594,23 @@ def run_serving(gsa, torch, dev, args):
     serving.serve_per_call(reg, stream(2)[:200], dev, keep_outputs=False)
     torch.cuda.synchronize()
 
-    srv = serving.Server(reg, ex, max_batch=1024, slots=2, keep_outputs=False)
-    reqs = stream(3)
-    with torch.cuda.device(dev):
-        srv.run(reqs)
-    torch.cuda.synchronize()
-    batched = srv.stats()
-    per_call = serving.serve_per_call(reg, stream(3), dev, keep_outputs=False)
+    def both(rate, duration, seed):
+        def mk():
+            reqs = serving.poisson_requests(reg, xs, rate=rate, duration=duration, k_lo=1, k_hi=kmax,
+                                            seed=seed)
+            t0 = time.perf_counter() + 0.05
+            for r in reqs:
+                r.arrival += t0
+            return reqs
+        srv = serving.Server(reg, ex, max_batch=1024, slots=2, keep_outputs=False)
+        reqs = mk()
+        with torch.cuda.device(dev):
+            srv.run(reqs)
+        torch.cuda.synchronize()
+        return len(reqs), srv.stats(), serving.serve_per_call(reg, mk(), dev, keep_outputs=False)
+
+    nreq, batched, per_call = both(args.serve_rate, args.serve_seconds, 3)
+    nreq2, batched2, per_call2 = both(args.serve_rate_low, args.serve_seconds_low, 4)
     nnz_total = sum(int(reg[i].nzval.numel()) for i in ids)
 
     def rnd(d):
@@ -611,10 +621,13 @@ def run_serving(gsa, torch, dev, args):
                     f"Poisson arrivals {args.serve_rate}/s for {args.serve_seconds}s, k uniform in [1, 32] "
                     "(X: the first k columns of a resident row-major n x 32 block per matrix), "
                     "150 GB HBM budget",
-        "requests": len(reqs), "registry_nnz": nnz_total, "registry_bytes": reg.resident,
+        "requests": nreq, "registry_nnz": nnz_total, "registry_bytes": reg.resident,
         "setup_s": round(t_gen, 1),
         "continuous_batching": rnd(batched), "per_call_mul": rnd(per_call),
         "speedup_mul_per_s": round(batched.get("mul_per_s", 0) / max(per_call.get("mul_per_s", 1e-9), 1e-9), 2),
+        f"below_capacity_{int(args.serve_rate_low)}_per_s": {
+            "requests": nreq2, "seconds": args.serve_seconds_low,
+            "continuous_batching": rnd(batched2), "per_call_mul": rnd(per_call2)},
     }
 
 
@@ -632,6 +645,8 @@ def main():
     ap.add_argument("--serve-n-hi", type=float, default=2e6)
     ap.add_argument("--serve-rate", type=float, default=20_000)
     ap.add_argument("--serve-seconds", type=float, default=1.0)
+    ap.add_argument("--serve-rate-low", type=float, default=400)
+    ap.add_argument("--serve-seconds-low", type=float, default=2.0)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

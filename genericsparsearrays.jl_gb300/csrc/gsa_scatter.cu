@@ -39,6 +39,9 @@ __global__ void rmul_or_fill_kernel(DenseOut<V> C, int64_t rows, int64_t k) {
 template <typename V>
 int launch_rmul_or_fill(cudaStream_t s, DenseOut<V> C, int64_t rows, int64_t k) {
     if (C.beta_mode == 1 || rows == 0 || k == 0) return GSA_OK;
+    if (C.beta_mode == 0)  // fill!(C, 0): all-zero bytes are +0 for every value type
+        return check_cuda(cudaMemset2DAsync(C.p, (size_t)C.ld * sizeof(V), 0, (size_t)rows * sizeof(V),
+                                            (size_t)k, s), "zero fill");
     int64_t blocks = ceil_div(rows * k, 256);
     if (blocks > 152 * 32) blocks = 152 * 32;
     rmul_or_fill_kernel<V><<<(unsigned)blocks, 256, 0, s>>>(C, rows, k);
@@ -128,22 +131,44 @@ __device__ __forceinline__ V alpha_times(const DenseOut<V> &C, V b) {
 }
 
 // C[idx_j, c0 + c] += conj?(a_j) * xa[c] for j = jb, jb+S, ... < je; entries whose index
-// falls outside C's rows are skipped.
-template <typename V, typename I, int KC, int S>
+// falls outside C's rows are skipped.  U entries are loaded before their atomics are
+// issued, so a lane keeps U loads in flight instead of one load per atomic.
+template <typename V, typename I, int KC, int S, int U>
 __device__ __forceinline__ void scatter_range(const CompressedArgs<V, I> &a, const DenseOut<V> &C,
                                               Off<I> j, Off<I> je, int64_t c0, int64_t k,
                                               const V (&xa)[KC]) {
     using O = Off<I>;
+    const I *__restrict__ idx = a.idx;
+    const V *__restrict__ val = a.val;
+    V *__restrict__ out = C.p;
     const O inner = sizeof(O) == 8 ? (O)a.inner_n
                                    : (O)(a.inner_n < 0xffffffffLL ? a.inner_n : 0xffffffffLL);
     const O base = (O)a.base;
+    if (U > 1) {
+        for (; j + (O)((U - 1) * S) < je; j += U * S) {
+            O r[U];
+            V av[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                r[u] = (O)ld_stream(idx + j + u * S) - base;
+                av[u] = conj_if(ld_stream(val + j + u * S), a.conjA);
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                if (r[u] >= inner) continue;
+#pragma unroll
+                for (int c = 0; c < KC; ++c)
+                    if (KC == 1 || c0 + c < k) atomic_add(out + (int64_t)r[u] + (c0 + c) * C.ld, mul(av[u], xa[c]));
+            }
+        }
+    }
     for (; j < je; j += S) {
-        const O r = (O)ld_stream(a.idx + j) - base;
-        const V av = conj_if(ld_stream(a.val + j), a.conjA);
+        const O r = (O)ld_stream(idx + j) - base;
+        const V av = conj_if(ld_stream(val + j), a.conjA);
         if (r >= inner) continue;
 #pragma unroll
         for (int c = 0; c < KC; ++c)
-            if (KC == 1 || c0 + c < k) atomic_add(C.p + (int64_t)r + (c0 + c) * C.ld, mul(av, xa[c]));
+            if (KC == 1 || c0 + c < k) atomic_add(out + (int64_t)r + (c0 + c) * C.ld, mul(av, xa[c]));
     }
 }
 
@@ -166,7 +191,7 @@ __device__ __forceinline__ void scatter_rows(const CompressedArgs<V, I> &a, int6
 #pragma unroll
         for (int c = 0; c < KC; ++c)
             xa[c] = (KC == 1 || c0 + c < k) ? alpha_times(C, B.at(o, c0 + c)) : VT<V>::zero();
-        scatter_range<V, I, KC, G>(a, C, qb + (O)(lane % G), qe, c0, k, xa);
+        scatter_range<V, I, KC, G, (G == 1 ? 4 : 2)>(a, C, qb + (O)(lane % G), qe, c0, k, xa);
     }
 }
 
@@ -198,7 +223,7 @@ scatter_block_kernel(CompressedArgs<V, I> a, int64_t k, DenseIn<V> B, DenseOut<V
 #pragma unroll
         for (int c = 0; c < KC; ++c)
             xa[c] = (KC == 1 || c0 + c < k) ? alpha_times(C, B.at(o, c0 + c)) : VT<V>::zero();
-        scatter_range<V, I, KC, 32>(a, C, jb + (O)lane, je, c0, k, xa);
+        scatter_range<V, I, KC, 32, UNROLL>(a, C, jb + (O)lane, je, c0, k, xa);
         return;
     }
     const int64_t row0 = unit * RB_THREADS + (threadIdx.x & ~31);

@@ -1,5 +1,6 @@
 # GenericSparseArraysCUDAExt -- CUDA package extension of GenericSparseArrays.jl that sends
-# sparse x dense mul! and COO -> CSR/CSC conversion on CuArray-backed matrices to libgsa
+# sparse x dense mul!, three-argument dot and COO -> CSR/CSC conversion on CuArray-backed
+# matrices to libgsa
 # (include/gsa.h).  It adds methods that are more specific than the package's generated
 # KernelAbstractions methods (src/matrix_csr/matrix_csr.jl:145-211,
 # src/matrix_csc/matrix_csc.jl:144-213, src/matrix_coo/matrix_coo.jl:155-221,
@@ -62,6 +63,31 @@ _ptrs(A::GenericSparseMatrixCOO) = (A.rowind, A.colind)
 _entry(::GenericSparseMatrixCSR) = :gsa_csr_mul
 _entry(::GenericSparseMatrixCSC) = :gsa_csc_mul
 
+# Plans (gsa_plan_create): made once per compressed structure and kept beside it, keyed on
+# the pointer array (the structure must not change in place while its plan lives); a
+# finalizer on the key frees the plan's device memory.
+const _PLANS = WeakKeyDict{Any, Ptr{Cvoid}}()
+const _PLANS_LOCK = ReentrantLock()
+
+function _plan(A::Union{GenericSparseMatrixCSR, GenericSparseMatrixCSC})
+    ptr = A isa GenericSparseMatrixCSR ? A.rowptr : A.colptr
+    lock(_PLANS_LOCK) do
+        get!(_PLANS, ptr) do
+            Ti = eltype(ptr)
+            h = Ref{Ptr{Cvoid}}(C_NULL)
+            outer = A isa GenericSparseMatrixCSR ? size(A, 1) : size(A, 2)
+            gsa_check(ccall((:gsa_plan_create, libgsa), Cint,
+                (CUstream, Cint, Int64, Int64, CuPtr{Ti}, Cint, Ref{Ptr{Cvoid}}),
+                CUDA.stream(), gsa_itype(Ti), outer, length(A.nzval), ptr, Cint(1), h))
+            finalizer(_ -> ccall((:gsa_plan_destroy, libgsa), Cint, (Ptr{Cvoid},), h[]), ptr)
+            h[]
+        end
+    end
+end
+
+_planned_entry(::GenericSparseMatrixCSR) = :gsa_csr_mul_planned
+_planned_entry(::GenericSparseMatrixCSC) = :gsa_csc_mul_planned
+
 function _gsa_mul!(C::CuVecOrMat{T}, A, B, α::Number, β::Number) where {T}
     _A, opA = _opA(A)
     P, ldb, opB = _opB(B)
@@ -87,12 +113,14 @@ function _gsa_mul!(C::CuVecOrMat{T}, A, B, α::Number, β::Number) where {T}
             stream, gsa_dtype(T), gsa_itype(Ti), _A.m, _A.n, length(_A.nzval), p0, p1, _A.nzval,
             Cint(1), opA, k, P, ldb, opB, C, ldc, a, b)
     else
-        # NULL workspace: libgsa takes it from the stream-ordered pool on `stream`
-        st = ccall((_entry(_A), libgsa), Cint,
+        # the structure's plan; NULL workspace: libgsa takes it from the stream-ordered pool
+        plan = _plan(_A)
+        st = ccall((_planned_entry(_A), libgsa), Cint,
             (CUstream, Cint, Cint, Int64, Int64, Int64, CuPtr{Ti}, CuPtr{Ti}, CuPtr{T}, Cint, Cint,
-             Int64, CuPtr{T}, Int64, Cint, CuPtr{T}, Int64, Ref{T}, Ref{T}, Cint, Ptr{Cvoid}, Csize_t),
+             Int64, CuPtr{T}, Int64, Cint, CuPtr{T}, Int64, Ref{T}, Ref{T}, Ptr{Cvoid}, Ptr{Cvoid},
+             Csize_t),
             stream, gsa_dtype(T), gsa_itype(Ti), _A.m, _A.n, length(_A.nzval), p0, p1, _A.nzval,
-            Cint(1), opA, k, P, ldb, opB, C, ldc, a, b, Cint(0), C_NULL, Csize_t(0))
+            Cint(1), opA, k, P, ldb, opB, C, ldc, a, b, plan, C_NULL, Csize_t(0))
     end
     gsa_check(st)
     return C  # asynchronous, like the package's kernels
@@ -109,6 +137,86 @@ for Fmt in (:CSRCu, :CSCCu, :COOCu)
         end
     end
 end
+
+# Three-argument dot (src/matrix_csr/matrix_csr.jl:213-277, src/matrix_csc/matrix_csc.jl:219,
+# src/matrix_coo/matrix_coo.jl:227): the scalar comes back to the host.
+_dot_entry(::GenericSparseMatrixCSR) = :gsa_csr_dot
+_dot_entry(::GenericSparseMatrixCSC) = :gsa_csc_dot
+
+function _gsa_dot(x::CuVector{T}, A, y::CuVector{T}) where {T}
+    _A, opA = _opA(A)
+    size(A, 1) == length(x) || throw(DimensionMismatch(
+        "first dimension of A, $(size(A, 1)), does not match the length of x, $(length(x))"))
+    size(A, 2) == length(y) || throw(DimensionMismatch(
+        "second dimension of A, $(size(A, 2)), does not match the length of y, $(length(y))"))
+    Ti = eltype(_ptrs(_A)[1])
+    p0, p1 = _ptrs(_A)
+    r = Ref{T}(zero(T))
+    if _A isa GenericSparseMatrixCOO
+        st = ccall((:gsa_coo_dot, libgsa), Cint,
+            (CUstream, Cint, Cint, Int64, Int64, Int64, CuPtr{Ti}, CuPtr{Ti}, CuPtr{T}, Cint, Cint,
+             CuPtr{T}, CuPtr{T}, Ref{T}, Ptr{Cvoid}, Csize_t),
+            CUDA.stream(), gsa_dtype(T), gsa_itype(Ti), _A.m, _A.n, length(_A.nzval), p0, p1,
+            _A.nzval, Cint(1), opA, x, y, r, C_NULL, Csize_t(0))
+    else
+        st = ccall((_dot_entry(_A), libgsa), Cint,
+            (CUstream, Cint, Cint, Int64, Int64, Int64, CuPtr{Ti}, CuPtr{Ti}, CuPtr{T}, Cint, Cint,
+             CuPtr{T}, CuPtr{T}, Ref{T}, Ptr{Cvoid}, Ptr{Cvoid}, Csize_t),
+            CUDA.stream(), gsa_dtype(T), gsa_itype(Ti), _A.m, _A.n, length(_A.nzval), p0, p1,
+            _A.nzval, Cint(1), opA, x, y, r, _plan(_A), C_NULL, Csize_t(0))
+    end
+    gsa_check(st)
+    return r[]
+end
+
+for Fmt in (:CSRCu, :CSCCu, :COOCu)
+    for TA in ((Fmt), :(Transpose{T, <:$Fmt{T, Ti}}), :(Adjoint{T, <:$Fmt{T, Ti}}))
+        SA = TA == Fmt ? :($Fmt{T, Ti}) : TA
+        @eval LinearAlgebra.dot(x::CuVector{T}, A::$SA, y::CuVector{T}) where {T <: GSAValue, Ti <: GSAIndex} =
+            _gsa_dot(x, A, y)
+    end
+end
+
+# Batched products: many mul!(C_i, A_i, B_i, α_i, β_i) of one element and index type in
+# one grouped launch, replayed from a CUDA graph (gsa_batch_*).  Not a method of the
+# reference; an addition for callers with thousands of small products.
+struct GsaGroupItem  # 128 bytes, field order of gsa_group_item
+    rowptr::CuPtr{Cvoid}; colval::CuPtr{Cvoid}; nzval::CuPtr{Cvoid}; B::CuPtr{Cvoid}; C::CuPtr{Cvoid}
+    m::Int64; n::Int64; nnz::Int64; ldb::Int64; ldc::Int64; k::Int32; b_rowmajor::Int32
+    first_tile::Int64
+    alpha::NTuple{16, UInt8}; beta::NTuple{16, UInt8}
+end
+
+_bytes16(v::T) where {T} = ntuple(i -> i <= sizeof(T) ? reinterpret(NTuple{sizeof(T), UInt8}, v)[i] : 0x00, 16)
+
+mutable struct GroupedMul{T, Ti}
+    handle::Ptr{Cvoid}
+    keep::Vector{Any}  # the operands stay alive while the batch does
+end
+
+function GroupedMul(products::AbstractVector) # [(C, A::CSRCu, B::CuVecOrMat, α, β), ...]
+    T = eltype(products[1][1]); Ti = eltype(products[1][2].rowptr)
+    items = GsaGroupItem[]
+    for (C, A, B, α, β) in products
+        ldb = B isa CuVector ? max(length(B), 1) : max(stride(B, 2), size(B, 1), 1)
+        ldc = C isa CuVector ? max(length(C), 1) : max(stride(C, 2), size(C, 1), 1)
+        push!(items, GsaGroupItem(pointer(A.rowptr), pointer(A.colval), pointer(A.nzval), pointer(B),
+                                  pointer(C), size(A, 1), size(A, 2), length(A.nzval), ldb, ldc,
+                                  Int32(size(C, 2)), Int32(0), 0, _bytes16(T(α)), _bytes16(T(β))))
+    end
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    gsa_check(ccall((:gsa_batch_create, libgsa), Cint,
+        (CUstream, Cint, Cint, Cint, Ptr{GsaGroupItem}, Int64, Cint, Cint, Ref{Ptr{Cvoid}}),
+        CUDA.stream(), gsa_dtype(T), gsa_itype(Ti), Cint(1), items, length(items), Cint(0), Cint(0), h))
+    g = GroupedMul{T, Ti}(h[], Any[products])
+    finalizer(g -> ccall((:gsa_batch_destroy, libgsa), Cint, (Ptr{Cvoid},), g.handle), g)
+    return g
+end
+
+# mode 0: one grouped launch, 1: replay of its captured CUDA graph, 2: one mul! per product
+run!(g::GroupedMul; mode::Integer = 1) =
+    gsa_check(ccall((:gsa_batch_run, libgsa), Cint, (Ptr{Cvoid}, CUstream, Cint), g.handle,
+                    CUDA.stream(), Cint(mode)))
 
 # COO -> CSR / CSC (src/conversions/conversions.jl:171-212, 282-323)
 for (Out, entry, colmajor) in ((:GenericSparseMatrixCSR, :gsa_coo_to_csr, 0),
