@@ -43,11 +43,15 @@ SIGNATURES = {
     "gsa_plan_workspace_size": ([_vp, _i32, _i64], _sz),
     "gsa_csr_mul_planned": (_MUL + [_vp, _vp, _sz], _i32),
     "gsa_csc_mul_planned": (_MUL + [_vp, _vp, _sz], _i32),
+    "gsa_plan_bin_order": ([_vp, ctypes.POINTER(_vp), ctypes.POINTER(_i64)], _i32),
+    "gsa_coo_plan_create": ([_vp, _i32, _i64, _i64, _i64, _vp, _i32, ctypes.POINTER(_vp)], _i32),
+    "gsa_coo_plan_info": ([_vp, ctypes.POINTER(_i32)], _i32),
+    "gsa_coo_mul_planned": (_MUL + [_vp, _vp, _sz], _i32),
     "gsa_csr_dot": ([_vp, _i32, _i32, _i64, _i64, _i64, _vp, _vp, _vp, _i32, _i32, _vp, _vp, _vp, _vp,
                      _vp, _sz], _i32),
     "gsa_csc_dot": ([_vp, _i32, _i32, _i64, _i64, _i64, _vp, _vp, _vp, _i32, _i32, _vp, _vp, _vp, _vp,
                      _vp, _sz], _i32),
-    "gsa_coo_dot": ([_vp, _i32, _i32, _i64, _i64, _i64, _vp, _vp, _vp, _i32, _i32, _vp, _vp, _vp,
+    "gsa_coo_dot": ([_vp, _i32, _i32, _i64, _i64, _i64, _vp, _vp, _vp, _i32, _i32, _vp, _vp, _vp, _vp,
                      _vp, _sz], _i32),
     "gsa_dot_workspace_size": ([_i32, _i32, _i32, _i64, _i64, _vp], _sz),
     "gsa_csr_spmv_noalloc": ([_vp, _i32, _i32, _i64, _i64, _i64, _vp, _vp, _vp, _i32, _vp, _vp,

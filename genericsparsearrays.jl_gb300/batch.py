@@ -18,13 +18,30 @@ import torch
 
 from . import _lib
 from .errors import ArgumentError, DimensionMismatch
-from .sparse import (BASE, GenericSparseMatrixCSR, _DTYPE, _ITYPE, _scalar_buf, _stream_ptr, nnz)
+from .sparse import (BASE, GenericSparseMatrixCSR, _DTYPE, _ITYPE, _gather_plan, _scalar_buf, _stream_ptr,
+                     nnz)
 
 ITEM_DTYPE = np.dtype([("rowptr", "<u8"), ("colval", "<u8"), ("nzval", "<u8"), ("B", "<u8"),
                        ("C", "<u8"), ("m", "<i8"), ("n", "<i8"), ("nnz", "<i8"), ("ldb", "<i8"),
                        ("ldc", "<i8"), ("k", "<i4"), ("b_rowmajor", "<i4"), ("first_tile", "<i8"),
+                       ("bin_order", "<u8"), ("bin_warps", "<i8"),
                        ("alpha", "u1", 16), ("beta", "u1", 16)])
-assert ITEM_DTYPE.itemsize == 128
+assert ITEM_DTYPE.itemsize == 144
+
+
+def bin_order_of(A) -> Tuple[int, int]:
+    """(device view, warps) of the bin order of A's plan when A's products are FP64-bound
+    (ComplexF64: every idle lane is lost FP64 time); (0, 0) otherwise.  Makes the plan on
+    first use (one synchronisation) and keeps it on the matrix."""
+    if A.dtype != torch.complex128:
+        return 0, 0
+    plan = _gather_plan(A)
+    if plan is None:
+        return 0, 0
+    view, warps = ctypes.c_void_p(0), ctypes.c_int64(0)
+    _lib.check(_lib.load().gsa_plan_bin_order(ctypes.c_void_p(plan.handle), ctypes.byref(view),
+                                              ctypes.byref(warps)))
+    return (view.value or 0), warps.value
 
 Product = Tuple[GenericSparseMatrixCSR, torch.Tensor, torch.Tensor, object, object]
 
@@ -54,8 +71,10 @@ def _dense_in(t: torch.Tensor) -> Tuple[int, int, int]:
     return k, ld, 0
 
 
-def pack_items(products: Sequence[Product], out: Optional[np.ndarray] = None) -> Tuple[np.ndarray, torch.dtype, torch.dtype]:
-    """The ``gsa_group_item`` array of a product list (checks as ``mul!`` does)."""
+def pack_items(products: Sequence[Product], out: Optional[np.ndarray] = None,
+               use_plans: bool = True) -> Tuple[np.ndarray, torch.dtype, torch.dtype]:
+    """The ``gsa_group_item`` array of a product list (checks as ``mul!`` does).  With
+    use_plans, ComplexF64 items carry their plan's bin order (see bin_order_of)."""
     if not products:
         raise ArgumentError("no products")
     dt, it = products[0][0].dtype, products[0][0].itype
@@ -83,6 +102,7 @@ def pack_items(products: Sequence[Product], out: Optional[np.ndarray] = None) ->
         row["B"], row["C"] = B.data_ptr(), C.data_ptr()
         row["m"], row["n"], row["nnz"], row["ldb"], row["ldc"], row["k"] = A.m, A.n, nnz(A), ldb, ldc, kb
         row["b_rowmajor"] = brow
+        row["bin_order"], row["bin_warps"] = bin_order_of(A) if use_plans else (0, 0)
         a = _scalar_buf(alpha, dt).view(np.uint8)
         b = _scalar_buf(beta, dt).view(np.uint8)
         row["alpha"][:] = 0
@@ -103,9 +123,10 @@ def tiles(items: np.ndarray, dtype: torch.dtype, columns: int) -> int:
 class BatchedMul:
     """All products of a fixed list in one grouped launch; see the module docstring."""
 
-    def __init__(self, products: Sequence[Product], columns: int = 0, g1_avg: int = 0):
+    def __init__(self, products: Sequence[Product], columns: int = 0, g1_avg: int = 0,
+                 use_plans: bool = True):
         self.products = list(products)  # keeps the operand buffers alive
-        items, self.dtype, self.itype = pack_items(self.products)
+        items, self.dtype, self.itype = pack_items(self.products, use_plans=use_plans)
         self.columns, self.g1_avg = columns, g1_avg
         self.device = self.products[0][0].device
         lib = _lib.load()

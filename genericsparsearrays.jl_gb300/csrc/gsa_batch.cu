@@ -4,8 +4,9 @@
 // matrices of uneven size the launches, not the bytes, set the time.
 //
 // The work list is implicit: item i owns tiles [first_tile_i, first_tile_i + tiles_i),
-// tiles_i = ceil(m_i / 128) row blocks x ceil(k_i / KC) column groups (host-side prefix,
-// gsa_grouped_tiles).  A persistent grid (SMs x resident CTAs) walks the tiles; a CTA
+// tiles_i = ceil(m_i / 128) row blocks -- or, for an item that carries its plan's bin
+// order, ceil(bin_warps_i / 4) CTAs of bin-order warps -- x ceil(k_i / KC) column groups
+// (host-side prefix, gsa_grouped_tiles).  A persistent grid (SMs x resident CTAs) walks the tiles; a CTA
 // finds its item by binary search over first_tile, then its warps run the same row
 // code as the single-product kernel (gsa_rows.cuh: G lanes per row chosen per warp).
 // A batch object (gsa_batch_*) keeps the item array on the device and can replay the
@@ -17,20 +18,38 @@
 
 namespace gsa {
 
-static_assert(sizeof(gsa_group_item) == 128, "gsa_group_item layout");
+static_assert(sizeof(gsa_group_item) == 144, "gsa_group_item layout");
 
 template <typename V, typename I, int KC>
 __global__ void __launch_bounds__(RB_THREADS)
 grouped_kernel(const gsa_group_item *__restrict__ items, int64_t count, int64_t ntiles, int base,
                int g1_avg) {
+    // One thread finds each tile's item -- forward from the previous one, since a CTA's tiles
+    // ascend -- and the CTA stages the item in shared memory: the other threads read its
+    // fields there instead of each running the search through global memory.
+    __shared__ gsa_group_item s_item;
+    __shared__ int64_t s_lo;
+    int64_t lo = 0;
     for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
-        int64_t lo = 0, hi = count - 1;  // last item with first_tile <= t
-        while (lo < hi) {
-            const int64_t mid = (lo + hi + 1) >> 1;
-            if (items[mid].first_tile <= t) lo = mid;
-            else hi = mid - 1;
+        if (threadIdx.x == 0) {
+            if (lo + 1 < count && __ldg(&items[lo + 1].first_tile) <= t) {
+                int64_t l = lo + 1, h = count - 1;  // last item with first_tile <= t, in (lo, count)
+                while (l < h) {
+                    const int64_t mid = (l + h + 1) >> 1;
+                    if (__ldg(&items[mid].first_tile) <= t) l = mid;
+                    else h = mid - 1;
+                }
+                lo = l;
+            }
+            s_lo = lo;
         }
-        const gsa_group_item &it = items[lo];
+        __syncthreads();
+        lo = s_lo;
+        if (threadIdx.x < sizeof(gsa_group_item) / 4)
+            reinterpret_cast<uint32_t *>(&s_item)[threadIdx.x] =
+                __ldg(reinterpret_cast<const uint32_t *>(items + lo) + threadIdx.x);
+        __syncthreads();
+        const gsa_group_item &it = s_item;
         const int64_t ncg = (it.k + KC - 1) / KC;
         const int64_t local = t - it.first_tile;
         const int64_t cg = ncg == 1 ? 0 : local % ncg;
@@ -56,8 +75,19 @@ grouped_kernel(const gsa_group_item *__restrict__ items, int64_t count, int64_t 
         C.beta = *reinterpret_cast<const V *>(it.beta);
         C.beta_mode = is_zero(C.beta) ? 0 : (is_one(C.beta) ? 1 : 2);
         C.alpha_one = alpha_one_of(C.alpha);
-        warp_unit<V, I, KC>(a, it.k, B, C, cg * KC, unit * RB_THREADS + (threadIdx.x & ~31), nullptr,
-                            g1_avg);
+        const int64_t kk = it.k;
+        const int64_t bin_warps = it.bin_warps;
+        const gsa_bin_order *bo = (const gsa_bin_order *)it.bin_order;
+        __syncthreads();  // every thread has its copy before the next tile overwrites s_item
+        if (bin_warps > 0) {  // the plan's bin order: warp w of it
+            const int64_t w = unit * RB_WARPS + (threadIdx.x >> 5);
+            if (w < bin_warps) {
+                const gsa_bin_order bv{__ldg(&bo->nwarps), bo->perm, bo->seg, bo->warp_bin, bo->bins};
+                binned_warp<V, I, KC>(a, kk, B, C, cg * KC, w, bv);
+            }
+        } else {
+            warp_unit<V, I, KC>(a, kk, B, C, cg * KC, unit * RB_THREADS + (threadIdx.x & ~31), nullptr, g1_avg);
+        }
     }
 }
 
@@ -129,6 +159,8 @@ int gsa_grouped_tiles(int dtype, gsa_group_item *items, int64_t count, int colum
             return fail(GSA_ERR_INVALID_ARG, "item %lld: NULL sparse array", (long long)i);
         if (it.m > 0 && it.k > 0 && (!it.C || (it.n > 0 && !it.B)))
             return fail(GSA_ERR_INVALID_ARG, "item %lld: NULL dense operand", (long long)i);
+        if (it.bin_warps < 0 || (it.bin_warps > 0) != (it.bin_order != nullptr))
+            return fail(GSA_ERR_INVALID_ARG, "item %lld: bin_order and bin_warps disagree", (long long)i);
     }
     // one column group width for the whole launch: k == 1 items still use KC-wide groups
     // in the kernel, so every item with k > 1 and k == 1 gets ceil(k / KC) groups
@@ -136,8 +168,11 @@ int gsa_grouped_tiles(int dtype, gsa_group_item *items, int64_t count, int colum
     int64_t t = 0;
     for (int64_t i = 0; i < count; ++i) {
         items[i].first_tile = t;
-        if (items[i].m > 0 && items[i].k > 0)
-            t += ceil_div(items[i].m, RB_THREADS) * ceil_div(items[i].k, KC);
+        if (items[i].m > 0 && items[i].k > 0) {
+            const int64_t units = items[i].bin_warps > 0 ? ceil_div(items[i].bin_warps, RB_WARPS)
+                                                         : ceil_div(items[i].m, RB_THREADS);
+            t += units * ceil_div(items[i].k, KC);
+        }
     }
     *ntiles = t;
     return GSA_OK;

@@ -257,9 +257,81 @@ int gsa_plan_create(void *stream, int itype, int64_t outer_n, int64_t nnz, const
     return GSA_OK;
 }
 
+int gsa_coo_plan_create(void *stream, int itype, int64_t m, int64_t n, int64_t nnz, const void *rowind,
+                        int base, gsa_plan **out) {
+    if (!out) return fail(GSA_ERR_INVALID_ARG, "out is NULL");
+    *out = nullptr;
+    const size_t is = itype_size(itype);
+    if (!is) return fail(GSA_ERR_UNSUPPORTED, "unsupported itype %d", itype);
+    if (m < 0 || n < 0 || nnz < 0) return fail(GSA_ERR_INVALID_ARG, "negative size");
+    if (nnz > 0 && !rowind) return fail(GSA_ERR_INVALID_ARG, "rowind is NULL");
+    if (misaligned(rowind, is)) return fail(GSA_ERR_INVALID_ARG, "rowind must be aligned to its element size");
+    if (itype == GSA_IDX32 && nnz > 0x7fffffffLL)
+        return fail(GSA_ERR_INVALID_ARG, "nnz=%lld exceeds what Int32 indices can address", (long long)nnz);
+    Plan *p = new (std::nothrow) Plan();
+    if (!p) return fail(GSA_ERR_ALLOC, "plan: host memory");
+    p->coo = 1;
+    p->outer_n = m;
+    p->nnz = nnz;
+    cudaStream_t s = (cudaStream_t)stream;
+    int rc = check_cuda(cudaMalloc(&p->coo_ptr, is * (size_t)(m + 1)), "coo plan: row pointers");
+    int sorted = 0;
+    if (!rc) rc = coo_row_pointers(s, itype, m, nnz, rowind, base, p->coo_ptr, &sorted);
+    if (!rc && sorted) {
+        p->coo_sorted = 1;
+        rc = plan_create(s, itype, m, nnz, p->coo_ptr, base, p);
+    }
+    if (!rc && !sorted) {  // the COO kernel keeps it; drop the pointers
+        cudaFree(p->coo_ptr);
+        p->coo_ptr = nullptr;
+    }
+    if (rc) {
+        if (p->mem) cudaFree(p->mem);
+        if (p->coo_ptr) cudaFree(p->coo_ptr);
+        delete p;
+        return rc;
+    }
+    *out = p;
+    return GSA_OK;
+}
+
+int gsa_plan_bin_order(const gsa_plan *plan, const void **view, int64_t *warps) {
+    if (!plan || !view || !warps) return fail(GSA_ERR_INVALID_ARG, "NULL argument");
+    // grouped launches take the bin order only without rows of more than one chunk (those
+    // need a call's partial sums)
+    const bool ok = plan->nbin_warps > 0 && plan->bin_view && plan->bin.nlong == 0;
+    *view = ok ? (const void *)plan->bin_view : nullptr;
+    *warps = ok ? plan->nbin_warps : 0;
+    return GSA_OK;
+}
+
+int gsa_coo_plan_info(const gsa_plan *plan, int *row_sorted) {
+    if (!plan || !row_sorted) return fail(GSA_ERR_INVALID_ARG, "NULL argument");
+    *row_sorted = plan->coo ? plan->coo_sorted : 0;
+    return GSA_OK;
+}
+
+int gsa_coo_mul_planned(void *stream, int dtype, int itype, int64_t m, int64_t n, int64_t nnz,
+                        const void *rowind, const void *colind, const void *nzval, int base, int opA,
+                        int64_t k, const void *B, int64_t ldb, int opB, void *C, int64_t ldc,
+                        const void *alpha, const void *beta, const gsa_plan *plan, void *workspace,
+                        size_t workspace_bytes) {
+    if (plan && !plan->coo) return fail(GSA_ERR_INVALID_ARG, "not a COO plan");
+    if (plan && (plan->outer_n != m || plan->nnz != nnz))
+        return fail(GSA_ERR_INVALID_ARG, "plan was made for another structure");
+    if (!plan || !plan->coo_sorted)
+        return gsa_coo_mul(stream, dtype, itype, m, n, nnz, rowind, colind, nzval, base, opA, k, B, ldb,
+                           opB, C, ldc, alpha, beta);
+    // row-sorted: the CSR kernels on (plan row pointers, colind, nzval)
+    return compressed_mul(true, stream, dtype, itype, m, n, nnz, plan->coo_ptr, colind, nzval, base, opA,
+                          k, B, ldb, opB, C, ldc, alpha, beta, GSA_ALGO_AUTO, workspace, workspace_bytes,
+                          plan);
+}
+
 int gsa_plan_destroy(gsa_plan *plan) {
     if (!plan) return GSA_OK;
     int rc = GSA_OK;
+    if (plan->coo_ptr) cudaFree(plan->coo_ptr);
     if (plan->mem) rc = check_cuda(cudaFree(plan->mem), "plan: free");
     delete plan;
     return rc;
@@ -278,7 +350,6 @@ int gsa_csr_mul_planned(void *stream, int dtype, int itype, int64_t m, int64_t n
                         int64_t k, const void *B, int64_t ldb, int opB, void *C, int64_t ldc,
                         const void *alpha, const void *beta, const gsa_plan *plan, void *workspace,
                         size_t workspace_bytes) {
-    if (opA != GSA_OP_N) plan = nullptr;  // the plan covers the row gather only
     return compressed_mul(true, stream, dtype, itype, m, n, nnz, rowptr, colval, nzval, base, opA,
                           k, B, ldb, opB, C, ldc, alpha, beta, GSA_ALGO_AUTO, workspace,
                           workspace_bytes, plan);
@@ -289,7 +360,6 @@ int gsa_csc_mul_planned(void *stream, int dtype, int itype, int64_t m, int64_t n
                         int64_t k, const void *B, int64_t ldb, int opB, void *C, int64_t ldc,
                         const void *alpha, const void *beta, const gsa_plan *plan, void *workspace,
                         size_t workspace_bytes) {
-    if (opA == GSA_OP_N) plan = nullptr;  // the plan covers the column gather (op T / C) only
     return compressed_mul(false, stream, dtype, itype, m, n, nnz, colptr, rowval, nzval, base, opA,
                           k, B, ldb, opB, C, ldc, alpha, beta, GSA_ALGO_AUTO, workspace,
                           workspace_bytes, plan);
@@ -381,13 +451,19 @@ int gsa_csc_dot(void *stream, int dtype, int itype, int64_t m, int64_t n, int64_
 
 int gsa_coo_dot(void *stream, int dtype, int itype, int64_t m, int64_t n, int64_t nnz, const void *rowind,
                 const void *colind, const void *nzval, int base, int opA, const void *x, const void *y,
-                void *result, void *workspace, size_t workspace_bytes) {
+                void *result, const gsa_plan *plan, void *workspace, size_t workspace_bytes) {
+    if (plan && (!plan->coo || plan->outer_n != m || plan->nnz != nnz))
+        return fail(GSA_ERR_INVALID_ARG, "plan is not a COO plan of this structure");
+    if (plan && plan->coo_sorted)  // row-sorted: the CSR dot on the plan's row pointers
+        return dot_call(0, stream, dtype, itype, m, n, nnz, plan->coo_ptr, colind, nzval, base, opA, x, y,
+                        result, plan, workspace, workspace_bytes);
     return dot_call(2, stream, dtype, itype, m, n, nnz, rowind, colind, nzval, base, opA, x, y, result,
                     nullptr, workspace, workspace_bytes);
 }
 
 size_t gsa_dot_workspace_size(int format, int dtype, int itype, int64_t m, int64_t n, const gsa_plan *plan) {
     if (format < 0 || format > 2) return 0;
+    if (format == 2 && plan && plan->coo_sorted) format = 0;  // served by the CSR dot
     DotWsBody body{format, format == 0 ? m : n, format == 2 ? nullptr : plan, 0};
     if (dispatch_vi(dtype, itype, body)) return 0;
     return body.out;

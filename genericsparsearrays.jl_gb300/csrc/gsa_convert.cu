@@ -444,4 +444,47 @@ template int launch_validate<int32_t>(cudaStream_t, int64_t, int64_t, int64_t, c
 template int launch_validate<int64_t>(cudaStream_t, int64_t, int64_t, int64_t, const int64_t *,
                                       const int64_t *, int, int *);
 
+// Row pointers of a row-sorted COO: entry i's predecessor and its own row bound the
+// pointer entries it writes (each written once); a decrease or a row outside [0, m)
+// clears *sorted instead.
+template <typename I>
+__global__ void coo_rowptr_kernel(int64_t nnz, const I *__restrict__ rowind, int base, int64_t m,
+                                  I *__restrict__ ptr_out, int *sorted) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i <= nnz;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t prev = i == 0 ? -1 : (int64_t)rowind[i - 1] - base;
+        const int64_t cur = i == nnz ? m : (int64_t)rowind[i] - base;
+        if (cur < prev || cur > m || (i < nnz && cur == m) || prev >= m) {
+            atomicExch(sorted, 0);
+            continue;
+        }
+        for (int64_t r = prev + 1; r <= cur; ++r) ptr_out[r] = (I)(i + base);
+    }
+}
+
+int coo_row_pointers(cudaStream_t s, int itype, int64_t m, int64_t nnz, const void *rowind, int base,
+                     void *ptr_out, int *sorted_host) {
+    int *flag = nullptr;
+    int rc = check_cuda(cudaMallocAsync((void **)&flag, sizeof(int), s), "coo plan: flag");
+    if (rc) return rc;
+    const int one = 1;
+    rc = check_cuda(cudaMemcpyAsync(flag, &one, sizeof(int), cudaMemcpyHostToDevice, s), "coo plan: flag");
+    if (!rc) {
+        int64_t blocks = ceil_div(nnz + 1, 256);
+        if (blocks > 152 * 64) blocks = 152 * 64;
+        if (itype == GSA_IDX32)
+            coo_rowptr_kernel<int32_t><<<(unsigned)blocks, 256, 0, s>>>(nnz, (const int32_t *)rowind, base, m,
+                                                                         (int32_t *)ptr_out, flag);
+        else
+            coo_rowptr_kernel<int64_t><<<(unsigned)blocks, 256, 0, s>>>(nnz, (const int64_t *)rowind, base, m,
+                                                                         (int64_t *)ptr_out, flag);
+        rc = check_cuda(cudaGetLastError(), "coo_rowptr_kernel");
+    }
+    if (!rc) rc = check_cuda(cudaMemcpyAsync(sorted_host, flag, sizeof(int), cudaMemcpyDeviceToHost, s),
+                             "coo plan: flag");
+    if (!rc) rc = check_cuda(cudaStreamSynchronize(s), "coo plan: sync");
+    cudaFreeAsync(flag, s);
+    return rc;
+}
+
 }  // namespace gsa

@@ -9,7 +9,8 @@
 // The reference gives each work item a stride of rows and sums the items' partials on
 // one thread per block, then on the host.  Here the compressed formats reuse the row
 // gather's layout: a warp owns 32 outer entries, G lanes per entry from their average
-// length (planned long entries get warps of their own, chunk by chunk), and sums along
+// length (planned long entries get warps of their own, chunk by chunk; ComplexF64 walks
+// the plan's bin order, rows grouped by length, as the product does), and sums along
 // each entry the vector that pairs with the inner index -- s_o = sum_j a_oj y_j when x
 // pairs with the outer index (CSR N, CSC T/C), t_o = sum_j conj(x_j) a_oj when y does
 // (CSR T/C, CSC N) -- with one fused multiply-add per entry, then multiplies once per
@@ -134,6 +135,67 @@ dot_compressed_kernel(CompressedArgs<V, I> a, DotVecs<V> d, int64_t nrb, PlanRow
     if (lane == 0) partial[slot] = t;
 }
 
+// The same over the plan's bin order (rows grouped by length, G lanes each), then the bin
+// set's chunks of rows over 512 entries: used where the FP64 pipe binds (ComplexF64).
+template <typename V, typename I, int G>
+__device__ __forceinline__ V dot_binned_rows(const CompressedArgs<V, I> &a, const DotVecs<V> &d, int64_t pos0,
+                                             int64_t pend, const gsa_bin_order &bv) {
+    using O = Off<I>;
+    const int lane = threadIdx.x & 31;
+    const int64_t i = pos0 + lane / G;
+    const bool valid = i < pend;
+    int64_t o = 0;
+    O b = 0, e = 0;
+    if (valid) {
+        o = __ldg(bv.perm + i);
+        const O nz = (O)a.nnz;
+        b = (O)__ldg(bv.seg + 2 * i);
+        e = (O)__ldg(bv.seg + 2 * i + 1);
+        b = b < nz ? b : nz;
+        e = e < nz ? e : nz;
+        e = e < b ? b : e;
+    }
+    V s = dot_range<V, I, G, (G == 1 ? 1 : 2)>(a, d, b + (O)(lane % G), e);
+    if (G > 1) {
+#pragma unroll
+        for (int m = G / 2; m > 0; m >>= 1) s = add(s, shfl_xor(s, m, G));
+    }
+    return (lane % G == 0 && valid && o < a.outer_n) ? outer_term(d, o, s) : VT<V>::zero();
+}
+
+template <typename V, typename I>
+__global__ void __launch_bounds__(RB_THREADS)
+dot_binned_kernel(CompressedArgs<V, I> a, DotVecs<V> d, gsa_bin_order bv, PlanRows L, V *partial) {
+    using O = Off<I>;
+    const int lane = threadIdx.x & 31;
+    const int64_t w = (int64_t)blockIdx.x * RB_WARPS + (threadIdx.x >> 5);
+    V t = VT<V>::zero();
+    if (w < bv.nwarps) {
+        const int bi = __ldg(bv.warp_bin + w);
+        const int64_t first_warp = __ldg(bv.bins + 4 * bi), pos = __ldg(bv.bins + 4 * bi + 1);
+        const int64_t pend = __ldg(bv.bins + 4 * bi + 2);
+        const int G = (int)__ldg(bv.bins + 4 * bi + 3);
+        const int64_t pos0 = pos + (w - first_warp) * (32 / G);
+        dispatch_lanes(G, 1, [&](auto g) { t = dot_binned_rows<V, I, decltype(g)::value>(a, d, pos0, pend, bv); });
+    } else if (w - bv.nwarps < L.nchunks) {  // a chunk of a row over 512 entries
+        const int64_t chunk = w - bv.nwarps;
+        const int sl = L.chunk_slot[chunk];
+        const int64_t o = L.row[sl];
+        const O nz = (O)a.nnz, base = (O)a.base;
+        O rb = (O)__ldg(a.ptr + o) - base;
+        O re = (O)__ldg(a.ptr + o + 1) - base;
+        rb = rb < nz ? rb : nz;
+        re = re < nz ? re : nz;
+        const O jb = rb + (O)(chunk - L.first[sl]) * (O)CHUNK;
+        const O je = jb < re && re - jb > (O)CHUNK ? jb + (O)CHUNK : re;
+        V s = jb < je ? dot_range<V, I, 32, UNROLL>(a, d, jb + (O)lane, je) : VT<V>::zero();
+        s = warp_sum(s);
+        if (lane == 0) t = outer_term(d, o, s);
+    }
+    t = warp_sum(t);
+    if (lane == 0) partial[w] = t;
+}
+
 constexpr int COO_DOT_CTAS = 1216;  // 152 SMs x 8, a fixed grid: the slot order is fixed
 
 template <typename V, typename I>
@@ -182,7 +244,24 @@ size_t dot_workspace_size(int fmt, int64_t outer_n, const Plan *plan) {
     int64_t slots;
     if (fmt == 2) slots = COO_DOT_CTAS;
     else slots = (ceil_div(outer_n, RB_THREADS) + ceil_div(plan ? plan->nat.nchunks : 0, RB_WARPS)) * RB_WARPS;
+    if (fmt != 2 && plan && plan->nbin_warps > 0) {  // room for the bin order too
+        const int64_t b = ceil_div(plan->nbin_warps + plan->bin.nchunks, RB_WARPS) * RB_WARPS;
+        slots = b > slots ? b : slots;
+    }
     return align_up((size_t)(slots + 1) * sizeof(V), 256);
+}
+
+// the slots' sum, in a fixed order, to the host
+template <typename V>
+static int finish_dot(cudaStream_t s, V *partial, int64_t slots, void *result_host) {
+    int rc = check_cuda(cudaGetLastError(), "dot kernel");
+    if (rc) return rc;
+    dot_finish_kernel<V><<<1, 1024, 0, s>>>(partial, slots, partial + slots);
+    rc = check_cuda(cudaGetLastError(), "dot_finish_kernel");
+    if (!rc) rc = check_cuda(cudaMemcpyAsync(result_host, partial + slots, sizeof(V), cudaMemcpyDeviceToHost, s),
+                             "dot: result");
+    if (!rc) rc = check_cuda(cudaStreamSynchronize(s), "dot: sync");
+    return rc;
 }
 
 template <typename V, typename I>
@@ -213,6 +292,19 @@ int launch_dot(cudaStream_t s, int fmt, int opA, int64_t m, int64_t n, int64_t n
         a.conjA = conjA;
         // CSR N and CSC T/C: x pairs with the outer index
         const DotVecs<V> d{x, y, csr ? !trans : trans};
+        if (plan && plan->nbin_warps > 0 && std::is_same<V, cf64>::value) {  // FP64-bound: bin order
+            if (plan->outer_n != a.outer_n || plan->nnz != nnz)
+                return fail(GSA_ERR_INVALID_ARG, "plan was made for another structure");
+            const gsa_bin_order bv{plan->nbin_warps, plan->perm, plan->seg, plan->warp_bin, plan->bins};
+            const PlanRows L = plan_rows(plan->bin);
+            const int64_t units = ceil_div(plan->nbin_warps + plan->bin.nchunks, RB_WARPS);
+            slots = units * RB_WARPS;
+            if (units > 0x7fffffffLL) return fail(GSA_ERR_UNSUPPORTED, "too many outer entries");
+            timer_before(s);
+            dot_binned_kernel<V, I><<<(unsigned)units, RB_THREADS, 0, s>>>(a, d, bv, L, partial);
+            timer_after(s);
+            return finish_dot<V>(s, partial, slots, result_host);
+        }
         const int64_t nrb = ceil_div(a.outer_n, RB_THREADS);
         PlanRows L{};
         int64_t units = nrb;
@@ -230,14 +322,7 @@ int launch_dot(cudaStream_t s, int fmt, int opA, int64_t m, int64_t n, int64_t n
             timer_after(s);
         }
     }
-    int rc = check_cuda(cudaGetLastError(), "dot kernel");
-    if (rc) return rc;
-    dot_finish_kernel<V><<<1, 1024, 0, s>>>(partial, slots, partial + slots);
-    rc = check_cuda(cudaGetLastError(), "dot_finish_kernel");
-    if (!rc) rc = check_cuda(cudaMemcpyAsync(result_host, partial + slots, sizeof(V), cudaMemcpyDeviceToHost, s),
-                             "dot: result");
-    if (!rc) rc = check_cuda(cudaStreamSynchronize(s), "dot: sync");
-    return rc;
+    return finish_dot<V>(s, partial, slots, result_host);
 }
 
 #define GSA_INST_DOT(V, I)                                                                        \

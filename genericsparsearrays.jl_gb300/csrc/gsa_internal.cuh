@@ -25,6 +25,15 @@ struct gsa_chunk_set {
     const int32_t *chunk_slot = nullptr;  // the chunked entry a chunk belongs to
     const uint32_t *skip_mask = nullptr;  // bit per outer entry, 1 = chunked
 };
+// A plan's bin order as the kernels read it (also copied into the plan's device memory,
+// for grouped launches whose items point at it).
+struct gsa_bin_order {
+    int64_t nwarps;            // warps of the bin order
+    const int64_t *perm;       // outer entries, bin by bin
+    const int64_t *seg;        // [begin, end) of each, 0-based
+    const uint8_t *warp_bin;   // bin of each warp
+    const int64_t *bins;       // per bin: first warp, first position, end position, lanes
+};
 struct gsa_plan {
     int64_t outer_n = 0, nnz = 0, max_len = 0;
     int64_t nplanned = 0;                 // entries the plan takes out of the natural order
@@ -36,7 +45,12 @@ struct gsa_plan {
     const int64_t *seg = nullptr;         // [begin, end) of each, 0-based
     const uint8_t *warp_bin = nullptr;    // bin of each warp of the bin order
     const int64_t *bins = nullptr;        // per bin: first warp, first position, end, lanes
+    const gsa_bin_order *bin_view = nullptr;  // device copy of the five fields above
     void *mem = nullptr;
+    // COO plans (gsa_coo_plan_create): row pointers of a row-sorted COO (owned), the rest of
+    // the plan describing them; coo_sorted = 0 leaves the COO kernel in charge
+    int coo = 0, coo_sorted = 0;
+    void *coo_ptr = nullptr;
 };
 
 namespace gsa {
@@ -408,6 +422,10 @@ size_t gather_workspace_size(int64_t outer_n, int64_t nnz, int64_t k, int algo, 
 
 using Plan = ::gsa_plan;
 int plan_create(cudaStream_t s, int itype, int64_t outer_n, int64_t nnz, const void *ptr, int base, Plan *p);
+// Row pointers of a COO whose row indices are non-decreasing and within [base, base + m)
+// (sets *sorted = 0 otherwise; synchronizes s).
+int coo_row_pointers(cudaStream_t s, int itype, int64_t m, int64_t nnz, const void *rowind, int base,
+                     void *ptr_out, int *sorted);
 
 // Row-block gather (thread per short row; long rows by warp, or by plan chunks): the default.
 template <typename V, typename I>

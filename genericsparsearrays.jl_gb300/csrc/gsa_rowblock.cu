@@ -129,53 +129,9 @@ rowblock_kernel(CompressedArgs<V, I> a, int64_t k, DenseIn<V> B, DenseOut<V> C, 
 // number of multiply-adds: FP64 products on GB300 are bound by the FP64 pipe, which
 // counts a warp instruction whole however few of its lanes are active.
 
-struct BinView {
-    int64_t nwarps;
-    const int64_t *perm, *seg;
-    const uint8_t *warp_bin;
-    const int64_t *bins;  // per bin: first warp, first position, end position, lanes per row
-};
-
-template <typename V, typename I, int KC, int G>
-__device__ __forceinline__ void binned_rows(const CompressedArgs<V, I> &a, int64_t k, const DenseIn<V> &B,
-                                            const DenseOut<V> &C, int64_t c0, int64_t pos0, int64_t pend,
-                                            const BinView &bv) {
-    using O = Off<I>;
-    const int lane = threadIdx.x & 31;
-    const int64_t i = pos0 + lane / G;
-    const bool valid = i < pend;
-    int64_t row = 0;
-    O b = 0, e = 0;
-    if (valid) {
-        row = __ldg(bv.perm + i);
-        const O nz = (O)a.nnz;
-        b = (O)__ldg(bv.seg + 2 * i);
-        e = (O)__ldg(bv.seg + 2 * i + 1);
-        b = b < nz ? b : nz;
-        e = e < nz ? e : nz;
-        e = e < b ? b : e;
-    }
-    V acc[KC];
-#pragma unroll
-    for (int c = 0; c < KC; ++c) acc[c] = VT<V>::zero();
-    accumulate_range<V, I, KC, G, (G == 1 ? 1 : 2)>(a, B, b + (O)(lane % G), e, c0, k, acc);
-    if (G > 1) {
-#pragma unroll
-        for (int c = 0; c < KC; ++c) {
-#pragma unroll
-            for (int m = G / 2; m > 0; m >>= 1) acc[c] = add(acc[c], shfl_xor(acc[c], m, G));
-        }
-    }
-    if (lane % G == 0 && valid && row < a.outer_n) {
-#pragma unroll
-        for (int c = 0; c < KC; ++c)
-            if (KC == 1 || c0 + c < k) C.store(row, c0 + c, acc[c]);
-    }
-}
-
 template <typename V, typename I, int KC>
 __global__ void __launch_bounds__(RB_THREADS, rb_min_blocks<V, KC>())
-binned_kernel(CompressedArgs<V, I> a, int64_t k, DenseIn<V> B, DenseOut<V> C, int64_t ncg, BinView bv,
+binned_kernel(CompressedArgs<V, I> a, int64_t k, DenseIn<V> B, DenseOut<V> C, int64_t ncg, gsa_bin_order bv,
               PlanRows L) {
     const unsigned cta = blockIdx.x;
     const unsigned cg = ncg == 1 ? 0u : cta % (unsigned)ncg;
@@ -186,14 +142,7 @@ binned_kernel(CompressedArgs<V, I> a, int64_t k, DenseIn<V> B, DenseOut<V> C, in
         chunk_unit<V, I, KC>(a, k, B, C, c0, cg, ncg, w - bv.nwarps, L);
         return;
     }
-    const int bi = __ldg(bv.warp_bin + w);
-    const int64_t first_warp = __ldg(bv.bins + 4 * bi), pos = __ldg(bv.bins + 4 * bi + 1);
-    const int64_t pend = __ldg(bv.bins + 4 * bi + 2);
-    const int G = (int)__ldg(bv.bins + 4 * bi + 3);
-    const int64_t pos0 = pos + (w - first_warp) * (32 / G);
-    dispatch_lanes(G, 1, [&](auto g) {  // G is a power of two: picks exactly G lanes
-        binned_rows<V, I, KC, decltype(g)::value>(a, k, B, C, c0, pos0, pend, bv);
-    });
+    binned_warp<V, I, KC>(a, k, B, C, c0, w, bv);
 }
 
 template <typename V, typename I>
@@ -235,7 +184,7 @@ int launch_rowblock(cudaStream_t s, const CompressedArgs<V, I> &a, int64_t k, De
     if (blocks > 0x7fffffffLL) return fail(GSA_ERR_UNSUPPORTED, "too many rows");
     timer_before(s);
     if (binned) {
-        const BinView bv{plan->nbin_warps, plan->perm, plan->seg, plan->warp_bin, plan->bins};
+        const gsa_bin_order bv{plan->nbin_warps, plan->perm, plan->seg, plan->warp_bin, plan->bins};
         if (KC == 1) binned_kernel<V, I, 1><<<(unsigned)blocks, RB_THREADS, 0, s>>>(a, k, B, C, ncg, bv, L);
         else if (KC == 2) binned_kernel<V, I, 2><<<(unsigned)blocks, RB_THREADS, 0, s>>>(a, k, B, C, ncg, bv, L);
         else if (KC == 4) binned_kernel<V, I, 4><<<(unsigned)blocks, RB_THREADS, 0, s>>>(a, k, B, C, ncg, bv, L);
@@ -347,8 +296,9 @@ static int build_plan(cudaStream_t s, int64_t outer_n, int64_t nnz, const I *ptr
                 mask_nat[(size_t)(w0 >> 5)] |= 1u << (r - w0);
         }
     }
-    // bin order when the natural one would leave over a quarter of the lanes idle
-    const bool binned = outer_n >= 4096 && natural_utilisation(len, mask_nat) < 0.75;
+    // bin order when the natural one would leave over a tenth of the lanes idle (only
+    // FP64-bound products use it, where every idle lane is lost FP64 time)
+    const bool binned = outer_n >= 32 && natural_utilisation(len, mask_nat) < 0.9;
     struct HostSet {
         std::vector<int64_t> row;
         std::vector<int32_t> first, count, slot;
@@ -405,7 +355,8 @@ static int build_plan(cudaStream_t s, int64_t outer_n, int64_t nnz, const I *ptr
     p->nplanned = binned ? outer_n : (int64_t)hs[0].row.size();
     if (p->nplanned == 0) return GSA_OK;
     size_t bytes = align_up(perm.size() * 8, 256) + align_up(seg.size() * 8, 256) +
-                   align_up(warp_bin.size(), 256) + align_up(bins.size() * 8, 256);
+                   align_up(warp_bin.size(), 256) + align_up(bins.size() * 8, 256) +
+                   align_up(sizeof(gsa_bin_order), 256);
     for (int t = 0; t < 2; ++t)
         bytes += align_up(hs[t].row.size() * 8, 256) + align_up(hs[t].first.size() * 4, 256) +
                  align_up(hs[t].count.size() * 4, 256) + align_up(hs[t].slot.size() * 4, 256) +
@@ -446,12 +397,18 @@ static int build_plan(cudaStream_t s, int64_t outer_n, int64_t nnz, const I *ptr
     up(d_seg, seg.data(), seg.size() * 8, "plan: extents");
     up(d_wb, warp_bin.data(), warp_bin.size(), "plan: warp bins");
     up(d_bins, bins.data(), bins.size() * 8, "plan: bins");
+    gsa_bin_order *d_view = cv.take<gsa_bin_order>(1);
+    if (binned) {
+        const gsa_bin_order view{p->nbin_warps, d_perm, d_seg, d_wb, d_bins};
+        up(d_view, &view, sizeof(view), "plan: bin view");
+    }
     if (rc) return rc;
     if (binned) {
         p->perm = d_perm;
         p->seg = d_seg;
         p->warp_bin = d_wb;
         p->bins = d_bins;
+        p->bin_view = d_view;
     }
     return GSA_OK;
 }

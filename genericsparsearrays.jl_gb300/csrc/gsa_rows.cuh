@@ -192,4 +192,60 @@ __device__ __forceinline__ void warp_unit(const CompressedArgs<V, I> &a, int64_t
     });
 }
 
+// ---------------------------------------------------------------------------
+// Bin order (a plan's): rows grouped by length, warp w of the order takes 32 / G
+// consecutive rows of its bin, G lanes each, so the lanes of a warp do equal work.
+
+template <typename V, typename I, int KC, int G>
+__device__ __forceinline__ void binned_rows(const CompressedArgs<V, I> &a, int64_t k, const DenseIn<V> &B,
+                                            const DenseOut<V> &C, int64_t c0, int64_t pos0, int64_t pend,
+                                            const gsa_bin_order &bv) {
+    using O = Off<I>;
+    const int lane = threadIdx.x & 31;
+    const int64_t i = pos0 + lane / G;
+    const bool valid = i < pend;
+    int64_t row = 0;
+    O b = 0, e = 0;
+    if (valid) {
+        row = __ldg(bv.perm + i);
+        const O nz = (O)a.nnz;
+        b = (O)__ldg(bv.seg + 2 * i);
+        e = (O)__ldg(bv.seg + 2 * i + 1);
+        b = b < nz ? b : nz;
+        e = e < nz ? e : nz;
+        e = e < b ? b : e;
+    }
+    V acc[KC];
+#pragma unroll
+    for (int c = 0; c < KC; ++c) acc[c] = VT<V>::zero();
+    accumulate_range<V, I, KC, G, (G == 1 ? 1 : 2)>(a, B, b + (O)(lane % G), e, c0, k, acc);
+    if (G > 1) {
+#pragma unroll
+        for (int c = 0; c < KC; ++c) {
+#pragma unroll
+            for (int m = G / 2; m > 0; m >>= 1) acc[c] = add(acc[c], shfl_xor(acc[c], m, G));
+        }
+    }
+    if (lane % G == 0 && valid && row < a.outer_n) {
+#pragma unroll
+        for (int c = 0; c < KC; ++c)
+            if (KC == 1 || c0 + c < k) C.store(row, c0 + c, acc[c]);
+    }
+}
+
+// Warp w of the bin order (w < bv.nwarps).
+template <typename V, typename I, int KC>
+__device__ __forceinline__ void binned_warp(const CompressedArgs<V, I> &a, int64_t k, const DenseIn<V> &B,
+                                            const DenseOut<V> &C, int64_t c0, int64_t w,
+                                            const gsa_bin_order &bv) {
+    const int bi = __ldg(bv.warp_bin + w);
+    const int64_t first_warp = __ldg(bv.bins + 4 * bi), pos = __ldg(bv.bins + 4 * bi + 1);
+    const int64_t pend = __ldg(bv.bins + 4 * bi + 2);
+    const int G = (int)__ldg(bv.bins + 4 * bi + 3);
+    const int64_t pos0 = pos + (w - first_warp) * (32 / G);
+    dispatch_lanes(G, 1, [&](auto g) {  // G is a power of two: picks exactly G lanes
+        binned_rows<V, I, KC, decltype(g)::value>(a, k, B, C, c0, pos0, pend, bv);
+    });
+}
+
 }  // namespace gsa

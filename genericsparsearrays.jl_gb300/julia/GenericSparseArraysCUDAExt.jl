@@ -69,16 +69,22 @@ _entry(::GenericSparseMatrixCSC) = :gsa_csc_mul
 const _PLANS = WeakKeyDict{Any, Ptr{Cvoid}}()
 const _PLANS_LOCK = ReentrantLock()
 
-function _plan(A::Union{GenericSparseMatrixCSR, GenericSparseMatrixCSC})
-    ptr = A isa GenericSparseMatrixCSR ? A.rowptr : A.colptr
+function _plan(A::Union{GenericSparseMatrixCSR, GenericSparseMatrixCSC, GenericSparseMatrixCOO})
+    ptr = A isa GenericSparseMatrixCSR ? A.rowptr : (A isa GenericSparseMatrixCSC ? A.colptr : A.rowind)
     lock(_PLANS_LOCK) do
         get!(_PLANS, ptr) do
             Ti = eltype(ptr)
             h = Ref{Ptr{Cvoid}}(C_NULL)
-            outer = A isa GenericSparseMatrixCSR ? size(A, 1) : size(A, 2)
-            gsa_check(ccall((:gsa_plan_create, libgsa), Cint,
-                (CUstream, Cint, Int64, Int64, CuPtr{Ti}, Cint, Ref{Ptr{Cvoid}}),
-                CUDA.stream(), gsa_itype(Ti), outer, length(A.nzval), ptr, Cint(1), h))
+            if A isa GenericSparseMatrixCOO  # row pointers when the rows are sorted
+                gsa_check(ccall((:gsa_coo_plan_create, libgsa), Cint,
+                    (CUstream, Cint, Int64, Int64, Int64, CuPtr{Ti}, Cint, Ref{Ptr{Cvoid}}),
+                    CUDA.stream(), gsa_itype(Ti), size(A, 1), size(A, 2), length(A.nzval), ptr, Cint(1), h))
+            else
+                outer = A isa GenericSparseMatrixCSR ? size(A, 1) : size(A, 2)
+                gsa_check(ccall((:gsa_plan_create, libgsa), Cint,
+                    (CUstream, Cint, Int64, Int64, CuPtr{Ti}, Cint, Ref{Ptr{Cvoid}}),
+                    CUDA.stream(), gsa_itype(Ti), outer, length(A.nzval), ptr, Cint(1), h))
+            end
             finalizer(_ -> ccall((:gsa_plan_destroy, libgsa), Cint, (Ptr{Cvoid},), h[]), ptr)
             h[]
         end
@@ -106,12 +112,13 @@ function _gsa_mul!(C::CuVecOrMat{T}, A, B, α::Number, β::Number) where {T}
     k = size(C, 2)
     ldc = C isa CuVector ? max(length(C), 1) : max(stride(C, 2), size(C, 1), 1)
     stream = CUDA.stream()
-    if _A isa GenericSparseMatrixCOO
-        st = ccall((:gsa_coo_mul, libgsa), Cint,
+    if _A isa GenericSparseMatrixCOO  # the COO kernel, or the CSR kernels for sorted rows
+        st = ccall((:gsa_coo_mul_planned, libgsa), Cint,
             (CUstream, Cint, Cint, Int64, Int64, Int64, CuPtr{Ti}, CuPtr{Ti}, CuPtr{T}, Cint, Cint,
-             Int64, CuPtr{T}, Int64, Cint, CuPtr{T}, Int64, Ref{T}, Ref{T}),
+             Int64, CuPtr{T}, Int64, Cint, CuPtr{T}, Int64, Ref{T}, Ref{T}, Ptr{Cvoid}, Ptr{Cvoid},
+             Csize_t),
             stream, gsa_dtype(T), gsa_itype(Ti), _A.m, _A.n, length(_A.nzval), p0, p1, _A.nzval,
-            Cint(1), opA, k, P, ldb, opB, C, ldc, a, b)
+            Cint(1), opA, k, P, ldb, opB, C, ldc, a, b, _plan(_A), C_NULL, Csize_t(0))
     else
         # the structure's plan; NULL workspace: libgsa takes it from the stream-ordered pool
         plan = _plan(_A)
@@ -155,9 +162,9 @@ function _gsa_dot(x::CuVector{T}, A, y::CuVector{T}) where {T}
     if _A isa GenericSparseMatrixCOO
         st = ccall((:gsa_coo_dot, libgsa), Cint,
             (CUstream, Cint, Cint, Int64, Int64, Int64, CuPtr{Ti}, CuPtr{Ti}, CuPtr{T}, Cint, Cint,
-             CuPtr{T}, CuPtr{T}, Ref{T}, Ptr{Cvoid}, Csize_t),
+             CuPtr{T}, CuPtr{T}, Ref{T}, Ptr{Cvoid}, Ptr{Cvoid}, Csize_t),
             CUDA.stream(), gsa_dtype(T), gsa_itype(Ti), _A.m, _A.n, length(_A.nzval), p0, p1,
-            _A.nzval, Cint(1), opA, x, y, r, C_NULL, Csize_t(0))
+            _A.nzval, Cint(1), opA, x, y, r, _plan(_A), C_NULL, Csize_t(0))
     else
         st = ccall((_dot_entry(_A), libgsa), Cint,
             (CUstream, Cint, Cint, Int64, Int64, Int64, CuPtr{Ti}, CuPtr{Ti}, CuPtr{T}, Cint, Cint,
@@ -180,10 +187,11 @@ end
 # Batched products: many mul!(C_i, A_i, B_i, α_i, β_i) of one element and index type in
 # one grouped launch, replayed from a CUDA graph (gsa_batch_*).  Not a method of the
 # reference; an addition for callers with thousands of small products.
-struct GsaGroupItem  # 128 bytes, field order of gsa_group_item
+struct GsaGroupItem  # 144 bytes, field order of gsa_group_item
     rowptr::CuPtr{Cvoid}; colval::CuPtr{Cvoid}; nzval::CuPtr{Cvoid}; B::CuPtr{Cvoid}; C::CuPtr{Cvoid}
     m::Int64; n::Int64; nnz::Int64; ldb::Int64; ldc::Int64; k::Int32; b_rowmajor::Int32
     first_tile::Int64
+    bin_order::Ptr{Cvoid}; bin_warps::Int64
     alpha::NTuple{16, UInt8}; beta::NTuple{16, UInt8}
 end
 
@@ -200,9 +208,15 @@ function GroupedMul(products::AbstractVector) # [(C, A::CSRCu, B::CuVecOrMat, α
     for (C, A, B, α, β) in products
         ldb = B isa CuVector ? max(length(B), 1) : max(stride(B, 2), size(B, 1), 1)
         ldc = C isa CuVector ? max(length(C), 1) : max(stride(C, 2), size(C, 1), 1)
+        view, warps = Ref{Ptr{Cvoid}}(C_NULL), Ref{Int64}(0)
+        if T === ComplexF64  # FP64-bound: walk the plan's bin order
+            gsa_check(ccall((:gsa_plan_bin_order, libgsa), Cint, (Ptr{Cvoid}, Ref{Ptr{Cvoid}}, Ref{Int64}),
+                            _plan(A), view, warps))
+        end
         push!(items, GsaGroupItem(pointer(A.rowptr), pointer(A.colval), pointer(A.nzval), pointer(B),
                                   pointer(C), size(A, 1), size(A, 2), length(A.nzval), ldb, ldc,
-                                  Int32(size(C, 2)), Int32(0), 0, _bytes16(T(α)), _bytes16(T(β))))
+                                  Int32(size(C, 2)), Int32(0), 0, view[], warps[],
+                                  _bytes16(T(α)), _bytes16(T(β))))
     end
     h = Ref{Ptr{Cvoid}}(C_NULL)
     gsa_check(ccall((:gsa_batch_create, libgsa), Cint,

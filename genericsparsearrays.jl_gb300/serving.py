@@ -60,11 +60,16 @@ class Registry:
         self._next = 0
 
     def add(self, A) -> int:
+        """Register a resident matrix (its bytes are charged).  A ComplexF64 matrix gets its
+        plan now (bin order for the grouped kernel), not at its first request."""
         b = matrix_bytes(A)
         if self.used + b > self.budget:
             raise BudgetExceeded(f"matrix of {b} bytes does not fit: {self.used} of {self.budget} in use")
         mid = self._next
         self._next += 1
+        if getattr(A, "device", None) is not None and A.device.type == "cuda":
+            from .batch import bin_order_of
+            bin_order_of(A)
         self._mats[mid] = A
         self._bytes[mid] = b
         self.used += b

@@ -435,6 +435,31 @@ def _gather_plan(A) -> Optional[_PlanHandle]:
     return A._plan
 
 
+def _coo_plan(A) -> Optional[_PlanHandle]:
+    """The plan of a COO matrix whose row indices are non-decreasing (row pointers built on
+    the GPU once and kept on the matrix, so the CSR kernels serve it); None otherwise.  Made
+    on first use (one stream synchronisation); the indices must not change in place after."""
+    cached = A.__dict__.get("_plan", False)
+    if cached is not False:
+        return cached
+    lib = _lib.load()
+    h = ctypes.c_void_p(0)
+    with torch.cuda.device(A.device):
+        st = lib.gsa_coo_plan_create(_stream_ptr(A.device), _ITYPE[A.itype], A.m, A.n, nnz(A),
+                                     _ptr(A.rowind), BASE, ctypes.byref(h))
+    _lib.check(st)
+    srt = ctypes.c_int(0)
+    lib.gsa_coo_plan_info(h, ctypes.byref(srt))
+    if not srt.value:
+        lib.gsa_plan_destroy(h)
+        A._plan = None
+    else:
+        ml, nl, nc = ctypes.c_int64(0), ctypes.c_int64(0), ctypes.c_int64(0)
+        lib.gsa_plan_info(h, ctypes.byref(ml), ctypes.byref(nl), ctypes.byref(nc))
+        A._plan = _PlanHandle(h.value, nl.value, nc.value, ml.value)
+    return A._plan
+
+
 def mul_(C: torch.Tensor, A, B, alpha=1, beta=0, algo: int = _lib.ALGO_AUTO,
          workspace: Optional[torch.Tensor] = None) -> torch.Tensor:
     """``mul!(C, A, B, α, β)``: ``C = β C + α op(A) op(B)`` on the GPU; returns ``C``.
@@ -516,11 +541,25 @@ def mul_(C: torch.Tensor, A, B, alpha=1, beta=0, algo: int = _lib.ALGO_AUTO,
                     _ptr(workspace) if ws_bytes else ctypes.c_void_p(0),
                     workspace.numel() if ws_bytes else 0)
         else:
-            st = lib.gsa_coo_mul(stream, _DTYPE[dt], _ITYPE[Ap.itype], Ap.m, Ap.n, nnz(Ap),
-                                 _ptr(Ap.rowind), _ptr(Ap.colind), _ptr(Ap.nzval), BASE, opA, k,
-                                 _ptr(Bbuf), ldb, opB, _ptr(Cw), ldc,
-                                 al.ctypes.data_as(ctypes.c_void_p),
-                                 be.ctypes.data_as(ctypes.c_void_p))
+            cplan = _coo_plan(Ap) if algo == _lib.ALGO_AUTO else None
+            if cplan is not None:  # row-sorted: the CSR kernels on the plan's row pointers
+                ws_bytes = lib.gsa_plan_workspace_size(ctypes.c_void_p(cplan.handle), _DTYPE[dt], k)
+                if ws_bytes and (workspace is None or workspace.numel() < ws_bytes):
+                    workspace = torch.empty(ws_bytes, dtype=torch.uint8, device=dev)
+                st = lib.gsa_coo_mul_planned(stream, _DTYPE[dt], _ITYPE[Ap.itype], Ap.m, Ap.n, nnz(Ap),
+                                             _ptr(Ap.rowind), _ptr(Ap.colind), _ptr(Ap.nzval), BASE, opA,
+                                             k, _ptr(Bbuf), ldb, opB, _ptr(Cw), ldc,
+                                             al.ctypes.data_as(ctypes.c_void_p),
+                                             be.ctypes.data_as(ctypes.c_void_p),
+                                             ctypes.c_void_p(cplan.handle),
+                                             _ptr(workspace) if ws_bytes else ctypes.c_void_p(0),
+                                             workspace.numel() if ws_bytes else 0)
+            else:
+                st = lib.gsa_coo_mul(stream, _DTYPE[dt], _ITYPE[Ap.itype], Ap.m, Ap.n, nnz(Ap),
+                                     _ptr(Ap.rowind), _ptr(Ap.colind), _ptr(Ap.nzval), BASE, opA, k,
+                                     _ptr(Bbuf), ldb, opB, _ptr(Cw), ldc,
+                                     al.ctypes.data_as(ctypes.c_void_p),
+                                     be.ctypes.data_as(ctypes.c_void_p))
     _lib.check(st)
     if not direct:
         C2.copy_(Cw)
@@ -577,9 +616,11 @@ def dot(x: torch.Tensor, A, y: torch.Tensor):
     stream = _stream_ptr(Ap.device)
     with torch.cuda.device(Ap.device):
         if isinstance(Ap, GenericSparseMatrixCOO):
+            cplan = _coo_plan(Ap)
             st = lib.gsa_coo_dot(stream, _DTYPE[dt], _ITYPE[Ap.itype], Ap.m, Ap.n, nnz(Ap), _ptr(Ap.rowind),
                                  _ptr(Ap.colind), _ptr(val), BASE, opA, _ptr(xv), _ptr(yv),
-                                 out.ctypes.data_as(ctypes.c_void_p), None, 0)
+                                 out.ctypes.data_as(ctypes.c_void_p),
+                                 ctypes.c_void_p(cplan.handle) if cplan is not None else None, None, 0)
         else:
             csr = isinstance(Ap, GenericSparseMatrixCSR)
             ptr, idx = (Ap.rowptr, Ap.colval) if csr else (Ap.colptr, Ap.rowval)

@@ -195,6 +195,22 @@ int gsa_csc_mul_planned(void *stream, int dtype, int itype, int64_t m, int64_t n
                         const void *alpha, const void *beta, const gsa_plan *plan, void *workspace,
                         size_t workspace_bytes);
 
+/* COO plans: when the row indices of a COO structure are non-decreasing and within
+ * [base, base + m), gsa_coo_plan_create builds its row pointers on the GPU (once; the
+ * stream is synchronized) together with an ordinary plan of them, and gsa_coo_mul_planned
+ * then runs the CSR kernels on (row pointers, colind, nzval) -- the gather for opA = N,
+ * the outer-block scatter for T/C -- instead of the COO kernel.  Otherwise the plan only
+ * records that the COO kernel keeps the structure (gsa_coo_plan_info: row_sorted = 0).
+ * Replaces the same reference methods as gsa_coo_mul. */
+int gsa_coo_plan_create(void *stream, int itype, int64_t m, int64_t n, int64_t nnz, const void *rowind,
+                        int base, gsa_plan **out);
+int gsa_coo_plan_info(const gsa_plan *plan, int *row_sorted);
+int gsa_coo_mul_planned(void *stream, int dtype, int itype, int64_t m, int64_t n, int64_t nnz,
+                        const void *rowind, const void *colind, const void *nzval, int base, int opA,
+                        int64_t k, const void *B, int64_t ldb, int opB, void *C, int64_t ldc,
+                        const void *alpha, const void *beta, const gsa_plan *plan, void *workspace,
+                        size_t workspace_bytes);
+
 /* ---- three-argument dot ---------------------------------------------------
  * *result = dot(x, op(A), y) = sum over stored entries of conj(x_l) * a * y_r (l = row,
  * r = col for opA = N, swapped for T/C, a conjugated for C); x has rows(op(A)) entries,
@@ -203,7 +219,8 @@ int gsa_csc_mul_planned(void *stream, int dtype, int itype, int64_t m, int64_t n
  * fixed order (deterministic).  Replace LinearAlgebra.dot methods generated at
  * src/matrix_csr/matrix_csr.jl:213-277, src/matrix_csc/matrix_csc.jl:219 and
  * src/matrix_coo/matrix_coo.jl:227 (kernels kernel_workgroup_dot_*_N! / _T!).  plan:
- * optional (NULL), a plan of the compressed structure for long outer entries.
+ * optional (NULL): a plan of the compressed structure for long outer entries, or for
+ * gsa_coo_dot a COO plan (a row-sorted COO then takes the CSR path).
  * workspace: NULL (stream-ordered allocation) or gsa_dot_workspace_size bytes. */
 int gsa_csr_dot(void *stream, int dtype, int itype, int64_t m, int64_t n, int64_t nnz,
                 const void *rowptr, const void *colval, const void *nzval, int base, int opA,
@@ -215,9 +232,9 @@ int gsa_csc_dot(void *stream, int dtype, int itype, int64_t m, int64_t n, int64_
                 void *workspace, size_t workspace_bytes);
 int gsa_coo_dot(void *stream, int dtype, int itype, int64_t m, int64_t n, int64_t nnz,
                 const void *rowind, const void *colind, const void *nzval, int base, int opA,
-                const void *x, const void *y, void *result, void *workspace,
-                size_t workspace_bytes);
-/* format: 0 CSR, 1 CSC, 2 COO (plan ignored for COO). */
+                const void *x, const void *y, void *result, const gsa_plan *plan,
+                void *workspace, size_t workspace_bytes);
+/* format: 0 CSR, 1 CSC, 2 COO (plan: a COO plan, or NULL). */
 size_t gsa_dot_workspace_size(int format, int dtype, int itype, int64_t m, int64_t n,
                               const gsa_plan *plan);
 
@@ -228,11 +245,12 @@ size_t gsa_mul_workspace_size(int format, int dtype, int itype, int64_t m, int64
 
 /* ---- grouped products -------------------------------------------------------
  * Many CSR products C_i = beta_i*C_i + alpha_i*A_i*B_i (A_i m x n with nnz entries,
- * B_i n x k column-major with leading dimension ldb, C_i m x k with ldc) in ONE
- * persistent launch that walks (item, row block, column group) tiles -- instead of
- * one launch per product, which is what dominates the time of thousands of small
- * products.  alpha/beta hold the bytes of one value of the call's dtype (a double,
- * or re then im).  No counterpart in the reference (one KA launch per mul!). */
+ * B_i n x k with leading dimension ldb, C_i m x k column-major with ldc) in ONE
+ * persistent launch that walks (item, row block or bin-order warps, column group)
+ * tiles -- instead of one launch per product, which is what dominates the time of
+ * thousands of small products.  alpha/beta hold the bytes of one value of the call's
+ * dtype (a double, or re then im).  No counterpart in the reference (one KA launch per
+ * mul!). */
 typedef struct {
     const void *rowptr, *colval, *nzval;
     const void *B;
@@ -242,9 +260,16 @@ typedef struct {
     int32_t b_rowmajor;        /* 0: B(i, c) at B[i + c*ldb] (ldb >= n); 1: at B[i*ldb + c]
                                   (ldb >= k) -- one entry's k values then share cache lines */
     int64_t first_tile;        /* filled by gsa_grouped_tiles */
+    const void *bin_order;     /* NULL (natural row blocks) or gsa_plan_bin_order's view of a
+                                  plan of this item's structure */
+    int64_t bin_warps;         /* its warp count (0 with a NULL bin_order) */
     unsigned char alpha[16];
     unsigned char beta[16];
-} gsa_group_item;
+} gsa_group_item;              /* 144 bytes */
+
+/* The device view of a plan's bin order for grouped items (NULL and 0 when the plan has no
+ * bin order, or has rows of more than 512 entries). */
+int gsa_plan_bin_order(const gsa_plan *plan, const void **view, int64_t *warps);
 
 /* Checks the items (host memory), fills first_tile and returns the tile count.
  * columns: right-hand-side columns a thread accumulates (0 = by dtype, 1, 2, 4, 8);

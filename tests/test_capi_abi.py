@@ -91,7 +91,7 @@ def test_dot_argument_checks(lib, gsa):
     # bad op, bad dtype, negative size, NULL vectors
     assert lib.gsa_csr_dot(None, 1, 0, 4, 3, 0, fake, None, None, 1, 7, fake, fake, res, None, None, 0) \
         == L.ERR_INVALID_ARG
-    assert lib.gsa_coo_dot(None, 99, 0, 4, 3, 0, None, None, None, 1, 0, fake, fake, res, None, 0) \
+    assert lib.gsa_coo_dot(None, 99, 0, 4, 3, 0, None, None, None, 1, 0, fake, fake, res, None, None, 0) \
         == L.ERR_UNSUPPORTED
     assert lib.gsa_csc_dot(None, 1, 0, -1, 3, 0, fake, None, None, 1, 0, fake, fake, res, None, None, 0) \
         == L.ERR_INVALID_ARG

@@ -35,7 +35,7 @@ def test_grouped_matches_per_call_and_oracle(gsa, oracle, cuda, dt):
     from genericsparsearrays_gb300 import batch, workloads as wl
     prods, host = make_products(gsa, wl, cuda, 96, dt, ks=(1, 4, 3, 8), seed=3)
     Y0s = [p[2].clone() for p in prods]
-    b = batch.BatchedMul(prods)
+    b = batch.BatchedMul(prods, use_plans=False)  # natural row blocks: the per-call code exactly
     b.run("grouped")
     grouped = [p[2].clone() for p in prods]
     for p, y0 in zip(prods, Y0s):
@@ -49,6 +49,21 @@ def test_grouped_matches_per_call_and_oracle(gsa, oracle, cuda, dt):
         ye, sc = oracle.mul_exact("csr", "N", m, m, p, c, v, 1, X, Y0, alpha=alpha, beta=beta)
         assert oracle.max_rel_error(g.cpu().numpy(), ye, sc) <= 1e-12
     b.close()
+    # with plans: ComplexF64 items walk their plans' bin order
+    for p, y0 in zip(prods, Y0s):
+        p[2].copy_(y0)
+    items, _, _ = batch.pack_items(prods)
+    if dt == np.complex128:
+        assert (items["bin_warps"] > 0).sum() > len(prods) // 2
+    else:
+        assert (items["bin_warps"] == 0).all()
+    b2 = batch.BatchedMul(prods)
+    b2.run("graph")
+    torch.cuda.synchronize()
+    for (p, c, v, X, Y0, alpha, beta, m), q in zip(host, prods):
+        ye, sc = oracle.mul_exact("csr", "N", m, m, p, c, v, 1, X, Y0, alpha=alpha, beta=beta)
+        assert oracle.max_rel_error(q[2].cpu().numpy(), ye, sc) <= 1e-12
+    b2.close()
 
 
 def test_graph_replay_after_refill(gsa, oracle, cuda):
@@ -114,7 +129,7 @@ def test_row_major_right_hand_sides(gsa, oracle, cuda):
         Y = Y if k == 1 else Y.t()
         prods.append((A, X, Y, 2.0, 0))
         host.append((p.cpu().numpy(), c.cpu().numpy(), v.cpu().numpy(), X.cpu().numpy(), m, k))
-    b = batch.BatchedMul(prods)
+    b = batch.BatchedMul(prods, use_plans=False)
     b.run("graph")
     got = [q[2].clone() for q in prods]
     b.run("per_call")

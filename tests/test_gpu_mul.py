@@ -307,3 +307,36 @@ def test_plan_orders(gsa, oracle, cuda, dt, k):
                 check(oracle, f, opA, mm, nn, rp, cv, vals, X, "N", C0, C, 2, beta, dt)
     finally:
         lib.gsa_set_tuning(_lib.TUNE_PLAN_ORDER, 0)
+
+
+@pytest.mark.parametrize("dt", [np.float64, np.complex128, np.int64])
+@pytest.mark.parametrize("it", INDEX_TYPES)
+def test_row_sorted_coo_uses_row_pointers(gsa, oracle, cuda, dt, it):
+    """A COO whose rows are non-decreasing (columns in any order, duplicates adjacent or not
+    within a row) gets a plan with row pointers and runs the CSR kernels: every op, k = 1 and
+    3, against the oracle; an unsorted COO keeps the COO kernel and gives the same answers."""
+    rng = np.random.default_rng(8)
+    m, n = 5000, 700
+    lengths = rng.poisson(6, m)
+    lengths[[7, 4000]] = [2000, 900]  # long rows: chunks
+    lengths[100:140] = 0
+    rows = np.repeat(np.arange(m), lengths)
+    cols = rng.integers(0, n, rows.size)  # repeats allowed, unsorted inside rows
+    vals = rand_values(rng, rows.size, dt)
+    r1, c1 = (rows + 1).astype(it), (cols + 1).astype(it)
+    for order in ("sorted", "shuffled"):
+        if order == "shuffled":
+            p = rng.permutation(rows.size)
+            r, c, v = r1[p], c1[p], vals[p]
+        else:
+            r, c, v = r1, c1, vals
+        A = make(gsa, "coo", m, n, r, c, v, cuda)
+        for opA in OPS:
+            rows_out, inner = (m, n) if opA == "N" else (n, m)
+            for k in (1, 3):
+                X = np.asfortranarray(rand_values(rng, (inner, k), dt))
+                C0 = np.asfortranarray(rand_values(rng, (rows_out, k), dt))
+                C = torch.from_numpy(C0).to(cuda)
+                gsa.mul_(C, wrap(gsa, A, opA), torch.from_numpy(X).to(cuda), 2, 3)
+                check(oracle, "coo", opA, m, n, r, c, v, X, "N", C0, C, 2, 3, dt)
+        assert (A._plan is not None) == (order == "sorted")
