@@ -16,9 +16,11 @@ from .sparse import (
     SparseMatrixCSC,
     Transpose,
     adapt,
+    add,
     adjoint,
     collect,
     dot,
+    dropzeros,
     mul,
     mul_,
     nnz,
@@ -34,5 +36,5 @@ __all__ = [
     "AbstractGenericSparseMatrix", "Adjoint", "ArgumentError", "DimensionMismatch",
     "GenericSparseMatrixCOO", "GenericSparseMatrixCSC", "GenericSparseMatrixCSR",
     "SparseMatrixCSC", "Transpose", "adapt", "adjoint", "collect", "mul", "mul_", "nnz", "size",
-    "transpose", "validate", "dot", "ALGO_AUTO", "ALGO_MERGE", "ALGO_VECTOR", "ALGO_PIPE",
+    "transpose", "validate", "dot", "add", "dropzeros", "ALGO_AUTO", "ALGO_MERGE", "ALGO_VECTOR", "ALGO_PIPE",
 ]

@@ -172,8 +172,10 @@ class GroupedLauncher:
         dev = torch.empty(cap * ITEM_DTYPE.itemsize, dtype=torch.uint8, device=self.device)
         return {"cap": cap, "host": host, "dev": dev, "event": None}
 
-    def launch(self, products: Sequence[Product], stream: Optional[torch.cuda.Stream] = None) -> None:
+    def launch(self, products: Sequence[Product], stream: Optional[torch.cuda.Stream] = None,
+               columns: Optional[int] = None) -> None:
         stream = stream or torch.cuda.current_stream(self.device)
+        columns = self.columns if columns is None else columns
         slot = self._slots[self._next]
         self._next ^= 1
         if slot["event"] is not None:
@@ -182,7 +184,7 @@ class GroupedLauncher:
             slot.update(self._alloc(max(len(products), 2 * slot["cap"])))
         view = slot["host"].numpy().view(ITEM_DTYPE)
         items, dt, it = pack_items(products, out=view)
-        ntiles = tiles(items, dt, self.columns)
+        ntiles = tiles(items, dt, columns)
         nbytes = len(products) * ITEM_DTYPE.itemsize
         with torch.cuda.stream(stream), torch.cuda.device(self.device):
             slot["dev"].record_stream(stream)  # a regrown slot frees the old buffer stream-safely
@@ -193,5 +195,5 @@ class GroupedLauncher:
             _lib.check(_lib.load().gsa_grouped_mul(ctypes.c_void_p(stream.cuda_stream), _DTYPE[dt],
                                                    _ITYPE[it], BASE,
                                                    ctypes.c_void_p(slot["dev"].data_ptr()),
-                                                   len(products), ntiles, self.columns,
+                                                   len(products), ntiles, columns,
                                                    self.g1_avg))

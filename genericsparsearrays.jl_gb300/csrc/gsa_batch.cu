@@ -20,69 +20,78 @@ namespace gsa {
 
 static_assert(sizeof(gsa_group_item) == 144, "gsa_group_item layout");
 
+// One value of V from an item's alpha/beta bytes (8-byte loads: the bytes are 8-aligned).
+template <typename V>
+__device__ __forceinline__ V scalar_at(const unsigned char *p) {
+    union { V v; unsigned long long w[sizeof(V) >= 8 ? sizeof(V) / 8 : 1]; unsigned int h; } u;
+    if (sizeof(V) >= 8) {
+#pragma unroll
+        for (int i = 0; i < (int)(sizeof(V) / 8); ++i) u.w[i] = __ldg((const unsigned long long *)p + i);
+    } else {
+        u.h = __ldg((const unsigned int *)p);
+    }
+    return u.v;
+}
+
 template <typename V, typename I, int KC>
 __global__ void __launch_bounds__(RB_THREADS)
 grouped_kernel(const gsa_group_item *__restrict__ items, int64_t count, int64_t ntiles, int base,
                int g1_avg) {
-    // One thread finds each tile's item -- forward from the previous one, since a CTA's tiles
-    // ascend -- and the CTA stages the item in shared memory: the other threads read its
-    // fields there instead of each running the search through global memory.
-    __shared__ gsa_group_item s_item;
-    __shared__ int64_t s_lo;
+    // Each warp finds its tile's item on its own -- lane 0 searches forward from the
+    // warp's previous item (a CTA's tiles ascend), the warp reads the item's fields with
+    // uniform loads -- so warps never wait for one another between tiles.
+    const int lane = threadIdx.x & 31;
     int64_t lo = 0;
     for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
-        if (threadIdx.x == 0) {
-            if (lo + 1 < count && __ldg(&items[lo + 1].first_tile) <= t) {
-                int64_t l = lo + 1, h = count - 1;  // last item with first_tile <= t, in (lo, count)
-                while (l < h) {
-                    const int64_t mid = (l + h + 1) >> 1;
-                    if (__ldg(&items[mid].first_tile) <= t) l = mid;
-                    else h = mid - 1;
-                }
-                lo = l;
+        if (lane == 0 && lo + 1 < count && __ldg(&items[lo + 1].first_tile) <= t) {
+            int64_t l = lo + 1, h = count - 1;  // last item with first_tile <= t, in (lo, count)
+            while (l < h) {
+                const int64_t mid = (l + h + 1) >> 1;
+                if (__ldg(&items[mid].first_tile) <= t) l = mid;
+                else h = mid - 1;
             }
-            s_lo = lo;
+            lo = l;
         }
-        __syncthreads();
-        lo = s_lo;
-        if (threadIdx.x < sizeof(gsa_group_item) / 4)
-            reinterpret_cast<uint32_t *>(&s_item)[threadIdx.x] =
-                __ldg(reinterpret_cast<const uint32_t *>(items + lo) + threadIdx.x);
-        __syncthreads();
-        const gsa_group_item &it = s_item;
-        const int64_t ncg = (it.k + KC - 1) / KC;
-        const int64_t local = t - it.first_tile;
+        lo = __shfl_sync(0xffffffffu, lo, 0);
+        const gsa_group_item *it = items + lo;
+        const int64_t kk = __ldg(&it->k);
+        const int64_t ncg = (kk + KC - 1) / KC;
+        const int64_t local = t - __ldg(&it->first_tile);
         const int64_t cg = ncg == 1 ? 0 : local % ncg;
         const int64_t unit = ncg == 1 ? local : local / ncg;
         CompressedArgs<V, I> a;
-        a.outer_n = it.m;
-        a.inner_n = it.n;
-        a.nnz = it.nnz;
-        a.ptr = (const I *)it.rowptr;
-        a.idx = (const I *)it.colval;
-        a.val = (const V *)it.nzval;
+        a.outer_n = __ldg(&it->m);
+        a.inner_n = __ldg(&it->n);
+        a.nnz = __ldg(&it->nnz);
+        a.ptr = (const I *)__ldg((const unsigned long long *)&it->rowptr);
+        a.idx = (const I *)__ldg((const unsigned long long *)&it->colval);
+        a.val = (const V *)__ldg((const unsigned long long *)&it->nzval);
         a.base = base;
         a.conjA = false;
+        const int64_t ldb = __ldg(&it->ldb);
+        const bool brow = __ldg(&it->b_rowmajor) != 0;
         DenseIn<V> B;
-        B.p = (const V *)it.B;
-        B.rs = it.b_rowmajor ? it.ldb : 1;
-        B.cs = it.b_rowmajor ? 1 : it.ldb;
+        B.p = (const V *)__ldg((const unsigned long long *)&it->B);
+        B.rs = brow ? ldb : 1;
+        B.cs = brow ? 1 : ldb;
         B.conj = false;
         DenseOut<V> C;
-        C.p = (V *)it.C;
-        C.ld = it.ldc;
-        C.alpha = *reinterpret_cast<const V *>(it.alpha);
-        C.beta = *reinterpret_cast<const V *>(it.beta);
+        C.p = (V *)__ldg((const unsigned long long *)&it->C);
+        C.ld = __ldg(&it->ldc);
+        C.alpha = scalar_at<V>(it->alpha);
+        C.beta = scalar_at<V>(it->beta);
         C.beta_mode = is_zero(C.beta) ? 0 : (is_one(C.beta) ? 1 : 2);
         C.alpha_one = alpha_one_of(C.alpha);
-        const int64_t kk = it.k;
-        const int64_t bin_warps = it.bin_warps;
-        const gsa_bin_order *bo = (const gsa_bin_order *)it.bin_order;
-        __syncthreads();  // every thread has its copy before the next tile overwrites s_item
+        const int64_t bin_warps = __ldg(&it->bin_warps);
         if (bin_warps > 0) {  // the plan's bin order: warp w of it
             const int64_t w = unit * RB_WARPS + (threadIdx.x >> 5);
             if (w < bin_warps) {
-                const gsa_bin_order bv{__ldg(&bo->nwarps), bo->perm, bo->seg, bo->warp_bin, bo->bins};
+                const gsa_bin_order *bo = (const gsa_bin_order *)__ldg((const unsigned long long *)&it->bin_order);
+                const gsa_bin_order bv{__ldg(&bo->nwarps),
+                                       (const int64_t *)__ldg((const unsigned long long *)&bo->perm),
+                                       (const int64_t *)__ldg((const unsigned long long *)&bo->seg),
+                                       (const uint8_t *)__ldg((const unsigned long long *)&bo->warp_bin),
+                                       (const int64_t *)__ldg((const unsigned long long *)&bo->bins)};
                 binned_warp<V, I, KC>(a, kk, B, C, cg * KC, w, bv);
             }
         } else {
@@ -183,6 +192,7 @@ int gsa_grouped_mul(void *stream, int dtype, int itype, int base, const gsa_grou
     if (!dtype_size(dtype) || !itype_size(itype))
         return fail(GSA_ERR_UNSUPPORTED, "unsupported dtype %d / itype %d", dtype, itype);
     if (count < 0 || ntiles < 0 || (count > 0 && !d_items)) return fail(GSA_ERR_INVALID_ARG, "bad arguments");
+    if ((uintptr_t)d_items % 8) return fail(GSA_ERR_INVALID_ARG, "items must be 8-byte aligned");
     if (columns != 0 && columns != 1 && columns != 2 && columns != 4 && columns != 8)
         return fail(GSA_ERR_INVALID_ARG, "columns must be 0, 1, 2, 4 or 8");
     if (count == 0) return GSA_OK;

@@ -461,6 +461,82 @@ int gsa_coo_dot(void *stream, int dtype, int itype, int64_t m, int64_t n, int64_
                     nullptr, workspace, workspace_bytes);
 }
 
+}  // extern "C"
+
+namespace gsa {
+struct DropCountBody {
+    cudaStream_t s; int64_t nnz; const void *val; void *ws; size_t ws_bytes; int64_t *kept;
+    template <typename V, typename I> int operator()() {
+        return launch_dropzeros_count<V>(s, nnz, (const V *)val, ws, ws_bytes, kept);
+    }
+};
+struct DropCopyBody {
+    cudaStream_t s; int fmt; int64_t outer_n, nnz; const void *p0, *p1, *val; int base; const void *ws;
+    void *o0, *o1, *ov;
+    template <typename V, typename I> int operator()() {
+        return launch_dropzeros_copy<V, I>(s, fmt, outer_n, nnz, (const I *)p0, (const I *)p1, (const V *)val,
+                                           base, ws, (I *)o0, (I *)o1, (V *)ov);
+    }
+};
+struct AddBody {
+    cudaStream_t s; int fmt; int64_t m, n, nnz; const void *p0, *p1, *val; int base; void *C; int64_t ldc;
+    template <typename V, typename I> int operator()() {
+        return launch_add_to_dense<V, I>(s, fmt, m, n, nnz, (const I *)p0, (const I *)p1, (const V *)val, base,
+                                         (V *)C, ldc);
+    }
+};
+}  // namespace gsa
+
+extern "C" {
+
+size_t gsa_dropzeros_workspace_size(int64_t nnz) { return nnz < 0 ? 0 : dropzeros_workspace_size(nnz); }
+
+int gsa_dropzeros_count(void *stream, int dtype, int64_t nnz, const void *nzval, void *workspace,
+                        size_t workspace_bytes, int64_t *kept) {
+    const size_t vs = dtype_size(dtype);
+    if (!vs) return fail(GSA_ERR_UNSUPPORTED, "unsupported dtype %d", dtype);
+    if (nnz < 0 || !kept || !workspace) return fail(GSA_ERR_INVALID_ARG, "bad arguments");
+    if (nnz > 0 && !nzval) return fail(GSA_ERR_INVALID_ARG, "nzval is NULL");
+    if (misaligned(nzval, vs)) return fail(GSA_ERR_INVALID_ARG, "nzval must be aligned to its element size");
+    DropCountBody body{(cudaStream_t)stream, nnz, nzval, workspace, workspace_bytes, kept};
+    return dispatch_vi(dtype, GSA_IDX64, body);
+}
+
+int gsa_dropzeros_copy(void *stream, int format, int dtype, int itype, int64_t outer_n, int64_t nnz,
+                       const void *p0, const void *p1, const void *nzval, int base, const void *workspace,
+                       void *p0_out, void *p1_out, void *val_out) {
+    size_t vs = dtype_size(dtype), is = itype_size(itype);
+    if (!vs || !is) return fail(GSA_ERR_UNSUPPORTED, "unsupported dtype %d / itype %d", dtype, itype);
+    if (format < 0 || format > 2) return fail(GSA_ERR_INVALID_ARG, "format must be 0 (CSR), 1 (CSC) or 2 (COO)");
+    if (outer_n < 0 || nnz < 0 || !workspace) return fail(GSA_ERR_INVALID_ARG, "bad arguments");
+    if (format != 2 && (!p0 || !p0_out)) return fail(GSA_ERR_INVALID_ARG, "pointer arrays are NULL");
+    if (nnz > 0 && (!p1 || !nzval || (format == 2 && !p0))) return fail(GSA_ERR_INVALID_ARG, "sparse arrays are NULL");
+    if (misaligned(p0, is) || misaligned(p1, is) || misaligned(nzval, vs) || misaligned(p0_out, is) ||
+        misaligned(p1_out, is) || misaligned(val_out, vs))
+        return fail(GSA_ERR_INVALID_ARG, "arrays must be aligned to their element size");
+    DropCopyBody body{(cudaStream_t)stream, format, outer_n, nnz, p0, p1, nzval, base, workspace, p0_out, p1_out,
+                      val_out};
+    return dispatch_vi(dtype, itype, body);
+}
+
+int gsa_add_to_dense(void *stream, int format, int dtype, int itype, int64_t m, int64_t n, int64_t nnz,
+                     const void *p0, const void *p1, const void *nzval, int base, void *C, int64_t ldc) {
+    size_t vs = dtype_size(dtype), is = itype_size(itype);
+    if (!vs || !is) return fail(GSA_ERR_UNSUPPORTED, "unsupported dtype %d / itype %d", dtype, itype);
+    if (format < 0 || format > 2) return fail(GSA_ERR_INVALID_ARG, "format must be 0 (CSR), 1 (CSC) or 2 (COO)");
+    if (m < 0 || n < 0 || nnz < 0) return fail(GSA_ERR_INVALID_ARG, "negative size");
+    if (itype == GSA_IDX32 && nnz > 0x7fffffffLL)
+        return fail(GSA_ERR_INVALID_ARG, "nnz=%lld exceeds what Int32 indices can address", (long long)nnz);
+    if (ldc < (m > 1 ? m : 1)) return fail(GSA_ERR_DIM, "ldc=%lld is smaller than %lld", (long long)ldc, (long long)m);
+    if (m > 0 && n > 0 && !C) return fail(GSA_ERR_INVALID_ARG, "C is NULL");
+    if (format != 2 && !p0) return fail(GSA_ERR_INVALID_ARG, "pointer array is NULL");
+    if (nnz > 0 && (!p0 || !p1 || !nzval)) return fail(GSA_ERR_INVALID_ARG, "sparse arrays are NULL");
+    if (misaligned(p0, is) || misaligned(p1, is) || misaligned(nzval, vs) || misaligned(C, vs))
+        return fail(GSA_ERR_INVALID_ARG, "arrays must be aligned to their element size");
+    AddBody body{(cudaStream_t)stream, format, m, n, nnz, p0, p1, nzval, base, C, ldc};
+    return dispatch_vi(dtype, itype, body);
+}
+
 size_t gsa_dot_workspace_size(int format, int dtype, int itype, int64_t m, int64_t n, const gsa_plan *plan) {
     if (format < 0 || format > 2) return 0;
     if (format == 2 && plan && plan->coo_sorted) format = 0;  // served by the CSR dot

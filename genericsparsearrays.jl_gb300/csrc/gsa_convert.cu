@@ -487,4 +487,98 @@ int coo_row_pointers(cudaStream_t s, int itype, int64_t m, int64_t nnz, const vo
     return rc;
 }
 
+// ---------------------------------------------------------------------------
+// dropzeros (src/matrix_csr/matrix_csr.jl:649-745 with kernel_count_nonzeros_csr! /
+// kernel_dropzeros_csr!, src/matrix_csr/matrix_csr_kernels.jl:409-443; the CSC and COO
+// counterparts): the stored entries that are not zero, in storage order.  Here one flag
+// per entry, one exclusive scan (the kept entries' new positions, and at [nnz] their
+// count), a scatter of the kept entries, and the new pointer of outer entry r is the
+// position of its first entry -- no per-row loop, so long rows cost nothing extra.
+
+template <typename V>
+__global__ void nonzero_flags_kernel(int64_t nnz, const V *__restrict__ val, uint32_t *__restrict__ flags) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i <= nnz; i += (int64_t)gridDim.x * blockDim.x)
+        flags[i] = i < nnz && !is_zero(ldg(val + i)) ? 1u : 0u;
+}
+
+template <typename V, typename I>
+__global__ void drop_scatter_kernel(int64_t nnz, const uint32_t *__restrict__ pos, const I *__restrict__ i0,
+                                    const I *__restrict__ i1, const V *__restrict__ val, I *__restrict__ o0,
+                                    I *__restrict__ o1, V *__restrict__ ov) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nnz; i += (int64_t)gridDim.x * blockDim.x) {
+        const uint32_t p = pos[i];
+        if (pos[i + 1] == p) continue;  // a zero
+        if (i0) o0[p] = i0[i];
+        o1[p] = i1[i];
+        ov[p] = val[i];
+    }
+}
+
+template <typename I>
+__global__ void drop_pointer_kernel(int64_t outer_n, int64_t nnz, const I *__restrict__ ptr, int base,
+                                    const uint32_t *__restrict__ pos, I *__restrict__ ptr_out) {
+    for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r <= outer_n; r += (int64_t)gridDim.x * blockDim.x) {
+        int64_t j = (int64_t)ptr[r] - base;
+        j = j < 0 ? 0 : (j > nnz ? nnz : j);
+        ptr_out[r] = (I)((int64_t)pos[j] + base);
+    }
+}
+
+size_t dropzeros_workspace_size(int64_t nnz) {
+    Carver cv(nullptr);
+    cv.take<uint32_t>(nnz + 1);
+    cv.take<uint32_t>(nnz + 1);
+    cv.take<uint32_t>(ceil_div(nnz + 1, SC_TILE) + 1);
+    return align_up(cv.off, 256);
+}
+
+template <typename V>
+int launch_dropzeros_count(cudaStream_t s, int64_t nnz, const V *val, void *ws, size_t ws_bytes, int64_t *kept) {
+    if (nnz + 1 > 0xffffffffLL) return fail(GSA_ERR_UNSUPPORTED, "dropzeros: more than 2^32 - 1 entries");
+    if (ws_bytes < dropzeros_workspace_size(nnz)) return fail(GSA_ERR_INVALID_ARG, "dropzeros workspace too small");
+    Carver cv(ws);
+    uint32_t *flags = cv.take<uint32_t>(nnz + 1);
+    uint32_t *pos = cv.take<uint32_t>(nnz + 1);
+    uint32_t *bsums = cv.take<uint32_t>(ceil_div(nnz + 1, SC_TILE) + 1);
+    int64_t blocks = ceil_div(nnz + 1, 256);
+    if (blocks > 152 * 64) blocks = 152 * 64;
+    nonzero_flags_kernel<V><<<(unsigned)blocks, 256, 0, s>>>(nnz, val, flags);
+    int rc = check_cuda(cudaGetLastError(), "nonzero_flags_kernel");
+    if (!rc) rc = exclusive_scan_u32(s, flags, pos, nnz + 1, bsums);
+    uint32_t total = 0;
+    if (!rc) rc = check_cuda(cudaMemcpyAsync(&total, pos + nnz, sizeof(uint32_t), cudaMemcpyDeviceToHost, s),
+                             "dropzeros: count");
+    if (!rc) rc = check_cuda(cudaStreamSynchronize(s), "dropzeros: sync");
+    if (!rc) *kept = (int64_t)total;
+    return rc;
+}
+
+template <typename V, typename I>
+int launch_dropzeros_copy(cudaStream_t s, int fmt, int64_t outer_n, int64_t nnz, const I *p0, const I *p1,
+                          const V *val, int base, const void *ws, I *o0, I *o1, V *ov) {
+    Carver cv(const_cast<void *>(ws));
+    cv.take<uint32_t>(nnz + 1);
+    const uint32_t *pos = cv.take<uint32_t>(nnz + 1);
+    int64_t blocks = ceil_div(nnz > outer_n ? nnz : outer_n + 1, 256);
+    if (blocks > 152 * 64) blocks = 152 * 64;
+    if (blocks < 1) blocks = 1;
+    if (nnz > 0)
+        drop_scatter_kernel<V, I><<<(unsigned)blocks, 256, 0, s>>>(nnz, pos, fmt == 2 ? p0 : nullptr, p1, val,
+                                                                  fmt == 2 ? o0 : nullptr, o1, ov);
+    if (fmt != 2)
+        drop_pointer_kernel<I><<<(unsigned)blocks, 256, 0, s>>>(outer_n, nnz, p0, base, pos, o0);
+    return check_cuda(cudaGetLastError(), "dropzeros copy");
+}
+
+#define GSA_INST_DROP_V(V) template int launch_dropzeros_count<V>(cudaStream_t, int64_t, const V *, void *, size_t, int64_t *);
+#define GSA_INST_DROP(V, I)                                                                          \
+    template int launch_dropzeros_copy<V, I>(cudaStream_t, int, int64_t, int64_t, const I *, const I *, \
+                                             const V *, int, const void *, I *, I *, V *);
+GSA_INST_DROP_V(float) GSA_INST_DROP_V(double) GSA_INST_DROP_V(cf32) GSA_INST_DROP_V(cf64)
+GSA_INST_DROP_V(int32_t) GSA_INST_DROP_V(int64_t)
+GSA_INST_DROP(float, int32_t) GSA_INST_DROP(float, int64_t) GSA_INST_DROP(double, int32_t)
+GSA_INST_DROP(double, int64_t) GSA_INST_DROP(cf32, int32_t) GSA_INST_DROP(cf32, int64_t)
+GSA_INST_DROP(cf64, int32_t) GSA_INST_DROP(cf64, int64_t) GSA_INST_DROP(int32_t, int32_t)
+GSA_INST_DROP(int32_t, int64_t) GSA_INST_DROP(int64_t, int32_t) GSA_INST_DROP(int64_t, int64_t)
+
 }  // namespace gsa

@@ -468,6 +468,19 @@ int launch_dot(cudaStream_t s, int fmt, int opA, int64_t m, int64_t n, int64_t n
                const I *p1, const V *val, int base, const V *x, const V *y, const Plan *plan,
                void *ws, size_t ws_bytes, void *result_host);
 
+// dropzeros: positions of the nonzero entries (count to the host), then the compaction.
+size_t dropzeros_workspace_size(int64_t nnz);
+template <typename V>
+int launch_dropzeros_count(cudaStream_t s, int64_t nnz, const V *val, void *ws, size_t ws_bytes, int64_t *kept);
+template <typename V, typename I>
+int launch_dropzeros_copy(cudaStream_t s, int fmt, int64_t outer_n, int64_t nnz, const I *p0, const I *p1,
+                          const V *val, int base, const void *ws, I *o0, I *o1, V *ov);
+
+// C += A for a dense column-major C (fmt 0 CSR, 1 CSC, 2 COO).
+template <typename V, typename I>
+int launch_add_to_dense(cudaStream_t s, int fmt, int64_t m, int64_t n, int64_t nnz, const I *p0, const I *p1,
+                        const V *val, int base, V *C, int64_t ldc);
+
 // COO: out[key_i, c] += conj?(val_i) * (op(B)(other_i, c) * alpha), after the beta pass.
 template <typename V, typename I>
 int launch_coo(cudaStream_t s, int64_t nnz, const I *out_idx, const I *in_idx, const V *val,

@@ -10,8 +10,9 @@ admitted under an HBM budget and coalesced into grouped launches (continuous bat
   budget allows and launches them together.  Requests that arrive while others are on the
   GPU are admitted as slots and memory free up, so their work overlaps the running launch
   on another stream.
-* ``GroupedExecutor``  runs one admitted set: one grouped launch (gsa_grouped_mul) per
-  element type on the slot's stream, timed by CUDA events mapped to the host clock.
+* ``GroupedExecutor``  runs one admitted set on the slot's stream: one grouped launch
+  (gsa_grouped_mul) per element type for the small products, a plain planned call for each
+  large one, timed by CUDA events mapped to the host clock.
 * ``serve_per_call``   the baseline: one public-API ``mul_`` per request as it arrives.
 
 The reference has no serving layer: its ``mul!`` (src/matrix_csr/matrix_csr.jl:153-209)
@@ -293,17 +294,21 @@ def summarize(reqs: Sequence[Request], launches: Optional[int] = None) -> dict:
 
 class GroupedExecutor:
     """Runs an admitted set on slot ``slot``'s CUDA stream: output allocation, then one
-    grouped launch per element type (pinned item staging, no allocation per launch in the
-    library), then a timing event.  Finish times are CUDA-event times mapped onto the host
-    clock through a reference event taken at construction."""
+    grouped launch per element type for the small products (pinned item staging, no
+    allocation per launch in the library), a plain planned call for each product of at least
+    ``solo_fma`` multiply-adds (there a launch is cheap against the work, and the plain call
+    has the plan's chunk warps), then a timing event.  Finish times are CUDA-event times
+    mapped onto the host clock through a reference event taken at construction."""
 
     def __init__(self, device, slots: int = 2, columns: int = 0, g1_avg: int = 0,
-                 clock: Callable[[], float] = time.perf_counter):
+                 clock: Callable[[], float] = time.perf_counter, solo_fma: int = 1 << 24):
         import torch
         from .batch import GroupedLauncher
         self.torch = torch
         self.device = torch.device(device)
         self.streams = [torch.cuda.Stream(self.device) for _ in range(slots)]
+        self.solo_fma = solo_fma
+        self.columns = columns
         self.launchers = [GroupedLauncher(self.device, 256, columns, g1_avg) for _ in range(slots)]
         self.ref = torch.cuda.Event(enable_timing=True)
         self.ref.record(torch.cuda.current_stream(self.device))
@@ -316,14 +321,20 @@ class GroupedExecutor:
         groups: Dict[Any, list] = collections.defaultdict(list)
         with torch.cuda.stream(s):
             torch.cuda.nvtx.range_push(f"gsa.serve.launch[{len(work)}]")
+            from .sparse import mul_, nnz
             for A, r in work:
                 if r.Y is None:
                     shape = (A.m,) if r.X.dim() == 1 else (r.k, A.m)
                     Y = torch.empty(shape, dtype=A.dtype, device=self.device)
                     r.Y = Y if r.X.dim() == 1 else Y.t()
-                groups[(A.dtype, A.itype)].append((A, r.X, r.Y, r.alpha, r.beta))
-            for prods in groups.values():
-                self.launchers[slot].launch(prods, s)
+                if nnz(A) * r.k >= self.solo_fma:
+                    mul_(r.Y, A, r.X, r.alpha, r.beta)
+                else:
+                    groups[(A.dtype, A.itype)].append((A, r.X, r.Y, r.alpha, r.beta))
+            for (dt, _), prods in groups.items():
+                # ComplexF64 rows of a row-major X: eight columns per thread fill a line
+                cols = self.columns or (8 if dt == torch.complex128 else 4)
+                self.launchers[slot].launch(prods, s, columns=cols)
             ev = torch.cuda.Event(enable_timing=True)
             ev.record(s)
             torch.cuda.nvtx.range_pop()

@@ -633,6 +633,73 @@ def dot(x: torch.Tensor, A, y: torch.Tensor):
     return out[0]
 
 
+def dropzeros(A):
+    """``dropzeros(A)``: a new matrix of A's format without the stored entries that are zero,
+    in storage order (src/matrix_csr/matrix_csr.jl:723-745 and the CSC/COO methods)."""
+    if not isinstance(A, AbstractGenericSparseMatrix):
+        raise ArgumentError("A must be a GenericSparseMatrixCSR/CSC/COO")
+    if A.device.type != "cuda":
+        raise ArgumentError("dropzeros runs on the GPU only; adapt the matrix to CUDA first")
+    lib = _lib.load()
+    nz = nnz(A)
+    ws = torch.empty(max(lib.gsa_dropzeros_workspace_size(nz), 1), dtype=torch.uint8, device=A.device)
+    kept = ctypes.c_int64(0)
+    stream = _stream_ptr(A.device)
+    with torch.cuda.device(A.device):
+        _lib.check(lib.gsa_dropzeros_count(stream, _DTYPE[A.dtype], nz, _ptr(A.nzval), _ptr(ws), ws.numel(),
+                                           ctypes.byref(kept)))
+        k = kept.value
+        it, dev = A.itype, A.device
+        if isinstance(A, GenericSparseMatrixCOO):
+            fmt, outer, p0, p1 = 2, 0, A.rowind, A.colind
+            o0 = torch.empty(k, dtype=it, device=dev)
+        elif isinstance(A, GenericSparseMatrixCSR):
+            fmt, outer, p0, p1 = 0, A.m, A.rowptr, A.colval
+            o0 = torch.empty(A.m + 1, dtype=it, device=dev)
+        else:
+            fmt, outer, p0, p1 = 1, A.n, A.colptr, A.rowval
+            o0 = torch.empty(A.n + 1, dtype=it, device=dev)
+        o1 = torch.empty(k, dtype=it, device=dev)
+        ov = torch.empty(k, dtype=A.dtype, device=dev)
+        _lib.check(lib.gsa_dropzeros_copy(stream, fmt, _DTYPE[A.dtype], _ITYPE[it], outer, nz, _ptr(p0), _ptr(p1),
+                                          _ptr(A.nzval), BASE, _ptr(ws), _ptr(o0), _ptr(o1), _ptr(ov)))
+    return type(A)(A.m, A.n, o0, o1, ov)
+
+
+def add(A, B: torch.Tensor) -> torch.Tensor:
+    """``A + B`` for a sparse ``A`` and a dense matrix ``B`` (src/core.jl:66-88): a new dense
+    column-major ``C = copy(B)`` with every stored entry of ``A`` added (duplicates add up).
+    Same checks and messages as the reference: ``DimensionMismatch`` on sizes, then
+    ``ArgumentError`` on backends.  ``B + A == A + B``; ``A - B`` is ``add(A, -B)``."""
+    if not isinstance(A, AbstractGenericSparseMatrix):
+        raise ArgumentError("A must be a GenericSparseMatrixCSR/CSC/COO")
+    if not isinstance(B, torch.Tensor) or B.dim() != 2:
+        raise ArgumentError("B must be a dense torch matrix")
+    if (A.m, A.n) != tuple(B.shape):
+        raise DimensionMismatch(f"dimensions must match: A has dims ({A.m}, {A.n}), B has dims "
+                                f"({B.shape[0]}, {B.shape[1]})")
+    if A.device != B.device:
+        raise ArgumentError("Both arrays must have the same backend")
+    if A.device.type != "cuda":
+        raise ArgumentError("sparse + dense runs on the GPU only; adapt the arrays to CUDA first")
+    if A.dtype != B.dtype:
+        raise ArgumentError(f"element types of A ({A.dtype}) and B ({B.dtype}) must match")
+    C = torch.empty((B.shape[1], B.shape[0]), dtype=B.dtype, device=B.device).t()  # column-major
+    C.copy_(B)
+    if isinstance(A, GenericSparseMatrixCOO):
+        fmt, p0, p1 = 2, A.rowind, A.colind
+    elif isinstance(A, GenericSparseMatrixCSR):
+        fmt, p0, p1 = 0, A.rowptr, A.colval
+    else:
+        fmt, p0, p1 = 1, A.colptr, A.rowval
+    with torch.cuda.device(A.device):
+        st = _lib.load().gsa_add_to_dense(_stream_ptr(A.device), fmt, _DTYPE[A.dtype], _ITYPE[A.itype], A.m,
+                                          A.n, nnz(A), _ptr(p0), _ptr(p1), _ptr(A.nzval), BASE, _ptr(C),
+                                          max(C.stride(1), A.m, 1))
+    _lib.check(st)
+    return C
+
+
 # ---------------------------------------------------------------------------
 # Conversions (src/conversions/conversions.jl)
 

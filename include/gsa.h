@@ -143,6 +143,29 @@ int gsa_coo_mul(void *stream, int dtype, int itype, int64_t m, int64_t n, int64_
                 int64_t k, const void *B, int64_t ldb, int opB, void *C, int64_t ldc,
                 const void *alpha, const void *beta);
 
+/* C += A for a dense m x n column-major C (leading dimension ldc): the kernel of `A + B`
+ * with a dense B (src/core.jl:66-88 -- C = copy(B), then _add_sparse_to_dense!, kernels
+ * kernel_add_sparse_to_dense_{csr,csc,coo}!, e.g. src/matrix_csr/matrix_csr_kernels.jl:133-145).
+ * format: 0 CSR (p0 rowptr, p1 colval), 1 CSC (colptr, rowval), 2 COO (rowind, colind).
+ * Duplicate entries add up; entries outside the matrix are skipped. */
+int gsa_add_to_dense(void *stream, int format, int dtype, int itype, int64_t m, int64_t n, int64_t nnz,
+                     const void *p0, const void *p1, const void *nzval, int base, void *C, int64_t ldc);
+
+/* dropzeros (src/matrix_csr/matrix_csr.jl:649-745, kernels kernel_count_nonzeros_csr! /
+ * kernel_dropzeros_csr! at src/matrix_csr/matrix_csr_kernels.jl:409-443, and the CSC / COO
+ * methods): the stored entries that are not zero, in storage order.  Two calls on ONE
+ * workspace of gsa_dropzeros_workspace_size(nnz) bytes: _count finds the kept entries'
+ * positions and returns their count on the host (synchronizes the stream); the caller
+ * allocates the outputs; _copy writes them -- for CSR/CSC p0_out is the new pointer array
+ * (outer_n + 1, same base) and p1_out/val_out the kept indices and values, for COO
+ * p0_out/p1_out/val_out the kept (rowind, colind, nzval).  At most 2^32 - 2 entries. */
+size_t gsa_dropzeros_workspace_size(int64_t nnz);
+int gsa_dropzeros_count(void *stream, int dtype, int64_t nnz, const void *nzval, void *workspace,
+                        size_t workspace_bytes, int64_t *kept);
+int gsa_dropzeros_copy(void *stream, int format, int dtype, int itype, int64_t outer_n, int64_t nnz,
+                       const void *p0, const void *p1, const void *nzval, int base, const void *workspace,
+                       void *p0_out, void *p1_out, void *val_out);
+
 /* y = beta*y + alpha*A*x for a CSR matrix and vectors x (n) and y (m), like
  * gsa_csr_mul with opA = opB = N and k = 1, but allocating nothing: no
  * cudaMalloc, no stream-ordered pool, no workspace argument.  No counterpart in

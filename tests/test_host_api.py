@@ -158,3 +158,13 @@ def test_dot_checks_match_reference_order(gsa):
         gsa.dot(x, gsa.transpose(A), y)  # op(A) is 5 x 6
     with pytest.raises(gsa.ArgumentError, match="GPU only"):
         gsa.dot(x, A, y)
+
+
+def test_add_checks_match_reference_order(gsa):
+    """A + B with a dense B (src/core.jl:66-88): DimensionMismatch on sizes, then the backend
+    ArgumentError; the GPU-only check last."""
+    A, S = small_csr(gsa)  # 6 x 5 on the host
+    with pytest.raises(gsa.DimensionMismatch, match=r"dimensions must match: A has dims \(6, 5\), B has dims \(5, 5\)"):
+        gsa.add(A, torch.zeros(5, 5, dtype=torch.float64))
+    with pytest.raises(gsa.ArgumentError, match="GPU only"):
+        gsa.add(A, torch.zeros(6, 5, dtype=torch.float64))
