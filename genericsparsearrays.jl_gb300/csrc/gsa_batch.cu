@@ -100,7 +100,7 @@ grouped_kernel(const gsa_group_item *__restrict__ items, int64_t count, int64_t 
     }
 }
 
-int default_columns(int dtype) { return dtype_size(dtype) >= 16 ? 2 : 4; }
+int default_columns(int dtype) { return dtype_size(dtype) == 8 ? 2 : 4; }  // column-major B
 
 struct GroupedBody {
     cudaStream_t s; const gsa_group_item *items; int64_t count, ntiles; int base, KC, g1;

@@ -74,19 +74,27 @@ radix_upsweep_kernel(const uint64_t *__restrict__ keys, int64_t n, int shift, ui
     for (int d = tid; d < RS_BINS; d += RS_THREADS) hist[(int64_t)d * num_tiles + blockIdx.x] = s_h[d];
 }
 
-// Stable scatter.  Warp w of a tile owns entries [w*32*ROUNDS, (w+1)*32*ROUNDS)
-// of the tile and ranks them round by round; per-warp digit counts then give
-// each (warp, digit) its offset inside the tile's slice of the digit bucket.
+// Stable scatter.  Warp w of a tile owns entries [w*32*ROUNDS, (w+1)*32*ROUNDS) of the
+// tile and ranks them round by round; per-warp digit counts give each entry its place in
+// the tile sorted by digit.  The tile is first written there, in shared memory, and then
+// copied out in that order: consecutive threads write consecutive addresses of one digit's
+// run, instead of every lane of a round writing to a different bucket.
 __global__ void __launch_bounds__(RS_THREADS)
 radix_downsweep_kernel(const uint64_t *__restrict__ keys_in, const uint32_t *__restrict__ perm_in,
                        uint64_t *__restrict__ keys_out, uint32_t *__restrict__ perm_out, int64_t n,
                        int shift, uint32_t mask, const uint32_t *__restrict__ offsets,
                        int64_t num_tiles) {
     __shared__ uint32_t s_wh[RS_WARPS][RS_BINS];
+    __shared__ uint32_t s_toff[RS_BINS];   // first position of each digit in the sorted tile
+    __shared__ uint32_t s_goff[RS_BINS];   // its first position in the output
+    __shared__ uint64_t s_key[RS_TILE];
+    __shared__ uint32_t s_perm[RS_TILE];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     for (int t = tid; t < RS_WARPS * RS_BINS; t += RS_THREADS) (&s_wh[0][0])[t] = 0;
     __syncthreads();
-    const int64_t w0 = (int64_t)blockIdx.x * RS_TILE + (int64_t)warp * 32 * RS_ROUNDS;
+    const int64_t tile0 = (int64_t)blockIdx.x * RS_TILE;
+    const int64_t w0 = tile0 + (int64_t)warp * 32 * RS_ROUNDS;
+    const int tile_n = (int)(n - tile0 < RS_TILE ? n - tile0 : RS_TILE);
     const unsigned lt = lanemask_lt();
     uint64_t key[RS_ROUNDS];
     uint32_t pv[RS_ROUNDS], rank[RS_ROUNDS], dig[RS_ROUNDS];
@@ -109,22 +117,57 @@ radix_downsweep_kernel(const uint64_t *__restrict__ keys_in, const uint32_t *__r
         __syncwarp();
     }
     __syncthreads();
-    for (int d = tid; d < RS_BINS; d += RS_THREADS) {
-        uint32_t run = offsets[(int64_t)d * num_tiles + blockIdx.x];
+    // per digit (a thread each, RS_THREADS == RS_BINS): the warps' starts inside the digit's
+    // run, the run's size; then an exclusive scan of the sizes gives the runs' tile offsets
+    static_assert(RS_THREADS == RS_BINS, "one thread per digit");
+    {
+        const int d = tid;
+        uint32_t run = 0;
         for (int w = 0; w < RS_WARPS; ++w) {
-            uint32_t c = s_wh[w][d];
+            const uint32_t c = s_wh[w][d];
             s_wh[w][d] = run;
             run += c;
+        }
+        s_toff[d] = run;  // the size for now
+        s_goff[d] = offsets[(int64_t)d * num_tiles + blockIdx.x];
+    }
+    __syncthreads();
+    if (warp == 0) {  // exclusive scan of the 256 run sizes by one warp, 8 per lane
+        uint32_t v[RS_BINS / 32], sum = 0;
+#pragma unroll
+        for (int q = 0; q < RS_BINS / 32; ++q) {
+            v[q] = s_toff[lane * (RS_BINS / 32) + q];
+            sum += v[q];
+        }
+        uint32_t incl = sum;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += y;
+        }
+        uint32_t run = incl - sum;
+#pragma unroll
+        for (int q = 0; q < RS_BINS / 32; ++q) {
+            s_toff[lane * (RS_BINS / 32) + q] = run;
+            run += v[q];
         }
     }
     __syncthreads();
 #pragma unroll
     for (int r = 0; r < RS_ROUNDS; ++r) {
         if (dig[r] < RS_BINS) {
-            uint32_t pos = s_wh[warp][dig[r]] + rank[r];
-            keys_out[pos] = key[r];
-            perm_out[pos] = pv[r];
+            const uint32_t lp = s_toff[dig[r]] + s_wh[warp][dig[r]] + rank[r];
+            s_key[lp] = key[r];
+            s_perm[lp] = pv[r];
         }
+    }
+    __syncthreads();
+    for (int i = tid; i < tile_n; i += RS_THREADS) {
+        const uint64_t k = s_key[i];
+        const uint32_t d = (uint32_t)(k >> shift) & mask;
+        const uint32_t pos = s_goff[d] + (uint32_t)i - s_toff[d];
+        keys_out[pos] = k;
+        perm_out[pos] = s_perm[i];
     }
 }
 

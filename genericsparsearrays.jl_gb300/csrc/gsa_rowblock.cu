@@ -152,10 +152,15 @@ int launch_rowblock(cudaStream_t s, const CompressedArgs<V, I> &a, int64_t k, De
     const int64_t nrb = ceil_div(a.outer_n, RB_THREADS);
     // columns a thread accumulates for SpMM: more columns share each entry load, fewer keep
     // registers (and so occupancy) low
-    // (by default 4; 2 for 16-byte values -- but 8 when B is row-major, where one entry's
-    // eight complex values share a 128-byte line)
+    // (measured defaults: with a column-major B each column is its own gather, and the
+    // FP64-bound 8-byte types do best with 2 columns, 16-byte ones with 4; with a row-major
+    // B an entry's values share cache lines, 4 columns for 8-byte and 8 for 16-byte values;
+    // 4-byte values take 4)
     int KC = get_spmm_columns();
-    if (KC == 0) KC = sizeof(V) >= 16 ? (B.cs == 1 && B.rs > 1 ? 8 : 2) : 4;
+    if (KC == 0) {
+        const bool rowmajor = B.cs == 1 && B.rs > 1;
+        KC = sizeof(V) >= 16 ? (rowmajor ? 8 : 4) : (sizeof(V) == 8 ? (rowmajor ? 4 : 2) : 4);
+    }
     if (k == 1) KC = 1;
     if (KC > k) KC = k <= 1 ? 1 : (k <= 2 ? 2 : (k <= 4 ? 4 : 8));
     const int64_t ncg = ceil_div(k, KC);

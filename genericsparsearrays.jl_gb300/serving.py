@@ -332,7 +332,7 @@ class GroupedExecutor:
                 else:
                     groups[(A.dtype, A.itype)].append((A, r.X, r.Y, r.alpha, r.beta))
             for (dt, _), prods in groups.items():
-                # ComplexF64 rows of a row-major X: eight columns per thread fill a line
+                # rows of a row-major X: 8 complex / 4 real values per thread share lines
                 cols = self.columns or (8 if dt == torch.complex128 else 4)
                 self.launchers[slot].launch(prods, s, columns=cols)
             ev = torch.cuda.Event(enable_timing=True)
