@@ -39,9 +39,9 @@ __global__ void rmul_or_fill_kernel(DenseOut<V> C, int64_t rows, int64_t k) {
 template <typename V>
 int launch_rmul_or_fill(cudaStream_t s, DenseOut<V> C, int64_t rows, int64_t k) {
     if (C.beta_mode == 1 || rows == 0 || k == 0) return GSA_OK;
-    if (C.beta_mode == 0)  // fill!(C, 0): all-zero bytes are +0 for every value type
-        return check_cuda(cudaMemset2DAsync(C.p, (size_t)C.ld * sizeof(V), 0, (size_t)rows * sizeof(V),
-                                            (size_t)k, s), "zero fill");
+    if (C.beta_mode == 0 && (k == 1 || C.ld == rows))  // fill!(C, 0) of one contiguous range:
+        return check_cuda(cudaMemsetAsync(C.p, 0, (size_t)rows * (size_t)k * sizeof(V), s),  // +0 bytes
+                          "zero fill");
     int64_t blocks = ceil_div(rows * k, 256);
     if (blocks > 152 * 32) blocks = 152 * 32;
     rmul_or_fill_kernel<V><<<(unsigned)blocks, 256, 0, s>>>(C, rows, k);
