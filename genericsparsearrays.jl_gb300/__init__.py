@@ -13,8 +13,10 @@ from .sparse import (
     GenericSparseMatrixCOO,
     GenericSparseMatrixCSC,
     GenericSparseMatrixCSR,
+    I,
     SparseMatrixCSC,
     Transpose,
+    UniformScaling,
     adapt,
     add,
     adjoint,
@@ -25,6 +27,7 @@ from .sparse import (
     mul_,
     nnz,
     size,
+    subtract,
     transpose,
     validate,
 )
@@ -36,5 +39,5 @@ __all__ = [
     "AbstractGenericSparseMatrix", "Adjoint", "ArgumentError", "DimensionMismatch",
     "GenericSparseMatrixCOO", "GenericSparseMatrixCSC", "GenericSparseMatrixCSR",
     "SparseMatrixCSC", "Transpose", "adapt", "adjoint", "collect", "mul", "mul_", "nnz", "size",
-    "transpose", "validate", "dot", "add", "dropzeros", "ALGO_AUTO", "ALGO_MERGE", "ALGO_VECTOR", "ALGO_PIPE",
+    "transpose", "validate", "dot", "add", "subtract", "dropzeros", "I", "UniformScaling", "ALGO_AUTO", "ALGO_MERGE", "ALGO_VECTOR", "ALGO_PIPE",
 ]

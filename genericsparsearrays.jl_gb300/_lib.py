@@ -19,6 +19,7 @@ F32, F64, C32, C64, I32, I64 = range(6)
 IDX32, IDX64 = 0, 1
 # op codes (gsa_op) and algorithms (gsa_algo)
 OP_N, OP_T, OP_C = 0, 1, 2
+SUM_NEGATE = 4
 ALGO_AUTO, ALGO_MERGE, ALGO_VECTOR, ALGO_PIPE = 0, 1, 2, 3
 TUNE_PIPE_THREADS, TUNE_SPMM_COLUMNS, TUNE_PLAN_ORDER = 1, 2, 3
 BATCH_GROUPED, BATCH_GRAPH, BATCH_PER_CALL = 0, 1, 2
@@ -57,6 +58,10 @@ SIGNATURES = {
     "gsa_dropzeros_workspace_size": ([_i64], _sz),
     "gsa_dropzeros_count": ([_vp, _i32, _i64, _vp, _vp, _sz, ctypes.POINTER(_i64)], _i32),
     "gsa_dropzeros_copy": ([_vp, _i32, _i32, _i32, _i64, _i64, _vp, _vp, _vp, _i32, _vp, _vp, _vp, _vp], _i32),
+    "gsa_coo_sum_workspace_size": ([_i32, _i64], _sz),
+    "gsa_coo_sum_count": ([_vp, _i32, _i32, _i64, _i64, _i64, _vp, _vp, _vp, _i32, _i64, _vp, _vp, _vp, _i32,
+                           _i64, _vp, _i32, _vp, _sz, ctypes.POINTER(_i64)], _i32),
+    "gsa_coo_sum_copy": ([_vp, _i32, _i32, _i64, _i64, _i64, _i32, _vp, _vp, _vp, _vp], _i32),
     "gsa_add_to_dense": ([_vp, _i32, _i32, _i32, _i64, _i64, _i64, _vp, _vp, _vp, _i32, _vp, _i64], _i32),
     "gsa_csr_spmv_noalloc": ([_vp, _i32, _i32, _i64, _i64, _i64, _vp, _vp, _vp, _i32, _vp, _vp,
                               _vp, _vp], _i32),

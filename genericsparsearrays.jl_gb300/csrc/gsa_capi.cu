@@ -478,6 +478,19 @@ struct DropCopyBody {
                                            base, ws, (I *)o0, (I *)o1, (V *)ov);
     }
 };
+struct SumCountBody {
+    cudaStream_t s; int64_t m, n; SumSources src; const void *lambda; int base; void *ws; size_t ws_bytes;
+    int64_t *kept;
+    template <typename V, typename I> int operator()() {
+        return launch_coo_sum_count<V, I>(s, m, n, src, (const V *)lambda, base, ws, ws_bytes, kept);
+    }
+};
+struct SumCopyBody {
+    cudaStream_t s; int64_t m, n, total; int base; const void *ws; void *ro, *co, *vo;
+    template <typename V, typename I> int operator()() {
+        return launch_coo_sum_copy<V, I>(s, m, n, total, base, ws, (I *)ro, (I *)co, (V *)vo);
+    }
+};
 struct AddBody {
     cudaStream_t s; int fmt; int64_t m, n, nnz; const void *p0, *p1, *val; int base; void *C; int64_t ldc;
     template <typename V, typename I> int operator()() {
@@ -516,6 +529,57 @@ int gsa_dropzeros_copy(void *stream, int format, int dtype, int itype, int64_t o
         return fail(GSA_ERR_INVALID_ARG, "arrays must be aligned to their element size");
     DropCopyBody body{(cudaStream_t)stream, format, outer_n, nnz, p0, p1, nzval, base, workspace, p0_out, p1_out,
                       val_out};
+    return dispatch_vi(dtype, itype, body);
+}
+
+size_t gsa_coo_sum_workspace_size(int dtype, int64_t total) {
+    const size_t vs = dtype_size(dtype);
+    return !vs || total < 0 ? 0 : coo_sum_workspace_size(vs, total);
+}
+
+int gsa_coo_sum_count(void *stream, int dtype, int itype, int64_t m, int64_t n, int64_t nnz_a,
+                      const void *rowind_a, const void *colind_a, const void *nzval_a, int op_a, int64_t nnz_b,
+                      const void *rowind_b, const void *colind_b, const void *nzval_b, int op_b, int64_t n_diag,
+                      const void *lambda, int base, void *workspace, size_t workspace_bytes, int64_t *kept) {
+    const size_t vs = dtype_size(dtype), is = itype_size(itype);
+    if (!vs || !is) return fail(GSA_ERR_UNSUPPORTED, "unsupported dtype %d / itype %d", dtype, itype);
+    if (m < 0 || n < 0 || nnz_a < 0 || nnz_b < 0 || n_diag < 0) return fail(GSA_ERR_INVALID_ARG, "negative size");
+    if (!kept || !workspace) return fail(GSA_ERR_INVALID_ARG, "bad arguments");
+    const int ops[2] = {op_a, op_b};
+    for (int w = 0; w < 2; ++w)
+        if ((ops[w] & ~GSA_SUM_NEGATE) < GSA_OP_N || (ops[w] & ~GSA_SUM_NEGATE) > GSA_OP_C)
+            return fail(GSA_ERR_INVALID_ARG, "op_%c must be GSA_OP_N, T or C, optionally | GSA_SUM_NEGATE",
+                        w ? 'b' : 'a');
+    if (n_diag > (m < n ? m : n)) return fail(GSA_ERR_DIM, "n_diag=%lld exceeds min(m, n)", (long long)n_diag);
+    if (n_diag > 0 && !lambda) return fail(GSA_ERR_INVALID_ARG, "lambda is NULL");
+    if ((nnz_a > 0 && (!rowind_a || !colind_a || !nzval_a)) || (nnz_b > 0 && (!rowind_b || !colind_b || !nzval_b)))
+        return fail(GSA_ERR_INVALID_ARG, "sparse arrays are NULL");
+    if (misaligned(rowind_a, is) || misaligned(colind_a, is) || misaligned(nzval_a, vs) || misaligned(rowind_b, is) ||
+        misaligned(colind_b, is) || misaligned(nzval_b, vs))
+        return fail(GSA_ERR_INVALID_ARG, "arrays must be aligned to their element size");
+    SumSources src{};
+    src.row[0] = rowind_a; src.col[0] = colind_a; src.val[0] = nzval_a; src.nnz[0] = nnz_a;
+    src.row[1] = rowind_b; src.col[1] = colind_b; src.val[1] = nzval_b; src.nnz[1] = nnz_b;
+    src.n_diag = n_diag;
+    for (int w = 0; w < 2; ++w) {
+        const int op = ops[w] & ~GSA_SUM_NEGATE;
+        src.trans[w] = op != GSA_OP_N;
+        src.conj[w] = op == GSA_OP_C;
+        src.neg[w] = (ops[w] & GSA_SUM_NEGATE) != 0;
+    }
+    SumCountBody body{(cudaStream_t)stream, m, n, src, lambda, base, workspace, workspace_bytes, kept};
+    return dispatch_vi(dtype, itype, body);
+}
+
+int gsa_coo_sum_copy(void *stream, int dtype, int itype, int64_t m, int64_t n, int64_t total, int base,
+                     const void *workspace, void *rowind_out, void *colind_out, void *nzval_out) {
+    const size_t vs = dtype_size(dtype), is = itype_size(itype);
+    if (!vs || !is) return fail(GSA_ERR_UNSUPPORTED, "unsupported dtype %d / itype %d", dtype, itype);
+    if (m < 0 || n < 0 || total < 0 || !workspace) return fail(GSA_ERR_INVALID_ARG, "bad arguments");
+    if (total > 0 && (!rowind_out || !colind_out || !nzval_out)) return fail(GSA_ERR_INVALID_ARG, "outputs are NULL");
+    if (misaligned(rowind_out, is) || misaligned(colind_out, is) || misaligned(nzval_out, vs))
+        return fail(GSA_ERR_INVALID_ARG, "arrays must be aligned to their element size");
+    SumCopyBody body{(cudaStream_t)stream, m, n, total, base, workspace, rowind_out, colind_out, nzval_out};
     return dispatch_vi(dtype, itype, body);
 }
 

@@ -18,6 +18,8 @@
 // CSR / CSC -> COO (src/conversions/conversion_kernels.jl:2-35): the major
 // index of every entry is written by merge-path tiles (balanced for any row
 // length mix); minor indices and values are plain copies.
+#include <type_traits>
+
 #include "gsa_internal.cuh"
 
 namespace gsa {
@@ -529,6 +531,206 @@ int coo_row_pointers(cudaStream_t s, int itype, int64_t m, int64_t nnz, const vo
     cudaFreeAsync(flag, s);
     return rc;
 }
+
+// ---------------------------------------------------------------------------
+// COO sums: A + B, A + λI and duplicate compaction (src/matrix_coo/matrix_coo.jl:300-385,
+// 387-458 and the transposed pairs at :460-575; kernels kernel_mark_unique_coo! and
+// kernel_compact_coo! at src/matrix_coo/matrix_coo_kernels.jl:257-311, followed there by
+// dropzeros).  The reference concatenates the sources, sorts column-major keys, marks run
+// starts, cumsums the marks, sums every run in its sorted order into a new COO and then
+// drops the zero sums with a second compaction.  Here the sources are read where they lie
+// (no concatenation): entry p < nnz_a is A's (indices swapped when A is transposed, value
+// conjugated when adjoint), then B's, then the n_diag diagonal entries of λI.  One stable
+// radix sort of 64-bit keys (col << row_bits | row); then one kernel sums each run where it
+// starts (left to right in sorted order, which is storage order within a source) and flags
+// the nonzero sums; one scan gives the positions and the count.  The copy phase writes the
+// flagged runs.  Zero sums never reach the output, so no second compaction is needed.
+
+template <typename I>
+__global__ void sum_keys_kernel(SumSources src, int64_t total, int base, int row_bits, uint64_t *__restrict__ keys,
+                                uint32_t *__restrict__ perm) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+        int64_t r, c;
+        if (i < src.nnz[0] + src.nnz[1]) {
+            const int w = i < src.nnz[0] ? 0 : 1;
+            const int64_t j = w ? i - src.nnz[0] : i;
+            const int64_t ri = (int64_t)ld_stream((const I *)src.row[w] + j) - base;
+            const int64_t ci = (int64_t)ld_stream((const I *)src.col[w] + j) - base;
+            r = src.trans[w] ? ci : ri;
+            c = src.trans[w] ? ri : ci;
+        } else {
+            r = c = i - src.nnz[0] - src.nnz[1];
+        }
+        keys[i] = row_bits >= 64 ? (uint64_t)r : (((uint64_t)c << row_bits) | (uint64_t)r);
+        perm[i] = (uint32_t)i;
+    }
+}
+
+template <typename V> __device__ __forceinline__ V negate_if(V a, bool c) {  // integers wrap, as in Julia
+    using U = typename std::make_unsigned<V>::type;
+    return c ? (V)(U(0) - (U)a) : a;
+}
+template <> __device__ __forceinline__ float negate_if(float a, bool c) { return flip_sign_if(a, c); }
+template <> __device__ __forceinline__ double negate_if(double a, bool c) { return flip_sign_if(a, c); }
+template <> __device__ __forceinline__ cf32 negate_if(cf32 a, bool c) {
+    return cf32{flip_sign_if(a.re, c), flip_sign_if(a.im, c)};
+}
+template <> __device__ __forceinline__ cf64 negate_if(cf64 a, bool c) {
+    return cf64{flip_sign_if(a.re, c), flip_sign_if(a.im, c)};
+}
+
+template <typename V>
+__device__ __forceinline__ V sum_source_value(const SumSources &src, uint32_t p, V lambda) {
+    if (p >= src.nnz[0] + src.nnz[1]) return lambda;
+    const int w = p < src.nnz[0] ? 0 : 1;
+    const V v = ldg((const V *)src.val[w] + (w ? p - src.nnz[0] : p));
+    return negate_if(conj_if(v, src.conj[w] != 0), src.neg[w] != 0);
+}
+
+// flags[i] = 1 where sorted entry i starts a run whose sum is nonzero; the sum goes to sums[i].
+template <typename V>
+__global__ void run_sum_kernel(SumSources src, int64_t total, const uint64_t *__restrict__ keys,
+                               const uint32_t *__restrict__ perm, V lambda, V *__restrict__ sums,
+                               uint32_t *__restrict__ flags) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i <= total; i += (int64_t)gridDim.x * blockDim.x) {
+        uint32_t f = 0;
+        if (i < total) {
+            const uint64_t k = keys[i];
+            if (i == 0 || keys[i - 1] != k) {
+                V acc = sum_source_value<V>(src, perm[i], lambda);
+                for (int64_t j = i + 1; j < total && keys[j] == k; ++j)
+                    acc = add(acc, sum_source_value<V>(src, perm[j], lambda));
+                sums[i] = acc;
+                f = is_zero(acc) ? 0u : 1u;
+            }
+        }
+        flags[i] = f;
+    }
+}
+
+template <typename V, typename I>
+__global__ void run_write_kernel(int64_t total, const uint64_t *__restrict__ keys, const uint32_t *__restrict__ pos,
+                                 const V *__restrict__ sums, int row_bits, int base, I *__restrict__ row_out,
+                                 I *__restrict__ col_out, V *__restrict__ val_out) {
+    const uint64_t mask = row_bits >= 64 ? ~0ull : ((1ull << row_bits) - 1);
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+        const uint32_t p = pos[i];
+        if (pos[i + 1] == p) continue;  // not a run start, or a zero sum
+        const uint64_t k = keys[i];
+        row_out[p] = (I)((int64_t)(k & mask) + base);
+        col_out[p] = (I)((int64_t)(row_bits >= 64 ? 0 : k >> row_bits) + base);
+        val_out[p] = sums[i];
+    }
+}
+
+struct SumLayout {
+    SortLayout sort;
+    size_t flags, pos, bsums, sums, bytes;
+};
+static SumLayout sum_layout(int64_t total, size_t vsize) {
+    SumLayout L;
+    L.sort = sort_layout(total);
+    Carver cv(nullptr);
+    cv.take<unsigned char>(L.sort.bytes);
+    L.flags = cv.off;
+    cv.take<uint32_t>(total + 1);
+    L.pos = cv.off;
+    cv.take<uint32_t>(total + 1);
+    L.bsums = cv.off;
+    cv.take<uint32_t>(ceil_div(total + 1, SC_TILE) + 1);
+    cv.off = align_up(cv.off, 16);
+    L.sums = cv.off;
+    cv.off += (size_t)total * vsize;
+    L.bytes = align_up(cv.off, 256);
+    return L;
+}
+
+size_t coo_sum_workspace_size(size_t vsize, int64_t total) { return total <= 0 ? 256 : sum_layout(total, vsize).bytes; }
+
+// The sorted keys live in the first or the second key buffer, by the parity of the pass count.
+static int sum_sort_passes(int64_t m, int64_t n) { return (bits_for(m) + bits_for(n) + RS_BITS - 1) / RS_BITS; }
+
+template <typename V, typename I>
+int launch_coo_sum_count(cudaStream_t s, int64_t m, int64_t n, const SumSources &src, const V *lambda, int base,
+                         void *ws, size_t ws_bytes, int64_t *kept) {
+    const int64_t total = src.nnz[0] + src.nnz[1] + src.n_diag;
+    if (total + 1 > 0xffffffffLL) return fail(GSA_ERR_UNSUPPORTED, "at most 2^32 - 2 entries in a sum");
+    const int row_bits = bits_for(m), col_bits = bits_for(n);
+    if (row_bits + col_bits > 64)
+        return fail(GSA_ERR_UNSUPPORTED, "matrix too large for 64-bit sort keys (%lld x %lld)", (long long)m,
+                    (long long)n);
+    if (ws_bytes < coo_sum_workspace_size(sizeof(V), total)) return fail(GSA_ERR_INVALID_ARG, "workspace too small");
+    if (total == 0) {
+        *kept = 0;
+        return GSA_OK;
+    }
+    const SumLayout L = sum_layout(total, sizeof(V));
+    char *w = (char *)ws;
+    Carver cv(ws);
+    uint64_t *ka = cv.take<uint64_t>(total), *kb = cv.take<uint64_t>(total);
+    uint32_t *pa = cv.take<uint32_t>(total), *pb = cv.take<uint32_t>(total);
+    uint32_t *hist = cv.take<uint32_t>(L.sort.hist_n);
+    uint32_t *bsums = cv.take<uint32_t>(ceil_div(L.sort.hist_n, SC_TILE) + 1);
+    uint32_t *flags = (uint32_t *)(w + L.flags), *pos = (uint32_t *)(w + L.pos);
+    uint32_t *bs2 = (uint32_t *)(w + L.bsums);
+    V *sums = (V *)(w + L.sums);
+    timer_before(s);
+    sum_keys_kernel<I><<<grid_for(total, 256), 256, 0, s>>>(src, total, base, row_bits, ka, pa);
+    int rc = check_cuda(cudaGetLastError(), "sum_keys_kernel");
+    const int total_bits = row_bits + col_bits;
+    for (int shift = 0; !rc && shift < total_bits; shift += RS_BITS) {
+        const int wb = total_bits - shift < RS_BITS ? total_bits - shift : RS_BITS;
+        const uint32_t mask = (1u << wb) - 1;
+        radix_upsweep_kernel<<<(unsigned)L.sort.num_tiles, RS_THREADS, 0, s>>>(ka, total, shift, mask, hist,
+                                                                               L.sort.num_tiles);
+        rc = exclusive_scan_u32(s, hist, hist, L.sort.hist_n, bsums);
+        if (rc) break;
+        radix_downsweep_kernel<<<(unsigned)L.sort.num_tiles, RS_THREADS, 0, s>>>(ka, pa, kb, pb, total, shift, mask,
+                                                                                 hist, L.sort.num_tiles);
+        rc = check_cuda(cudaGetLastError(), "radix pass");
+        uint64_t *tk = ka; ka = kb; kb = tk;
+        uint32_t *tp = pa; pa = pb; pb = tp;
+    }
+    if (!rc) {
+        const V lam = lambda ? *lambda : V{};
+        run_sum_kernel<V><<<grid_for(total + 1, 256), 256, 0, s>>>(src, total, ka, pa, lam, sums, flags);
+        rc = check_cuda(cudaGetLastError(), "run_sum_kernel");
+    }
+    if (!rc) rc = exclusive_scan_u32(s, flags, pos, total + 1, bs2);
+    timer_after(s);
+    uint32_t u = 0;
+    if (!rc) rc = check_cuda(cudaMemcpyAsync(&u, pos + total, sizeof(u), cudaMemcpyDeviceToHost, s), "coo sum: count");
+    if (!rc) rc = check_cuda(cudaStreamSynchronize(s), "coo sum: sync");
+    if (!rc) *kept = (int64_t)u;
+    return rc;
+}
+
+template <typename V, typename I>
+int launch_coo_sum_copy(cudaStream_t s, int64_t m, int64_t n, int64_t total, int base, const void *ws, I *row_out,
+                        I *col_out, V *val_out) {
+    if (total <= 0) return GSA_OK;
+    const SumLayout L = sum_layout(total, sizeof(V));
+    const char *w = (const char *)ws;
+    const bool second = sum_sort_passes(m, n) % 2 != 0;
+    const uint64_t *keys = (const uint64_t *)w + (second ? total : 0);
+    const uint32_t *pos = (const uint32_t *)(w + L.pos);
+    const V *sums = (const V *)(w + L.sums);
+    timer_before(s);
+    run_write_kernel<V, I><<<grid_for(total, 256), 256, 0, s>>>(total, keys, pos, sums, bits_for(m), base, row_out,
+                                                               col_out, val_out);
+    timer_after(s);
+    return check_cuda(cudaGetLastError(), "run_write_kernel");
+}
+
+#define GSA_INST_COOSUM(V, I)                                                                                  \
+    template int launch_coo_sum_count<V, I>(cudaStream_t, int64_t, int64_t, const SumSources &, const V *, int, \
+                                            void *, size_t, int64_t *);                                       \
+    template int launch_coo_sum_copy<V, I>(cudaStream_t, int64_t, int64_t, int64_t, int, const void *, I *, I *, \
+                                           V *);
+GSA_INST_COOSUM(float, int32_t) GSA_INST_COOSUM(float, int64_t) GSA_INST_COOSUM(double, int32_t)
+GSA_INST_COOSUM(double, int64_t) GSA_INST_COOSUM(cf32, int32_t) GSA_INST_COOSUM(cf32, int64_t)
+GSA_INST_COOSUM(cf64, int32_t) GSA_INST_COOSUM(cf64, int64_t) GSA_INST_COOSUM(int32_t, int32_t)
+GSA_INST_COOSUM(int32_t, int64_t) GSA_INST_COOSUM(int64_t, int32_t) GSA_INST_COOSUM(int64_t, int64_t)
 
 // ---------------------------------------------------------------------------
 // dropzeros (src/matrix_csr/matrix_csr.jl:649-745 with kernel_count_nonzeros_csr! /

@@ -476,6 +476,21 @@ template <typename V, typename I>
 int launch_dropzeros_copy(cudaStream_t s, int fmt, int64_t outer_n, int64_t nnz, const I *p0, const I *p1,
                           const V *val, int base, const void *ws, I *o0, I *o1, V *ov);
 
+// COO sums (A + B, A - B, A + λI): up to two COO sources, each optionally transposed (row
+// and column indices swapped), conjugated and negated, then n_diag diagonal entries of value λ.
+struct SumSources {
+    const void *row[2], *col[2], *val[2];
+    int64_t nnz[2], n_diag;
+    int trans[2], conj[2], neg[2];
+};
+size_t coo_sum_workspace_size(size_t vsize, int64_t total);
+template <typename V, typename I>
+int launch_coo_sum_count(cudaStream_t s, int64_t m, int64_t n, const SumSources &src, const V *lambda, int base,
+                         void *ws, size_t ws_bytes, int64_t *kept);
+template <typename V, typename I>
+int launch_coo_sum_copy(cudaStream_t s, int64_t m, int64_t n, int64_t total, int base, const void *ws, I *row_out,
+                        I *col_out, V *val_out);
+
 // C += A for a dense column-major C (fmt 0 CSR, 1 CSC, 2 COO).
 template <typename V, typename I>
 int launch_add_to_dense(cudaStream_t s, int fmt, int64_t m, int64_t n, int64_t nnz, const I *p0, const I *p1,

@@ -96,6 +96,18 @@ class AbstractGenericSparseMatrix:
     def __matmul__(self, B):
         return mul(self, B)
 
+    def __add__(self, B):
+        return add(self, B)
+
+    def __radd__(self, B):
+        return add(self, B)
+
+    def __sub__(self, B):
+        return subtract(self, B)
+
+    def __rsub__(self, B):
+        return subtract(B, self)
+
     @property
     def T(self):
         return transpose(self)
@@ -242,6 +254,18 @@ class Transpose:
 
     def __matmul__(self, B):
         return mul(self, B)
+
+    def __add__(self, B):
+        return add(self, B)
+
+    def __radd__(self, B):
+        return add(self, B)
+
+    def __sub__(self, B):
+        return subtract(self, B)
+
+    def __rsub__(self, B):
+        return subtract(B, self)
 
 
 class Adjoint(Transpose):
@@ -666,11 +690,139 @@ def dropzeros(A):
     return type(A)(A.m, A.n, o0, o1, ov)
 
 
-def add(A, B: torch.Tensor) -> torch.Tensor:
-    """``A + B`` for a sparse ``A`` and a dense matrix ``B`` (src/core.jl:66-88): a new dense
-    column-major ``C = copy(B)`` with every stored entry of ``A`` added (duplicates add up).
-    Same checks and messages as the reference: ``DimensionMismatch`` on sizes, then
-    ``ArgumentError`` on backends.  ``B + A == A + B``; ``A - B`` is ``add(A, -B)``."""
+class UniformScaling:
+    """``LinearAlgebra.UniformScaling``: ``λ * I`` of any square size."""
+
+    def __init__(self, lam=1):
+        self.lam = lam
+
+    def __mul__(self, c):
+        return UniformScaling(self.lam * c)
+
+    __rmul__ = __mul__
+
+    def __neg__(self):
+        return UniformScaling(-self.lam)
+
+    def __repr__(self):
+        return f"UniformScaling({self.lam})"
+
+
+I = UniformScaling(1)
+
+
+def _coo_operand(X):
+    """(parent COO, op code) of a COO matrix or its lazy Transpose / Adjoint, else None."""
+    if isinstance(X, GenericSparseMatrixCOO):
+        return X, _lib.OP_N
+    if isinstance(X, Transpose) and isinstance(X.parent, GenericSparseMatrixCOO):
+        conj = isinstance(X, Adjoint) and not _is_real(X.parent.dtype)
+        return X.parent, _lib.OP_C if conj else _lib.OP_T
+    return None
+
+
+def _coo_sum(m: int, n: int, a, op_a: int, b=None, op_b: int = _lib.OP_N, n_diag: int = 0, lam=0,
+             dtype=None):
+    """The COO sum of (up to) two COO parents and n_diag diagonal entries of lam, zero sums
+    dropped (gsa_coo_sum_count / _copy)."""
+    lib = _lib.load()
+    dev, it = a.device, a.itype
+    dtype = dtype or a.dtype
+    parts = []
+    for X in (a, b):
+        if X is None:
+            parts.append((None, None, None, 0))
+            continue
+        val = X.nzval if X.dtype == dtype else X.nzval.to(dtype)
+        r = X.rowind if X.itype == it else X.rowind.to(it)
+        c = X.colind if X.itype == it else X.colind.to(it)
+        parts.append((r, c, val, nnz(X)))
+    total = parts[0][3] + parts[1][3] + n_diag
+    ws = torch.empty(max(lib.gsa_coo_sum_workspace_size(_DTYPE[dtype], total), 1), dtype=torch.uint8, device=dev)
+    lam_buf = _scalar_buf(lam, dtype)
+    kept = ctypes.c_int64(0)
+    stream = _stream_ptr(dev)
+    (ra, ca, va, na), (rb, cb, vb, nb) = parts
+    with torch.cuda.device(dev):
+        _lib.check(lib.gsa_coo_sum_count(stream, _DTYPE[dtype], _ITYPE[it], m, n, na, _ptr(ra), _ptr(ca), _ptr(va),
+                                         op_a, nb, _ptr(rb), _ptr(cb), _ptr(vb), op_b, n_diag,
+                                         lam_buf.ctypes.data_as(ctypes.c_void_p), BASE,
+                                         _ptr(ws), ws.numel(), ctypes.byref(kept)))
+        k = kept.value
+        ro = torch.empty(k, dtype=it, device=dev)
+        co = torch.empty(k, dtype=it, device=dev)
+        vo = torch.empty(k, dtype=dtype, device=dev)
+        _lib.check(lib.gsa_coo_sum_copy(stream, _DTYPE[dtype], _ITYPE[it], m, n, total, BASE, _ptr(ws), _ptr(ro),
+                                        _ptr(co), _ptr(vo)))
+    return GenericSparseMatrixCOO(m, n, ro, co, vo)
+
+
+def _sparse_add(A, B, negate_b: bool):
+    """Sparse + sparse and sparse + λI (src/matrix_coo/matrix_coo.jl:300-575)."""
+    if isinstance(B, UniformScaling) or isinstance(A, UniformScaling):
+        if isinstance(A, UniformScaling):  # J + A, J - A
+            J, X, neg_x, neg_j = A, B, negate_b, False
+        else:
+            J, X, neg_x, neg_j = B, A, False, negate_b
+        op = _coo_operand(X)
+        if op is None:
+            raise ArgumentError("sparse + UniformScaling is provided for GenericSparseMatrixCOO")
+        P, code = op
+        m, n = X.shape
+        if m != n:
+            raise DimensionMismatch("Matrix must be square to add UniformScaling.")
+        lam = -J.lam if neg_j else J.lam
+        dtype = torch.result_type(P.nzval, lam)  # a Python scalar keeps A's precision
+        if lam == 0:  # iszero(λ) && return copy(A), A being -X for J - X
+            m_, n_, r, c, v = _coo_parts(P, code, dtype)
+            return GenericSparseMatrixCOO(m_, n_, r, c, -v if neg_x else v)
+        if P.device.type != "cuda":
+            raise ArgumentError("sparse addition runs on the GPU only; adapt the matrix to CUDA first")
+        return _coo_sum(m, n, P, code | (_lib.SUM_NEGATE if neg_x else 0), n_diag=n, lam=lam, dtype=dtype)
+    oa, ob = _coo_operand(A), _coo_operand(B)
+    if oa is None or ob is None:
+        raise ArgumentError("sparse + sparse is provided for GenericSparseMatrixCOO (and its transposes)")
+    if tuple(A.shape) != tuple(B.shape):
+        raise DimensionMismatch(f"dimensions must match: A has dims ({A.shape[0]}, {A.shape[1]}), B has dims "
+                                f"({B.shape[0]}, {B.shape[1]})")
+    (PA, ca), (PB, cb) = oa, ob
+    if PA.device != PB.device:
+        raise ArgumentError("Both matrices must have the same backend")
+    if PA.device.type != "cuda":
+        raise ArgumentError("sparse addition runs on the GPU only; adapt the matrices to CUDA first")
+    dtype = torch.promote_types(PA.dtype, PB.dtype)
+    m, n = A.shape
+    return _coo_sum(m, n, PA, ca, PB, cb | (_lib.SUM_NEGATE if negate_b else 0), dtype=dtype)
+
+
+def _coo_parts(P, code, dtype):
+    """copy(op(P)) as COO arrays (the reference's `iszero(λ) && return copy(A)`)."""
+    r, c = (P.colind, P.rowind) if code != _lib.OP_N else (P.rowind, P.colind)
+    v = P.nzval.to(dtype)
+    if code == _lib.OP_C:
+        v = v.conj().resolve_conj()
+    m, n = (P.n, P.m) if code != _lib.OP_N else (P.m, P.n)
+    return m, n, r, c, v
+
+
+def subtract(A, B):
+    """``A - B``: for COO matrices (and their transposes, and ``λ * I``) the sparse sum
+    ``A + (-B)`` with zeros dropped (src/matrix_coo/matrix_coo.jl:572-574); for a dense ``B``
+    the dense result ``A + (-B)``."""
+    if isinstance(B, torch.Tensor):
+        return add(A, -B)
+    return _sparse_add(A, B, True)
+
+
+def add(A, B):
+    """``A + B``.  With a dense matrix ``B`` (src/core.jl:66-88): a new dense column-major
+    ``C = copy(B)`` with every stored entry of ``A`` added (duplicates add up).  With COO
+    matrices (or their lazy transposes / adjoints) on both sides, or a ``UniformScaling`` on
+    one side (src/matrix_coo/matrix_coo.jl:300-575): a new COO holding the sum, column-major,
+    entries at equal positions summed in order, zero sums dropped.  Same checks and messages
+    as the reference: ``DimensionMismatch`` on sizes, then ``ArgumentError`` on backends."""
+    if not isinstance(B, torch.Tensor):
+        return _sparse_add(A, B, False)
     if not isinstance(A, AbstractGenericSparseMatrix):
         raise ArgumentError("A must be a GenericSparseMatrixCSR/CSC/COO")
     if not isinstance(B, torch.Tensor) or B.dim() != 2:

@@ -166,6 +166,31 @@ int gsa_dropzeros_copy(void *stream, int format, int dtype, int itype, int64_t o
                        const void *p0, const void *p1, const void *nzval, int base, const void *workspace,
                        void *p0_out, void *p1_out, void *val_out);
 
+/* Sums of COO matrices -- Base.:+ for GenericSparseMatrixCOO: A + B
+ * (src/matrix_coo/matrix_coo.jl:300-385), A + λI (:387-458) and the transposed / adjoint
+ * pairs and A - B (:460-575), kernels kernel_mark_unique_coo! / kernel_compact_coo!
+ * (src/matrix_coo/matrix_coo_kernels.jl:257-311) and the dropzeros that ends each of them.
+ * The result is m x n: the entries of source a (nnz_a entries), then of source b (nnz_b,
+ * may be 0), then n_diag diagonal entries (i, i), i = 1..n_diag, of value *lambda (the
+ * dtype's type, host memory; NULL allowed when n_diag = 0).  op_a / op_b: GSA_OP_N, T (row
+ * and column indices swapped) or C (swapped and conjugated), optionally OR'ed with
+ * GSA_SUM_NEGATE (values negated: A - B = A + (-B)).  Entries at the same (row, col) are
+ * summed left to right in that order; sums that are zero are dropped; the output is in
+ * column-major order (sorted by column, then row), as the reference's column-major keys
+ * give it.  Two calls on ONE workspace of gsa_coo_sum_workspace_size(dtype, nnz_a + nnz_b +
+ * n_diag) bytes: _count sorts and sums, returns the result's entry count on the host
+ * (synchronizes the stream); the caller allocates the outputs (kept entries each); _copy,
+ * given the same m, n, base and total = nnz_a + nnz_b + n_diag, writes them.  At most
+ * 2^32 - 2 entries in all. */
+#define GSA_SUM_NEGATE 4
+size_t gsa_coo_sum_workspace_size(int dtype, int64_t total);
+int gsa_coo_sum_count(void *stream, int dtype, int itype, int64_t m, int64_t n, int64_t nnz_a,
+                      const void *rowind_a, const void *colind_a, const void *nzval_a, int op_a, int64_t nnz_b,
+                      const void *rowind_b, const void *colind_b, const void *nzval_b, int op_b, int64_t n_diag,
+                      const void *lambda, int base, void *workspace, size_t workspace_bytes, int64_t *kept);
+int gsa_coo_sum_copy(void *stream, int dtype, int itype, int64_t m, int64_t n, int64_t total, int base,
+                     const void *workspace, void *rowind_out, void *colind_out, void *nzval_out);
+
 /* y = beta*y + alpha*A*x for a CSR matrix and vectors x (n) and y (m), like
  * gsa_csr_mul with opA = opB = N and k = 1, but allocating nothing: no
  * cudaMalloc, no stream-ordered pool, no workspace argument.  No counterpart in

@@ -90,6 +90,8 @@ static inline cf32 cf32_add(cf32 a, cf32 b) { cf32 r = {a.re + b.re, a.im + b.im
 static inline cf64 cf64_add(cf64 a, cf64 b) { cf64 r = {a.re + b.re, a.im + b.im}; return r; }
 static inline cf32 cf32_conj(cf32 a) { cf32 r = {a.re, -a.im}; return r; }
 static inline cf64 cf64_conj(cf64 a) { cf64 r = {a.re, -a.im}; return r; }
+static inline cf32 cf32_neg(cf32 a) { cf32 r = {-a.re, -a.im}; return r; }
+static inline cf64 cf64_neg(cf64 a) { cf64 r = {-a.re, -a.im}; return r; }
 static const cf32 cf32_zero = {0.0f, 0.0f};
 static const cf64 cf64_zero = {0.0, 0.0};
 
@@ -105,6 +107,7 @@ static const cf64 cf64_zero = {0.0, 0.0};
 #define V_ADD(a, b) ((a) + (b))
 #define V_MUL(a, b) ((a) * (b))
 #define V_CONJ(a) (a)
+#define V_NEG(a) (-(a))
 #define V_EQ_ONE(a) ((a) == 1.0f)
 #define V_IS_ZERO(a) ((a) == 0.0f)
 #define V_TO_C(a, r, i) do { (r) = (double)(a); (i) = 0.0; } while (0)
@@ -143,6 +146,7 @@ static const cf64 cf64_zero = {0.0, 0.0};
 #undef V_ADD
 #undef V_MUL
 #undef V_CONJ
+#undef V_NEG
 #undef V_EQ_ONE
 #undef V_IS_ZERO
 #undef V_TO_C
@@ -153,6 +157,7 @@ static const cf64 cf64_zero = {0.0, 0.0};
 #define V_ADD(a, b) cf32_add((a), (b))
 #define V_MUL(a, b) cf32_mul((a), (b))
 #define V_CONJ(a) cf32_conj(a)
+#define V_NEG(a) cf32_neg(a)
 #define V_EQ_ONE(a) ((a).re == 1.0f && (a).im == 0.0f)
 #define V_IS_ZERO(a) ((a).re == 0.0f && (a).im == 0.0f)
 #define V_TO_C(a, r, i) do { (r) = (double)(a).re; (i) = (double)(a).im; } while (0)
@@ -171,6 +176,7 @@ static const cf64 cf64_zero = {0.0, 0.0};
 #undef V_ADD
 #undef V_MUL
 #undef V_CONJ
+#undef V_NEG
 #undef V_EQ_ONE
 #undef V_IS_ZERO
 #undef V_TO_C
@@ -181,6 +187,7 @@ static const cf64 cf64_zero = {0.0, 0.0};
 #define V_ADD(a, b) cf64_add((a), (b))
 #define V_MUL(a, b) cf64_mul((a), (b))
 #define V_CONJ(a) cf64_conj(a)
+#define V_NEG(a) cf64_neg(a)
 #define V_EQ_ONE(a) ((a).re == 1.0 && (a).im == 0.0)
 #define V_IS_ZERO(a) ((a).re == 0.0 && (a).im == 0.0)
 #define V_TO_C(a, r, i) do { (r) = (a).re; (i) = (a).im; } while (0)
@@ -199,6 +206,7 @@ static const cf64 cf64_zero = {0.0, 0.0};
 #undef V_ADD
 #undef V_MUL
 #undef V_CONJ
+#undef V_NEG
 #undef V_EQ_ONE
 #undef V_IS_ZERO
 #undef V_TO_C
@@ -209,6 +217,7 @@ static const cf64 cf64_zero = {0.0, 0.0};
 #define V_ADD(a, b) I32_ADD(a, b)
 #define V_MUL(a, b) I32_MUL(a, b)
 #define V_CONJ(a) (a)
+#define V_NEG(a) ((int32_t)(0u - (uint32_t)(a)))
 #define V_EQ_ONE(a) ((a) == 1)
 #define V_IS_ZERO(a) ((a) == 0)
 #define V_TO_C(a, r, i) do { (r) = (double)(a); (i) = 0.0; } while (0)
@@ -232,6 +241,8 @@ static const cf64 cf64_zero = {0.0, 0.0};
 #define V_ZERO 0
 #define V_ADD(a, b) I64_ADD(a, b)
 #define V_MUL(a, b) I64_MUL(a, b)
+#undef V_NEG
+#define V_NEG(a) ((int64_t)(0ull - (uint64_t)(a)))
 #define I int32_t
 #define SUFFIX i64_i32
 #include "gsa_oracle_impl.h"
@@ -307,6 +318,15 @@ int oracle_compressed_to_coo(int colmajor, int dtype, int itype, int64_t m, int6
     if (dtype < 0 || dtype > 5 || itype < 0 || itype > 1) return 3;
     DISPATCH(compressed_to_coo, colmajor, m, n, nnz, ptr, idx, val, base, rowind_out,
              colind_out, val_out)
+}
+
+int oracle_coo_sum(int dtype, int itype, int64_t m, int64_t n, int64_t nnz_a, const void *ra, const void *ca,
+                   const void *va, int op_a, int64_t nnz_b, const void *rb, const void *cb, const void *vb,
+                   int op_b, int64_t n_diag, const void *lambda, int base, void *row_out, void *col_out,
+                   void *val_out, int64_t *kept) {
+    if (dtype < 0 || dtype > 5 || itype < 0 || itype > 1) return 3;
+    DISPATCH(coo_sum, m, n, nnz_a, ra, ca, va, op_a, nnz_b, rb, cb, vb, op_b, n_diag, lambda, base, row_out,
+             col_out, val_out, kept)
 }
 
 int oracle_max_threads(void) {

@@ -308,6 +308,73 @@ static int FN(coo_to_compressed)(int colmajor, int64_t m, int64_t n, int64_t nnz
     return 0;
 }
 
+/* Sums of COO matrices, following Base.:+ for GenericSparseMatrixCOO
+ * (src/matrix_coo/matrix_coo.jl:300-385 A + B, :387-458 A + lambda*I, :460-575 the
+ * transposed / adjoint pairs, A - B = A + (-B)): concatenate A's entries (indices swapped
+ * when transposed, values conjugated when adjoint, negated for a subtraction), B's, then
+ * the n_diag diagonal entries of lambda; keys col * m + row (kernel_make_csc_keys!,
+ * src/conversions/conversion_kernels.jl:38-46; unsigned 64-bit here); a stable sortperm;
+ * kernel_mark_unique_coo! and kernel_compact_coo! (src/matrix_coo/matrix_coo_kernels.jl:
+ * 257-311: each run summed left to right in sorted order); then dropzeros (the entries whose
+ * sum is zero removed, src/matrix_coo/matrix_coo.jl dropzeros).  ops: 0 N, 1 T, 2 C, | 4 to
+ * negate.  Outputs hold room for nnz_a + nnz_b + n_diag entries; *kept gets the count. */
+static int FN(coo_sum)(int64_t m, int64_t n, int64_t nnz_a, const void *ra, const void *ca, const void *va,
+                       int op_a, int64_t nnz_b, const void *rb, const void *cb, const void *vb, int op_b,
+                       int64_t n_diag, const void *lambdav, int base, void *row_outv, void *col_outv,
+                       void *val_outv, int64_t *kept) {
+    (void)n;
+    const int64_t total = nnz_a + nnz_b + n_diag;
+    I *row_out = (I *)row_outv, *col_out = (I *)col_outv;
+    V *val_out = (V *)val_outv;
+    *kept = 0;
+    if (total == 0) return 0;
+    int64_t *rc = (int64_t *)malloc((size_t)total * 2 * sizeof(int64_t));
+    V *vc = (V *)malloc((size_t)total * sizeof(V));
+    uint64_t *keys = (uint64_t *)malloc((size_t)total * sizeof(uint64_t));
+    int64_t *perm = (int64_t *)malloc((size_t)total * sizeof(int64_t));
+    int64_t *tmp = (int64_t *)malloc((size_t)total * sizeof(int64_t));
+    if (!rc || !vc || !keys || !perm || !tmp) { free(rc); free(vc); free(keys); free(perm); free(tmp); return 2; }
+    int64_t e = 0;
+    for (int w = 0; w < 2; ++w) {
+        const int64_t cnt = w ? nnz_b : nnz_a;
+        const I *r = (const I *)(w ? rb : ra), *c = (const I *)(w ? cb : ca);
+        const V *v = (const V *)(w ? vb : va);
+        const int op = (w ? op_b : op_a) & 3, neg = ((w ? op_b : op_a) & 4) != 0;
+        for (int64_t i = 0; i < cnt; ++i, ++e) {
+            const int64_t ri = (int64_t)r[i] - base, ci = (int64_t)c[i] - base;
+            rc[2 * e] = op ? ci : ri;
+            rc[2 * e + 1] = op ? ri : ci;
+            V x = op == 2 ? V_CONJ(v[i]) : v[i];
+            vc[e] = neg ? V_NEG(x) : x;
+        }
+    }
+    for (int64_t d = 0; d < n_diag; ++d, ++e) {
+        rc[2 * e] = rc[2 * e + 1] = d;
+        vc[e] = *(const V *)lambdav;
+    }
+    for (int64_t i = 0; i < total; ++i) {
+        keys[i] = (uint64_t)rc[2 * i + 1] * (uint64_t)m + (uint64_t)rc[2 * i];
+        perm[i] = i;
+    }
+    stable_sortperm(keys, perm, tmp, total);
+    int64_t out = 0;
+    for (int64_t i = 0; i < total;) {
+        V sum = vc[perm[i]];
+        int64_t j = i + 1;
+        while (j < total && keys[perm[j]] == keys[perm[i]]) sum = V_ADD(sum, vc[perm[j++]]);
+        if (!V_IS_ZERO(sum)) {
+            row_out[out] = (I)(rc[2 * perm[i]] + base);
+            col_out[out] = (I)(rc[2 * perm[i] + 1] + base);
+            val_out[out] = sum;
+            ++out;
+        }
+        i = j;
+    }
+    *kept = out;
+    free(rc); free(vc); free(keys); free(perm); free(tmp);
+    return 0;
+}
+
 /* Compressed -> COO expansion: kernel_csr_to_coo! / kernel_csc_to_coo!
  * (src/conversions/conversion_kernels.jl:2-35).  Every stored entry of outer
  * o gets major index o (in the index base); minor indices and values copy. */

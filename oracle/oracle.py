@@ -75,8 +75,10 @@ def lib():
                                                    i32, vp, vp, vp]
             L.oracle_dot.argtypes = [i32, i32, i32, i32, i64, i64, i64, vp, vp, vp, i32,
                                      vp, vp, vp, vp, vp, vp]
+            L.oracle_coo_sum.argtypes = [i32, i32, i64, i64, i64, vp, vp, vp, i32, i64, vp, vp, vp, i32,
+                                         i64, vp, i32, vp, vp, vp, ctypes.POINTER(i64)]
             for f in ("oracle_mul", "oracle_mul_exact", "oracle_coo_to_compressed",
-                      "oracle_compressed_to_coo", "oracle_max_threads", "oracle_dot"):
+                      "oracle_compressed_to_coo", "oracle_max_threads", "oracle_dot", "oracle_coo_sum"):
                 getattr(L, f).restype = ctypes.c_int
             _lib = L
     return _lib
@@ -227,6 +229,37 @@ def csr_to_coo(m, n, rowptr, colval, nzval, base=1):
 def csc_to_coo(m, n, colptr, rowval, nzval, base=1):
     """GenericSparseMatrixCOO(::GenericSparseMatrixCSC) -> (rowind, colind, nzval)."""
     return _to_coo(1, m, n, colptr, rowval, nzval, base)
+
+
+_OPS = {"N": 0, "T": 1, "C": 2}
+
+
+def coo_sum(m, n, a, op_a="N", b=None, op_b="N", neg_b=False, n_diag=0, lam=0, base=1, neg_a=False):
+    """Base.:+ of COO matrices (A + B, A - B with neg_b, -A + lam*I with neg_a, A + lam*I with n_diag = n), dropzeros
+    included: a and b are (rowind, colind, nzval) triplets of the stored (parent) matrices,
+    op_a / op_b "N", "T" or "C".  Returns the result's (rowind, colind, nzval), column-major."""
+    ra, ca, va = (np.ascontiguousarray(x) for x in a)
+    ca = ca.astype(ra.dtype, copy=False)
+    if b is None:
+        rb = cb = np.empty(0, dtype=ra.dtype)
+        vb = np.empty(0, dtype=va.dtype)
+    else:
+        rb, cb, vb = (np.ascontiguousarray(x) for x in b)
+        rb, cb = rb.astype(ra.dtype, copy=False), cb.astype(ra.dtype, copy=False)
+    vb = vb.astype(va.dtype, copy=False)
+    total = va.size + vb.size + n_diag
+    r = np.empty(max(total, 1), dtype=ra.dtype)
+    c = np.empty(max(total, 1), dtype=ra.dtype)
+    v = np.empty(max(total, 1), dtype=va.dtype)
+    lamv = np.array([lam], dtype=va.dtype)
+    kept = ctypes.c_int64(0)
+    rc = lib().oracle_coo_sum(DTYPE[va.dtype], ITYPE[ra.dtype], m, n, va.size, _p(ra), _p(ca), _p(va),
+                              _OPS[op_a] | (4 if neg_a else 0), vb.size, _p(rb), _p(cb), _p(vb), _OPS[op_b] | (4 if neg_b else 0),
+                              n_diag, _p(lamv), base, _p(r), _p(c), _p(v), ctypes.byref(kept))
+    if rc != 0:
+        raise RuntimeError(f"oracle_coo_sum failed: {rc}")
+    k = kept.value
+    return r[:k].copy(), c[:k].copy(), v[:k].copy()
 
 
 def max_rel_error(y, y_exact, scale):

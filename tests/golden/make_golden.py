@@ -88,6 +88,20 @@ def main():
     cases["empty_0x0"] = {"source": "test/shared/matrix_csr.jl:32", "m": 0, "n": 0,
                           "expected_csr": {"rowptr": [1], "colval": [], "nzval": []}}
 
+    # test/shared/matrix_coo.jl:388-395 -- A_overlap = sparse([1,2,3],[1,2,3],T[1,2,3],50,40),
+    # B_overlap = sparse([1,2,4],[1,2,4],T[4,5,6],50,40); A + B of their COO forms
+    Ao = sparse([1, 2, 3], [1, 2, 3], [1, 2, 3], 50, 40)
+    Bo = sparse([1, 2, 4], [1, 2, 4], [4, 5, 6], 50, 40)
+    cases["coo_add_overlap"] = {
+        "source": "test/shared/matrix_coo.jl:388-395", "m": 50, "n": 40, "a": coo_from_csc(Ao),
+        "b": coo_from_csc(Bo), "expected": coo_from_csc(Ao + Bo)}
+
+    # test/shared/matrix_coo.jl:276-281 -- A_nodiag = sparse([1,2],[2,1],T[1,2],3,3); A + I
+    An = sparse([1, 2], [2, 1], [1, 2], 3, 3)
+    cases["coo_add_identity_nodiag"] = {
+        "source": "test/shared/matrix_coo.jl:276-281", "m": 3, "n": 3, "a": coo_from_csc(An),
+        "lambda": 1.0, "expected": coo_from_csc(An + sp.identity(3))}
+
     with open(os.path.join(HERE, "known_answers.json"), "w") as f:
         json.dump(cases, f, indent=1, sort_keys=True)
         f.write("\n")

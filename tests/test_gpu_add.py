@@ -94,3 +94,115 @@ def test_dropzeros(gsa, oracle, cuda, fmt, dt, it):
     assert np.array_equal(D.nzval.cpu().numpy(), v[keep])
     Z = gsa.dropzeros(gsa.adapt(cuda, getattr(gsa, CLS[fmt])(m, n, p0, p1, np.zeros_like(v))))
     assert gsa.nnz(Z) == 0
+
+
+# ---------------------------------------------------------------------------
+# Sparse + sparse for COO (src/matrix_coo/matrix_coo.jl:300-575): the GPU result equals the
+# oracle's restatement entry for entry -- same column-major order, same sums (summed in the
+# same order, so the same bits), zero sums dropped.
+
+def _coo_tuple(X):
+    return (X.rowind.cpu().numpy(), X.colind.cpu().numpy(), X.nzval.cpu().numpy())
+
+
+def _assert_same(got, want):
+    for g, w in zip(got, want):
+        assert g.dtype == w.dtype and g.shape == w.shape
+        assert np.array_equal(g, w)
+
+
+def _shuffled_with_duplicates(rng, S, it, extra):
+    r, c, v = parts(S, "coo", it)
+    pick = rng.integers(0, v.size, extra)
+    r, c = np.concatenate([r, r[pick]]), np.concatenate([c, c[pick]])
+    v = np.concatenate([v, rand_values(rng, extra, v.dtype)])
+    p = rng.permutation(v.size)
+    return r[p], c[p], v[p]
+
+
+@pytest.mark.parametrize("op_a", ["N", "T", "C"])
+@pytest.mark.parametrize("op_b", ["N", "T", "C"])
+@pytest.mark.parametrize("it", INDEX_TYPES)
+@pytest.mark.parametrize("dt", VALUE_TYPES)
+def test_coo_plus_coo(gsa, cuda, oracle, op_a, op_b, it, dt):
+    rng = np.random.default_rng(21)
+    m = n = 70
+    a = _shuffled_with_duplicates(rng, sprand(rng, m, n, 0.1, dt), it, 60)
+    b = _shuffled_with_duplicates(rng, sprand(rng, m, n, 0.15, dt), it, 60)
+    A = gsa.adapt(cuda, gsa.GenericSparseMatrixCOO(m, n, *a))
+    B = gsa.adapt(cuda, gsa.GenericSparseMatrixCOO(m, n, *b))
+    wrap = {"N": lambda X: X, "T": gsa.transpose, "C": gsa.adjoint}
+    C = wrap[op_a](A) + wrap[op_b](B)
+    assert isinstance(C, gsa.GenericSparseMatrixCOO) and C.shape == (m, n)
+    _assert_same(_coo_tuple(C), oracle.coo_sum(m, n, a, op_a=op_a, b=b, op_b=op_b))
+    D = wrap[op_a](A) - wrap[op_b](B)
+    _assert_same(_coo_tuple(D), oracle.coo_sum(m, n, a, op_a=op_a, b=b, op_b=op_b, neg_b=True))
+    # test/shared/matrix_coo.jl:383-386: op(A) - op(A) stores nothing (A without duplicates:
+    # with them, a1 + a2 - a1 - a2 need not round to zero)
+    U = gsa.adapt(cuda, gsa.GenericSparseMatrixCOO(m, n, *parts(sprand(rng, m, n, 0.1, dt), "coo", it)))
+    assert gsa.nnz(wrap[op_a](U) - wrap[op_a](U)) == 0
+
+
+@pytest.mark.parametrize("it", INDEX_TYPES)
+def test_coo_plus_coo_rectangular_known_answer(gsa, cuda, it):
+    """test/shared/matrix_coo.jl:388-395 on the GPU."""
+    import json, os
+    g = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "known_answers.json")))["coo_add_overlap"]
+    mk = lambda d: gsa.adapt(cuda, gsa.GenericSparseMatrixCOO(g["m"], g["n"], np.array(d["rowind"], it),
+                                                             np.array(d["colind"], it), np.array(d["nzval"])))
+    C = mk(g["a"]) + mk(g["b"])
+    r, c, v = _coo_tuple(C)
+    assert (r.tolist(), c.tolist(), v.tolist()) == (g["expected"]["rowind"], g["expected"]["colind"],
+                                                    g["expected"]["nzval"])
+
+
+@pytest.mark.parametrize("dt", VALUE_TYPES)
+def test_coo_plus_uniform_scaling(gsa, cuda, oracle, dt):
+    rng = np.random.default_rng(22)
+    n = 50
+    a = _shuffled_with_duplicates(rng, sprand(rng, n, n, 0.2, dt), np.int64, 20)
+    A = gsa.adapt(cuda, gsa.GenericSparseMatrixCOO(n, n, *a))
+    lam = {np.dtype(np.complex64): 2 + 1j, np.dtype(np.complex128): 2 + 1j}.get(np.dtype(dt), 3)
+    _assert_same(_coo_tuple(A + gsa.I), oracle.coo_sum(n, n, a, n_diag=n, lam=1))
+    _assert_same(_coo_tuple(gsa.I + A), oracle.coo_sum(n, n, a, n_diag=n, lam=1))
+    _assert_same(_coo_tuple(A + lam * gsa.I), oracle.coo_sum(n, n, a, n_diag=n, lam=lam))
+    _assert_same(_coo_tuple(A - lam * gsa.I), oracle.coo_sum(n, n, a, n_diag=n, lam=-lam))
+    # J - A = J + (-A) = (-A) + J (src/core.jl:89,94): A's negated entries first, then the diagonal
+    _assert_same(_coo_tuple(lam * gsa.I - A), oracle.coo_sum(n, n, a, neg_a=True, n_diag=n, lam=lam))
+    Z = A + 0 * gsa.I  # iszero(λ): copy(A), duplicates kept
+    _assert_same(_coo_tuple(Z), a)
+
+
+def test_coo_plus_identity_known_answer(gsa, cuda):
+    """test/shared/matrix_coo.jl:276-281: A_nodiag + I."""
+    import json, os
+    g = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "known_answers.json")))
+    g = g["coo_add_identity_nodiag"]
+    A = gsa.adapt(cuda, gsa.GenericSparseMatrixCOO(3, 3, np.array(g["a"]["rowind"]), np.array(g["a"]["colind"]),
+                                                   np.array(g["a"]["nzval"])))
+    r, c, v = _coo_tuple(A + gsa.I)
+    assert (r.tolist(), c.tolist(), v.tolist()) == (g["expected"]["rowind"], g["expected"]["colind"],
+                                                    g["expected"]["nzval"])
+
+
+def test_coo_sum_large_with_long_runs(gsa, cuda, oracle):
+    """200k entries over few positions (runs of up to a few thousand) plus a power-law spread."""
+    rng = np.random.default_rng(23)
+    m, n = 3000, 5000
+    k = 200_000
+    r = np.where(rng.random(k) < 0.3, rng.integers(1, 4, k), rng.integers(1, m + 1, k)).astype(np.int32)
+    c = np.where(rng.random(k) < 0.3, rng.integers(1, 3, k), rng.integers(1, n + 1, k)).astype(np.int32)
+    v = rng.standard_normal(k)
+    A = gsa.adapt(cuda, gsa.GenericSparseMatrixCOO(m, n, r, c, v))
+    B = gsa.adapt(cuda, gsa.GenericSparseMatrixCOO(m, n, c[:1000] % m + 1, r[:1000], v[:1000]))
+    _assert_same(_coo_tuple(A + B), oracle.coo_sum(m, n, (r, c, v), b=(c[:1000] % m + 1, r[:1000], v[:1000])))
+
+
+def test_coo_sum_empty(gsa, cuda):
+    e = np.zeros(0, np.int64)
+    A = gsa.adapt(cuda, gsa.GenericSparseMatrixCOO(4, 4, e, e, np.zeros(0)))
+    C = A + A
+    assert gsa.nnz(C) == 0 and C.shape == (4, 4)
+    D = A + gsa.I
+    r, c, v = _coo_tuple(D)
+    assert r.tolist() == [1, 2, 3, 4] and c.tolist() == [1, 2, 3, 4] and v.tolist() == [1.0] * 4

@@ -168,3 +168,30 @@ def test_add_checks_match_reference_order(gsa):
         gsa.add(A, torch.zeros(5, 5, dtype=torch.float64))
     with pytest.raises(gsa.ArgumentError, match="GPU only"):
         gsa.add(A, torch.zeros(6, 5, dtype=torch.float64))
+
+
+def test_sparse_add_checks_match_reference_order(gsa):
+    """COO + COO (src/matrix_coo/matrix_coo.jl:300-311): DimensionMismatch on sizes, then the
+    backend ArgumentError; A + J needs a square A (:389); operators map to add / subtract."""
+    e = np.zeros(0, np.int64)
+    A = gsa.GenericSparseMatrixCOO(6, 5, np.array([1, 2]), np.array([1, 5]), np.array([1.0, 2.0]))
+    B = gsa.GenericSparseMatrixCOO(5, 5, e, e, np.zeros(0))
+    with pytest.raises(gsa.DimensionMismatch, match=r"dimensions must match: A has dims \(6, 5\), B has dims \(5, 5\)"):
+        A + B
+    with pytest.raises(gsa.DimensionMismatch, match=r"A has dims \(5, 6\), B has dims \(5, 5\)"):
+        gsa.transpose(A) - B
+    with pytest.raises(gsa.DimensionMismatch, match="Matrix must be square to add UniformScaling."):
+        A + gsa.I
+    with pytest.raises(gsa.DimensionMismatch, match="square"):
+        2 * gsa.I - A
+    with pytest.raises(gsa.ArgumentError, match="GPU only"):
+        A + gsa.GenericSparseMatrixCOO(6, 5, e, e, np.zeros(0))
+    C = gsa.GenericSparseMatrixCSR(6, 5, np.ones(7, np.int64), e, np.zeros(0))
+    with pytest.raises(gsa.ArgumentError, match="GenericSparseMatrixCOO"):
+        C + C
+    # iszero(λ) returns a copy without touching the device: op(A) with the promoted type
+    Sq = gsa.GenericSparseMatrixCOO(3, 3, np.array([1, 1]), np.array([2, 2]), np.array([1.0, 0.0]))
+    Z = Sq + 0 * gsa.I
+    assert gsa.nnz(Z) == 2 and Z.nzval.tolist() == [1.0, 0.0]
+    Zn = 0 * gsa.I - Sq
+    assert Zn.nzval.tolist() == [-1.0, -0.0]
