@@ -58,10 +58,10 @@ SIGNATURES = {
     "gsa_dropzeros_workspace_size": ([_i64], _sz),
     "gsa_dropzeros_count": ([_vp, _i32, _i64, _vp, _vp, _sz, ctypes.POINTER(_i64)], _i32),
     "gsa_dropzeros_copy": ([_vp, _i32, _i32, _i32, _i64, _i64, _vp, _vp, _vp, _i32, _vp, _vp, _vp, _vp], _i32),
-    "gsa_coo_sum_workspace_size": ([_i32, _i64], _sz),
+    "gsa_coo_sum_workspace_size": ([_i32, _i64, _i64, _i64], _sz),
     "gsa_coo_sum_count": ([_vp, _i32, _i32, _i64, _i64, _i64, _vp, _vp, _vp, _i32, _i64, _vp, _vp, _vp, _i32,
                            _i64, _vp, _i32, _vp, _sz, ctypes.POINTER(_i64)], _i32),
-    "gsa_coo_sum_copy": ([_vp, _i32, _i32, _i64, _i64, _i64, _i32, _vp, _vp, _vp, _vp], _i32),
+    "gsa_coo_sum_copy": ([_vp, _i32, _i32, _i64, _i64, _i64, _i64, _i32, _vp, _vp, _vp, _vp], _i32),
     "gsa_add_to_dense": ([_vp, _i32, _i32, _i32, _i64, _i64, _i64, _vp, _vp, _vp, _i32, _vp, _i64], _i32),
     "gsa_csr_spmv_noalloc": ([_vp, _i32, _i32, _i64, _i64, _i64, _vp, _vp, _vp, _i32, _vp, _vp,
                               _vp, _vp], _i32),

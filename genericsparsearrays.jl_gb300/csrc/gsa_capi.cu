@@ -532,9 +532,9 @@ int gsa_dropzeros_copy(void *stream, int format, int dtype, int itype, int64_t o
     return dispatch_vi(dtype, itype, body);
 }
 
-size_t gsa_coo_sum_workspace_size(int dtype, int64_t total) {
+size_t gsa_coo_sum_workspace_size(int dtype, int64_t m, int64_t n, int64_t total) {
     const size_t vs = dtype_size(dtype);
-    return !vs || total < 0 ? 0 : coo_sum_workspace_size(vs, total);
+    return !vs || total < 0 || m < 0 || n < 0 ? 0 : coo_sum_workspace_size(vs, m, n, total);
 }
 
 int gsa_coo_sum_count(void *stream, int dtype, int itype, int64_t m, int64_t n, int64_t nnz_a,
@@ -571,12 +571,14 @@ int gsa_coo_sum_count(void *stream, int dtype, int itype, int64_t m, int64_t n, 
     return dispatch_vi(dtype, itype, body);
 }
 
-int gsa_coo_sum_copy(void *stream, int dtype, int itype, int64_t m, int64_t n, int64_t total, int base,
-                     const void *workspace, void *rowind_out, void *colind_out, void *nzval_out) {
+int gsa_coo_sum_copy(void *stream, int dtype, int itype, int64_t m, int64_t n, int64_t total, int64_t kept,
+                     int base, const void *workspace, void *rowind_out, void *colind_out, void *nzval_out) {
     const size_t vs = dtype_size(dtype), is = itype_size(itype);
     if (!vs || !is) return fail(GSA_ERR_UNSUPPORTED, "unsupported dtype %d / itype %d", dtype, itype);
-    if (m < 0 || n < 0 || total < 0 || !workspace) return fail(GSA_ERR_INVALID_ARG, "bad arguments");
-    if (total > 0 && (!rowind_out || !colind_out || !nzval_out)) return fail(GSA_ERR_INVALID_ARG, "outputs are NULL");
+    if (m < 0 || n < 0 || total < 0 || kept < 0 || kept > total || !workspace)
+        return fail(GSA_ERR_INVALID_ARG, "bad arguments");
+    if (kept == 0) return GSA_OK;
+    if (!rowind_out || !colind_out || !nzval_out) return fail(GSA_ERR_INVALID_ARG, "outputs are NULL");
     if (misaligned(rowind_out, is) || misaligned(colind_out, is) || misaligned(nzval_out, vs))
         return fail(GSA_ERR_INVALID_ARG, "arrays must be aligned to their element size");
     SumCopyBody body{(cudaStream_t)stream, m, n, total, base, workspace, rowind_out, colind_out, nzval_out};

@@ -4,16 +4,21 @@
 // reference builds key = major*minor_dim + minor in the index type (wrapping
 // for Int32 once major_dim*minor_dim >= 2^31), sortperms the keys with
 // AcceleratedKernels, gathers the three arrays and binary-searches every
-// major index.  Here:
+// major index.  Here the same order (by major, then minor, ties in input order)
+// comes from a bucket sort on the major index (gsa_bucket.cuh): a count per
+// major index, one scan -- which is the output's pointer array -- a placement of
+// (minor << 32 | position) keys into their buckets, and a sort of each bucket on
+// its own, whose emitter writes the minor index and gathers the value.  Matrices
+// whose sizes do not fit the bucket keys' 32-bit fields take the LSD radix sort:
 //   1. make_keys_kernel: key = (major << minor_bits) | minor as an unsigned
 //      64-bit word (no multiply, no wrap), payload = the entry's position
-//   2. LSD radix sort, 8-bit digits, only over the key bits that can be set;
-//      each pass = per-tile digit histograms, one exclusive scan, a stable
-//      scatter (warp match_any ranking in storage order)
+//   2. 8-bit digits, only over the key bits that can be set; each pass =
+//      per-tile digit histograms, one exclusive scan, a stable scatter (warp
+//      match_any ranking in storage order)
 //   3. finalize_kernel: minor index straight from the key, value gathered by
 //      the payload; pointer_kernel: pointer entries from the boundaries of the
 //      sorted major indices (every entry written exactly once)
-// LSD radix sort is stable, so duplicate (row, col) pairs keep input order.
+// Both sorts are stable, so duplicate (row, col) pairs keep input order.
 //
 // CSR / CSC -> COO (src/conversions/conversion_kernels.jl:2-35): the major
 // index of every entry is written by merge-path tiles (balanced for any row
@@ -21,6 +26,7 @@
 #include <type_traits>
 
 #include "gsa_internal.cuh"
+#include "gsa_bucket.cuh"
 
 namespace gsa {
 
@@ -312,12 +318,52 @@ static SortLayout sort_layout(int64_t nnz) {
     return L;
 }
 
+// The bucket sort applies when the major count, the minor indices and the entry count fit
+// its 32-bit fields; the radix sort covers the rest.
+static bool bucket_fits(int64_t major_n, int64_t minor_n, int64_t nnz) {
+    return major_n + 2 < 0xffffffffLL && minor_n <= 0x100000000LL && nnz < 0xffffffffLL;
+}
+
 template <typename V, typename I>
 size_t coo_to_compressed_workspace_size(int64_t m, int64_t n, int64_t nnz, bool colmajor) {
-    (void)m; (void)n; (void)colmajor;
     if (nnz == 0) return 0;
+    const int64_t major_n = colmajor ? n : m, minor_n = colmajor ? m : n;
+    if (bucket_fits(major_n, minor_n, nnz)) return bucket::layout(major_n, nnz, sizeof(V), SC_TILE).bytes;
     return sort_layout(nnz).bytes;
 }
+
+template <typename I>
+struct PairSource {
+    const I *mj, *mn;
+    int base;
+    __device__ __forceinline__ int64_t major(int64_t i) const { return (int64_t)__ldg(mj + i) - base; }
+    __device__ __forceinline__ void get(int64_t i, int64_t &a, int64_t &b) const {
+        a = (int64_t)__ldg(mj + i) - base;
+        b = (int64_t)__ldg(mn + i) - base;
+    }
+};
+
+// Conversion output: pointers from the row starts, minor index from the key, the value
+// carried with the key (or gathered by the key's input position).
+template <typename V, typename I>
+struct CompressedEmit {
+    I *ptr_out, *idx_out;
+    V *val_out;
+    const V *val_in;
+    int base;
+    int64_t major_n, nnz;
+    __device__ __forceinline__ void pointer(int64_t r, uint32_t first) const {
+        if (r < major_n) ptr_out[r] = (I)((int64_t)first + base);
+        else ptr_out[major_n] = (I)(nnz + base);
+    }
+    __device__ __forceinline__ void put(uint32_t p, uint64_t, uint64_t key, V v) const {
+        idx_out[p] = (I)((int64_t)(key >> 32) + base);
+        val_out[p] = v;
+    }
+    __device__ __forceinline__ void gather(uint32_t p, uint64_t r, uint64_t key) const {
+        put(p, r, key, ldg(val_in + (uint32_t)key));
+    }
+};
 
 static unsigned grid_for(int64_t n, int threads) {
     int64_t b = ceil_div(n, threads);
@@ -341,6 +387,16 @@ int launch_coo_to_compressed(cudaStream_t s, bool colmajor, int64_t m, int64_t n
     if (nnz == 0) {
         pointer_kernel<I><<<1, 256, 0, s>>>(0, nullptr, minor_bits, major_n, base, ptr_out);
         return check_cuda(cudaGetLastError(), "pointer_kernel");
+    }
+    if (bucket_fits(major_n, minor_n, nnz)) {
+        if (ws_bytes < bucket::layout(major_n, nnz, sizeof(V), SC_TILE).bytes)
+            return fail(GSA_ERR_INVALID_ARG, "conversion workspace too small");
+        PairSource<I> src{major, minor, base};
+        CompressedEmit<V, I> emit{ptr_out, idx_out, val_out, val, base, major_n, nnz};
+        timer_before(s);
+        int rc = bucket::sort(s, major_n, nnz, src, val, emit, ws, exclusive_scan_u32, SC_TILE);
+        timer_after(s);
+        return rc;
     }
     SortLayout L = sort_layout(nnz);
     if (ws_bytes < L.bytes) return fail(GSA_ERR_INVALID_ARG, "conversion workspace too small");
@@ -623,32 +679,79 @@ __global__ void run_write_kernel(int64_t total, const uint64_t *__restrict__ key
     }
 }
 
-struct SumLayout {
-    SortLayout sort;
-    size_t flags, pos, bsums, sums, bytes;
+// Column-major order: buckets are columns, the minor index is the row.
+template <typename I>
+struct SumSource {
+    SumSources s;
+    int base;
+    __device__ __forceinline__ void get(int64_t i, int64_t &col, int64_t &row) const {
+        if (i < s.nnz[0] + s.nnz[1]) {
+            const int w = i < s.nnz[0] ? 0 : 1;
+            const int64_t j = w ? i - s.nnz[0] : i;
+            const int64_t ri = (int64_t)__ldg((const I *)s.row[w] + j) - base;
+            const int64_t ci = (int64_t)__ldg((const I *)s.col[w] + j) - base;
+            row = s.trans[w] ? ci : ri;
+            col = s.trans[w] ? ri : ci;
+        } else {
+            row = col = i - s.nnz[0] - s.nnz[1];
+        }
+    }
+    __device__ __forceinline__ int64_t major(int64_t i) const {
+        int64_t c, r;
+        get(i, c, r);
+        return c;
+    }
 };
-static SumLayout sum_layout(int64_t total, size_t vsize) {
+
+// Sorted (col << 32 | row) keys and input positions, for the run kernels.
+struct KeyEmit {
+    uint64_t *keys;
+    uint32_t *perm;
+    __device__ __forceinline__ void pointer(int64_t, uint32_t) const {}
+    __device__ __forceinline__ void gather(uint32_t p, uint64_t col, uint64_t key) const {
+        keys[p] = (col << 32) | (key >> 32);
+        perm[p] = (uint32_t)key;
+    }
+};
+
+struct SumLayout {
+    bool bucket;
+    SortLayout sort;
+    size_t keys, perm, flags, pos, bsums, sums, bytes;
+};
+static SumLayout sum_layout(int64_t m, int64_t n, int64_t total, size_t vsize) {
     SumLayout L;
-    L.sort = sort_layout(total);
+    L.bucket = bucket_fits(n, m, total);
     Carver cv(nullptr);
-    cv.take<unsigned char>(L.sort.bytes);
-    L.flags = cv.off;
-    cv.take<uint32_t>(total + 1);
-    L.pos = cv.off;
-    cv.take<uint32_t>(total + 1);
-    L.bsums = cv.off;
-    cv.take<uint32_t>(ceil_div(total + 1, SC_TILE) + 1);
-    cv.off = align_up(cv.off, 16);
-    L.sums = cv.off;
-    cv.off += (size_t)total * vsize;
+    if (L.bucket) {
+        cv.reserve<unsigned char>(bucket::layout(n, total, 0, SC_TILE).bytes);
+        L.keys = cv.reserve<uint64_t>(total);
+        L.perm = cv.reserve<uint32_t>(total);
+    } else {
+        L.sort = sort_layout(total);
+        cv.take<unsigned char>(L.sort.bytes);
+        // the radix sort leaves its result in the first or second key buffer, by the parity
+        // of its pass count
+        const int passes = (bits_for(m) + bits_for(n) + RS_BITS - 1) / RS_BITS;
+        Carver sc(nullptr);  // the buffers in the order the sort takes them
+        sc.reserve<uint64_t>(total);
+        const size_t kb = sc.reserve<uint64_t>(total);
+        const size_t pa = sc.reserve<uint32_t>(total);
+        const size_t pb = sc.reserve<uint32_t>(total);
+        L.keys = passes % 2 ? kb : 0;
+        L.perm = passes % 2 ? pb : pa;
+    }
+    L.flags = cv.reserve<uint32_t>(total + 1);
+    L.pos = cv.reserve<uint32_t>(total + 1);
+    L.bsums = cv.reserve<uint32_t>(ceil_div(total + 1, SC_TILE) + 1);
+    L.sums = cv.reserve<unsigned char>((size_t)total * vsize);
     L.bytes = align_up(cv.off, 256);
     return L;
 }
 
-size_t coo_sum_workspace_size(size_t vsize, int64_t total) { return total <= 0 ? 256 : sum_layout(total, vsize).bytes; }
-
-// The sorted keys live in the first or the second key buffer, by the parity of the pass count.
-static int sum_sort_passes(int64_t m, int64_t n) { return (bits_for(m) + bits_for(n) + RS_BITS - 1) / RS_BITS; }
+size_t coo_sum_workspace_size(size_t vsize, int64_t m, int64_t n, int64_t total) {
+    return total <= 0 ? 256 : sum_layout(m, n, total, vsize).bytes;
+}
 
 template <typename V, typename I>
 int launch_coo_sum_count(cudaStream_t s, int64_t m, int64_t n, const SumSources &src, const V *lambda, int base,
@@ -659,41 +762,52 @@ int launch_coo_sum_count(cudaStream_t s, int64_t m, int64_t n, const SumSources 
     if (row_bits + col_bits > 64)
         return fail(GSA_ERR_UNSUPPORTED, "matrix too large for 64-bit sort keys (%lld x %lld)", (long long)m,
                     (long long)n);
-    if (ws_bytes < coo_sum_workspace_size(sizeof(V), total)) return fail(GSA_ERR_INVALID_ARG, "workspace too small");
+    if (ws_bytes < coo_sum_workspace_size(sizeof(V), m, n, total))
+        return fail(GSA_ERR_INVALID_ARG, "workspace too small");
     if (total == 0) {
         *kept = 0;
         return GSA_OK;
     }
-    const SumLayout L = sum_layout(total, sizeof(V));
+    const SumLayout L = sum_layout(m, n, total, sizeof(V));
     char *w = (char *)ws;
-    Carver cv(ws);
-    uint64_t *ka = cv.take<uint64_t>(total), *kb = cv.take<uint64_t>(total);
-    uint32_t *pa = cv.take<uint32_t>(total), *pb = cv.take<uint32_t>(total);
-    uint32_t *hist = cv.take<uint32_t>(L.sort.hist_n);
-    uint32_t *bsums = cv.take<uint32_t>(ceil_div(L.sort.hist_n, SC_TILE) + 1);
+    uint64_t *keys = (uint64_t *)(w + L.keys);
+    uint32_t *perm = (uint32_t *)(w + L.perm);
     uint32_t *flags = (uint32_t *)(w + L.flags), *pos = (uint32_t *)(w + L.pos);
     uint32_t *bs2 = (uint32_t *)(w + L.bsums);
     V *sums = (V *)(w + L.sums);
+    int rc = GSA_OK;
     timer_before(s);
-    sum_keys_kernel<I><<<grid_for(total, 256), 256, 0, s>>>(src, total, base, row_bits, ka, pa);
-    int rc = check_cuda(cudaGetLastError(), "sum_keys_kernel");
-    const int total_bits = row_bits + col_bits;
-    for (int shift = 0; !rc && shift < total_bits; shift += RS_BITS) {
-        const int wb = total_bits - shift < RS_BITS ? total_bits - shift : RS_BITS;
-        const uint32_t mask = (1u << wb) - 1;
-        radix_upsweep_kernel<<<(unsigned)L.sort.num_tiles, RS_THREADS, 0, s>>>(ka, total, shift, mask, hist,
-                                                                               L.sort.num_tiles);
-        rc = exclusive_scan_u32(s, hist, hist, L.sort.hist_n, bsums);
-        if (rc) break;
-        radix_downsweep_kernel<<<(unsigned)L.sort.num_tiles, RS_THREADS, 0, s>>>(ka, pa, kb, pb, total, shift, mask,
-                                                                                 hist, L.sort.num_tiles);
-        rc = check_cuda(cudaGetLastError(), "radix pass");
-        uint64_t *tk = ka; ka = kb; kb = tk;
-        uint32_t *tp = pa; pa = pb; pb = tp;
+    if (L.bucket) {
+        SumSource<I> bs{src, base};
+        rc = bucket::sort(s, n, total, bs, (const bucket::NoValue *)nullptr, KeyEmit{keys, perm}, ws,
+                          exclusive_scan_u32, SC_TILE);
+    } else {
+        Carver cv(ws);
+        uint64_t *ka = cv.take<uint64_t>(total), *kb = cv.take<uint64_t>(total);
+        uint32_t *pa = cv.take<uint32_t>(total), *pb = cv.take<uint32_t>(total);
+        uint32_t *hist = cv.take<uint32_t>(L.sort.hist_n);
+        uint32_t *bsums = cv.take<uint32_t>(ceil_div(L.sort.hist_n, SC_TILE) + 1);
+        sum_keys_kernel<I><<<grid_for(total, 256), 256, 0, s>>>(src, total, base, row_bits, ka, pa);
+        rc = check_cuda(cudaGetLastError(), "sum_keys_kernel");
+        const int total_bits = row_bits + col_bits;
+        for (int shift = 0; !rc && shift < total_bits; shift += RS_BITS) {
+            const int wb = total_bits - shift < RS_BITS ? total_bits - shift : RS_BITS;
+            const uint32_t mask = (1u << wb) - 1;
+            radix_upsweep_kernel<<<(unsigned)L.sort.num_tiles, RS_THREADS, 0, s>>>(ka, total, shift, mask, hist,
+                                                                                   L.sort.num_tiles);
+            rc = exclusive_scan_u32(s, hist, hist, L.sort.hist_n, bsums);
+            if (rc) break;
+            radix_downsweep_kernel<<<(unsigned)L.sort.num_tiles, RS_THREADS, 0, s>>>(ka, pa, kb, pb, total, shift,
+                                                                                     mask, hist, L.sort.num_tiles);
+            rc = check_cuda(cudaGetLastError(), "radix pass");
+            uint64_t *tk = ka; ka = kb; kb = tk;
+            uint32_t *tp = pa; pa = pb; pb = tp;
+        }
+        if (!rc && (ka != keys || pa != perm)) rc = fail(GSA_ERR_CUDA, "coo sum: sorted keys not where expected");
     }
     if (!rc) {
         const V lam = lambda ? *lambda : V{};
-        run_sum_kernel<V><<<grid_for(total + 1, 256), 256, 0, s>>>(src, total, ka, pa, lam, sums, flags);
+        run_sum_kernel<V><<<grid_for(total + 1, 256), 256, 0, s>>>(src, total, keys, perm, lam, sums, flags);
         rc = check_cuda(cudaGetLastError(), "run_sum_kernel");
     }
     if (!rc) rc = exclusive_scan_u32(s, flags, pos, total + 1, bs2);
@@ -709,15 +823,14 @@ template <typename V, typename I>
 int launch_coo_sum_copy(cudaStream_t s, int64_t m, int64_t n, int64_t total, int base, const void *ws, I *row_out,
                         I *col_out, V *val_out) {
     if (total <= 0) return GSA_OK;
-    const SumLayout L = sum_layout(total, sizeof(V));
+    const SumLayout L = sum_layout(m, n, total, sizeof(V));
     const char *w = (const char *)ws;
-    const bool second = sum_sort_passes(m, n) % 2 != 0;
-    const uint64_t *keys = (const uint64_t *)w + (second ? total : 0);
+    const uint64_t *keys = (const uint64_t *)(w + L.keys);
     const uint32_t *pos = (const uint32_t *)(w + L.pos);
     const V *sums = (const V *)(w + L.sums);
     timer_before(s);
-    run_write_kernel<V, I><<<grid_for(total, 256), 256, 0, s>>>(total, keys, pos, sums, bits_for(m), base, row_out,
-                                                               col_out, val_out);
+    run_write_kernel<V, I><<<grid_for(total, 256), 256, 0, s>>>(total, keys, pos, sums, L.bucket ? 32 : bits_for(m),
+                                                               base, row_out, col_out, val_out);
     timer_after(s);
     return check_cuda(cudaGetLastError(), "run_write_kernel");
 }

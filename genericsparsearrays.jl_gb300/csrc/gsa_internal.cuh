@@ -358,6 +358,13 @@ struct Carver {
         off += count * sizeof(T);
         return p;
     }
+    // the offset of the next region (256-byte aligned), for layouts that record offsets
+    template <typename T> size_t reserve(size_t count) {
+        off = align_up(off, 256);
+        const size_t at = off;
+        off += count * sizeof(T);
+        return at;
+    }
 };
 
 // Dispatch helpers: call F.template operator()<V, I>() for runtime codes.
@@ -483,7 +490,7 @@ struct SumSources {
     int64_t nnz[2], n_diag;
     int trans[2], conj[2], neg[2];
 };
-size_t coo_sum_workspace_size(size_t vsize, int64_t total);
+size_t coo_sum_workspace_size(size_t vsize, int64_t m, int64_t n, int64_t total);
 template <typename V, typename I>
 int launch_coo_sum_count(cudaStream_t s, int64_t m, int64_t n, const SumSources &src, const V *lambda, int base,
                          void *ws, size_t ws_bytes, int64_t *kept);

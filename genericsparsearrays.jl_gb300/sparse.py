@@ -738,7 +738,7 @@ def _coo_sum(m: int, n: int, a, op_a: int, b=None, op_b: int = _lib.OP_N, n_diag
         c = X.colind if X.itype == it else X.colind.to(it)
         parts.append((r, c, val, nnz(X)))
     total = parts[0][3] + parts[1][3] + n_diag
-    ws = torch.empty(max(lib.gsa_coo_sum_workspace_size(_DTYPE[dtype], total), 1), dtype=torch.uint8, device=dev)
+    ws = torch.empty(max(lib.gsa_coo_sum_workspace_size(_DTYPE[dtype], m, n, total), 1), dtype=torch.uint8, device=dev)
     lam_buf = _scalar_buf(lam, dtype)
     kept = ctypes.c_int64(0)
     stream = _stream_ptr(dev)
@@ -752,7 +752,7 @@ def _coo_sum(m: int, n: int, a, op_a: int, b=None, op_b: int = _lib.OP_N, n_diag
         ro = torch.empty(k, dtype=it, device=dev)
         co = torch.empty(k, dtype=it, device=dev)
         vo = torch.empty(k, dtype=dtype, device=dev)
-        _lib.check(lib.gsa_coo_sum_copy(stream, _DTYPE[dtype], _ITYPE[it], m, n, total, BASE, _ptr(ws), _ptr(ro),
+        _lib.check(lib.gsa_coo_sum_copy(stream, _DTYPE[dtype], _ITYPE[it], m, n, total, k, BASE, _ptr(ws), _ptr(ro),
                                         _ptr(co), _ptr(vo)))
     return GenericSparseMatrixCOO(m, n, ro, co, vo)
 

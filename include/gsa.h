@@ -177,19 +177,20 @@ int gsa_dropzeros_copy(void *stream, int format, int dtype, int itype, int64_t o
  * GSA_SUM_NEGATE (values negated: A - B = A + (-B)).  Entries at the same (row, col) are
  * summed left to right in that order; sums that are zero are dropped; the output is in
  * column-major order (sorted by column, then row), as the reference's column-major keys
- * give it.  Two calls on ONE workspace of gsa_coo_sum_workspace_size(dtype, nnz_a + nnz_b +
+ * give it.  Two calls on ONE workspace of gsa_coo_sum_workspace_size(dtype, m, n, nnz_a + nnz_b +
  * n_diag) bytes: _count sorts and sums, returns the result's entry count on the host
  * (synchronizes the stream); the caller allocates the outputs (kept entries each); _copy,
- * given the same m, n, base and total = nnz_a + nnz_b + n_diag, writes them.  At most
+ * given the same m, n, base, total = nnz_a + nnz_b + n_diag and the kept count, writes
+ * them (nothing, and NULL outputs allowed, when kept is 0).  At most
  * 2^32 - 2 entries in all. */
 #define GSA_SUM_NEGATE 4
-size_t gsa_coo_sum_workspace_size(int dtype, int64_t total);
+size_t gsa_coo_sum_workspace_size(int dtype, int64_t m, int64_t n, int64_t total);
 int gsa_coo_sum_count(void *stream, int dtype, int itype, int64_t m, int64_t n, int64_t nnz_a,
                       const void *rowind_a, const void *colind_a, const void *nzval_a, int op_a, int64_t nnz_b,
                       const void *rowind_b, const void *colind_b, const void *nzval_b, int op_b, int64_t n_diag,
                       const void *lambda, int base, void *workspace, size_t workspace_bytes, int64_t *kept);
-int gsa_coo_sum_copy(void *stream, int dtype, int itype, int64_t m, int64_t n, int64_t total, int base,
-                     const void *workspace, void *rowind_out, void *colind_out, void *nzval_out);
+int gsa_coo_sum_copy(void *stream, int dtype, int itype, int64_t m, int64_t n, int64_t total, int64_t kept,
+                     int base, const void *workspace, void *rowind_out, void *colind_out, void *nzval_out);
 
 /* y = beta*y + alpha*A*x for a CSR matrix and vectors x (n) and y (m), like
  * gsa_csr_mul with opA = opB = N and k = 1, but allocating nothing: no

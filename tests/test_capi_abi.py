@@ -75,8 +75,9 @@ def test_workspace_size_queries(lib):
     assert auto == 0 and v == 0 and g > 0 and p > 0 and s == 0 and sm > 0
     assert lib.gsa_mul_workspace_size(0, 1, 0, 1000, 1000, 5000, 0, 16, 1) > g
     assert lib.gsa_mul_workspace_size(0, 99, 0, 10, 10, 5, 0, 1, 0) == 0
+    # bucket sort: two 8-byte keys per entry, counters per row
     w = lib.gsa_coo_to_compressed_workspace_size(0, 1, 0, 1000, 1000, 5000)
-    assert w >= 5000 * 24
+    assert w >= 5000 * 16 + 1000 * 8
     assert lib.gsa_coo_to_compressed_workspace_size(0, 1, 0, 10, 10, 0) == 0
 
 

@@ -123,3 +123,35 @@ def test_power_law_rows_conversion(gsa, oracle, cuda):
     B = gsa.GenericSparseMatrixCSR(A)
     assert np.array_equal(np_(B.rowptr), rp) and np.array_equal(np_(B.colval), cv)
     assert np.array_equal(np_(B.nzval), nz)
+
+
+@pytest.mark.parametrize("it", INDEX_TYPES)
+def test_bucket_sizes_with_duplicates(gsa, oracle, cuda, it):
+    """Rows and columns of 0..16 (sorted by a thread), 17..256 (a warp), 257..4096 (a CTA in
+    shared memory) and beyond 4096 entries (CTA chunks merged pairwise), each with repeated
+    (row, col) pairs carrying different values, shuffled: CSR and CSC equal the oracle's bit
+    for bit, so ties keep their input order in every bucket size."""
+    rng = np.random.default_rng(41)
+    m, n = 600, 20_000
+    lengths = {3: 17, 10: 256, 11: 257, 40: 4096, 41: 4097, 77: 9000, 500: 16, 501: 1}
+    rows, cols = [], []
+    for r, L in lengths.items():
+        c = rng.integers(1, n + 1, L)
+        c[: L // 3] = c[0]  # a run of equal columns
+        rows.append(np.full(L, r + 1))
+        cols.append(c)
+    base_r = rng.integers(1, m + 1, 3000)
+    base_c = rng.integers(1, 50, 3000)  # few columns: long columns for CSC
+    r = np.concatenate(rows + [base_r]).astype(it)
+    c = np.concatenate(cols + [base_c]).astype(it)
+    v = rng.standard_normal(r.size)
+    p = rng.permutation(r.size)
+    r, c, v = r[p], c[p], v[p]
+    A = coo(gsa, cuda, m, n, r, c, v)
+    for cls, f in ((gsa.GenericSparseMatrixCSR, oracle.coo_to_csr), (gsa.GenericSparseMatrixCSC, oracle.coo_to_csc)):
+        B = cls(A)
+        ptr, idx = (B.rowptr, B.colval) if cls is gsa.GenericSparseMatrixCSR else (B.colptr, B.rowval)
+        e_ptr, e_idx, e_val = f(m, n, r, c, v)
+        assert np.array_equal(np_(ptr), e_ptr)
+        assert np.array_equal(np_(idx), e_idx)
+        assert np.array_equal(np_(B.nzval), e_val)
