@@ -62,6 +62,10 @@ SIGNATURES = {
     "gsa_coo_sum_count": ([_vp, _i32, _i32, _i64, _i64, _i64, _vp, _vp, _vp, _i32, _i64, _vp, _vp, _vp, _i32,
                            _i64, _vp, _i32, _vp, _sz, ctypes.POINTER(_i64)], _i32),
     "gsa_coo_sum_copy": ([_vp, _i32, _i32, _i64, _i64, _i64, _i64, _i32, _vp, _vp, _vp, _vp], _i32),
+    "gsa_spgemm_create": ([_vp, _i32, _i32, _i32, _i64, _i64, _i64, _vp, _vp, _vp, _i64, _vp, _vp, _vp, _i64, _i32,
+                           _vp, ctypes.POINTER(_i64), ctypes.POINTER(_vp)], _i32),
+    "gsa_spgemm_compute": ([_vp, _vp, _vp, _vp], _i32),
+    "gsa_spgemm_destroy": ([_vp], _i32),
     "gsa_add_to_dense": ([_vp, _i32, _i32, _i32, _i64, _i64, _i64, _vp, _vp, _vp, _i32, _vp, _i64], _i32),
     "gsa_csr_spmv_noalloc": ([_vp, _i32, _i32, _i64, _i64, _i64, _vp, _vp, _vp, _i32, _vp, _vp,
                               _vp, _vp], _i32),

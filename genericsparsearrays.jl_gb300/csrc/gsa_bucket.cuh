@@ -9,19 +9,21 @@
 // Two levels, so that no pass writes single entries to random addresses (a random 8-byte
 // store costs a whole DRAM sector, and more):
 //   A. coarse_count_kernel: entries per coarse bucket (2^cs consecutive rows, at most 4096
-//      rows and 4096 buckets), histograms in shared memory; one scan of the bucket counts.
+//      rows and 8192 buckets), histograms in shared memory; one scan of the bucket counts.
 //   B. coarse_place_kernel: a CTA takes a tile of 4096 entries, ranks them per coarse bucket
 //      in shared memory and reserves one contiguous run per bucket with one global atomic,
 //      so the tile's writes land in runs that L2 merges into whole sectors.  Keys, the row
 //      inside the bucket and the value (conversions) are moved together.
 //   C. fine_kernel: a CTA per coarse bucket counts its rows in shared memory, scans them --
 //      the row pointers of the result -- and places the bucket's entries in row order into
-//      a second buffer (a region of L2-resident size); then each thread sorts rows of up to
-//      16 entries in registers (rank counting) and emits them while the region is still in
-//      L2.  Longer rows are listed for warp_kernel (up to 256 entries, rank counting in
-//      shared memory) and cta_kernel (bitonic sort of 4096-entry chunks in shared memory,
-//      merged pairwise; values then gathered by input position).
-// Matrices with more than 4095 x 4096 rows take the one-level form (count, place, and
+//      shared memory (96 KB of staging; cs is chosen so that an average bucket fills at most
+//      half of it).  Rows of up to 16 entries are sorted there by a thread in registers (rank
+//      counting), rows of up to 256 by a warp, and emitted; longer rows go to cta_kernel
+//      (bitonic sort of 4096-entry chunks in shared memory, merged pairwise; values then
+//      gathered by input position).  A bucket larger than the staging is placed in global
+//      memory instead, with its rows of more than 16 entries listed for warp_kernel and
+//      cta_kernel.
+// Matrices with more than 8191 x 4096 rows take the one-level form (count, place, and
 // small_kernel per row), whose stores are random.
 //
 // A source gives, for entry i, its 0-based major index (`major(i)`) and both indices

@@ -274,6 +274,11 @@ static int exclusive_scan_u32(cudaStream_t s, const uint32_t *in, uint32_t *out,
     return check_cuda(cudaGetLastError(), "exclusive_scan_u32");
 }
 
+static_assert(SC_TILE == SCAN_TILE, "one scan tile size");
+int scan_u32(cudaStream_t s, const uint32_t *in, uint32_t *out, int64_t n, uint32_t *block_sums) {
+    return exclusive_scan_u32(s, in, out, n, block_sums);
+}
+
 template <typename V, typename I>
 __global__ void finalize_kernel(int64_t nnz, const uint64_t *__restrict__ keys,
                                 const uint32_t *__restrict__ perm, int minor_bits, int base,

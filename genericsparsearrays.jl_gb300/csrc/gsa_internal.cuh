@@ -312,6 +312,12 @@ void timer_after(cudaStream_t s);
 
 inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
 
+// Exclusive scan of n uint32 counts (in and out may be the same array); block_sums holds
+// scan_block_sums(n) entries of scratch.
+constexpr int SCAN_TILE = 4096;
+inline int64_t scan_block_sums(int64_t n) { return ceil_div(n, SCAN_TILE) + 1; }
+int scan_u32(cudaStream_t s, const uint32_t *in, uint32_t *out, int64_t n, uint32_t *block_sums);
+
 // Scratch of one call: the caller's buffer, or a stream-ordered allocation freed on the
 // same stream when the call returns.
 struct Workspace {

@@ -590,9 +590,72 @@ def mul_(C: torch.Tensor, A, B, alpha=1, beta=0, algo: int = _lib.ALGO_AUTO,
     return C
 
 
-def mul(A, B) -> torch.Tensor:
-    """``A * B`` for a sparse ``A`` (LinearAlgebra's generic ``*`` -> ``mul!``): a new
-    column-major result with ``β = 0``."""
+def _is_sparse_operand(X) -> bool:
+    return isinstance(X, AbstractGenericSparseMatrix) or (
+        isinstance(X, Transpose) and isinstance(X.parent, AbstractGenericSparseMatrix))
+
+
+def _spgemm(A, B):
+    """C = A * B for two unwrapped matrices of the same compressed format (gsa_spgemm_*)."""
+    csr = isinstance(A, GenericSparseMatrixCSR)
+    cls = type(A)
+    dtype = torch.promote_types(A.dtype, B.dtype)
+    it, dev = A.itype, A.device
+    pa, ia = (A.rowptr, A.colval) if csr else (A.colptr, A.rowval)
+    pb, ib = (B.rowptr, B.colval) if csr else (B.colptr, B.rowval)
+    pb, ib = pb.to(it), ib.to(it)
+    va, vb = A.nzval.to(dtype), B.nzval.to(dtype)
+    outer = A.m if csr else B.n
+    ptr = torch.empty(outer + 1, dtype=it, device=dev)
+    lib = _lib.load()
+    nnz_c = ctypes.c_int64(0)
+    handle = ctypes.c_void_p(0)
+    stream = _stream_ptr(dev)
+    with torch.cuda.device(dev):
+        _lib.check(lib.gsa_spgemm_create(stream, 0 if csr else 1, _DTYPE[dtype], _ITYPE[it], A.m, A.n, B.n, _ptr(pa),
+                                         _ptr(ia), _ptr(va), va.numel(), _ptr(pb), _ptr(ib), _ptr(vb), vb.numel(),
+                                         BASE, _ptr(ptr), ctypes.byref(nnz_c), ctypes.byref(handle)))
+        try:
+            idx = torch.empty(nnz_c.value, dtype=it, device=dev)
+            val = torch.empty(nnz_c.value, dtype=dtype, device=dev)
+            _lib.check(lib.gsa_spgemm_compute(stream, handle, _ptr(idx), _ptr(val)))
+        finally:
+            lib.gsa_spgemm_destroy(handle)
+    return cls(A.m, B.n, ptr, idx, val)
+
+
+def _sparse_mul(A, B):
+    """``A * B`` of two sparse matrices (src/matrix_csr/matrix_csr.jl:498-609 and the CSC and
+    COO methods): CSR * CSR and CSC * CSC directly; COO through CSC and back; with a
+    transpose or adjoint on either side, CSR operands are converted to CSC (CSC operands to
+    CSR) and the result converted back, as the reference does."""
+    if A.shape[1] != B.shape[0]:
+        raise DimensionMismatch(f"second dimension of A, {A.shape[1]}, does not match first dimension of B, "
+                                f"{B.shape[0]}")
+    PA = A.parent if isinstance(A, Transpose) else A
+    PB = B.parent if isinstance(B, Transpose) else B
+    if PA.device != PB.device:
+        raise ArgumentError("Both matrices must have the same backend")
+    if type(PA) is not type(PB):
+        raise ArgumentError(f"no method for {type(PA).__name__} * {type(PB).__name__}")
+    if PA.device.type != "cuda":
+        raise ArgumentError("sparse * sparse runs on the GPU only; adapt the matrices to CUDA first")
+    wrapped = isinstance(A, Transpose) or isinstance(B, Transpose)
+    if isinstance(PA, GenericSparseMatrixCOO):
+        return GenericSparseMatrixCOO(_spgemm(GenericSparseMatrixCSC(A), GenericSparseMatrixCSC(B)))
+    if not wrapped:
+        return _spgemm(A, B)
+    if isinstance(PA, GenericSparseMatrixCSR):
+        return GenericSparseMatrixCSR(_spgemm(GenericSparseMatrixCSC(A), GenericSparseMatrixCSC(B)))
+    return GenericSparseMatrixCSC(_spgemm(GenericSparseMatrixCSR(A), GenericSparseMatrixCSR(B)))
+
+
+def mul(A, B):
+    """``A * B`` for a sparse ``A``.  With a dense ``B`` (LinearAlgebra's generic ``*`` ->
+    ``mul!``): a new column-major result with ``β = 0``.  With a sparse ``B``: the sparse
+    product (SpGEMM)."""
+    if _is_sparse_operand(B):
+        return _sparse_mul(A, B)
     Ap, opA = _unwrap_sparse(A)
     Am = Ap.m if opA == _lib.OP_N else Ap.n
     _, _, _, Br, Bc = _dense_operand(B)

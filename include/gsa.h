@@ -192,6 +192,28 @@ int gsa_coo_sum_count(void *stream, int dtype, int itype, int64_t m, int64_t n, 
 int gsa_coo_sum_copy(void *stream, int dtype, int itype, int64_t m, int64_t n, int64_t total, int64_t kept,
                      int base, const void *workspace, void *rowind_out, void *colind_out, void *nzval_out);
 
+/* Sparse x sparse product C = A * B (SpGEMM) -- Base.:* for two GenericSparseMatrixCSR
+ * (src/matrix_csr/matrix_csr.jl:498-556, kernels kernel_count_nnz_spgemm_csr! /
+ * kernel_spgemm_csr! at src/matrix_csr/matrix_csr_kernels.jl:250-343) or two
+ * GenericSparseMatrixCSC (src/matrix_csc/matrix_csc.jl:500-560, kernels at
+ * src/matrix_csc/matrix_csc_kernels.jl:255-345).  A is m x k, B is k x n, both in `format`
+ * (0 CSR: ptr = rowptr, idx = colval; 1 CSC: ptr = colptr, idx = rowval) with the same
+ * dtype and itype.  C has the same format; every position that a product reaches is stored
+ * (zero sums included), indices increasing within each outer entry, and each entry is the
+ * sum from zero, in the reference's order, of Julia-rounded products (the reference's bits).
+ * _create runs the symbolic phase: it writes C's pointer array ptr_c (m + 1 for CSR, n + 1
+ * for CSC) and returns the entry count in *nnz_c (synchronizes the stream); the handle
+ * keeps device scratch and refers to A's and B's arrays, which must stay unchanged until
+ * _compute.  _compute writes idx_c / val_c (nnz_c each).  _destroy frees the handle.  At
+ * most 2^32 - 2 products (stored A entries times the lengths of the B rows they select). */
+typedef struct gsa_spgemm gsa_spgemm;
+int gsa_spgemm_create(void *stream, int format, int dtype, int itype, int64_t m, int64_t k, int64_t n,
+                      const void *ptr_a, const void *idx_a, const void *val_a, int64_t nnz_a, const void *ptr_b,
+                      const void *idx_b, const void *val_b, int64_t nnz_b, int base, void *ptr_c, int64_t *nnz_c,
+                      gsa_spgemm **handle);
+int gsa_spgemm_compute(void *stream, gsa_spgemm *handle, void *idx_c, void *val_c);
+int gsa_spgemm_destroy(gsa_spgemm *handle);
+
 /* y = beta*y + alpha*A*x for a CSR matrix and vectors x (n) and y (m), like
  * gsa_csr_mul with opA = opB = N and k = 1, but allocating nothing: no
  * cudaMalloc, no stream-ordered pool, no workspace argument.  No counterpart in

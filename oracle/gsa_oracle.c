@@ -329,6 +329,13 @@ int oracle_coo_sum(int dtype, int itype, int64_t m, int64_t n, int64_t nnz_a, co
              col_out, val_out, kept)
 }
 
+int oracle_spgemm(int fmt, int dtype, int itype, int64_t m, int64_t kk, int64_t n, const void *pa, const void *ia,
+                  const void *va, const void *pb, const void *ib, const void *vb, int base, void *ptr_out,
+                  void *idx_out, void *val_out, int64_t cap, int64_t *nnz_out) {
+    if (dtype < 0 || dtype > 5 || itype < 0 || itype > 1) return 3;
+    DISPATCH(spgemm, fmt, m, kk, n, pa, ia, va, pb, ib, vb, base, ptr_out, idx_out, val_out, cap, nnz_out)
+}
+
 int oracle_max_threads(void) {
 #ifdef _OPENMP
     return omp_get_max_threads();

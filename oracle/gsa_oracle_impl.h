@@ -375,6 +375,63 @@ static int FN(coo_sum)(int64_t m, int64_t n, int64_t nnz_a, const void *ra, cons
     return 0;
 }
 
+/* Sparse x sparse product, following kernel_count_nnz_spgemm_csr! / kernel_spgemm_csr!
+ * (src/matrix_csr/matrix_csr_kernels.jl:250-343, method src/matrix_csr/matrix_csr.jl:498-556)
+ * and kernel_count_nnz_spgemm_csc! / kernel_spgemm_csc! (src/matrix_csc/matrix_csc_kernels.jl:
+ * 255-345, method src/matrix_csc/matrix_csc.jl:500-560).  fmt 0 (CSR): for each row i of A,
+ * for each stored A[i,k] in storage order, for each stored B[k,j] in storage order,
+ * acc[j] += A[i,k] * B[k,j]; fmt 1 (CSC): for each column j of B, for each stored B[k,j],
+ * for each stored A[i,k], acc[i] += A[i,k] * B[k,j].  acc starts at zero; every position
+ * reached is stored (zero sums included), in increasing index order.  m x kk times kk x n.
+ * Outputs: ptr_out (outer + 1, index base), and when idx_out is not NULL the indices and
+ * values (room for `cap` entries); *nnz_out gets the entry count. */
+static int FN(spgemm)(int fmt, int64_t m, int64_t kk, int64_t n, const void *pav, const void *iav,
+                      const void *vav, const void *pbv, const void *ibv, const void *vbv, int base,
+                      void *ptr_outv, void *idx_outv, void *val_outv, int64_t cap, int64_t *nnz_out) {
+    (void)kk;
+    const I *pa = (const I *)pav, *ia = (const I *)iav, *pb = (const I *)pbv, *ib = (const I *)ibv;
+    const V *va = (const V *)vav, *vb = (const V *)vbv;
+    I *ptr_out = (I *)ptr_outv, *idx_out = (I *)idx_outv;
+    V *val_out = (V *)val_outv;
+    /* the outer loop runs over P's outer entries, the inner over Q's: CSR P = A, Q = B;
+     * CSC P = B, Q = A */
+    const int csr = fmt == 0;
+    const int64_t outer_n = csr ? m : n, width = csr ? n : m;
+    const I *pp = csr ? pa : pb, *pi = csr ? ia : ib, *qp = csr ? pb : pa, *qi = csr ? ib : ia;
+    const V *pv = csr ? va : vb, *qv = csr ? vb : va;
+    V *acc = (V *)malloc((size_t)(width > 0 ? width : 1) * sizeof(V));
+    unsigned char *seen = (unsigned char *)calloc((size_t)(width > 0 ? width : 1), 1);
+    if (!acc || !seen) { free(acc); free(seen); return 2; }
+    for (int64_t j = 0; j < width; ++j) acc[j] = V_ZERO;
+    int64_t out = 0;
+    for (int64_t o = 0; o < outer_n; ++o) {
+        ptr_out[o] = (I)(out + base);
+        for (int64_t e = (int64_t)pp[o] - base; e < (int64_t)pp[o + 1] - base; ++e) {
+            const int64_t k = (int64_t)pi[e] - base;
+            for (int64_t f = (int64_t)qp[k] - base; f < (int64_t)qp[k + 1] - base; ++f) {
+                const int64_t j = (int64_t)qi[f] - base;
+                const V prod = csr ? V_MUL(pv[e], qv[f]) : V_MUL(qv[f], pv[e]);
+                acc[j] = V_ADD(acc[j], prod);
+                seen[j] = 1;
+            }
+        }
+        for (int64_t j = 0; j < width; ++j) {
+            if (!seen[j]) continue;
+            if (idx_out && out < cap) {
+                idx_out[out] = (I)(j + base);
+                val_out[out] = acc[j];
+            }
+            ++out;
+            seen[j] = 0;
+            acc[j] = V_ZERO;
+        }
+    }
+    ptr_out[outer_n] = (I)(out + base);
+    *nnz_out = out;
+    free(acc); free(seen);
+    return 0;
+}
+
 /* Compressed -> COO expansion: kernel_csr_to_coo! / kernel_csc_to_coo!
  * (src/conversions/conversion_kernels.jl:2-35).  Every stored entry of outer
  * o gets major index o (in the index base); minor indices and values copy. */

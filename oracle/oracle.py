@@ -77,8 +77,10 @@ def lib():
                                      vp, vp, vp, vp, vp, vp]
             L.oracle_coo_sum.argtypes = [i32, i32, i64, i64, i64, vp, vp, vp, i32, i64, vp, vp, vp, i32,
                                          i64, vp, i32, vp, vp, vp, ctypes.POINTER(i64)]
-            for f in ("oracle_mul", "oracle_mul_exact", "oracle_coo_to_compressed",
-                      "oracle_compressed_to_coo", "oracle_max_threads", "oracle_dot", "oracle_coo_sum"):
+            L.oracle_spgemm.argtypes = [i32, i32, i32, i64, i64, i64, vp, vp, vp, vp, vp, vp, i32, vp, vp, vp, i64,
+                                        ctypes.POINTER(i64)]
+            for f in ("oracle_mul", "oracle_mul_exact", "oracle_coo_to_compressed", "oracle_compressed_to_coo",
+                      "oracle_max_threads", "oracle_dot", "oracle_coo_sum", "oracle_spgemm"):
                 getattr(L, f).restype = ctypes.c_int
             _lib = L
     return _lib
@@ -260,6 +262,30 @@ def coo_sum(m, n, a, op_a="N", b=None, op_b="N", neg_b=False, n_diag=0, lam=0, b
         raise RuntimeError(f"oracle_coo_sum failed: {rc}")
     k = kept.value
     return r[:k].copy(), c[:k].copy(), v[:k].copy()
+
+
+def spgemm(fmt, m, kk, n, a, b, base=1):
+    """A * B for CSR (fmt "csr": a, b = (rowptr, colval, nzval)) or CSC (fmt "csc": (colptr,
+    rowval, nzval)) operands of sizes m x kk and kk x n, restating the reference's kernels.
+    Returns the product's (ptr, idx, val); zero sums stay stored."""
+    pa, ia, va = (np.ascontiguousarray(x) for x in a)
+    pb, ib, vb = (np.ascontiguousarray(x) for x in b)
+    ia, pb, ib = ia.astype(pa.dtype, copy=False), pb.astype(pa.dtype, copy=False), ib.astype(pa.dtype, copy=False)
+    vb = vb.astype(va.dtype, copy=False)
+    f = 0 if fmt == "csr" else 1
+    outer = m if f == 0 else n
+    ptr = np.empty(outer + 1, dtype=pa.dtype)
+    cnt = ctypes.c_int64(0)
+    args = (f, DTYPE[va.dtype], ITYPE[pa.dtype], m, kk, n, _p(pa), _p(ia), _p(va), _p(pb), _p(ib), _p(vb), base)
+    rc = lib().oracle_spgemm(*args, _p(ptr), ctypes.c_void_p(0), ctypes.c_void_p(0), 0, ctypes.byref(cnt))
+    if rc != 0:
+        raise RuntimeError(f"oracle_spgemm failed: {rc}")
+    idx = np.empty(max(cnt.value, 1), dtype=pa.dtype)
+    val = np.empty(max(cnt.value, 1), dtype=va.dtype)
+    rc = lib().oracle_spgemm(*args, _p(ptr), _p(idx), _p(val), idx.size, ctypes.byref(cnt))
+    if rc != 0:
+        raise RuntimeError(f"oracle_spgemm failed: {rc}")
+    return ptr, idx[:cnt.value].copy(), val[:cnt.value].copy()
 
 
 def max_rel_error(y, y_exact, scale):

@@ -185,3 +185,24 @@ def test_coo_sum_matches_scipy(oracle, dt):
         sums[(ci, ri)] = sums.get((ci, ri), 0) + vi
     want = sorted((k, s) for k, s in sums.items() if s != 0)
     assert [(ci, ri) for ri, ci in zip(r.tolist(), c.tolist())] == [k for k, _ in want]
+
+
+@pytest.mark.parametrize("dt", VALUE_TYPES)
+@pytest.mark.parametrize("fmt", ["csr", "csc"])
+def test_spgemm_matches_scipy(oracle, dt, fmt):
+    """The SpGEMM restatement against scipy: scipy drops sums that cancel to zero and the
+    reference keeps every reached position, so values are compared densely and the oracle's
+    structure is checked to be a superset of scipy's, with zeros only where scipy has none."""
+    import scipy.sparse as sp
+    rng = np.random.default_rng(66)
+    SA, SB = sprand(rng, 40, 30, 0.12, dt), sprand(rng, 30, 45, 0.12, dt)
+    a, b = parts(SA, fmt, np.int64), parts(SB, fmt, np.int64)
+    ptr, idx, val = oracle.spgemm(fmt, 40, 30, 45, a, b)
+    M = (sp.csr_matrix if fmt == "csr" else sp.csc_matrix)((val, idx - 1, ptr - 1), shape=(40, 45))
+    want = (SA @ SB).toarray()
+    assert np.allclose(M.toarray(), want, rtol=tol(dt), atol=tol(dt) if not is_int(dt) else 0)
+    pattern = lambda S: sp.csr_matrix((np.ones(S.nnz), S.indices, S.indptr), shape=S.shape)
+    structure = (pattern(SA) @ pattern(SB)) != 0  # positions reached by a stored product
+    assert M.nnz == structure.nnz
+    for o in range(ptr.size - 1):  # indices increasing in every outer entry
+        assert np.all(np.diff(idx[ptr[o] - 1:ptr[o + 1] - 1]) > 0)
