@@ -450,8 +450,38 @@ def run_extras(gsa, wl, torch, dev, lib, timer, args):
     C = gsa.adapt(dev, gsa.GenericSparseMatrixCOO(m, n, r.astype(np.int64), c.astype(np.int64), v))
     bc = cv.size * (8 + 16) + cv.size * (8 + 8) + (m + 1) * 8
     t, tk = time_call(lambda: gsa.GenericSparseMatrixCSR(C))
-    out["laplacian_coo_to_csr_f64_i64"] = {"GBps": round(bc / t / 1e9, 1), "us": round(t * 1e6, 1)}
-    del C, A
+    out["laplacian_coo_to_csr_f64_i64"] = {"GBps": round(bc / t / 1e9, 1), "us": round(t * 1e6, 1),
+                                           "sort_GBps": round(bc / tk / 1e9, 1), "sort_us": round(tk * 1e6, 1)}
+
+    def wall(fn, reps=max(3, steps // 2)):
+        fn()
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(reps):
+            timer.flush()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            fn()
+            torch.cuda.synchronize()
+            ts.append(time.perf_counter() - t0)
+        return float(np.median(ts))
+
+    # COO sum A + transpose(A): 2 x 21M entries sorted column-major, runs summed, zeros dropped
+    t = wall(lambda: C + gsa.transpose(C))
+    out["laplacian_coo_plus_transpose_f64_i64"] = {
+        "us": round(t * 1e6, 1), "entries_per_s": round(2 * cv.size / t, 1),
+        "note": "wall time of A + transpose(A) through the API (count, allocation, copy)"}
+    del C
+    # SpGEMM A * A of the Laplacian: 25 products per interior row, all rows in shared memory
+    fl = int(np.diff(rp.astype(np.int64))[cv.astype(np.int64) - 1].sum())  # products of A * A
+    sq = A @ A
+    nnz_sq = gsa.nnz(sq)
+    del sq
+    t = wall(lambda: A @ A)
+    out["laplacian_spgemm_a_times_a_f64_i32"] = {
+        "us": round(t * 1e6, 1), "products": fl, "products_per_s": round(fl / t, 1), "nnz_c": nnz_sq,
+        "note": "wall time of A * A through the API (symbolic, allocation, numeric)"}
+    del A
     # power-law ComplexF64 CSR and COO
     m, n, rp, cv, nz = wl.power_law(1_000_000, seed=0, itype=np.int64, dtype=np.complex128)
     A = gsa.adapt(dev, gsa.GenericSparseMatrixCSR(m, n, rp, cv, nz))

@@ -8,6 +8,8 @@ Cases (the bench workloads, same seeds):
   laplacian_spmm16        the same matrix times a 16-column column-major X
   laplacian_csc_f64_i32   CSC SpMV of the Laplacian (outer-block scatter)
   laplacian_coo_to_csr    COO -> CSR of the Laplacian's randomly permuted triplets
+  laplacian_coo_plus_t    the same triplets as a COO, A + transpose(A) (COO sum)
+  laplacian_spgemm        A * A of the Laplacian (Float64 / Int32 CSR)
   powerlaw_csr_c64        n = 1e6 power-law ComplexF64 CSR SpMV (planned row blocks)
   powerlaw_coo_c64        the same matrix as row-sorted COO
   batched_mix             4096 banded ComplexF64 products in one grouped launch
@@ -40,7 +42,7 @@ def main(argv=None):
     rng = np.random.default_rng(0)
     c = args.case
     if c.startswith("laplacian"):
-        it = np.int64 if c.endswith("i64") or c == "laplacian_coo_to_csr" else np.int32
+        it = np.int64 if c.endswith("i64") or c in ("laplacian_coo_to_csr", "laplacian_coo_plus_t") else np.int32
         m, n, rp, cv, nz = wl.laplacian_2d(2048, itype=it, dtype=np.float64)
         x = torch.from_numpy(rng.uniform(-1, 1, n)).to(dev)
         y = torch.empty(m, dtype=torch.float64, device=dev)
@@ -55,10 +57,16 @@ def main(argv=None):
         elif c == "laplacian_csc_f64_i32":
             K = gsa.adapt(dev, gsa.GenericSparseMatrixCSC(*wl.csr_to_csc(m, n, rp, cv, nz)))
             run = lambda: gsa.mul_(y, K, x)
-        elif c == "laplacian_coo_to_csr":
+        elif c in ("laplacian_coo_to_csr", "laplacian_coo_plus_t"):
             _, _, r, cc, v = wl.permuted_coo(m, n, rp, cv, nz, seed=7)
             C = gsa.adapt(dev, gsa.GenericSparseMatrixCOO(m, n, r, cc, v))
-            run = lambda: gsa.GenericSparseMatrixCSR(C)
+            if c == "laplacian_coo_to_csr":
+                run = lambda: gsa.GenericSparseMatrixCSR(C)
+            else:
+                run = lambda: C + gsa.transpose(C)
+        elif c == "laplacian_spgemm":
+            A = gsa.adapt(dev, gsa.GenericSparseMatrixCSR(m, n, rp, cv, nz))
+            run = lambda: A @ A
         else:
             raise SystemExit(f"unknown case {c}")
     elif c.startswith("powerlaw"):
