@@ -10,7 +10,7 @@
 // store costs a whole DRAM sector, and more):
 //   A. coarse_count_kernel: entries per coarse bucket (2^cs consecutive rows, at most 4096
 //      rows and 8192 buckets), histograms in shared memory; one scan of the bucket counts.
-//   B. coarse_place_kernel: a CTA takes a tile of 4096 entries, ranks them per coarse bucket
+//   B. coarse_place_kernel: a CTA takes a tile of 2048 entries, ranks them per coarse bucket
 //      in shared memory and reserves one contiguous run per bucket with one global atomic,
 //      so the tile's writes land in runs that L2 merges into whole sectors.  Keys, the row
 //      inside the bucket and the value (conversions) are moved together.
@@ -51,7 +51,7 @@ constexpr int WARP_CTA_THREADS = 256;
 constexpr int MERGE_ITEMS = 8;
 constexpr int ROWS_MAX = 4096;     // rows per coarse bucket
 constexpr int COARSE_MAX = 8192;   // coarse buckets, the invalid-row bucket included
-constexpr int PB_THREADS = 256, PB_ITEMS = 16;
+constexpr int PB_THREADS = 256, PB_ITEMS = 8;
 constexpr int PC_THREADS = 512;
 constexpr int STAGE_BYTES = 96 * 1024;  // fine_kernel's shared staging of one coarse bucket
 
@@ -193,26 +193,36 @@ coarse_count_kernel(Src src, int64_t nnz, int64_t major_n, int cs, int64_t nb, u
 }
 
 template <class Src, class VT>
-__global__ void __launch_bounds__(PB_THREADS, 4)
+__global__ void __launch_bounds__(PB_THREADS, 3)
 coarse_place_kernel(Src src, const VT *__restrict__ vals_in, int64_t nnz, int64_t major_n, int cs, int64_t nb,
                     uint32_t *__restrict__ cfill, uint64_t *__restrict__ key1, uint16_t *__restrict__ row1,
                     VT *__restrict__ val1) {
     // per bucket: the tile's count, then (in place) the first slot of the tile's run
     __shared__ uint32_t s_run[COARSE_MAX];
+    constexpr bool HAS_VAL = !std::is_same<VT, NoValue>::value;
     constexpr int64_t TILE = (int64_t)PB_THREADS * PB_ITEMS;
     for (int64_t t0 = (int64_t)blockIdx.x * TILE; t0 < nnz; t0 += (int64_t)gridDim.x * TILE) {
         for (int64_t d = threadIdx.x; d < nb; d += blockDim.x) s_run[d] = 0;
         __syncthreads();
+        // every entry is read once: its indices and value stay in registers across the
+        // reservation
         uint32_t packed[PB_ITEMS];  // bucket << 16 | rank in the tile's run
+        uint32_t minor[PB_ITEMS];
+        uint16_t lrow[PB_ITEMS];
+        typename std::conditional<HAS_VAL, VT, char>::type val[PB_ITEMS];
 #pragma unroll
         for (int q = 0; q < PB_ITEMS; ++q) {
             const int64_t e = t0 + (int64_t)q * PB_THREADS + threadIdx.x;
-            packed[q] = 0;
+            int64_t mj = -1, mn = 0;
             if (e < nnz) {
-                const int64_t mj = src.major(e);
-                const uint32_t d = (uint32_t)((uint64_t)mj < (uint64_t)major_n ? mj >> cs : nb - 1);
-                packed[q] = (d << 16) | atomicAdd(&s_run[d], 1u);
+                src.get(e, mj, mn);
+                if constexpr (HAS_VAL) val[q] = vals_in[e];
             }
+            const bool in = (uint64_t)mj < (uint64_t)major_n;
+            const uint32_t d = (uint32_t)(in ? mj >> cs : nb - 1);
+            minor[q] = (uint32_t)mn;
+            lrow[q] = (uint16_t)(in ? mj - ((int64_t)d << cs) : 0);
+            packed[q] = e < nnz ? (d << 16) | atomicAdd(&s_run[d], 1u) : 0u;
         }
         __syncthreads();
         // one reservation per bucket the tile touches; eight independent atomics in flight
@@ -234,13 +244,10 @@ coarse_place_kernel(Src src, const VT *__restrict__ vals_in, int64_t nnz, int64_
         for (int q = 0; q < PB_ITEMS; ++q) {
             const int64_t e = t0 + (int64_t)q * PB_THREADS + threadIdx.x;
             if (e < nnz) {
-                int64_t mj, mn;
-                src.get(e, mj, mn);
-                const uint32_t d = packed[q] >> 16;
-                const uint32_t slot = s_run[d] + (packed[q] & 0xffffu);
-                key1[slot] = ((uint64_t)(uint32_t)mn << 32) | (uint32_t)e;
-                row1[slot] = (uint16_t)((int64_t)d == nb - 1 ? 0 : mj - ((int64_t)d << cs));
-                if constexpr (!std::is_same<VT, NoValue>::value) val1[slot] = vals_in[e];
+                const uint32_t slot = s_run[packed[q] >> 16] + (packed[q] & 0xffffu);
+                key1[slot] = ((uint64_t)minor[q] << 32) | (uint32_t)e;
+                row1[slot] = lrow[q];
+                if constexpr (HAS_VAL) val1[slot] = val[q];
             }
         }
         __syncthreads();

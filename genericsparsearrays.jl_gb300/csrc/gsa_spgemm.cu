@@ -10,8 +10,9 @@
 // reference's bits -- without a dense accumulator:
 //   1. entry_flops_kernel: products of every stored entry of P (the length of the Q row it
 //      selects); one scan; row_flops_kernel: products per output row from the scan at the row
-//      pointers, rows listed as small (at most 256 products) or big.
-//   2. small rows, a warp each (small_kernel): the row's products (column, value) expanded into
+//      pointers, rows listed as tiny, small or big.
+//   2. tiny rows (at most 32 products), a thread each (tiny_kernel), and small rows (at most
+//      256), a warp each (small_kernel): the row's products (column, value) expanded into
 //      shared memory in order; a product is the first of its column when no earlier one has
 //      the column; the count of first products is the row's entry count (symbolic pass); its
 //      position is the number of first products of smaller columns and its value the in-order
@@ -33,11 +34,11 @@ struct gsa_spgemm {
     const void *pp = nullptr, *pi = nullptr, *pv = nullptr;  // P: pointers, indices, values
     const void *qp = nullptr, *qi = nullptr, *qv = nullptr;  // Q
     int64_t nnz_c = 0;
-    uint32_t nsmall = 0, nbig = 0;
+    uint32_t ntiny = 0, nsmall = 0, nbig = 0;
     uint64_t pbig = 0;          // products of the big rows
     void *mem = nullptr;        // per-row arrays
     void *big = nullptr;        // big-row expansion and sort
-    size_t cnt_off = 0, cptr_off = 0, small_off = 0, big_off = 0, counters_off = 0;
+    size_t cnt_off = 0, cptr_off = 0, tiny_off = 0, small_off = 0, big_off = 0, counters_off = 0;
     size_t bflops_off = 0, boff_off = 0, exmaj_off = 0, exmin_off = 0, exval_off = 0, sort_off = 0;
     size_t keys_off = 0, perm_off = 0, flags_off = 0, rpos_off = 0, sums_off = 0, bbsums_off = 0;
 };
@@ -45,6 +46,8 @@ struct gsa_spgemm {
 namespace gsa {
 namespace {
 
+constexpr int SG_TINY_P = 32;     // products a thread sums in shared memory
+constexpr int SG_TINY_WARPS = 2;
 constexpr int SG_WARP_P = 256;    // products a warp sums in shared memory
 constexpr int SG_THREADS = 256;   // 8 warps
 constexpr int SG_WARPS = SG_THREADS / 32;
@@ -97,12 +100,13 @@ __global__ void entry_flops_kernel(int64_t nnz_p, const I *__restrict__ pi, cons
 
 // Products per outer entry of P from the scanned entry counts (the host has checked that all
 // products together number fewer than 2^32, so the scan does not wrap); rows listed small or
-// big; counters: [0] small rows, [1] big rows; totals[1]: big-row products.
+// big; counters: [2] tiny rows (at most 32 products), [0] small rows (at most 256), [1] big
+// rows; totals[1]: big-row products.
 template <typename I>
 __global__ void row_flops_kernel(int64_t outer_n, const I *__restrict__ pp, int base, const uint32_t *__restrict__ S,
-                                 uint32_t *__restrict__ cnt, uint32_t *__restrict__ small_list,
-                                 uint32_t *__restrict__ big_list, uint32_t *__restrict__ counters,
-                                 unsigned long long *__restrict__ totals) {
+                                 uint32_t *__restrict__ cnt, uint32_t *__restrict__ tiny_list,
+                                 uint32_t *__restrict__ small_list, uint32_t *__restrict__ big_list,
+                                 uint32_t *__restrict__ counters, unsigned long long *__restrict__ totals) {
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     for (int64_t o0 = (int64_t)blockIdx.x * blockDim.x; o0 < outer_n; o0 += stride) {
         const int64_t o = o0 + threadIdx.x;
@@ -113,27 +117,94 @@ __global__ void row_flops_kernel(int64_t outer_n, const I *__restrict__ pp, int 
             f = e > b ? S[e] - S[b] : 0u;
             cnt[o] = 0;
         }
-        const bool is_small = valid && f > 0 && f <= (uint32_t)SG_WARP_P;
+        const bool is_tiny = valid && f > 0 && f <= (uint32_t)SG_TINY_P;
+        const bool is_small = valid && f > (uint32_t)SG_TINY_P && f <= (uint32_t)SG_WARP_P;
         const bool is_big = valid && f > (uint32_t)SG_WARP_P;
         const unsigned ms = __ballot_sync(0xffffffffu, is_small), mb = __ballot_sync(0xffffffffu, is_big);
+        const unsigned mt = __ballot_sync(0xffffffffu, is_tiny);
         const int lane = threadIdx.x & 31;
         const unsigned lt = lane_lt();
         unsigned long long fb = is_big ? f : 0;
 #pragma unroll
         for (int d = 16; d > 0; d >>= 1) fb += __shfl_xor_sync(0xffffffffu, fb, d);
-        uint32_t bs = 0, bb = 0;
+        uint32_t bs = 0, bb = 0, bt = 0;
         if (lane == 0) {
+            if (mt) bt = atomicAdd(&counters[2], (uint32_t)__popc(mt));
             if (ms) bs = atomicAdd(&counters[0], (uint32_t)__popc(ms));
             if (mb) bb = atomicAdd(&counters[1], (uint32_t)__popc(mb));
             if (fb) atomicAdd(&totals[1], fb);
         }
         bs = __shfl_sync(0xffffffffu, bs, 0);
         bb = __shfl_sync(0xffffffffu, bb, 0);
+        bt = __shfl_sync(0xffffffffu, bt, 0);
+        if (is_tiny) tiny_list[bt + __popc(mt & lt)] = (uint32_t)o;
         if (is_small) small_list[bs + __popc(ms & lt)] = (uint32_t)o;
         if (is_big) big_list[bb + __popc(mb & lt)] = (uint32_t)o;
     }
 }
 
+
+// Thread per listed tiny row (at most SG_TINY_P products): the same expansion, sums and
+// positions as small_kernel, each thread in its own column of the warp's shared block
+// (slot s of lane l at s * 32 + l, so the lanes never share a bank), the first products of
+// each column kept as a bit mask.
+template <typename V, typename I, bool NUMERIC>
+__global__ void __launch_bounds__(SG_TINY_WARPS * 32)
+tiny_kernel(const uint32_t *__restrict__ list, const uint32_t *__restrict__ counters, const I *__restrict__ pp,
+            const I *__restrict__ pi, const V *__restrict__ pv, const I *__restrict__ qp, const I *__restrict__ qi,
+            const V *__restrict__ qv, int64_t q_outer, int base, bool csr, uint32_t *__restrict__ cnt,
+            const uint32_t *__restrict__ cptr, I *__restrict__ idx_out, V *__restrict__ val_out) {
+    __shared__ uint32_t tj[SG_TINY_WARPS][SG_TINY_P * 32];
+    __shared__ V tv[NUMERIC ? SG_TINY_WARPS : 1][NUMERIC ? SG_TINY_P * 32 : 1];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const uint32_t nlisted = counters[2];
+    for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < nlisted; q += gridDim.x * blockDim.x) {
+        const uint32_t o = list[q];
+        const int64_t b = (int64_t)__ldg(pp + o) - base, e = (int64_t)__ldg(pp + o + 1) - base;
+        uint32_t P = 0;
+        for (int64_t t = b; t < e; ++t) {
+            const int64_t k = (int64_t)__ldg(pi + t) - base;
+            if ((uint64_t)k >= (uint64_t)q_outer) continue;
+            const int64_t qb = (int64_t)__ldg(qp + k) - base;
+            const uint32_t len = (uint32_t)((int64_t)__ldg(qp + k + 1) - base - qb);
+            V a{};
+            if constexpr (NUMERIC) a = ldg(pv + t);
+            for (uint32_t u = 0; u < len && P < (uint32_t)SG_TINY_P; ++u, ++P) {
+                tj[w][P * 32 + lane] = (uint32_t)((int64_t)__ldg(qi + qb + u) - base);
+                if constexpr (NUMERIC) tv[w][P * 32 + lane] = product(a, ldg(qv + qb + u), csr);
+            }
+        }
+        uint32_t firsts = 0;
+        for (uint32_t s2 = 0; s2 < P; ++s2) {
+            const uint32_t j = tj[w][s2 * 32 + lane];
+            bool first = true;
+            for (uint32_t t = 0; t < s2; ++t)
+                if (tj[w][t * 32 + lane] == j) {
+                    first = false;
+                    break;
+                }
+            if (first) firsts |= 1u << s2;
+        }
+        if constexpr (!NUMERIC) {
+            cnt[o] = (uint32_t)__popc(firsts);
+        } else {
+            const uint32_t out0 = cptr[o];
+            for (uint32_t rest = firsts; rest; rest &= rest - 1) {
+                const uint32_t s2 = (uint32_t)(__ffs(rest) - 1);
+                const uint32_t j = tj[w][s2 * 32 + lane];
+                uint32_t pos = 0;
+                V acc = VT<V>::zero();
+                for (uint32_t t = 0; t < P; ++t) {
+                    const uint32_t jt = tj[w][t * 32 + lane];
+                    pos += (((firsts >> t) & 1u) && jt < j) ? 1u : 0u;
+                    if (t >= s2 && jt == j) acc = add(acc, tv[w][t * 32 + lane]);
+                }
+                idx_out[out0 + pos] = (I)((int64_t)j + base);
+                val_out[out0 + pos] = acc;
+            }
+        }
+    }
+}
 
 // Warp per listed small row.  The row's products go to shared memory in the reference's
 // order (P entries in storage order, each Q row in storage order): the lanes take 32 P
@@ -385,7 +456,7 @@ unsigned sg_grid(int64_t n, int64_t per_cta, int64_t cap) {
 // Per-row arrays of a product (one allocation): entry flops and their scan, row counts and
 // their scan, the two row lists, counters and totals, scan scratch.
 struct RowLayout {
-    size_t L, cnt, cptr, small, big, counters, totals, bsums, bytes;
+    size_t L, cnt, cptr, tiny, small, big, counters, totals, bsums, bytes;
 };
 RowLayout row_layout(int64_t outer_n, int64_t nnz_p) {
     RowLayout R;
@@ -393,6 +464,7 @@ RowLayout row_layout(int64_t outer_n, int64_t nnz_p) {
     R.L = cv.reserve<uint32_t>(nnz_p + 1);
     R.cnt = cv.reserve<uint32_t>(outer_n + 2);
     R.cptr = cv.reserve<uint32_t>(outer_n + 2);
+    R.tiny = cv.reserve<uint32_t>(outer_n > 0 ? outer_n : 1);
     R.small = cv.reserve<uint32_t>(outer_n > 0 ? outer_n : 1);
     R.big = cv.reserve<uint32_t>(outer_n > 0 ? outer_n : 1);
     R.counters = cv.reserve<uint32_t>(4);
@@ -446,11 +518,12 @@ int spgemm_create(cudaStream_t s, gsa_spgemm *h, int64_t nnz_p, I *ptr_c) {
     if (rc) return rc;
     char *m = (char *)h->mem;
     uint32_t *L = (uint32_t *)(m + R.L), *cnt = (uint32_t *)(m + R.cnt), *cptr = (uint32_t *)(m + R.cptr);
-    uint32_t *small = (uint32_t *)(m + R.small), *big = (uint32_t *)(m + R.big);
+    uint32_t *tiny = (uint32_t *)(m + R.tiny), *small = (uint32_t *)(m + R.small), *big = (uint32_t *)(m + R.big);
     uint32_t *counters = (uint32_t *)(m + R.counters), *bsums = (uint32_t *)(m + R.bsums);
     unsigned long long *totals = (unsigned long long *)(m + R.totals);
     h->cnt_off = R.cnt;
     h->cptr_off = R.cptr;
+    h->tiny_off = R.tiny;
     h->small_off = R.small;
     h->big_off = R.big;
     h->counters_off = R.counters;
@@ -469,7 +542,7 @@ int spgemm_create(cudaStream_t s, gsa_spgemm *h, int64_t nnz_p, I *ptr_c) {
     rc = scan_u32(s, L, L, nnz_p + 1, bsums);
     if (rc) return rc;
     if (outer_n > 0)
-        row_flops_kernel<I><<<sg_grid(outer_n, 256, 152 * 32), 256, 0, s>>>(outer_n, pp, h->base, L, cnt, small, big,
+        row_flops_kernel<I><<<sg_grid(outer_n, 256, 152 * 32), 256, 0, s>>>(outer_n, pp, h->base, L, cnt, tiny, small, big,
                                                                           counters, totals);
     rc = check_cuda(cudaGetLastError(), "spgemm: row_flops_kernel");
     uint32_t ctr[4] = {0, 0, 0, 0};
@@ -478,6 +551,12 @@ int spgemm_create(cudaStream_t s, gsa_spgemm *h, int64_t nnz_p, I *ptr_c) {
     if (rc) return rc;
     h->nsmall = ctr[0];
     h->nbig = ctr[1];
+    h->ntiny = ctr[2];
+    if (h->ntiny)
+        tiny_kernel<V, I, false><<<sg_grid(h->ntiny, SG_TINY_WARPS * 32, 152 * 32), SG_TINY_WARPS * 32, 0, s>>>(
+            tiny, counters, pp, pi, pv, qp, qi, qv, h->q_outer, h->base, h->csr != 0, cnt, nullptr, nullptr, nullptr);
+    rc = check_cuda(cudaGetLastError(), "spgemm: tiny_kernel");
+    if (rc) return rc;
     h->pbig = tot[1];
     if (h->nsmall)
         small_kernel<V, I, false><<<sg_grid(h->nsmall, SG_WARPS, 152 * 16), SG_THREADS, 0, s>>>(
@@ -539,8 +618,14 @@ int spgemm_compute(cudaStream_t s, const gsa_spgemm *h, I *idx_c, V *val_c) {
     const char *m = (const char *)h->mem;
     const uint32_t *cptr = (const uint32_t *)(m + h->cptr_off);
     const uint32_t *small = (const uint32_t *)(m + h->small_off), *big = (const uint32_t *)(m + h->big_off);
+    const uint32_t *tiny = (const uint32_t *)(m + h->tiny_off);
     const uint32_t *counters = (const uint32_t *)(m + h->counters_off);
-    int rc = GSA_OK;
+    if (h->ntiny)
+        tiny_kernel<V, I, true><<<sg_grid(h->ntiny, SG_TINY_WARPS * 32, 152 * 32), SG_TINY_WARPS * 32, 0, s>>>(
+            tiny, counters, (const I *)h->pp, (const I *)h->pi, (const V *)h->pv, (const I *)h->qp, (const I *)h->qi,
+            (const V *)h->qv, h->q_outer, h->base, h->csr != 0, nullptr, cptr, idx_c, val_c);
+    int rc = check_cuda(cudaGetLastError(), "spgemm: tiny_kernel");
+    if (rc) return rc;
     if (h->nsmall)
         small_kernel<V, I, true><<<sg_grid(h->nsmall, SG_WARPS, 152 * 16), SG_THREADS, 0, s>>>(
             small, counters, (const I *)h->pp, (const I *)h->pi, (const V *)h->pv, (const I *)h->qp, (const I *)h->qi,
