@@ -270,4 +270,69 @@ for (In, entry) in ((:CSRCu, :gsa_csr_to_coo), (:CSCCu, :gsa_csc_to_coo))
     end
 end
 
+# Sparse x sparse (src/matrix_csr/matrix_csr.jl:498-556, src/matrix_csc/matrix_csc.jl:500-560).
+# The reference's COO and transposed methods convert their operands and call these.
+for (Fmt, fmt) in ((:CSRCu, 0), (:CSCCu, 1))
+    @eval function Base.:(*)(A::$Fmt{T, Ti}, B::$Fmt{T, Ti}) where {T <: GSAValue, Ti <: GSAIndex}
+        size(A, 2) == size(B, 1) || throw(DimensionMismatch(
+            "second dimension of A, $(size(A, 2)), does not match first dimension of B, $(size(B, 1))"))
+        m, k, n = size(A, 1), size(A, 2), size(B, 2)
+        pa, ia = _ptrs(A)
+        pb, ib = _ptrs(B)
+        ptr = CuVector{Ti}(undef, ($fmt == 0 ? m : n) + 1)
+        nnz_c = Ref{Int64}(0)
+        h = Ref{Ptr{Cvoid}}(C_NULL)
+        gsa_check(ccall((:gsa_spgemm_create, libgsa), Cint,
+            (CUstream, Cint, Cint, Cint, Int64, Int64, Int64, CuPtr{Ti}, CuPtr{Ti}, CuPtr{T}, Int64,
+             CuPtr{Ti}, CuPtr{Ti}, CuPtr{T}, Int64, Cint, CuPtr{Ti}, Ref{Int64}, Ref{Ptr{Cvoid}}),
+            CUDA.stream(), Cint($fmt), gsa_dtype(T), gsa_itype(Ti), m, k, n, pa, ia, A.nzval,
+            length(A.nzval), pb, ib, B.nzval, length(B.nzval), Cint(1), ptr, nnz_c, h))
+        idx = CuVector{Ti}(undef, nnz_c[])
+        val = CuVector{T}(undef, nnz_c[])
+        try
+            gsa_check(ccall((:gsa_spgemm_compute, libgsa), Cint, (CUstream, Ptr{Cvoid}, CuPtr{Ti}, CuPtr{T}),
+                            CUDA.stream(), h[], idx, val))
+        finally
+            ccall((:gsa_spgemm_destroy, libgsa), Cint, (Ptr{Cvoid},), h[])
+        end
+        return $(Fmt === :CSRCu ? :GenericSparseMatrixCSR : :GenericSparseMatrixCSC)(m, n, ptr, idx, val)
+    end
+end
+
+# COO sums (src/matrix_coo/matrix_coo.jl:300-385 A + B, :387-458 A + λI), dropzeros included:
+# one sort of the sources where they lie, in-order run sums, zero sums dropped.
+function _coo_sum(m, n, A::COOCu{T, Ti}, opa, B, opb, ndiag, λ::T) where {T, Ti}
+    na = length(A.nzval)
+    nb = B === nothing ? 0 : length(B.nzval)
+    total = na + nb + ndiag
+    ws = CuVector{UInt8}(undef, ccall((:gsa_coo_sum_workspace_size, libgsa), Csize_t,
+                                      (Cint, Int64, Int64, Int64), gsa_dtype(T), m, n, total))
+    kept = Ref{Int64}(0)
+    nul = CU_NULL
+    gsa_check(ccall((:gsa_coo_sum_count, libgsa), Cint,
+        (CUstream, Cint, Cint, Int64, Int64, Int64, CuPtr{Ti}, CuPtr{Ti}, CuPtr{T}, Cint, Int64,
+         CuPtr{Ti}, CuPtr{Ti}, CuPtr{T}, Cint, Int64, Ref{T}, Cint, CuPtr{UInt8}, Csize_t, Ref{Int64}),
+        CUDA.stream(), gsa_dtype(T), gsa_itype(Ti), m, n, na, A.rowind, A.colind, A.nzval, opa, nb,
+        B === nothing ? nul : B.rowind, B === nothing ? nul : B.colind, B === nothing ? nul : B.nzval,
+        opb, ndiag, Ref(λ), Cint(1), ws, length(ws), kept))
+    r = CuVector{Ti}(undef, kept[]); c = CuVector{Ti}(undef, kept[]); v = CuVector{T}(undef, kept[])
+    gsa_check(ccall((:gsa_coo_sum_copy, libgsa), Cint,
+        (CUstream, Cint, Cint, Int64, Int64, Int64, Int64, Cint, CuPtr{UInt8}, CuPtr{Ti}, CuPtr{Ti}, CuPtr{T}),
+        CUDA.stream(), gsa_dtype(T), gsa_itype(Ti), m, n, total, kept[], Cint(1), ws, r, c, v))
+    return GenericSparseMatrixCOO(m, n, r, c, v)
+end
+
+function Base.:+(A::COOCu{T, Ti}, B::COOCu{T, Ti}) where {T <: GSAValue, Ti <: GSAIndex}
+    size(A) == size(B) || throw(DimensionMismatch(
+        "dimensions must match: A has dims $(size(A)), B has dims $(size(B))"))
+    return _coo_sum(size(A)..., A, Cint(0), B, Cint(0), 0, zero(T))
+end
+
+function Base.:+(A::COOCu{T, Ti}, J::UniformScaling{T}) where {T <: GSAValue, Ti <: GSAIndex}
+    m, n = size(A)
+    m == n || throw(DimensionMismatch("Matrix must be square to add UniformScaling."))
+    iszero(J.λ) && return copy(A)
+    return _coo_sum(m, n, A, Cint(0), nothing, Cint(0), n, J.λ)
+end
+
 end # module
