@@ -329,6 +329,44 @@ static bool bucket_fits(int64_t major_n, int64_t minor_n, int64_t nnz) {
     return major_n + 2 < 0xffffffffLL && minor_n <= 0x100000000LL && nnz < 0xffffffffLL;
 }
 
+// Stable LSD radix sort of n (key, payload) pairs over the low total_bits key bits, for
+// other translation units: the caller fills the first key and payload buffers of a
+// radix_sort_workspace(n)-byte workspace (radix_sort_inputs), and gets back the buffers that
+// hold the sorted pairs.
+size_t radix_sort_workspace(int64_t n) { return sort_layout(n > 0 ? n : 1).bytes; }
+void radix_sort_inputs(void *ws, int64_t n, uint64_t **keys, uint32_t **perm) {
+    Carver cv(ws);
+    *keys = cv.take<uint64_t>(n);
+    cv.take<uint64_t>(n);
+    *perm = cv.take<uint32_t>(n);
+}
+int radix_sort_pairs(cudaStream_t s, void *ws, int64_t n, int total_bits, uint64_t **keys_out, uint32_t **perm_out) {
+    const SortLayout L = sort_layout(n > 0 ? n : 1);
+    Carver cv(ws);
+    uint64_t *ka = cv.take<uint64_t>(n), *kb = cv.take<uint64_t>(n);
+    uint32_t *pa = cv.take<uint32_t>(n), *pb = cv.take<uint32_t>(n);
+    uint32_t *hist = cv.take<uint32_t>(L.hist_n);
+    uint32_t *bsums = cv.take<uint32_t>(ceil_div(L.hist_n, SC_TILE) + 1);
+    int rc = GSA_OK;
+    for (int shift = 0; n > 0 && shift < total_bits; shift += RS_BITS) {
+        const int w = total_bits - shift < RS_BITS ? total_bits - shift : RS_BITS;
+        const uint32_t mask = (1u << w) - 1;
+        radix_upsweep_kernel<<<(unsigned)L.num_tiles, RS_THREADS, 0, s>>>(ka, n, shift, mask, hist, L.num_tiles);
+        rc = exclusive_scan_u32(s, hist, hist, L.hist_n, bsums);
+        if (rc) return rc;
+        radix_downsweep_kernel<<<(unsigned)L.num_tiles, RS_THREADS, 0, s>>>(ka, pa, kb, pb, n, shift, mask, hist,
+                                                                           L.num_tiles);
+        rc = check_cuda(cudaGetLastError(), "radix pass");
+        if (rc) return rc;
+        uint64_t *tk = ka; ka = kb; kb = tk;
+        uint32_t *tp = pa; pa = pb; pb = tp;
+    }
+    *keys_out = ka;
+    *perm_out = pa;
+    return rc;
+}
+int radix_bits_for(int64_t count) { return bits_for(count); }
+
 template <typename V, typename I>
 size_t coo_to_compressed_workspace_size(int64_t m, int64_t n, int64_t nnz, bool colmajor) {
     if (nnz == 0) return 0;

@@ -318,6 +318,14 @@ constexpr int SCAN_TILE = 4096;
 inline int64_t scan_block_sums(int64_t n) { return ceil_div(n, SCAN_TILE) + 1; }
 int scan_u32(cudaStream_t s, const uint32_t *in, uint32_t *out, int64_t n, uint32_t *block_sums);
 
+// Stable LSD radix sort of (uint64 key, uint32 payload) pairs over the low total_bits bits
+// (8-bit digits).  Fill the buffers radix_sort_inputs returns, then sort; the sorted pairs
+// are in *keys_out / *perm_out (one of the workspace's two buffer pairs).
+size_t radix_sort_workspace(int64_t n);
+void radix_sort_inputs(void *ws, int64_t n, uint64_t **keys, uint32_t **perm);
+int radix_sort_pairs(cudaStream_t s, void *ws, int64_t n, int total_bits, uint64_t **keys_out, uint32_t **perm_out);
+int radix_bits_for(int64_t count);  // bits that values 0 .. count - 1 need
+
 // Scratch of one call: the caller's buffer, or a stream-ordered allocation freed on the
 // same stream when the call returns.
 struct Workspace {

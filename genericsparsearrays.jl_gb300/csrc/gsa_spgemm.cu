@@ -18,15 +18,16 @@
 //      position is the number of first products of smaller columns and its value the in-order
 //      sum of the products of its column, starting from zero (numeric pass).
 //   3. big rows: expanded into global memory (expand_kernel: a CTA per row, 256 P entries at a
-//      time, products spread evenly over the threads by a search of the chunk's offsets),
-//      sorted by (row, column, position) with the bucket sort, summed run by run in order.
+//      time, products spread evenly over the threads by a search of the chunk's offsets) with
+//      keys row << cb | column, sorted by the library's stable LSD radix sort (the expansion is
+//      in row order and in the reference's order within a row, so equal keys keep it), and
+//      summed run by run in order.
 // P and Q: CSR C = A * B runs over A's rows (P = A, Q = B); CSC C = A * B over B's columns
 // (P = B, Q = A).  Products are A-value times B-value with Julia's arithmetic (separate
 // multiply and add, textbook complex product), so the sums are the reference's bit for bit.
 #include <type_traits>
 
 #include "gsa_internal.cuh"
-#include "gsa_bucket.cuh"
 
 struct gsa_spgemm {
     int dtype = 0, itype = 0, csr = 1, base = 1;
@@ -39,8 +40,8 @@ struct gsa_spgemm {
     void *mem = nullptr;        // per-row arrays
     void *big = nullptr;        // big-row expansion and sort
     size_t cnt_off = 0, cptr_off = 0, tiny_off = 0, small_off = 0, big_off = 0, counters_off = 0;
-    size_t bflops_off = 0, boff_off = 0, exmaj_off = 0, exmin_off = 0, exval_off = 0, sort_off = 0;
-    size_t keys_off = 0, perm_off = 0, flags_off = 0, rpos_off = 0, sums_off = 0, bbsums_off = 0;
+    size_t boff_off = 0, keys_off = 0, flags_off = 0, rpos_off = 0, sums_off = 0;
+    int cb = 0;                 // column bits of the big-row sort keys
 };
 
 namespace gsa {
@@ -49,7 +50,7 @@ namespace {
 constexpr int SG_TINY_P = 32;     // products a thread sums in shared memory
 constexpr int SG_TINY_WARPS = 2;
 constexpr int SG_WARP_P = 256;    // products a warp sums in shared memory
-constexpr int SG_THREADS = 256;   // 8 warps
+constexpr int SG_THREADS = 128;   // 4 warps
 constexpr int SG_WARPS = SG_THREADS / 32;
 constexpr int EX_THREADS_SG = 256;
 
@@ -206,21 +207,23 @@ tiny_kernel(const uint32_t *__restrict__ list, const uint32_t *__restrict__ coun
     }
 }
 
-// Warp per listed small row.  The row's products go to shared memory in the reference's
-// order (P entries in storage order, each Q row in storage order): the lanes take 32 P
-// entries at a time, scan their Q-row lengths for the offsets, and write their own rows.
-// NUMERIC = false: cnt[o] = distinct columns.  NUMERIC = true: the entries, written from
-// cptr[o].
+// Warp per listed small row (at most SG_WARP_P products).  The row's products go to shared
+// memory in the reference's order (P entries in storage order, each Q row in storage order):
+// the lanes take 32 P entries at a time, scan their Q-row lengths for the offsets, and write
+// their own rows as keys column << 8 | slot (values by slot).  A warp bitonic sort of the keys
+// puts each column's products together in slot order; run starts are the entries (symbolic:
+// cnt[o] = runs), their scanned count the positions, and each run is summed in order from zero
+// (numeric, written from cptr[o]).
 template <typename V, typename I, bool NUMERIC>
 __global__ void __launch_bounds__(SG_THREADS)
 small_kernel(const uint32_t *__restrict__ list, const uint32_t *__restrict__ counters, const I *__restrict__ pp,
              const I *__restrict__ pi, const V *__restrict__ pv, const I *__restrict__ qp, const I *__restrict__ qi,
              const V *__restrict__ qv, int64_t q_outer, int base, bool csr, uint32_t *__restrict__ cnt,
              const uint32_t *__restrict__ cptr, I *__restrict__ idx_out, V *__restrict__ val_out) {
-    __shared__ uint32_t sj[SG_WARPS][SG_WARP_P];
+    __shared__ uint64_t sk[SG_WARPS][SG_WARP_P];
     __shared__ V sv[NUMERIC ? SG_WARPS : 1][NUMERIC ? SG_WARP_P : 1];
-    __shared__ uint8_t sf[NUMERIC ? SG_WARPS : 1][NUMERIC ? SG_WARP_P : 1];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const unsigned lt = lane_lt();
     const uint32_t nlisted = counters[0];
     for (uint32_t q = blockIdx.x * SG_WARPS + w; q < nlisted; q += gridDim.x * SG_WARPS) {
         const uint32_t o = list[q];
@@ -251,45 +254,53 @@ small_kernel(const uint32_t *__restrict__ list, const uint32_t *__restrict__ cou
             // the bound also holds for a malformed structure
             for (uint32_t u = 0; u < len && P + off + u < (uint32_t)SG_WARP_P; ++u) {
                 const uint32_t slot = P + off + u;
-                sj[w][slot] = (uint32_t)((int64_t)__ldg(qi + qb + u) - base);
+                const uint64_t j = (uint32_t)((int64_t)__ldg(qi + qb + u) - base);
+                sk[w][slot] = (j << 8) | slot;
                 if constexpr (NUMERIC) sv[w][slot] = product(a, ldg(qv + qb + u), csr);
             }
             P += total;
         }
         if (P > (uint32_t)SG_WARP_P) P = SG_WARP_P;
+        uint32_t P2 = 32;
+        while (P2 < P) P2 <<= 1;
+        for (uint32_t i = P + lane; i < P2; i += 32) sk[w][i] = ~0ull;
         __syncwarp();
-        uint32_t firsts = 0;
-        for (uint32_t s = lane; s < P; s += 32) {
-            const uint32_t j = sj[w][s];
-            bool first = true;
-            for (uint32_t t = 0; t < s; ++t)
-                if (sj[w][t] == j) {
-                    first = false;
-                    break;
+        for (uint32_t kk = 2; kk <= P2; kk <<= 1) {
+            for (uint32_t jj = kk >> 1; jj > 0; jj >>= 1) {
+                for (uint32_t i = lane; i < P2; i += 32) {
+                    const uint32_t ixj = i ^ jj;
+                    if (ixj > i) {
+                        const uint64_t x = sk[w][i], y = sk[w][ixj];
+                        if ((x > y) == ((i & kk) == 0)) {
+                            sk[w][i] = y;
+                            sk[w][ixj] = x;
+                        }
+                    }
                 }
-            if constexpr (NUMERIC) sf[w][s] = first ? 1 : 0;
-            firsts += first ? 1u : 0u;
+                __syncwarp();
+            }
+        }
+        uint32_t before = 0;  // run starts in earlier rounds
+        const uint32_t out0 = NUMERIC ? cptr[o] : 0;
+        for (uint32_t i0 = 0; i0 < P; i0 += 32) {
+            const uint32_t i = i0 + lane;
+            bool start = false;
+            if (i < P) start = i == 0 || (sk[w][i] >> 8) != (sk[w][i - 1] >> 8);
+            const unsigned ms = __ballot_sync(0xffffffffu, start);
+            if constexpr (NUMERIC) {
+                if (start) {
+                    const uint64_t j = sk[w][i] >> 8;
+                    V acc = VT<V>::zero();
+                    for (uint32_t u = i; u < P && (sk[w][u] >> 8) == j; ++u) acc = add(acc, sv[w][sk[w][u] & 0xffu]);
+                    const uint32_t pos = before + __popc(ms & lt);
+                    idx_out[out0 + pos] = (I)((int64_t)j + base);
+                    val_out[out0 + pos] = acc;
+                }
+            }
+            before += __popc(ms);
         }
         if constexpr (!NUMERIC) {
-#pragma unroll
-            for (int d = 16; d > 0; d >>= 1) firsts += __shfl_xor_sync(0xffffffffu, firsts, d);
-            if (lane == 0) cnt[o] = firsts;
-        } else {
-            __syncwarp();
-            const uint32_t out0 = cptr[o];
-            for (uint32_t s = lane; s < P; s += 32) {
-                if (!sf[w][s]) continue;
-                const uint32_t j = sj[w][s];
-                uint32_t pos = 0;
-                V acc = VT<V>::zero();
-                for (uint32_t t = 0; t < P; ++t) {
-                    const uint32_t jt = sj[w][t];
-                    pos += (sf[w][t] && jt < j) ? 1u : 0u;
-                    if (t >= s && jt == j) acc = add(acc, sv[w][t]);
-                }
-                idx_out[out0 + pos] = (I)((int64_t)j + base);
-                val_out[out0 + pos] = acc;
-            }
+            if (lane == 0) cnt[o] = before;
         }
         __syncwarp();
     }
@@ -311,16 +322,16 @@ __global__ void big_flops_kernel(const uint32_t *__restrict__ list, uint32_t nbi
     }
 }
 
-// CTA per big row: its products written from boff[q], in the reference's order, as (row q,
-// column, value) triplets.  256 P entries at a time: their Q-row lengths are scanned, then
+// CTA per big row: its products written from boff[q], in the reference's order, as key
+// (q << cb | column), position and value.  256 P entries at a time: their Q-row lengths are scanned, then
 // product p of the chunk goes to thread p mod 256, which finds its P entry by a binary search
 // of the chunk's offsets.
 template <typename V, typename I>
 __global__ void __launch_bounds__(EX_THREADS_SG)
 expand_kernel(const uint32_t *__restrict__ list, uint32_t nbig, const uint32_t *__restrict__ boff,
               const I *__restrict__ pp, const I *__restrict__ pi, const V *__restrict__ pv, const I *__restrict__ qp,
-              const I *__restrict__ qi, const V *__restrict__ qv, int64_t q_outer, int base, bool csr,
-              uint32_t *__restrict__ ex_major, uint32_t *__restrict__ ex_minor, V *__restrict__ ex_val) {
+              const I *__restrict__ qi, const V *__restrict__ qv, int64_t q_outer, int base, bool csr, int cb,
+              uint64_t *__restrict__ ex_key, uint32_t *__restrict__ ex_pos, V *__restrict__ ex_val) {
     constexpr int T = EX_THREADS_SG;
     __shared__ uint32_t s_off[T + 1];
     __shared__ int64_t s_qb[T];
@@ -369,8 +380,10 @@ expand_kernel(const uint32_t *__restrict__ list, uint32_t nbig, const uint32_t *
                 }
                 const int64_t f = s_qb[lo] + (p - s_off[lo]);
                 const uint32_t slot = run + p;
-                ex_major[slot] = q;
-                ex_minor[slot] = (uint32_t)((int64_t)__ldg(qi + f) - base);
+                // masked to its field, so that an index outside the matrix cannot reach the row bits
+                const uint64_t col = (uint64_t)((int64_t)__ldg(qi + f) - base) & ((1ull << cb) - 1);
+                ex_key[slot] = ((uint64_t)q << cb) | col;
+                ex_pos[slot] = slot;
                 ex_val[slot] = product(s_a[lo], ldg(qv + f), csr);
             }
             run += total;
@@ -378,26 +391,6 @@ expand_kernel(const uint32_t *__restrict__ list, uint32_t nbig, const uint32_t *
         }
     }
 }
-
-struct ExpSource {
-    const uint32_t *maj, *mnr;
-    __device__ __forceinline__ int64_t major(int64_t i) const { return (int64_t)__ldg(maj + i); }
-    __device__ __forceinline__ void get(int64_t i, int64_t &a, int64_t &b) const {
-        a = (int64_t)__ldg(maj + i);
-        b = (int64_t)__ldg(mnr + i);
-    }
-};
-
-// Sorted (big row << 32 | column) keys and expansion positions.
-struct ExpEmit {
-    uint64_t *keys;
-    uint32_t *perm;
-    __device__ __forceinline__ void pointer(int64_t, uint32_t) const {}
-    __device__ __forceinline__ void gather(uint32_t p, uint64_t r, uint64_t key) const {
-        keys[p] = (r << 32) | (key >> 32);
-        perm[p] = (uint32_t)key;
-    }
-};
 
 // One thread per run of equal keys: the in-order sum from zero; flags[i] = 1 at run starts.
 template <typename V>
@@ -418,25 +411,27 @@ __global__ void big_runs_kernel(int64_t total, const uint64_t *__restrict__ keys
     }
 }
 
-// Entries of each big row: the run starts between its first and last sorted positions.
-__global__ void big_count_kernel(const uint32_t *__restrict__ list, uint32_t nbig, const uint32_t *__restrict__ bstart,
+// Entries of each big row: the run starts in its range of the sorted products (sorting by
+// (row, column) keeps every row in the range its expansion had).
+__global__ void big_count_kernel(const uint32_t *__restrict__ list, uint32_t nbig, const uint32_t *__restrict__ boff,
                                  const uint32_t *__restrict__ rpos, uint32_t *__restrict__ cnt) {
     for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < nbig; q += gridDim.x * blockDim.x)
-        cnt[list[q]] = rpos[bstart[q + 1]] - rpos[bstart[q]];
+        cnt[list[q]] = rpos[boff[q + 1]] - rpos[boff[q]];
 }
 
 template <typename V, typename I>
 __global__ void big_write_kernel(int64_t total, const uint64_t *__restrict__ keys, const uint32_t *__restrict__ flags,
                                  const uint32_t *__restrict__ rpos, const V *__restrict__ sums,
-                                 const uint32_t *__restrict__ list, const uint32_t *__restrict__ bstart,
+                                 const uint32_t *__restrict__ list, const uint32_t *__restrict__ boff, int cb,
                                  const uint32_t *__restrict__ cptr, int base, I *__restrict__ idx_out,
                                  V *__restrict__ val_out) {
+    const uint64_t mask = cb >= 64 ? ~0ull : ((1ull << cb) - 1);
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
         if (!flags[i]) continue;
         const uint64_t k = keys[i];
-        const uint32_t q = (uint32_t)(k >> 32);
-        const uint32_t out = cptr[list[q]] + (rpos[i] - rpos[bstart[q]]);
-        idx_out[out] = (I)((int64_t)(k & 0xffffffffull) + base);
+        const uint32_t q = (uint32_t)(k >> cb);
+        const uint32_t out = cptr[list[q]] + (rpos[i] - rpos[boff[q]]);
+        idx_out[out] = (I)((int64_t)(k & mask) + base);
         val_out[out] = sums[i];
     }
 }
@@ -477,19 +472,15 @@ RowLayout row_layout(int64_t outer_n, int64_t nnz_p) {
 
 // Big-row arrays, once their products are known.
 struct BigLayout {
-    size_t bflops, boff, exmaj, exmin, exval, sort, keys, perm, flags, rpos, sums, bsums, bytes;
+    size_t bflops, boff, exval, sort, flags, rpos, sums, bsums, bytes;
 };
 BigLayout big_layout(uint32_t nbig, uint64_t pbig, size_t vsize) {
     BigLayout B;
     Carver cv(nullptr);
     B.bflops = cv.reserve<uint32_t>((size_t)nbig + 1);
     B.boff = cv.reserve<uint32_t>((size_t)nbig + 1);
-    B.exmaj = cv.reserve<uint32_t>(pbig);
-    B.exmin = cv.reserve<uint32_t>(pbig);
     B.exval = cv.reserve<unsigned char>(pbig * vsize);
-    B.sort = cv.reserve<unsigned char>(bucket::layout(nbig, (int64_t)pbig, 0, SCAN_TILE).bytes);
-    B.keys = cv.reserve<uint64_t>(pbig);
-    B.perm = cv.reserve<uint32_t>(pbig);
+    B.sort = cv.reserve<unsigned char>(radix_sort_workspace((int64_t)pbig));
     B.flags = cv.reserve<uint32_t>(pbig + 1);
     B.rpos = cv.reserve<uint32_t>(pbig + 1);
     B.sums = cv.reserve<unsigned char>(pbig * vsize);
@@ -570,35 +561,39 @@ int spgemm_create(cudaStream_t s, gsa_spgemm *h, int64_t nnz_p, I *ptr_c) {
         char *g = (char *)h->big;
         h->flags_off = B.flags;
         h->rpos_off = B.rpos;
-        h->keys_off = B.keys;
         h->sums_off = B.sums;
-        h->sort_off = B.sort;
+        h->boff_off = B.boff;
+        h->cb = radix_bits_for(h->width);
+        const int qb = radix_bits_for(h->nbig);
         uint32_t *bflops = (uint32_t *)(g + B.bflops), *boff = (uint32_t *)(g + B.boff);
-        uint32_t *exmaj = (uint32_t *)(g + B.exmaj), *exmin = (uint32_t *)(g + B.exmin);
         V *exval = (V *)(g + B.exval), *sums = (V *)(g + B.sums);
-        uint64_t *keys = (uint64_t *)(g + B.keys);
-        uint32_t *perm = (uint32_t *)(g + B.perm), *flags = (uint32_t *)(g + B.flags);
+        uint32_t *flags = (uint32_t *)(g + B.flags);
         uint32_t *rpos = (uint32_t *)(g + B.rpos), *gbsums = (uint32_t *)(g + B.bsums);
+        uint64_t *exkey;
+        uint32_t *expos;
+        radix_sort_inputs(g + B.sort, (int64_t)h->pbig, &exkey, &expos);
         big_flops_kernel<I><<<sg_grid((int64_t)h->nbig + 1, 256, 152 * 8), 256, 0, s>>>(big, h->nbig, pp, h->base, L,
                                                                                        bflops);
         rc = check_cuda(cudaGetLastError(), "spgemm: big_flops_kernel");
         if (!rc) rc = scan_u32(s, bflops, boff, (int64_t)h->nbig + 1, gbsums);
         if (rc) return rc;
         expand_kernel<V, I><<<sg_grid(h->nbig, 1, 152 * 4), EX_THREADS_SG, 0, s>>>(
-            big, h->nbig, boff, pp, pi, pv, qp, qi, qv, h->q_outer, h->base, h->csr != 0, exmaj, exmin, exval);
+            big, h->nbig, boff, pp, pi, pv, qp, qi, qv, h->q_outer, h->base, h->csr != 0, h->cb, exkey, expos, exval);
         rc = check_cuda(cudaGetLastError(), "spgemm: expand_kernel");
         if (rc) return rc;
-        rc = bucket::sort(s, (int64_t)h->nbig, (int64_t)h->pbig, ExpSource{exmaj, exmin},
-                          (const bucket::NoValue *)nullptr, ExpEmit{keys, perm}, g + B.sort, scan_u32, SCAN_TILE);
+        // stable by (row, column): the expansion is in row order and, within a row, in the
+        // reference's order, so equal columns keep that order
+        uint64_t *keys;
+        uint32_t *perm;
+        rc = radix_sort_pairs(s, g + B.sort, (int64_t)h->pbig, h->cb + qb, &keys, &perm);
         if (rc) return rc;
+        h->keys_off = (size_t)((char *)keys - g);
         big_runs_kernel<V><<<sg_grid((int64_t)h->pbig + 1, 256, 152 * 32), 256, 0, s>>>((int64_t)h->pbig, keys, perm,
                                                                                         exval, sums, flags);
         rc = check_cuda(cudaGetLastError(), "spgemm: big_runs_kernel");
         if (!rc) rc = scan_u32(s, flags, rpos, (int64_t)h->pbig + 1, gbsums);
         if (rc) return rc;
-        const bucket::Layout SL = bucket::layout(h->nbig, (int64_t)h->pbig, 0, SCAN_TILE);
-        const uint32_t *bstart = (const uint32_t *)(g + B.sort + SL.start);
-        big_count_kernel<<<sg_grid(h->nbig, 256, 152 * 8), 256, 0, s>>>(big, h->nbig, bstart, rpos, cnt);
+        big_count_kernel<<<sg_grid(h->nbig, 256, 152 * 8), 256, 0, s>>>(big, h->nbig, boff, rpos, cnt);
         rc = check_cuda(cudaGetLastError(), "spgemm: big_count_kernel");
         if (rc) return rc;
     }
@@ -633,11 +628,10 @@ int spgemm_compute(cudaStream_t s, const gsa_spgemm *h, I *idx_c, V *val_c) {
     rc = check_cuda(cudaGetLastError(), "spgemm: small_kernel");
     if (rc || !h->nbig) return rc;
     const char *g = (const char *)h->big;
-    const bucket::Layout SL = bucket::layout(h->nbig, (int64_t)h->pbig, 0, SCAN_TILE);
     big_write_kernel<V, I><<<sg_grid((int64_t)h->pbig, 256, 152 * 32), 256, 0, s>>>(
         (int64_t)h->pbig, (const uint64_t *)(g + h->keys_off), (const uint32_t *)(g + h->flags_off),
         (const uint32_t *)(g + h->rpos_off), (const V *)(g + h->sums_off), big,
-        (const uint32_t *)(g + h->sort_off + SL.start), cptr, h->base, idx_c, val_c);
+        (const uint32_t *)(g + h->boff_off), h->cb, cptr, h->base, idx_c, val_c);
     return check_cuda(cudaGetLastError(), "spgemm: big_write_kernel");
 }
 

@@ -12,6 +12,8 @@ Cases (the bench workloads, same seeds):
   laplacian_spgemm        A * A of the Laplacian (Float64 / Int32 CSR)
   powerlaw_csr_c64        n = 1e6 power-law ComplexF64 CSR SpMV (planned row blocks)
   powerlaw_coo_c64        the same matrix as row-sorted COO
+  powerlaw_coo_to_csr     COO -> CSR of the power-law matrix's randomly permuted triplets
+  powerlaw_spgemm_1e5     A * A of an n = 1e5 power-law ComplexF64 CSR matrix
   batched_mix             4096 banded ComplexF64 products in one grouped launch
 
 Each case makes its inputs, runs the product ``--reps`` times (default 3) and synchronizes;
@@ -77,9 +79,20 @@ def main(argv=None):
             A = gsa.adapt(dev, gsa.GenericSparseMatrixCSR(m, n, rp, cv, nz))
         elif c == "powerlaw_coo_c64":
             A = gsa.adapt(dev, gsa.GenericSparseMatrixCOO(m, n, wl.csr_rows(rp), cv, nz))
+        elif c == "powerlaw_coo_to_csr":
+            _, _, r, cc, v = wl.permuted_coo(m, n, rp, cv, nz, seed=2)
+            A = gsa.adapt(dev, gsa.GenericSparseMatrixCOO(m, n, r, cc, v))
+        elif c == "powerlaw_spgemm_1e5":
+            m, n, rp, cv, nz = wl.power_law(100_000, seed=0, itype=np.int64, dtype=np.complex128)
+            A = gsa.adapt(dev, gsa.GenericSparseMatrixCSR(m, n, rp, cv, nz))
         else:
             raise SystemExit(f"unknown case {c}")
-        run = lambda: gsa.mul_(y, A, x)
+        if c == "powerlaw_coo_to_csr":
+            run = lambda: gsa.GenericSparseMatrixCSR(A)
+        elif c == "powerlaw_spgemm_1e5":
+            run = lambda: A @ A
+        else:
+            run = lambda: gsa.mul_(y, A, x)
     elif c == "batched_mix":
         from genericsparsearrays_gb300 import batch
         sys.path.insert(0, ROOT)
