@@ -12,8 +12,9 @@
 //      rows and 8192 buckets), histograms in shared memory; one scan of the bucket counts.
 //   B. coarse_place_kernel: a CTA takes a tile of 2048 entries, ranks them per coarse bucket
 //      in shared memory and reserves one contiguous run per bucket with one global atomic,
-//      so the tile's writes land in runs that L2 merges into whole sectors.  Keys, the row
-//      inside the bucket and the value (conversions) are moved together.
+//      so the tile's writes land in runs that L2 merges into whole sectors.  Each entry is one
+//      record: the key row-in-bucket << (mb + pb) | minor << pb | position (sorting a row by it
+//      is sorting by (minor, position)) and the value (conversions), one 16- or 32-byte store.
 //   C. fine_kernel: a CTA per coarse bucket counts its rows in shared memory, scans them --
 //      the row pointers of the result -- and places the bucket's entries in row order into
 //      shared memory (96 KB of staging; cs is chosen so that an average bucket fills at most
@@ -67,32 +68,77 @@ struct Coarse {
     bool ok;
     int cs;       // rows per coarse bucket = 2^cs
     int64_t nb;   // coarse buckets, the last one for invalid rows
+    int mb, pb;   // bits of the minor index and of the entry position in the packed keys
 };
+inline int nbits(int64_t count) {  // bits that values 0 .. count - 1 need
+    int b = 0;
+    while (b < 63 && ((int64_t)1 << b) < count) ++b;
+    return b;
+}
 // The fewest rows per bucket that keep the bucket count in bounds, raised while a bucket of
-// average rows still fills at most half the shared staging.
-inline Coarse coarse_plan(int64_t major_n, int64_t nnz, int stage) {
-    Coarse c{false, 0, 0};
+// average rows still fills at most half the shared staging.  The two-level form packs the
+// row inside the bucket, the minor index and the position into one 64-bit key, so the three
+// must fit.
+inline Coarse coarse_plan(int64_t major_n, int64_t minor_n, int64_t nnz, int stage) {
+    Coarse c{false, 0, 0, 0, 0};
     int cs = 0;
     while (cs < 40 && ((major_n + ((int64_t)1 << cs) - 1) >> cs) + 1 > COARSE_MAX) ++cs;
     const double avg = major_n > 0 ? (double)nnz / (double)major_n : 0.0;
     while (cs < 12 && (double)((int64_t)2 << cs) * avg <= 0.5 * stage) ++cs;
     if (((int64_t)1 << cs) > ROWS_MAX) return c;
+    c.mb = nbits(minor_n);
+    c.pb = nbits(nnz);
+    if (c.mb + c.pb + cs > 64) return c;
     c.ok = true;
     c.cs = cs;
     c.nb = ((major_n + ((int64_t)1 << cs) - 1) >> cs) + 1;
     return c;
 }
 
+// Pass B's record: the packed key and the carried value, stored together (one 16- or 32-byte
+// store per entry).
+template <class VT, bool HAS = !std::is_same<VT, NoValue>::value> struct Rec;
+template <class VT> struct alignas(16) Rec<VT, true> {
+    uint64_t key;
+    VT val;
+};
+template <class VT> struct Rec<VT, false> {
+    uint64_t key;
+};
+constexpr size_t rec_size(size_t vsize) { return vsize == 0 ? 8 : (vsize <= 8 ? 16 : 32); }
+
+__host__ __device__ __forceinline__ uint64_t shl64(uint64_t x, int n) { return n >= 64 ? 0 : x << n; }
+__host__ __device__ __forceinline__ uint64_t shr64(uint64_t x, int n) { return n >= 64 ? 0 : x >> n; }
+__host__ __device__ __forceinline__ uint64_t low_mask(int n) { return n >= 64 ? ~0ull : (1ull << n) - 1; }
+
+// row << (mb + pb) | minor << pb | position  ->  minor << 32 | position
+__device__ __forceinline__ uint64_t canonical_key(uint64_t k, int mb, int pb) {
+    return (((k >> pb) & low_mask(mb)) << 32) | (k & low_mask(pb));
+}
+
+// An emitter seen through packed keys: keys are turned back into minor << 32 | position.
+template <class Emit> struct PackedEmit {
+    Emit e;
+    int mb, pb;
+    __device__ __forceinline__ void pointer(int64_t r, uint32_t first) const { e.pointer(r, first); }
+    template <class V> __device__ __forceinline__ void put(uint32_t p, uint64_t r, uint64_t key, V v) const {
+        e.put(p, r, canonical_key(key, mb, pb), v);
+    }
+    __device__ __forceinline__ void gather(uint32_t p, uint64_t r, uint64_t key) const {
+        e.gather(p, r, canonical_key(key, mb, pb));
+    }
+};
+
 struct Layout {
     Coarse co;
     int64_t ncnt;
-    size_t cnt, cstart, start, bsums, key1, row1, val1, key2, val2, list, counters, bytes;
+    size_t cnt, cstart, start, bsums, key1, rec1, key2, val2, list, counters, bytes;
 };
 
 // vsize: bytes of a carried value (0: none)
-inline Layout layout(int64_t major_n, int64_t nnz, size_t vsize, size_t sc_tile) {
+inline Layout layout(int64_t major_n, int64_t minor_n, int64_t nnz, size_t vsize, size_t sc_tile) {
     Layout L;
-    L.co = coarse_plan(major_n, nnz, (int)(STAGE_BYTES / (8 + vsize)));
+    L.co = coarse_plan(major_n, minor_n, nnz, (int)(STAGE_BYTES / (8 + vsize)));
     const int64_t n = nnz > 0 ? nnz : 1;
     L.ncnt = (L.co.ok ? L.co.nb : major_n) + 2;
     const int64_t nscan = L.ncnt > major_n + 2 ? L.ncnt : major_n + 2;
@@ -103,8 +149,7 @@ inline Layout layout(int64_t major_n, int64_t nnz, size_t vsize, size_t sc_tile)
     L.bsums = cv.reserve<uint32_t>(ceil_div(nscan, (int64_t)sc_tile) + 1);
     L.key1 = cv.reserve<uint64_t>(n);
     L.key2 = cv.reserve<uint64_t>(n);
-    L.row1 = L.co.ok ? cv.reserve<uint16_t>(n) : 0;
-    L.val1 = L.co.ok && vsize ? cv.reserve<unsigned char>((size_t)n * vsize) : 0;
+    L.rec1 = L.co.ok ? cv.reserve<unsigned char>((size_t)n * rec_size(vsize)) : 0;
     L.val2 = L.co.ok && vsize ? cv.reserve<unsigned char>((size_t)n * vsize) : 0;
     L.list = cv.reserve<uint32_t>(major_n + 1);
     L.counters = cv.reserve<uint32_t>(4);
@@ -194,9 +239,10 @@ coarse_count_kernel(Src src, int64_t nnz, int64_t major_n, int cs, int64_t nb, u
 
 template <class Src, class VT>
 __global__ void __launch_bounds__(PB_THREADS, 3)
-coarse_place_kernel(Src src, const VT *__restrict__ vals_in, int64_t nnz, int64_t major_n, int cs, int64_t nb,
-                    uint32_t *__restrict__ cfill, uint64_t *__restrict__ key1, uint16_t *__restrict__ row1,
-                    VT *__restrict__ val1) {
+coarse_place_kernel(Src src, const VT *__restrict__ vals_in, int64_t nnz, int64_t major_n, Coarse co,
+                    uint32_t *__restrict__ cfill, Rec<VT> *__restrict__ rec1) {
+    const int cs = co.cs;
+    const int64_t nb = co.nb;
     // per bucket: the tile's count, then (in place) the first slot of the tile's run
     __shared__ uint32_t s_run[COARSE_MAX];
     constexpr bool HAS_VAL = !std::is_same<VT, NoValue>::value;
@@ -207,8 +253,7 @@ coarse_place_kernel(Src src, const VT *__restrict__ vals_in, int64_t nnz, int64_
         // every entry is read once: its indices and value stay in registers across the
         // reservation
         uint32_t packed[PB_ITEMS];  // bucket << 16 | rank in the tile's run
-        uint32_t minor[PB_ITEMS];
-        uint16_t lrow[PB_ITEMS];
+        uint64_t key[PB_ITEMS];     // row in the bucket << (mb + pb) | minor << pb | position
         typename std::conditional<HAS_VAL, VT, char>::type val[PB_ITEMS];
 #pragma unroll
         for (int q = 0; q < PB_ITEMS; ++q) {
@@ -220,8 +265,10 @@ coarse_place_kernel(Src src, const VT *__restrict__ vals_in, int64_t nnz, int64_
             }
             const bool in = (uint64_t)mj < (uint64_t)major_n;
             const uint32_t d = (uint32_t)(in ? mj >> cs : nb - 1);
-            minor[q] = (uint32_t)mn;
-            lrow[q] = (uint16_t)(in ? mj - ((int64_t)d << cs) : 0);
+            const uint64_t lrow = in ? (uint64_t)(mj - ((int64_t)d << cs)) : 0;
+            // the minor index masked to its field, so that an index outside the matrix cannot
+            // reach the row bits
+            key[q] = shl64(lrow, co.mb + co.pb) | ((((uint64_t)mn) & low_mask(co.mb)) << co.pb) | (uint64_t)e;
             packed[q] = e < nnz ? (d << 16) | atomicAdd(&s_run[d], 1u) : 0u;
         }
         __syncthreads();
@@ -245,9 +292,8 @@ coarse_place_kernel(Src src, const VT *__restrict__ vals_in, int64_t nnz, int64_
             const int64_t e = t0 + (int64_t)q * PB_THREADS + threadIdx.x;
             if (e < nnz) {
                 const uint32_t slot = s_run[packed[q] >> 16] + (packed[q] & 0xffffu);
-                key1[slot] = ((uint64_t)minor[q] << 32) | (uint32_t)e;
-                row1[slot] = lrow[q];
-                if constexpr (HAS_VAL) val1[slot] = val[q];
+                if constexpr (HAS_VAL) rec1[slot] = Rec<VT>{key[q], val[q]};
+                else rec1[slot] = Rec<VT>{key[q]};
             }
         }
         __syncthreads();
@@ -268,11 +314,14 @@ template <class VT> inline size_t fine_smem_bytes(int cs) {
 // warp_kernel and cta_kernel.
 template <class VT, class Emit>
 __global__ void __launch_bounds__(PC_THREADS, 2)
-fine_kernel(int64_t major_n, int cs, int64_t nb, const uint32_t *__restrict__ cstart,
-            const uint64_t *__restrict__ key1, const uint16_t *__restrict__ row1, const VT *__restrict__ val1,
+fine_kernel(int64_t major_n, Coarse co, const uint32_t *__restrict__ cstart, const Rec<VT> *__restrict__ rec1,
             uint64_t *key2, VT *val2, uint32_t *__restrict__ start, uint32_t *__restrict__ list,
             uint32_t *__restrict__ counters, Emit emit) {
     constexpr bool HAS_VAL = !std::is_same<VT, NoValue>::value;
+    const int cs = co.cs;
+    const int64_t nb = co.nb;
+    const int rshift = co.mb + co.pb;  // the row inside the bucket sits above minor and position
+    const PackedEmit<Emit> pemit{emit, co.mb, co.pb};
     constexpr int STAGE = stage_entries<VT>();
     constexpr int ITEMS = ROWS_MAX / PC_THREADS;
     extern __shared__ __align__(16) unsigned char dsm[];
@@ -299,7 +348,8 @@ fine_kernel(int64_t major_n, int cs, int64_t nb, const uint32_t *__restrict__ cs
         }
         __syncthreads();
 #pragma unroll 4
-        for (uint32_t i = B0 + threadIdx.x; i < B1; i += PC_THREADS) atomicAdd(&s_fill[row1[i]], 1u);
+        for (uint32_t i = B0 + threadIdx.x; i < B1; i += PC_THREADS)
+            atomicAdd(&s_fill[(uint32_t)shr64(rec1[i].key, rshift)], 1u);
         __syncthreads();
         // exclusive scan of the R row counts: each thread takes ITEMS consecutive rows
         uint32_t v[ITEMS], sum = 0;
@@ -348,14 +398,16 @@ fine_kernel(int64_t major_n, int cs, int64_t nb, const uint32_t *__restrict__ cs
         if (staged) {
 #pragma unroll 4
             for (uint32_t i = B0 + threadIdx.x; i < B1; i += PC_THREADS) {
-                const uint32_t row = row1[i];
+                const Rec<VT> r = rec1[i];
+                const uint32_t row = (uint32_t)shr64(r.key, rshift);
                 const uint32_t slot = s_off[row] + atomicAdd(&s_fill[row], 1u);
-                s_key[slot] = key1[i];
-                if constexpr (HAS_VAL) s_val[slot] = val1[i];
+                s_key[slot] = r.key;
+                if constexpr (HAS_VAL) s_val[slot] = r.val;
             }
             __syncthreads();
-            if (s_long) {  // rows for cta_kernel read their keys from key2
-                for (uint32_t j = threadIdx.x; j < E; j += PC_THREADS) key2[B0 + j] = s_key[j];
+            if (s_long) {  // rows for cta_kernel read their (plain) keys from key2
+                for (uint32_t j = threadIdx.x; j < E; j += PC_THREADS)
+                    key2[B0 + j] = canonical_key(s_key[j], co.mb, co.pb);
             }
             __syncthreads();  // s_fill becomes the list of warp-sized rows
             for (int j0 = 0; j0 < R; j0 += PC_THREADS) {
@@ -366,7 +418,7 @@ fine_kernel(int64_t major_n, int cs, int64_t nb, const uint32_t *__restrict__ cs
                     len = s_off[j + 1] - s_off[j];
                     if (len <= (uint32_t)SMALL)
                         sort_short_row(s_key + s_off[j], HAS_VAL ? s_val + s_off[j] : nullptr, B0 + s_off[j], len,
-                                       (uint64_t)(row0 + j), emit);
+                                       (uint64_t)(row0 + j), pemit);
                     else if (len <= (uint32_t)WARP_MAX)
                         s_fill[atomicAdd(&s_nlist, 1u)] = (uint32_t)j;
                 }
@@ -381,15 +433,16 @@ fine_kernel(int64_t major_n, int cs, int64_t nb, const uint32_t *__restrict__ cs
                     const uint64_t kt = s_key[o + t];
                     uint32_t rank = 0;
                     for (uint32_t u = 0; u < len; ++u) rank += s_key[o + u] < kt ? 1u : 0u;
-                    emit_one(emit, B0 + o + rank, (uint64_t)(row0 + j), kt, HAS_VAL ? s_val + o : nullptr, t);
+                    emit_one(pemit, B0 + o + rank, (uint64_t)(row0 + j), kt, HAS_VAL ? s_val + o : nullptr, t);
                 }
             }
         } else {
             for (uint32_t i = B0 + threadIdx.x; i < B1; i += PC_THREADS) {
-                const uint32_t row = row1[i];
+                const Rec<VT> r = rec1[i];
+                const uint32_t row = (uint32_t)shr64(r.key, rshift);
                 const uint32_t slot = B0 + s_off[row] + atomicAdd(&s_fill[row], 1u);
-                key2[slot] = key1[i];
-                if constexpr (HAS_VAL) val2[slot] = val1[i];
+                key2[slot] = canonical_key(r.key, co.mb, co.pb);
+                if constexpr (HAS_VAL) val2[slot] = r.val;
             }
             __syncthreads();
             for (int j0 = 0; j0 < R; j0 += PC_THREADS) {
@@ -567,10 +620,11 @@ inline unsigned grid_for(int64_t n, int64_t per_cta, int64_t cap) {
 // The whole sort.  vals_in: the values to carry (VT = NoValue: none).  scan(s, in, out, n,
 // bsums) is the library's exclusive scan of uint32.
 template <class Src, class VT, class Emit, class Scan>
-int sort(cudaStream_t s, int64_t major_n, int64_t nnz, const Src &src, const VT *vals_in, const Emit &emit,
-         void *ws, Scan scan, size_t sc_tile) {
+int sort(cudaStream_t s, int64_t major_n, int64_t minor_n, int64_t nnz, const Src &src, const VT *vals_in,
+         const Emit &emit, void *ws, Scan scan, size_t sc_tile) {
     constexpr size_t VS = std::is_same<VT, NoValue>::value ? 0 : sizeof(VT);
-    const Layout L = layout(major_n, nnz, VS, sc_tile);
+    static_assert(sizeof(Rec<VT>) == rec_size(VS), "record size of the layout");
+    const Layout L = layout(major_n, minor_n, nnz, VS, sc_tile);
     char *w = (char *)ws;
     uint32_t *cnt = (uint32_t *)(w + L.cnt), *start = (uint32_t *)(w + L.start);
     uint32_t *bsums = (uint32_t *)(w + L.bsums), *list = (uint32_t *)(w + L.list);
@@ -583,8 +637,8 @@ int sort(cudaStream_t s, int64_t major_n, int64_t nnz, const Src &src, const VT 
     if (L.co.ok) {
         const Coarse co = L.co;
         uint32_t *cstart = (uint32_t *)(w + L.cstart);
-        uint16_t *row1 = (uint16_t *)(w + L.row1);
-        VT *val1 = VS ? (VT *)(w + L.val1) : nullptr, *val2 = VS ? (VT *)(w + L.val2) : nullptr;
+        Rec<VT> *rec1 = (Rec<VT> *)(w + L.rec1);
+        VT *val2 = VS ? (VT *)(w + L.val2) : nullptr;
         if (nnz > 0)
             coarse_count_kernel<Src><<<grid_for(nnz, PB_THREADS * PB_ITEMS, cap), PB_THREADS, 0, s>>>(
                 src, nnz, major_n, co.cs, co.nb, cnt);
@@ -598,14 +652,14 @@ int sort(cudaStream_t s, int64_t major_n, int64_t nnz, const Src &src, const VT 
         if (rc) return rc;
         if (nnz > 0)
             coarse_place_kernel<Src, VT><<<grid_for(nnz, PB_THREADS * PB_ITEMS, cap), PB_THREADS, 0, s>>>(
-                src, vals_in, nnz, major_n, co.cs, co.nb, cnt, key1, row1, val1);
+                src, vals_in, nnz, major_n, co, cnt, rec1);
         const size_t smem = fine_smem_bytes<VT>(co.cs);
         rc = check_cuda(cudaFuncSetAttribute(fine_kernel<VT, Emit>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)smem),
                         "bucket: fine_kernel shared memory");
         if (rc) return rc;
         fine_kernel<VT, Emit><<<grid_for(co.nb, 1, 152 * 2), PC_THREADS, smem, s>>>(
-            major_n, co.cs, co.nb, cstart, key1, row1, val1, key2, val2, start, list, counters, emit);
+            major_n, co, cstart, rec1, key2, val2, start, list, counters, emit);
         warp_kernel<VT, Emit><<<152 * 8, WARP_CTA_THREADS, 0, s>>>(start, key2, val2, list, counters, emit);
         cta_kernel<Emit><<<152 * 2, CTA_THREADS, 0, s>>>(major_n, start, key2, key1, list, counters, emit);
         return check_cuda(cudaGetLastError(), "bucket sort kernels");

@@ -371,7 +371,7 @@ template <typename V, typename I>
 size_t coo_to_compressed_workspace_size(int64_t m, int64_t n, int64_t nnz, bool colmajor) {
     if (nnz == 0) return 0;
     const int64_t major_n = colmajor ? n : m, minor_n = colmajor ? m : n;
-    if (bucket_fits(major_n, minor_n, nnz)) return bucket::layout(major_n, nnz, sizeof(V), SC_TILE).bytes;
+    if (bucket_fits(major_n, minor_n, nnz)) return bucket::layout(major_n, minor_n, nnz, sizeof(V), SC_TILE).bytes;
     return sort_layout(nnz).bytes;
 }
 
@@ -432,12 +432,12 @@ int launch_coo_to_compressed(cudaStream_t s, bool colmajor, int64_t m, int64_t n
         return check_cuda(cudaGetLastError(), "pointer_kernel");
     }
     if (bucket_fits(major_n, minor_n, nnz)) {
-        if (ws_bytes < bucket::layout(major_n, nnz, sizeof(V), SC_TILE).bytes)
+        if (ws_bytes < bucket::layout(major_n, minor_n, nnz, sizeof(V), SC_TILE).bytes)
             return fail(GSA_ERR_INVALID_ARG, "conversion workspace too small");
         PairSource<I> src{major, minor, base};
         CompressedEmit<V, I> emit{ptr_out, idx_out, val_out, val, base, major_n, nnz};
         timer_before(s);
-        int rc = bucket::sort(s, major_n, nnz, src, val, emit, ws, exclusive_scan_u32, SC_TILE);
+        int rc = bucket::sort(s, major_n, minor_n, nnz, src, val, emit, ws, exclusive_scan_u32, SC_TILE);
         timer_after(s);
         return rc;
     }
@@ -767,7 +767,7 @@ static SumLayout sum_layout(int64_t m, int64_t n, int64_t total, size_t vsize) {
     L.bucket = bucket_fits(n, m, total);
     Carver cv(nullptr);
     if (L.bucket) {
-        cv.reserve<unsigned char>(bucket::layout(n, total, 0, SC_TILE).bytes);
+        cv.reserve<unsigned char>(bucket::layout(n, m, total, 0, SC_TILE).bytes);
         L.keys = cv.reserve<uint64_t>(total);
         L.perm = cv.reserve<uint32_t>(total);
     } else {
@@ -822,7 +822,7 @@ int launch_coo_sum_count(cudaStream_t s, int64_t m, int64_t n, const SumSources 
     timer_before(s);
     if (L.bucket) {
         SumSource<I> bs{src, base};
-        rc = bucket::sort(s, n, total, bs, (const bucket::NoValue *)nullptr, KeyEmit{keys, perm}, ws,
+        rc = bucket::sort(s, n, m, total, bs, (const bucket::NoValue *)nullptr, KeyEmit{keys, perm}, ws,
                           exclusive_scan_u32, SC_TILE);
     } else {
         Carver cv(ws);

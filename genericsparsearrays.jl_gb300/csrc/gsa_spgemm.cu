@@ -84,19 +84,20 @@ template <typename I>
 __global__ void entry_flops_kernel(int64_t nnz_p, const I *__restrict__ pi, const I *__restrict__ qp, int64_t q_outer,
                                    int base, uint32_t *__restrict__ L, unsigned long long *__restrict__ totals) {
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t t0 = (int64_t)blockIdx.x * blockDim.x; t0 <= nnz_p; t0 += stride) {
-        const int64_t t = t0 + threadIdx.x;
+    unsigned long long sum = 0;  // one reduction and atomic per warp at the end
+#pragma unroll 4
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t <= nnz_p; t += stride) {
         uint32_t len = 0;
         if (t < nnz_p) {
             const int64_t k = (int64_t)__ldg(pi + t) - base;
             if ((uint64_t)k < (uint64_t)q_outer) len = (uint32_t)((int64_t)__ldg(qp + k + 1) - __ldg(qp + k));
         }
-        if (t <= nnz_p) L[t] = len;
-        unsigned long long sum = len;
-#pragma unroll
-        for (int d = 16; d > 0; d >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, d);
-        if ((threadIdx.x & 31) == 0 && sum) atomicAdd(&totals[0], sum);
+        L[t] = len;
+        sum += len;
     }
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, d);
+    if ((threadIdx.x & 31) == 0 && sum) atomicAdd(&totals[0], sum);
 }
 
 // Products per outer entry of P from the scanned entry counts (the host has checked that all
