@@ -49,6 +49,7 @@ namespace {
 
 constexpr int SG_TINY_P = 32;     // products a thread sums in shared memory
 constexpr int SG_TINY_WARPS = 2;
+constexpr int SG_TINY_A = 8;      // A entries of a tiny row whose loads are issued together
 constexpr int SG_WARP_P = 256;    // products a warp sums in shared memory
 constexpr int SG_THREADS = 128;   // 4 warps
 constexpr int SG_WARPS = SG_THREADS / 32;
@@ -164,16 +165,92 @@ tiny_kernel(const uint32_t *__restrict__ list, const uint32_t *__restrict__ coun
         const uint32_t o = list[q];
         const int64_t b = (int64_t)__ldg(pp + o) - base, e = (int64_t)__ldg(pp + o + 1) - base;
         uint32_t P = 0;
-        for (int64_t t = b; t < e; ++t) {
-            const int64_t k = (int64_t)__ldg(pi + t) - base;
-            if ((uint64_t)k >= (uint64_t)q_outer) continue;
-            const int64_t qb = (int64_t)__ldg(qp + k) - base;
-            const uint32_t len = (uint32_t)((int64_t)__ldg(qp + k + 1) - base - qb);
-            V a{};
-            if constexpr (NUMERIC) a = ldg(pv + t);
-            for (uint32_t u = 0; u < len && P < (uint32_t)SG_TINY_P; ++u, ++P) {
-                tj[w][P * 32 + lane] = (uint32_t)((int64_t)__ldg(qi + qb + u) - base);
-                if constexpr (NUMERIC) tv[w][P * 32 + lane] = product(a, ldg(qv + qb + u), csr);
+        auto expand = [&](int64_t qb, uint32_t len, V a) {
+#pragma unroll 4
+            for (uint32_t u = 0; u < len; ++u) {
+                if (P + u < (uint32_t)SG_TINY_P) {
+                    tj[w][(P + u) * 32 + lane] = (uint32_t)((int64_t)__ldg(qi + qb + u) - base);
+                    if constexpr (NUMERIC) tv[w][(P + u) * 32 + lane] = product(a, ldg(qv + qb + u), csr);
+                }
+            }
+            P = P + len < (uint32_t)SG_TINY_P ? P + len : (uint32_t)SG_TINY_P;
+        };
+        if (e - b <= SG_TINY_A) {
+            // rows of up to SG_TINY_A entries: their indices, Q-row bounds and values loaded
+            // together first, so the loads overlap instead of forming one chain per entry
+            int64_t qb[SG_TINY_A];
+            uint32_t len[SG_TINY_A];
+            V a[SG_TINY_A];
+#pragma unroll
+            for (int c = 0; c < SG_TINY_A; ++c) {
+                const int64_t t = b + c;
+                qb[c] = (int64_t)(t < e ? __ldg(pi + t) : (I)0) - base;  // k for now
+                if constexpr (NUMERIC) a[c] = t < e ? ldg(pv + t) : V{};
+            }
+#pragma unroll
+            for (int c = 0; c < SG_TINY_A; ++c) {
+                const int64_t k = qb[c];
+                const bool ok = b + c < e && (uint64_t)k < (uint64_t)q_outer;
+                const int64_t q0 = ok ? (int64_t)__ldg(qp + k) - base : 0;
+                len[c] = ok ? (uint32_t)((int64_t)__ldg(qp + k + 1) - base - q0) : 0u;
+                qb[c] = q0;
+            }
+#pragma unroll
+            for (int c = 0; c < SG_TINY_A; ++c)
+                if (len[c]) expand(qb[c], len[c], NUMERIC ? a[c] : V{});
+            // The products are SG_TINY_A runs, one per A entry, in A order.  When every run is
+            // sorted by column (sorted Q rows), a merge of the runs visits the columns in
+            // increasing order and, for each, its products in the reference's order (runs in A
+            // order, each run in its own order): no quadratic scan.
+            uint32_t hs[SG_TINY_A], he[SG_TINY_A];
+            uint32_t off = 0;
+            bool sorted = true;
+#pragma unroll
+            for (int c = 0; c < SG_TINY_A; ++c) {
+                hs[c] = off < P ? off : P;
+                off += len[c];
+                he[c] = off < P ? off : P;
+                for (uint32_t u = hs[c] + 1; u < he[c]; ++u)
+                    if (tj[w][u * 32 + lane] < tj[w][(u - 1) * 32 + lane]) sorted = false;
+            }
+            if (sorted) {
+                uint64_t jc[SG_TINY_A];
+#pragma unroll
+                for (int c = 0; c < SG_TINY_A; ++c) jc[c] = hs[c] < he[c] ? tj[w][hs[c] * 32 + lane] : ~0ull;
+                const uint32_t out0 = NUMERIC ? cptr[o] : 0;
+                uint32_t count = 0;
+                for (uint32_t guard = 0; guard <= (uint32_t)SG_TINY_P; ++guard) {
+                    uint64_t jmin = jc[0];
+#pragma unroll
+                    for (int c = 1; c < SG_TINY_A; ++c) jmin = jc[c] < jmin ? jc[c] : jmin;
+                    if (jmin == ~0ull) break;
+                    V acc = VT<V>::zero();
+#pragma unroll
+                    for (int c = 0; c < SG_TINY_A; ++c) {
+                        while (jc[c] == jmin) {
+                            if constexpr (NUMERIC) acc = add(acc, tv[w][hs[c] * 32 + lane]);
+                            ++hs[c];
+                            jc[c] = hs[c] < he[c] ? tj[w][hs[c] * 32 + lane] : ~0ull;
+                        }
+                    }
+                    if constexpr (NUMERIC) {
+                        idx_out[out0 + count] = (I)((int64_t)jmin + base);
+                        val_out[out0 + count] = acc;
+                    }
+                    ++count;
+                }
+                if constexpr (!NUMERIC) cnt[o] = count;
+                continue;
+            }
+        } else {
+            for (int64_t t = b; t < e; ++t) {
+                const int64_t k = (int64_t)__ldg(pi + t) - base;
+                if ((uint64_t)k >= (uint64_t)q_outer) continue;
+                const int64_t q0 = (int64_t)__ldg(qp + k) - base;
+                const uint32_t l = (uint32_t)((int64_t)__ldg(qp + k + 1) - base - q0);
+                V av{};
+                if constexpr (NUMERIC) av = ldg(pv + t);
+                expand(q0, l, av);
             }
         }
         uint32_t firsts = 0;

@@ -157,3 +157,28 @@ def test_checks(gsa, cuda):
     K, _ = _csc(gsa, cuda, sprand(rng, 8, 8, 0.3, np.float64), np.int64)
     with pytest.raises(gsa.ArgumentError):
         A @ K
+
+
+@pytest.mark.parametrize("dt", [np.float64, np.complex64])
+def test_unsorted_and_duplicate_rows(gsa, cuda, oracle, dt):
+    """B rows in shuffled order and with repeated columns (what a COO-built matrix can hold):
+    the same reached positions and in-order sums as the reference's dense accumulator, for
+    rows of every size class (the sorted-run merge must not be used on such rows)."""
+    rng = np.random.default_rng(67)
+    m, k, n = 200, 150, 120
+    SA, SB = sprand(rng, m, k, 0.03, dt), sprand(rng, k, n, 0.05, dt)
+    a = parts(SA, "csr", np.int64)
+    bp, bi, bv = parts(SB, "csr", np.int64)
+    rows_i, rows_v, ptr = [], [], [1]
+    for r in range(k):  # shuffle each row and repeat a column in every third row
+        lo, hi = bp[r] - 1, bp[r + 1] - 1
+        i, v = bi[lo:hi].copy(), bv[lo:hi].copy()
+        if r % 3 == 0 and i.size:
+            i, v = np.append(i, i[0]), np.append(v, rand_values(rng, 1, dt))
+        p = rng.permutation(i.size)
+        rows_i.append(i[p]); rows_v.append(v[p]); ptr.append(ptr[-1] + i.size)
+    b = (np.array(ptr, np.int64), np.concatenate(rows_i), np.concatenate(rows_v).astype(dt))
+    A = gsa.adapt(cuda, gsa.GenericSparseMatrixCSR(m, k, *a))
+    B = gsa.adapt(cuda, gsa.GenericSparseMatrixCSR(k, n, *b))
+    C = A @ B
+    _same((np_(C.rowptr), np_(C.colval), np_(C.nzval)), oracle.spgemm("csr", m, k, n, a, b))
