@@ -20,7 +20,7 @@
 //      shared memory (96 KB of staging; cs is chosen so that an average bucket fills at most
 //      half of it).  Rows of up to 16 entries are sorted there by a thread in registers (rank
 //      counting), rows of up to 256 by a warp, and emitted; longer rows go to cta_kernel
-//      (bitonic sort of 4096-entry chunks in shared memory, merged pairwise; values then
+//      (bitonic sort of 16384-entry chunks in shared memory, merged pairwise; values then
 //      gathered by input position).  A bucket larger than the staging is placed in global
 //      memory instead, with its rows of more than 16 entries listed for warp_kernel and
 //      cta_kernel.
@@ -46,8 +46,8 @@ namespace bucket {
 
 constexpr int SMALL = 16;          // a thread sorts rows of up to 16 entries in registers
 constexpr int WARP_MAX = 256;      // a warp sorts rows of up to 256 entries
-constexpr int CTA_THREADS = 512;
-constexpr int CTA_TILE = 4096;     // a CTA sorts 4096 entries in shared memory at once
+constexpr int CTA_THREADS = 1024;
+constexpr int CTA_TILE = 16384;    // a CTA sorts 16384 entries in shared memory at once (128 KB)
 constexpr int WARP_CTA_THREADS = 256;
 constexpr int MERGE_ITEMS = 8;
 constexpr int ROWS_MAX = 4096;     // rows per coarse bucket
@@ -575,7 +575,7 @@ template <class Emit>
 __global__ void __launch_bounds__(CTA_THREADS)
 cta_kernel(int64_t major_n, const uint32_t *__restrict__ start, uint64_t *keys, uint64_t *scratch,
            const uint32_t *__restrict__ list, const uint32_t *__restrict__ counters, Emit emit) {
-    __shared__ uint64_t s[CTA_TILE];
+    extern __shared__ __align__(16) uint64_t s[];  // CTA_TILE keys
     const uint32_t nlisted = counters[1];
     for (uint32_t q = blockIdx.x; q < nlisted; q += gridDim.x) {
         const uint32_t r = list[major_n - q];
@@ -609,6 +609,17 @@ cta_kernel(int64_t major_n, const uint32_t *__restrict__ start, uint64_t *keys, 
         for (uint32_t j = threadIdx.x; j < len; j += blockDim.x) emit.gather(b + j, (uint64_t)r, src[j]);
         __syncthreads();
     }
+}
+
+template <class Emit>
+int launch_cta(cudaStream_t s, int64_t major_n, const uint32_t *start, uint64_t *keys, uint64_t *scratch,
+               const uint32_t *list, const uint32_t *counters, const Emit &emit) {
+    const size_t smem = (size_t)CTA_TILE * sizeof(uint64_t);
+    int rc = check_cuda(cudaFuncSetAttribute(cta_kernel<Emit>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                        "bucket: cta_kernel shared memory");
+    if (rc) return rc;
+    cta_kernel<Emit><<<152, CTA_THREADS, smem, s>>>(major_n, start, keys, scratch, list, counters, emit);
+    return check_cuda(cudaGetLastError(), "bucket cta_kernel");
 }
 
 inline unsigned grid_for(int64_t n, int64_t per_cta, int64_t cap) {
@@ -661,7 +672,8 @@ int sort(cudaStream_t s, int64_t major_n, int64_t minor_n, int64_t nnz, const Sr
         fine_kernel<VT, Emit><<<grid_for(co.nb, 1, 152 * 2), PC_THREADS, smem, s>>>(
             major_n, co, cstart, rec1, key2, val2, start, list, counters, emit);
         warp_kernel<VT, Emit><<<152 * 8, WARP_CTA_THREADS, 0, s>>>(start, key2, val2, list, counters, emit);
-        cta_kernel<Emit><<<152 * 2, CTA_THREADS, 0, s>>>(major_n, start, key2, key1, list, counters, emit);
+        rc = launch_cta(s, major_n, start, key2, key1, list, counters, emit);
+        if (rc) return rc;
         return check_cuda(cudaGetLastError(), "bucket sort kernels");
     }
     if (nnz > 0) count_kernel<Src><<<grid_for(nnz, 256, cap), 256, 0, s>>>(src, nnz, major_n, cnt);
@@ -673,7 +685,8 @@ int sort(cudaStream_t s, int64_t major_n, int64_t minor_n, int64_t nnz, const Sr
     small_kernel<Emit><<<grid_for(major_n + 1, 256, 152 * 32), 256, 0, s>>>(major_n, start, key1, list, counters,
                                                                              emit);
     warp_kernel<NoValue, Emit><<<152 * 8, WARP_CTA_THREADS, 0, s>>>(start, key1, nullptr, list, counters, emit);
-    cta_kernel<Emit><<<152 * 2, CTA_THREADS, 0, s>>>(major_n, start, key1, key2, list, counters, emit);
+    rc = launch_cta(s, major_n, start, key1, key2, list, counters, emit);
+    if (rc) return rc;
     return check_cuda(cudaGetLastError(), "bucket sort kernels");
 }
 

@@ -127,13 +127,13 @@ def test_power_law_rows_conversion(gsa, oracle, cuda):
 
 @pytest.mark.parametrize("it", INDEX_TYPES)
 def test_bucket_sizes_with_duplicates(gsa, oracle, cuda, it):
-    """Rows and columns of 0..16 (sorted by a thread), 17..256 (a warp), 257..4096 (a CTA in
-    shared memory) and beyond 4096 entries (CTA chunks merged pairwise), each with repeated
+    """Rows and columns of 0..16 (sorted by a thread), 17..256 (a warp), 257..16384 (a CTA in
+    shared memory) and beyond 16384 entries (CTA chunks merged pairwise), each with repeated
     (row, col) pairs carrying different values, shuffled: CSR and CSC equal the oracle's bit
     for bit, so ties keep their input order in every bucket size."""
     rng = np.random.default_rng(41)
     m, n = 600, 20_000
-    lengths = {3: 17, 10: 256, 11: 257, 40: 4096, 41: 4097, 77: 9000, 500: 16, 501: 1}
+    lengths = {3: 17, 10: 256, 11: 257, 40: 4096, 41: 4097, 77: 9000, 90: 16384, 91: 40000, 500: 16, 501: 1}
     rows, cols = [], []
     for r, L in lengths.items():
         c = rng.integers(1, n + 1, L)
