@@ -299,23 +299,25 @@ def run_gpu(args, world, rank, local):
         achieved = nbytes / kern_avg_s / 1e9
 
         # e2e through the public API: every step copies its x from pinned host memory to the
-        # device, runs mul!, and copies its y back to pinned host memory.  Steps alternate
-        # between two streams and two buffer sets, so one step's upload overlaps the previous
-        # step's download (the host link is full duplex); a step's buffers are reused only
-        # after its result is on the host.  The sequential form (one stream, a synchronize
-        # per step) is reported beside it.
-        xh = [torch.from_numpy(x_host).pin_memory() for _ in range(2)]
-        yh = [torch.empty(m, dtype=torch.float64).pin_memory() for _ in range(2)]
-        xd = [torch.empty(n, dtype=torch.float64, device=dev) for _ in range(2)]
-        yd = [torch.empty(m, dtype=torch.float64, device=dev) for _ in range(2)]
-        streams = [torch.cuda.Stream(dev) for _ in range(2)]
+        # device, runs mul!, and copies its y back to pinned host memory.  Steps rotate over
+        # three streams and three buffer sets, so one step's upload, the previous step's
+        # product and the one before's download run at once (the host link is full duplex;
+        # three sets measured 0.211 ms per step against 0.248 ms with two); a step's buffers
+        # are reused only after its result is on the host.  The sequential form (one stream,
+        # a synchronize per step) is reported beside it.
+        SETS = 3
+        xh = [torch.from_numpy(x_host).pin_memory() for _ in range(SETS)]
+        yh = [torch.empty(m, dtype=torch.float64).pin_memory() for _ in range(SETS)]
+        xd = [torch.empty(n, dtype=torch.float64, device=dev) for _ in range(SETS)]
+        yd = [torch.empty(m, dtype=torch.float64, device=dev) for _ in range(SETS)]
+        streams = [torch.cuda.Stream(dev) for _ in range(SETS)]
 
         def e2e_run(nsteps):
             done = []
             for i in range(nsteps):
-                j = i % 2
-                if i >= 2:
-                    done[i - 2].synchronize()  # step i-2's y is on the host: its buffers are free
+                j = i % SETS
+                if i >= SETS:
+                    done[i - SETS].synchronize()  # that step's y is on the host: its buffers are free
                 with torch.cuda.stream(streams[j]):
                     xd[j].copy_(xh[j], non_blocking=True)
                     gsa.mul_(yd[j], A, xd[j])
@@ -323,7 +325,7 @@ def run_gpu(args, world, rank, local):
                     ev = torch.cuda.Event()
                     ev.record(streams[j])
                     done.append(ev)
-            for ev in done[-2:]:
+            for ev in done[-SETS:]:
                 ev.synchronize()
 
         def e2e_seq():
@@ -332,7 +334,7 @@ def run_gpu(args, world, rank, local):
             yh[0].copy_(yd[0], non_blocking=True)
             torch.cuda.current_stream().synchronize()
 
-        e2e_run(max(args.warmup, 2))
+        e2e_run(max(args.warmup, SETS))
         t0 = time.perf_counter()
         e2e_run(args.steps)
         e2e_s = time.perf_counter() - t0
@@ -388,7 +390,7 @@ def run_gpu(args, world, rank, local):
         "e2e": {"value": round(e2e_value, 2), "unit": "GB/s", "h2d_bytes_per_step": n * 8,
                 "d2h_bytes_per_step": m * 8, "ms_per_step": round(e2e_s / args.steps * 1e3, 4),
                 "matches_oracle": e2e_ok, "api": "genericsparsearrays_gb300.mul_",
-                "steps_overlap": "two streams: a step's upload overlaps the previous step's download",
+                "steps_overlap": "three streams and buffer sets: upload, product and download of consecutive steps run at once",
                 "sequential": {"value": round(nbytes * args.steps / e2e_seq_s / 1e9, 2),
                                "ms_per_step": round(e2e_seq_s / args.steps * 1e3, 4)}},
         "gpu_launches": args.steps,  # one rowblock_kernel per SpMV
