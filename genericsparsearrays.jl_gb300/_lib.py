@@ -62,6 +62,10 @@ SIGNATURES = {
     "gsa_coo_sum_count": ([_vp, _i32, _i32, _i64, _i64, _i64, _vp, _vp, _vp, _i32, _i64, _vp, _vp, _vp, _i32,
                            _i64, _vp, _i32, _vp, _sz, ctypes.POINTER(_i64)], _i32),
     "gsa_coo_sum_copy": ([_vp, _i32, _i32, _i64, _i64, _i64, _i64, _i32, _vp, _vp, _vp, _vp], _i32),
+    "gsa_compressed_add_workspace_size": ([_i64], _sz),
+    "gsa_compressed_add_count": ([_vp, _i32, _i64, _vp, _vp, _vp, _vp, _i32, _vp, _sz, _vp, ctypes.POINTER(_i64)], _i32),
+    "gsa_compressed_add_copy": ([_vp, _i32, _i32, _i64, _vp, _vp, _vp, _vp, _vp, _vp, _i32, _vp, _i32, _vp, _vp, _vp],
+                                _i32),
     "gsa_spgemm_create": ([_vp, _i32, _i32, _i32, _i64, _i64, _i64, _vp, _vp, _vp, _i64, _vp, _vp, _vp, _i64, _i32,
                            _vp, ctypes.POINTER(_i64), ctypes.POINTER(_vp)], _i32),
     "gsa_spgemm_compute": ([_vp, _vp, _vp, _vp], _i32),

@@ -820,16 +820,68 @@ def _coo_sum(m: int, n: int, a, op_a: int, b=None, op_b: int = _lib.OP_N, n_diag
     return GenericSparseMatrixCOO(m, n, ro, co, vo)
 
 
+def _compressed_sum(A, B=None, negate_b=False, lam=None):
+    """A + B (two unwrapped CSR or two CSC matrices; dropzeros after, as the reference) or
+    A + lam*I (B None; no dropzeros), through gsa_compressed_add_count / _copy."""
+    csr = isinstance(A, GenericSparseMatrixCSR)
+    cls = type(A)
+    it, dev = A.itype, A.device
+    outer = A.m if csr else A.n
+    pa, ia = (A.rowptr, A.colval) if csr else (A.colptr, A.rowval)
+    if B is not None:
+        dtype = torch.promote_types(A.dtype, B.dtype)
+        pb, ib = (B.rowptr, B.colval) if csr else (B.colptr, B.rowval)
+        pb, ib, vb = pb.to(it), ib.to(it), B.nzval.to(dtype)
+        lam_buf = None
+    else:
+        dtype = torch.result_type(A.nzval, lam)
+        pb = ib = vb = None
+        lam_buf = _scalar_buf(lam, dtype)
+    va = A.nzval.to(dtype)
+    lib = _lib.load()
+    ws = torch.empty(max(lib.gsa_compressed_add_workspace_size(outer), 1), dtype=torch.uint8, device=dev)
+    ptr = torch.empty(outer + 1, dtype=it, device=dev)
+    cnt = ctypes.c_int64(0)
+    stream = _stream_ptr(dev)
+    with torch.cuda.device(dev):
+        _lib.check(lib.gsa_compressed_add_count(stream, _ITYPE[it], outer, _ptr(pa), _ptr(ia), _ptr(pb), _ptr(ib),
+                                                BASE, _ptr(ws), ws.numel(), _ptr(ptr), ctypes.byref(cnt)))
+        idx = torch.empty(cnt.value, dtype=it, device=dev)
+        val = torch.empty(cnt.value, dtype=dtype, device=dev)
+        _lib.check(lib.gsa_compressed_add_copy(
+            stream, _DTYPE[dtype], _ITYPE[it], outer, _ptr(pa), _ptr(ia), _ptr(va), _ptr(pb), _ptr(ib), _ptr(vb),
+            1 if negate_b else 0, lam_buf.ctypes.data_as(ctypes.c_void_p) if lam_buf is not None else None, BASE,
+            _ptr(ws), _ptr(idx), _ptr(val)))
+    C = cls(A.m, A.n, ptr, idx, val)
+    return dropzeros(C) if B is not None else C
+
+
+def _neg_copy(X):
+    """-X for an unwrapped sparse matrix (Base.:-, src/matrix_csr/matrix_csr.jl:88-90)."""
+    return _same_structure(X, -X.nzval)
+
+
 def _sparse_add(A, B, negate_b: bool):
-    """Sparse + sparse and sparse + λI (src/matrix_coo/matrix_coo.jl:300-575)."""
+    """Sparse + sparse and sparse + λI (src/matrix_coo/matrix_coo.jl:300-575,
+    src/matrix_csr/matrix_csr.jl:290-458, src/matrix_csc/matrix_csc.jl:292-460)."""
     if isinstance(B, UniformScaling) or isinstance(A, UniformScaling):
         if isinstance(A, UniformScaling):  # J + A, J - A
             J, X, neg_x, neg_j = A, B, negate_b, False
         else:
             J, X, neg_x, neg_j = B, A, False, negate_b
+        if isinstance(X, (GenericSparseMatrixCSR, GenericSparseMatrixCSC)):
+            if X.m != X.n:
+                raise DimensionMismatch("Matrix must be square to add UniformScaling.")
+            lam = -J.lam if neg_j else J.lam
+            Y = _neg_copy(X) if neg_x else X  # J - X = (-X) + J (src/core.jl:89,94)
+            if lam == 0:  # iszero(λ) && return copy(A)
+                return _same_structure(Y, Y.nzval.to(torch.result_type(Y.nzval, lam)).clone())
+            if Y.device.type != "cuda":
+                raise ArgumentError("sparse addition runs on the GPU only; adapt the matrix to CUDA first")
+            return _compressed_sum(Y, lam=lam)
         op = _coo_operand(X)
         if op is None:
-            raise ArgumentError("sparse + UniformScaling is provided for GenericSparseMatrixCOO")
+            raise ArgumentError("sparse + UniformScaling is provided for unwrapped CSR / CSC and COO matrices")
         P, code = op
         m, n = X.shape
         if m != n:
@@ -842,9 +894,30 @@ def _sparse_add(A, B, negate_b: bool):
         if P.device.type != "cuda":
             raise ArgumentError("sparse addition runs on the GPU only; adapt the matrix to CUDA first")
         return _coo_sum(m, n, P, code | (_lib.SUM_NEGATE if neg_x else 0), n_diag=n, lam=lam, dtype=dtype)
+    if not _is_sparse_operand(A) or not _is_sparse_operand(B):
+        raise ArgumentError("A and B must be sparse matrices (or their transposes)")
+    PA = A.parent if isinstance(A, Transpose) else A
+    PB = B.parent if isinstance(B, Transpose) else B
+    if isinstance(PA, (GenericSparseMatrixCSR, GenericSparseMatrixCSC)):
+        if tuple(A.shape) != tuple(B.shape):
+            raise DimensionMismatch(f"dimensions must match: A has dims ({A.shape[0]}, {A.shape[1]}), B has dims "
+                                    f"({B.shape[0]}, {B.shape[1]})")
+        if PA.device != PB.device:
+            raise ArgumentError("Both matrices must have the same backend")
+        if type(PA) is not type(PB):
+            raise ArgumentError(f"no method for {type(PA).__name__} + {type(PB).__name__}")
+        if PA.device.type != "cuda":
+            raise ArgumentError("sparse addition runs on the GPU only; adapt the matrices to CUDA first")
+        if not isinstance(A, Transpose) and not isinstance(B, Transpose):
+            return _compressed_sum(A, B, negate_b)
+        # transposed / adjoint pairs: to the other compressed format, add, convert back
+        # (src/matrix_csr/matrix_csr.jl:405-436, src/matrix_csc/matrix_csc.jl:410-442)
+        cls, other = type(PA), (GenericSparseMatrixCSC if isinstance(PA, GenericSparseMatrixCSR)
+                                else GenericSparseMatrixCSR)
+        return cls(_compressed_sum(other(A), other(B), negate_b))
     oa, ob = _coo_operand(A), _coo_operand(B)
     if oa is None or ob is None:
-        raise ArgumentError("sparse + sparse is provided for GenericSparseMatrixCOO (and its transposes)")
+        raise ArgumentError("sparse + sparse needs two matrices of one format")
     if tuple(A.shape) != tuple(B.shape):
         raise DimensionMismatch(f"dimensions must match: A has dims ({A.shape[0]}, {A.shape[1]}), B has dims "
                                 f"({B.shape[0]}, {B.shape[1]})")

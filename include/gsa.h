@@ -192,6 +192,29 @@ int gsa_coo_sum_count(void *stream, int dtype, int itype, int64_t m, int64_t n, 
 int gsa_coo_sum_copy(void *stream, int dtype, int itype, int64_t m, int64_t n, int64_t total, int64_t kept,
                      int base, const void *workspace, void *rowind_out, void *colind_out, void *nzval_out);
 
+/* Sums of compressed matrices of one format -- Base.:+ for two GenericSparseMatrixCSR
+ * (src/matrix_csr/matrix_csr.jl:290-356, kernels kernel_count_nnz_per_row_csr! /
+ * kernel_merge_csr! at src/matrix_csr/matrix_csr_kernels.jl:146-248) or two
+ * GenericSparseMatrixCSC (src/matrix_csc/matrix_csc.jl:292-357), and A + λI
+ * (src/matrix_csr/matrix_csr.jl:358-402, kernels kernel_count_diag_entries_csr! /
+ * kernel_add_uniformscaling_csr! at src/matrix_csr/matrix_csr_kernels.jl:446-507; CSC alike).
+ * Per outer entry (row of CSR, column of CSC) the reference's sequential walk: for A + B a
+ * two-pointer merge of the stored entries in storage order, equal indices summed a + b (the
+ * reference then drops zeros: gsa_dropzeros_* on the result); for A + λI (ptr_b = idx_b = NULL)
+ * one more entry where no diagonal is stored, λ added to every stored diagonal and inserted
+ * before the first larger index.  Two calls on ONE workspace of
+ * gsa_compressed_add_workspace_size(outer_n) bytes: _count writes the result's pointer array
+ * ptr_c (outer_n + 1, same base) and returns its entry count (synchronizes the stream); _copy
+ * writes idx_c / val_c.  negate_b: B's values negated (A - B = A + (-B)).  lambda: host pointer
+ * to one value of the dtype (A + λI only). */
+size_t gsa_compressed_add_workspace_size(int64_t outer_n);
+int gsa_compressed_add_count(void *stream, int itype, int64_t outer_n, const void *ptr_a, const void *idx_a,
+                             const void *ptr_b, const void *idx_b, int base, void *workspace, size_t workspace_bytes,
+                             void *ptr_c, int64_t *nnz_c);
+int gsa_compressed_add_copy(void *stream, int dtype, int itype, int64_t outer_n, const void *ptr_a, const void *idx_a,
+                            const void *val_a, const void *ptr_b, const void *idx_b, const void *val_b, int negate_b,
+                            const void *lambda, int base, const void *workspace, void *idx_c, void *val_c);
+
 /* Sparse x sparse product C = A * B (SpGEMM) -- Base.:* for two GenericSparseMatrixCSR
  * (src/matrix_csr/matrix_csr.jl:498-556, kernels kernel_count_nnz_spgemm_csr! /
  * kernel_spgemm_csr! at src/matrix_csr/matrix_csr_kernels.jl:250-343) or two

@@ -336,6 +336,20 @@ int oracle_spgemm(int fmt, int dtype, int itype, int64_t m, int64_t kk, int64_t 
     DISPATCH(spgemm, fmt, m, kk, n, pa, ia, va, pb, ib, vb, base, ptr_out, idx_out, val_out, cap, nnz_out)
 }
 
+int oracle_compressed_add(int dtype, int itype, int64_t outer_n, const void *pa, const void *ia, const void *va,
+                          const void *pb, const void *ib, const void *vb, int neg_b, int base, void *ptr_out,
+                          void *idx_out, void *val_out, int64_t *nnz_out) {
+    if (dtype < 0 || dtype > 5 || itype < 0 || itype > 1) return 3;
+    DISPATCH(compressed_add, outer_n, pa, ia, va, pb, ib, vb, neg_b, base, ptr_out, idx_out, val_out, nnz_out)
+}
+
+int oracle_compressed_add_diag(int dtype, int itype, int64_t n, const void *pa, const void *ia, const void *va,
+                               const void *lam, int base, void *ptr_out, void *idx_out, void *val_out,
+                               int64_t *nnz_out) {
+    if (dtype < 0 || dtype > 5 || itype < 0 || itype > 1) return 3;
+    DISPATCH(compressed_add_diag, n, pa, ia, va, lam, base, ptr_out, idx_out, val_out, nnz_out)
+}
+
 int oracle_max_threads(void) {
 #ifdef _OPENMP
     return omp_get_max_threads();

@@ -432,6 +432,94 @@ static int FN(spgemm)(int fmt, int64_t m, int64_t kk, int64_t n, const void *pav
     return 0;
 }
 
+/* Sum of two compressed matrices of one format, following kernel_count_nnz_per_row_csr! and
+ * kernel_merge_csr! (src/matrix_csr/matrix_csr_kernels.jl:146-248; the CSC kernels at
+ * src/matrix_csc/matrix_csc_kernels.jl:146-250) inside Base.:+ (src/matrix_csr/matrix_csr.jl:
+ * 290-356, src/matrix_csc/matrix_csc.jl:292-357): per outer entry a two-pointer walk over A's and
+ * B's stored entries in storage order -- the smaller index first, equal indices summed a + b --
+ * then dropzeros.  neg_b negates B's values (A - B = A + (-B), src/core.jl:91).  Outputs have
+ * room for nnz_a + nnz_b entries. */
+static int FN(compressed_add)(int64_t outer_n, const void *pav, const void *iav, const void *vav, const void *pbv,
+                              const void *ibv, const void *vbv, int neg_b, int base, void *ptr_outv, void *idx_outv,
+                              void *val_outv, int64_t *nnz_out) {
+    const I *pa = (const I *)pav, *ia = (const I *)iav, *pb = (const I *)pbv, *ib = (const I *)ibv;
+    const V *va = (const V *)vav, *vb = (const V *)vbv;
+    I *ptr_out = (I *)ptr_outv, *idx_out = (I *)idx_outv;
+    V *val_out = (V *)val_outv;
+    int64_t w = 0;
+    for (int64_t o = 0; o < outer_n; ++o) {
+        ptr_out[o] = (I)(w + base);
+        int64_t a = (int64_t)pa[o] - base, ae = (int64_t)pa[o + 1] - base;
+        int64_t b = (int64_t)pb[o] - base, be = (int64_t)pb[o + 1] - base;
+        while (a < ae || b < be) {
+            I idx;
+            V v;
+            if (a < ae && b < be && ia[a] == ib[b]) {
+                idx = ia[a];
+                v = V_ADD(va[a], neg_b ? V_NEG(vb[b]) : vb[b]);
+                ++a; ++b;
+            } else if (b >= be || (a < ae && ia[a] < ib[b])) {
+                idx = ia[a]; v = va[a]; ++a;
+            } else {
+                idx = ib[b]; v = neg_b ? V_NEG(vb[b]) : vb[b]; ++b;
+            }
+            if (V_IS_ZERO(v)) continue;  /* dropzeros */
+            idx_out[w] = idx;
+            val_out[w] = v;
+            ++w;
+        }
+    }
+    ptr_out[outer_n] = (I)(w + base);
+    *nnz_out = w;
+    return 0;
+}
+
+/* A + lambda*I for a square compressed matrix, following kernel_count_diag_entries_csr! and
+ * kernel_add_uniformscaling_csr! (src/matrix_csr/matrix_csr_kernels.jl:446-507; the CSC kernels
+ * at src/matrix_csc/matrix_csc_kernels.jl:446-510) inside Base.:+ (src/matrix_csr/matrix_csr.jl:
+ * 358-402): an outer entry without a stored diagonal gets one more entry; the walk copies the
+ * entries, adds lambda to every stored diagonal, and inserts (o, lambda) before the first entry
+ * past the diagonal or at the end.  No dropzeros.  Writes stay inside each entry's counted room
+ * (the reference writes past it for a row whose diagonal follows a larger index). */
+static int FN(compressed_add_diag)(int64_t n, const void *pav, const void *iav, const void *vav, const void *lamv,
+                                   int base, void *ptr_outv, void *idx_outv, void *val_outv, int64_t *nnz_out) {
+    const I *pa = (const I *)pav, *ia = (const I *)iav;
+    const V *va = (const V *)vav;
+    const V lam = *(const V *)lamv;
+    I *ptr_out = (I *)ptr_outv, *idx_out = (I *)idx_outv;
+    V *val_out = (V *)val_outv;
+    int64_t w0 = 0;
+    for (int64_t o = 0; o < n; ++o) {
+        const int64_t b = (int64_t)pa[o] - base, e = (int64_t)pa[o + 1] - base;
+        int found = 0;
+        for (int64_t j = b; j < e; ++j)
+            if ((int64_t)ia[j] - base == o) { found = 1; break; }
+        const int64_t end = w0 + (e - b) + (found ? 0 : 1);
+        ptr_out[o] = (I)(w0 + base);
+        int64_t w = w0;
+        int written = 0;
+        for (int64_t j = b; j < e; ++j) {
+            const int64_t col = (int64_t)ia[j] - base;
+            if (!written && col > o) {
+                if (w < end) { idx_out[w] = (I)(o + base); val_out[w] = lam; }
+                ++w;
+                written = 1;
+            }
+            if (w < end) {
+                idx_out[w] = ia[j];
+                if (col == o) { val_out[w] = V_ADD(va[j], lam); written = 1; }
+                else val_out[w] = va[j];
+            }
+            ++w;
+        }
+        if (!written && w < end) { idx_out[w] = (I)(o + base); val_out[w] = lam; }
+        w0 = end;
+    }
+    ptr_out[n] = (I)(w0 + base);
+    *nnz_out = w0;
+    return 0;
+}
+
 /* Compressed -> COO expansion: kernel_csr_to_coo! / kernel_csc_to_coo!
  * (src/conversions/conversion_kernels.jl:2-35).  Every stored entry of outer
  * o gets major index o (in the index base); minor indices and values copy. */

@@ -79,8 +79,13 @@ def lib():
                                          i64, vp, i32, vp, vp, vp, ctypes.POINTER(i64)]
             L.oracle_spgemm.argtypes = [i32, i32, i32, i64, i64, i64, vp, vp, vp, vp, vp, vp, i32, vp, vp, vp, i64,
                                         ctypes.POINTER(i64)]
+            L.oracle_compressed_add.argtypes = [i32, i32, i64, vp, vp, vp, vp, vp, vp, i32, i32, vp, vp, vp,
+                                                ctypes.POINTER(i64)]
+            L.oracle_compressed_add_diag.argtypes = [i32, i32, i64, vp, vp, vp, vp, i32, vp, vp, vp,
+                                                     ctypes.POINTER(i64)]
             for f in ("oracle_mul", "oracle_mul_exact", "oracle_coo_to_compressed", "oracle_compressed_to_coo",
-                      "oracle_max_threads", "oracle_dot", "oracle_coo_sum", "oracle_spgemm"):
+                      "oracle_max_threads", "oracle_dot", "oracle_coo_sum", "oracle_spgemm", "oracle_compressed_add",
+                      "oracle_compressed_add_diag"):
                 getattr(L, f).restype = ctypes.c_int
             _lib = L
     return _lib
@@ -285,6 +290,41 @@ def spgemm(fmt, m, kk, n, a, b, base=1):
     rc = lib().oracle_spgemm(*args, _p(ptr), _p(idx), _p(val), idx.size, ctypes.byref(cnt))
     if rc != 0:
         raise RuntimeError(f"oracle_spgemm failed: {rc}")
+    return ptr, idx[:cnt.value].copy(), val[:cnt.value].copy()
+
+
+def compressed_add(outer_n, a, b, neg_b=False, base=1):
+    """CSR + CSR (or CSC + CSC) as the reference computes it: a, b = (ptr, idx, val); the
+    result's (ptr, idx, val) after dropzeros."""
+    pa, ia, va = (np.ascontiguousarray(x) for x in a)
+    pb, ib, vb = (np.ascontiguousarray(x) for x in b)
+    ia, pb, ib = ia.astype(pa.dtype, copy=False), pb.astype(pa.dtype, copy=False), ib.astype(pa.dtype, copy=False)
+    vb = vb.astype(va.dtype, copy=False)
+    ptr = np.empty(outer_n + 1, dtype=pa.dtype)
+    idx = np.empty(max(va.size + vb.size, 1), dtype=pa.dtype)
+    val = np.empty(max(va.size + vb.size, 1), dtype=va.dtype)
+    cnt = ctypes.c_int64(0)
+    rc = lib().oracle_compressed_add(DTYPE[va.dtype], ITYPE[pa.dtype], outer_n, _p(pa), _p(ia), _p(va), _p(pb),
+                                     _p(ib), _p(vb), 1 if neg_b else 0, base, _p(ptr), _p(idx), _p(val),
+                                     ctypes.byref(cnt))
+    if rc != 0:
+        raise RuntimeError(f"oracle_compressed_add failed: {rc}")
+    return ptr, idx[:cnt.value].copy(), val[:cnt.value].copy()
+
+
+def compressed_add_diag(n, a, lam, base=1):
+    """CSR + lam*I (or CSC + lam*I) as the reference computes it; no dropzeros."""
+    pa, ia, va = (np.ascontiguousarray(x) for x in a)
+    ia = ia.astype(pa.dtype, copy=False)
+    ptr = np.empty(n + 1, dtype=pa.dtype)
+    idx = np.empty(va.size + n + 1, dtype=pa.dtype)
+    val = np.empty(va.size + n + 1, dtype=va.dtype)
+    lv = np.array([lam], dtype=va.dtype)
+    cnt = ctypes.c_int64(0)
+    rc = lib().oracle_compressed_add_diag(DTYPE[va.dtype], ITYPE[pa.dtype], n, _p(pa), _p(ia), _p(va), _p(lv), base,
+                                          _p(ptr), _p(idx), _p(val), ctypes.byref(cnt))
+    if rc != 0:
+        raise RuntimeError(f"oracle_compressed_add_diag failed: {rc}")
     return ptr, idx[:cnt.value].copy(), val[:cnt.value].copy()
 
 

@@ -206,3 +206,94 @@ def test_coo_sum_empty(gsa, cuda):
     D = A + gsa.I
     r, c, v = _coo_tuple(D)
     assert r.tolist() == [1, 2, 3, 4] and c.tolist() == [1, 2, 3, 4] and v.tolist() == [1.0] * 4
+
+
+# ---------------------------------------------------------------------------
+# CSR + CSR, CSC + CSC (src/matrix_csr/matrix_csr.jl:290-356 and the CSC method) and
+# A + λI (:358-402): the reference's per-row walks, bit-exact against the oracle.
+
+def _cmp(C, want, csr):
+    ptr, idx = (C.rowptr, C.colval) if csr else (C.colptr, C.rowval)
+    _assert_same((ptr.cpu().numpy(), idx.cpu().numpy(), C.nzval.cpu().numpy()), want)
+
+
+@pytest.mark.parametrize("fmt", ["csr", "csc"])
+@pytest.mark.parametrize("it", INDEX_TYPES)
+@pytest.mark.parametrize("dt", VALUE_TYPES)
+def test_compressed_plus_compressed(gsa, cuda, oracle, fmt, it, dt):
+    rng = np.random.default_rng(31)
+    m, n = 60, 45
+    SA, SB = sprand(rng, m, n, 0.1, dt), sprand(rng, m, n, 0.15, dt)
+    a, b = parts(SA, fmt, it), parts(SB, fmt, it)
+    cls = gsa.GenericSparseMatrixCSR if fmt == "csr" else gsa.GenericSparseMatrixCSC
+    A, B = gsa.adapt(cuda, cls(m, n, *a)), gsa.adapt(cuda, cls(m, n, *b))
+    outer = m if fmt == "csr" else n
+    C = A + B
+    assert isinstance(C, cls) and C.shape == (m, n)
+    _cmp(C, oracle.compressed_add(outer, a, b), fmt == "csr")
+    _cmp(A - B, oracle.compressed_add(outer, a, b, neg_b=True), fmt == "csr")
+    assert gsa.nnz(A - A) == 0
+
+
+@pytest.mark.parametrize("fmt", ["csr", "csc"])
+def test_compressed_sum_unsorted_duplicates(gsa, cuda, oracle, fmt):
+    """Rows in shuffled order with repeated indices: the two-pointer walk's own result."""
+    rng = np.random.default_rng(32)
+    m = n = 40
+    def messy(S):
+        p, i, v = parts(S, fmt, np.int64)
+        pi, vi, pp = [], [], [1]
+        for r in range(p.size - 1):
+            ii, vv = i[p[r] - 1:p[r + 1] - 1].copy(), v[p[r] - 1:p[r + 1] - 1].copy()
+            if r % 4 == 0 and ii.size:
+                ii, vv = np.append(ii, ii[-1]), np.append(vv, 1.5)
+            q = rng.permutation(ii.size)
+            pi.append(ii[q]); vi.append(vv[q]); pp.append(pp[-1] + ii.size)
+        return np.array(pp, np.int64), np.concatenate(pi), np.concatenate(vi)
+    a, b = messy(sprand(rng, m, n, 0.15, np.float64)), messy(sprand(rng, m, n, 0.15, np.float64))
+    cls = gsa.GenericSparseMatrixCSR if fmt == "csr" else gsa.GenericSparseMatrixCSC
+    C = gsa.adapt(cuda, cls(m, n, *a)) + gsa.adapt(cuda, cls(m, n, *b))
+    _cmp(C, oracle.compressed_add(m, a, b), fmt == "csr")
+
+
+@pytest.mark.parametrize("fmt", ["csr", "csc"])
+@pytest.mark.parametrize("op_a", ["N", "T", "C"])
+@pytest.mark.parametrize("op_b", ["N", "T", "C"])
+def test_compressed_sum_transposes(gsa, cuda, fmt, op_a, op_b):
+    rng = np.random.default_rng(33)
+    n = 35
+    dt = np.complex128
+    SA, SB = sprand(rng, n, n, 0.15, dt), sprand(rng, n, n, 0.15, dt)
+    cls = gsa.GenericSparseMatrixCSR if fmt == "csr" else gsa.GenericSparseMatrixCSC
+    A = gsa.adapt(cuda, cls(n, n, *parts(SA, fmt, np.int64)))
+    B = gsa.adapt(cuda, cls(n, n, *parts(SB, fmt, np.int64)))
+    wrap = {"N": lambda X: X, "T": gsa.transpose, "C": gsa.adjoint}
+    op = {"N": lambda S: S, "T": lambda S: S.T, "C": lambda S: S.conj().T}
+    C = wrap[op_a](A) + wrap[op_b](B)
+    assert isinstance(C, cls)
+    want = (op[op_a](SA) + op[op_b](SB)).toarray()
+    assert np.allclose(gsa.collect(C), want, rtol=0, atol=1e-14)
+    D = wrap[op_a](A) - wrap[op_b](B)
+    assert np.allclose(gsa.collect(D), (op[op_a](SA) - op[op_b](SB)).toarray(), rtol=0, atol=1e-14)
+
+
+@pytest.mark.parametrize("fmt", ["csr", "csc"])
+@pytest.mark.parametrize("dt", VALUE_TYPES)
+def test_compressed_plus_uniform_scaling(gsa, cuda, oracle, fmt, dt):
+    rng = np.random.default_rng(34)
+    n = 50
+    S = sprand(rng, n, n, 0.1, dt).tolil()
+    for r in (3, 7, 8, 9):  # rows without a stored diagonal get one more entry
+        S[r, r] = 0
+    S = S.tocsr()
+    a = parts(S, fmt, np.int64)
+    cls = gsa.GenericSparseMatrixCSR if fmt == "csr" else gsa.GenericSparseMatrixCSC
+    A = gsa.adapt(cuda, cls(n, n, *a))
+    lam = {np.dtype(np.complex64): 2 + 1j, np.dtype(np.complex128): 2 + 1j}.get(np.dtype(dt), 3)
+    _cmp(A + lam * gsa.I, oracle.compressed_add_diag(n, a, lam), fmt == "csr")
+    _cmp(gsa.I + A, oracle.compressed_add_diag(n, a, 1), fmt == "csr")
+    _cmp(A - lam * gsa.I, oracle.compressed_add_diag(n, a, -lam), fmt == "csr")
+    neg = (a[0], a[1], -a[2])
+    _cmp(lam * gsa.I - A, oracle.compressed_add_diag(n, neg, lam), fmt == "csr")
+    Z = A + 0 * gsa.I
+    _cmp(Z, a, fmt == "csr")

@@ -187,8 +187,13 @@ def test_sparse_add_checks_match_reference_order(gsa):
     with pytest.raises(gsa.ArgumentError, match="GPU only"):
         A + gsa.GenericSparseMatrixCOO(6, 5, e, e, np.zeros(0))
     C = gsa.GenericSparseMatrixCSR(6, 5, np.ones(7, np.int64), e, np.zeros(0))
-    with pytest.raises(gsa.ArgumentError, match="GenericSparseMatrixCOO"):
+    K = gsa.GenericSparseMatrixCSC(6, 5, np.ones(6, np.int64), e, np.zeros(0))
+    with pytest.raises(gsa.ArgumentError, match="GPU only"):
         C + C
+    with pytest.raises(gsa.ArgumentError, match="no method"):
+        C + K
+    with pytest.raises(gsa.DimensionMismatch, match="square"):
+        C + gsa.I
     # iszero(λ) returns a copy without touching the device: op(A) with the promoted type
     Sq = gsa.GenericSparseMatrixCOO(3, 3, np.array([1, 1]), np.array([2, 2]), np.array([1.0, 0.0]))
     Z = Sq + 0 * gsa.I
