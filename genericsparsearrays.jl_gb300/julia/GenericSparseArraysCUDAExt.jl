@@ -335,4 +335,41 @@ function Base.:+(A::COOCu{T, Ti}, J::UniformScaling{T}) where {T <: GSAValue, Ti
     return _coo_sum(m, n, A, Cint(0), nothing, Cint(0), n, J.λ)
 end
 
+# CSR + CSR, CSC + CSC (src/matrix_csr/matrix_csr.jl:290-356, then dropzeros) and A + λI
+# (:358-402): the reference's per-row walks, counted, scanned and written on the GPU.
+function _compressed_sum(A::Union{CSRCu{T, Ti}, CSCCu{T, Ti}}, B, λ) where {T, Ti}
+    csr = A isa GenericSparseMatrixCSR
+    outer = csr ? size(A, 1) : size(A, 2)
+    pa, ia = _ptrs(A)
+    pb, ib = B === nothing ? (CU_NULL, CU_NULL) : _ptrs(B)
+    ws = CuVector{UInt8}(undef, ccall((:gsa_compressed_add_workspace_size, libgsa), Csize_t, (Int64,), outer))
+    ptr = CuVector{Ti}(undef, outer + 1)
+    cnt = Ref{Int64}(0)
+    gsa_check(ccall((:gsa_compressed_add_count, libgsa), Cint,
+        (CUstream, Cint, Int64, CuPtr{Ti}, CuPtr{Ti}, CuPtr{Ti}, CuPtr{Ti}, Cint, CuPtr{UInt8}, Csize_t, CuPtr{Ti},
+         Ref{Int64}), CUDA.stream(), gsa_itype(Ti), outer, pa, ia, pb, ib, Cint(1), ws, length(ws), ptr, cnt))
+    idx = CuVector{Ti}(undef, cnt[]); val = CuVector{T}(undef, cnt[])
+    gsa_check(ccall((:gsa_compressed_add_copy, libgsa), Cint,
+        (CUstream, Cint, Cint, Int64, CuPtr{Ti}, CuPtr{Ti}, CuPtr{T}, CuPtr{Ti}, CuPtr{Ti}, CuPtr{T}, Cint,
+         Ptr{T}, Cint, CuPtr{UInt8}, CuPtr{Ti}, CuPtr{T}),
+        CUDA.stream(), gsa_dtype(T), gsa_itype(Ti), outer, pa, ia, A.nzval, pb, ib,
+        B === nothing ? CU_NULL : B.nzval, Cint(0), λ === nothing ? C_NULL : Ref(T(λ)), Cint(1), ws, idx, val))
+    C = (csr ? GenericSparseMatrixCSR : GenericSparseMatrixCSC)(size(A)..., ptr, idx, val)
+    return B === nothing ? C : dropzeros(C)
+end
+
+for Fmt in (:CSRCu, :CSCCu)
+    @eval function Base.:+(A::$Fmt{T, Ti}, B::$Fmt{T, Ti}) where {T <: GSAValue, Ti <: GSAIndex}
+        size(A) == size(B) || throw(DimensionMismatch(
+            "dimensions must match: A has dims $(size(A)), B has dims $(size(B))"))
+        return _compressed_sum(A, B, nothing)
+    end
+    @eval function Base.:+(A::$Fmt{T, Ti}, J::UniformScaling{T}) where {T <: GSAValue, Ti <: GSAIndex}
+        m, n = size(A)
+        m == n || throw(DimensionMismatch("Matrix must be square to add UniformScaling."))
+        iszero(J.λ) && return copy(A)
+        return _compressed_sum(A, nothing, J.λ)
+    end
+end
+
 end # module
