@@ -255,14 +255,23 @@ coarse_place_kernel(Src src, const VT *__restrict__ vals_in, int64_t nnz, int64_
         uint32_t packed[PB_ITEMS];  // bucket << 16 | rank in the tile's run
         uint64_t key[PB_ITEMS];     // row in the bucket << (mb + pb) | minor << pb | position
         typename std::conditional<HAS_VAL, VT, char>::type val[PB_ITEMS];
+        int64_t mjs[PB_ITEMS], mns[PB_ITEMS];
+        // all loads first, so that they are in flight together (the shared-memory atomics below
+        // would otherwise keep each entry's loads behind the previous entry's atomic)
 #pragma unroll
         for (int q = 0; q < PB_ITEMS; ++q) {
             const int64_t e = t0 + (int64_t)q * PB_THREADS + threadIdx.x;
-            int64_t mj = -1, mn = 0;
+            mjs[q] = -1;
+            mns[q] = 0;
             if (e < nnz) {
-                src.get(e, mj, mn);
+                src.get(e, mjs[q], mns[q]);
                 if constexpr (HAS_VAL) val[q] = vals_in[e];
             }
+        }
+#pragma unroll
+        for (int q = 0; q < PB_ITEMS; ++q) {
+            const int64_t e = t0 + (int64_t)q * PB_THREADS + threadIdx.x;
+            const int64_t mj = mjs[q], mn = mns[q];
             const bool in = (uint64_t)mj < (uint64_t)major_n;
             const uint32_t d = (uint32_t)(in ? mj >> cs : nb - 1);
             const uint64_t lrow = in ? (uint64_t)(mj - ((int64_t)d << cs)) : 0;
