@@ -104,3 +104,41 @@ def test_dot_argument_checks(lib, gsa):
     assert lib.gsa_dot_workspace_size(2, 1, 0, 10, 10, None) > 0
     assert lib.gsa_dot_workspace_size(0, 3, 1, 1000, 10, None) >= (1000 // 128 + 1) * 4 * 16
     assert lib.gsa_dot_workspace_size(5, 1, 0, 10, 10, None) == 0
+
+
+def test_sum_and_spgemm_argument_checks(lib, gsa):
+    """The COO sum, compressed sum and SpGEMM entry points refuse bad arguments before any
+    device work (no GPU needed)."""
+    L = gsa._lib
+    fake = ctypes.c_void_p(8 * 4096)  # never dereferenced: the checks fail first
+    kept = ctypes.c_int64(0)
+    lam = np.ones(1).ctypes.data_as(ctypes.c_void_p)
+    # COO sum: bad op code, n_diag beyond min(m, n), lambda missing, unsupported dtype
+    assert lib.gsa_coo_sum_count(None, 1, 1, 4, 4, 1, fake, fake, fake, 7, 0, None, None, None, 0, 0, None, 1,
+                                 fake, 1 << 20, ctypes.byref(kept)) == L.ERR_INVALID_ARG
+    assert lib.gsa_coo_sum_count(None, 1, 1, 4, 3, 0, None, None, None, 0, 0, None, None, None, 0, 4, lam, 1,
+                                 fake, 1 << 20, ctypes.byref(kept)) == L.ERR_DIM
+    assert lib.gsa_coo_sum_count(None, 1, 1, 4, 4, 0, None, None, None, 0, 0, None, None, None, 0, 4, None, 1,
+                                 fake, 1 << 20, ctypes.byref(kept)) == L.ERR_INVALID_ARG
+    assert lib.gsa_coo_sum_count(None, 9, 1, 4, 4, 0, None, None, None, 0, 0, None, None, None, 0, 0, None, 1,
+                                 fake, 1 << 20, ctypes.byref(kept)) == L.ERR_UNSUPPORTED
+    assert lib.gsa_coo_sum_copy(None, 1, 1, 4, 4, 3, 5, 1, fake, None, None, None) == L.ERR_INVALID_ARG  # kept > total
+    assert lib.gsa_coo_sum_workspace_size(1, 4, 4, 10) > 0 and lib.gsa_coo_sum_workspace_size(9, 4, 4, 10) == 0
+    # compressed sum: NULL pointers, a workspace too small, no B and no lambda
+    nnz = ctypes.c_int64(0)
+    assert lib.gsa_compressed_add_count(None, 1, 4, None, None, None, None, 1, fake, 1 << 20, fake,
+                                        ctypes.byref(nnz)) == L.ERR_INVALID_ARG
+    assert lib.gsa_compressed_add_count(None, 1, 1000, fake, fake, fake, fake, 1, fake, 16, fake,
+                                        ctypes.byref(nnz)) == L.ERR_INVALID_ARG
+    assert lib.gsa_compressed_add_copy(None, 1, 1, 4, fake, fake, fake, None, None, None, 0, None, 1, fake, fake,
+                                       fake) == L.ERR_INVALID_ARG
+    assert lib.gsa_compressed_add_workspace_size(1000) >= 2 * 1001 * 4
+    # SpGEMM: bad format, NULL handle, negative size; destroy(NULL) is a no-op
+    h = ctypes.c_void_p(0)
+    args = (fake, fake, fake, 4, fake, fake, fake, 4, 1, fake, ctypes.byref(nnz), ctypes.byref(h))
+    assert lib.gsa_spgemm_create(None, 2, 1, 1, 4, 4, 4, *args) == L.ERR_INVALID_ARG
+    assert lib.gsa_spgemm_create(None, 0, 1, 1, -4, 4, 4, *args) == L.ERR_INVALID_ARG
+    assert lib.gsa_spgemm_create(None, 0, 9, 1, 4, 4, 4, *args) == L.ERR_UNSUPPORTED
+    assert h.value is None
+    assert lib.gsa_spgemm_compute(None, None, fake, fake) == L.ERR_INVALID_ARG
+    assert lib.gsa_spgemm_destroy(None) == 0
