@@ -240,6 +240,12 @@ class GenericSparseMatrixCOO(AbstractGenericSparseMatrix):
         return f"GenericSparseMatrixCOO({self.m}x{self.n}, nnz={nnz(self)}, {self.dtype}, {self.device})"
 
 
+# the three array fields of each format
+_FIELDS = {GenericSparseMatrixCSR: ("rowptr", "colval", "nzval"),
+           GenericSparseMatrixCSC: ("colptr", "rowval", "nzval"),
+           GenericSparseMatrixCOO: ("rowind", "colind", "nzval")}
+
+
 # ---------------------------------------------------------------------------
 # Lazy Transpose / Adjoint wrappers (LinearAlgebra.Transpose / Adjoint)
 
@@ -301,6 +307,18 @@ def _conj_copy(p):
         return p.conj().resolve_conj()
     q = _same_structure(p, p.nzval.conj().resolve_conj())
     return q
+
+
+def _owned(cls, m, n, p0, p1, val):
+    """A matrix that takes ownership of arrays the library has just allocated (no copy; the
+    public constructors copy, as the reference's do)."""
+    X = cls.__new__(cls)
+    X.m, X.n = int(m), int(n)
+    f0, f1, f2 = _FIELDS[cls]
+    setattr(X, f0, p0.contiguous())
+    setattr(X, f1, p1.contiguous())
+    setattr(X, f2, val.contiguous())
+    return X
 
 
 def _same_structure(A, nzval):
@@ -621,7 +639,7 @@ def _spgemm(A, B):
             _lib.check(lib.gsa_spgemm_compute(stream, handle, _ptr(idx), _ptr(val)))
         finally:
             lib.gsa_spgemm_destroy(handle)
-    return cls(A.m, B.n, ptr, idx, val)
+    return _owned(cls, A.m, B.n, ptr, idx, val)
 
 
 def _sparse_mul(A, B):
@@ -750,7 +768,7 @@ def dropzeros(A):
         ov = torch.empty(k, dtype=A.dtype, device=dev)
         _lib.check(lib.gsa_dropzeros_copy(stream, fmt, _DTYPE[A.dtype], _ITYPE[it], outer, nz, _ptr(p0), _ptr(p1),
                                           _ptr(A.nzval), BASE, _ptr(ws), _ptr(o0), _ptr(o1), _ptr(ov)))
-    return type(A)(A.m, A.n, o0, o1, ov)
+    return _owned(type(A), A.m, A.n, o0, o1, ov)
 
 
 class UniformScaling:
@@ -817,7 +835,7 @@ def _coo_sum(m: int, n: int, a, op_a: int, b=None, op_b: int = _lib.OP_N, n_diag
         vo = torch.empty(k, dtype=dtype, device=dev)
         _lib.check(lib.gsa_coo_sum_copy(stream, _DTYPE[dtype], _ITYPE[it], m, n, total, k, BASE, _ptr(ws), _ptr(ro),
                                         _ptr(co), _ptr(vo)))
-    return GenericSparseMatrixCOO(m, n, ro, co, vo)
+    return _owned(GenericSparseMatrixCOO, m, n, ro, co, vo)
 
 
 def _compressed_sum(A, B=None, negate_b=False, lam=None):
@@ -852,7 +870,7 @@ def _compressed_sum(A, B=None, negate_b=False, lam=None):
             stream, _DTYPE[dtype], _ITYPE[it], outer, _ptr(pa), _ptr(ia), _ptr(va), _ptr(pb), _ptr(ib), _ptr(vb),
             1 if negate_b else 0, lam_buf.ctypes.data_as(ctypes.c_void_p) if lam_buf is not None else None, BASE,
             _ptr(ws), _ptr(idx), _ptr(val)))
-    C = cls(A.m, A.n, ptr, idx, val)
+    C = _owned(cls, A.m, A.n, ptr, idx, val)
     return dropzeros(C) if B is not None else C
 
 
@@ -1085,14 +1103,14 @@ def _convert_to(cls, A):
             r, c, v = _compressed_to_coo(A, colmajor=True)
         else:
             raise ArgumentError(f"cannot convert {type(A).__name__} to COO")
-        return GenericSparseMatrixCOO(A.m, A.n, r, c, v)
+        return _owned(GenericSparseMatrixCOO, A.m, A.n, r, c, v)
     if isinstance(A, (GenericSparseMatrixCSR, GenericSparseMatrixCSC)):
         # CSC <-> CSR through COO (conversions.jl:85-86,104-105)
         return cls(GenericSparseMatrixCOO(A))
     if isinstance(A, GenericSparseMatrixCOO):
         colmajor = cls is GenericSparseMatrixCSC
         ptr, idx, val = _coo_to_compressed(A, colmajor)  # conversions.jl:171-212 / 282-323
-        return cls(A.m, A.n, ptr, idx, val)
+        return _owned(cls, A.m, A.n, ptr, idx, val)
     raise ArgumentError(f"cannot convert {type(A).__name__} to {cls.__name__}")
 
 
