@@ -1,6 +1,6 @@
 # GenericSparseArraysCUDAExt -- CUDA package extension of GenericSparseArrays.jl that sends
-# sparse x dense mul!, three-argument dot and COO -> CSR/CSC conversion on CuArray-backed
-# matrices to libgsa
+# sparse x dense mul!, three-argument dot, COO -> CSR/CSC conversion, sparse + dense / sparse
+# sums, dropzeros and sparse x sparse products on CuArray-backed matrices to libgsa
 # (include/gsa.h).  It adds methods that are more specific than the package's generated
 # KernelAbstractions methods (src/matrix_csr/matrix_csr.jl:145-211,
 # src/matrix_csc/matrix_csc.jl:144-213, src/matrix_coo/matrix_coo.jl:155-221,
@@ -16,6 +16,7 @@ using CUDA
 using LinearAlgebra
 using GenericSparseArrays
 using GenericSparseArrays: GenericSparseMatrixCSR, GenericSparseMatrixCSC, GenericSparseMatrixCOO
+using SparseArrays: SparseArrays
 
 const libgsa = get(ENV, "GSA_LIBRARY", joinpath(@__DIR__, "..", "deps", "libgsa.so"))
 
@@ -370,6 +371,44 @@ for Fmt in (:CSRCu, :CSCCu)
         iszero(J.λ) && return copy(A)
         return _compressed_sum(A, nothing, J.λ)
     end
+end
+
+# dropzeros (src/matrix_csr/matrix_csr.jl:649-745 and the CSC / COO methods): flags, one scan,
+# a compaction; the count comes back to the host so the outputs can be allocated.
+_fmt(::GenericSparseMatrixCSR) = Cint(0)
+_fmt(::GenericSparseMatrixCSC) = Cint(1)
+_fmt(::GenericSparseMatrixCOO) = Cint(2)
+_parts(A::GenericSparseMatrixCSR) = (A.rowptr, A.colval, size(A, 1))
+_parts(A::GenericSparseMatrixCSC) = (A.colptr, A.rowval, size(A, 2))
+_parts(A::GenericSparseMatrixCOO) = (A.rowind, A.colind, 0)
+
+function SparseArrays.dropzeros(A::Union{CSRCu{T, Ti}, CSCCu{T, Ti}, COOCu{T, Ti}}) where {T <: GSAValue, Ti <: GSAIndex}
+    nz = length(A.nzval)
+    p0, p1, outer = _parts(A)
+    ws = CuVector{UInt8}(undef, ccall((:gsa_dropzeros_workspace_size, libgsa), Csize_t, (Int64,), nz))
+    kept = Ref{Int64}(0)
+    gsa_check(ccall((:gsa_dropzeros_count, libgsa), Cint, (CUstream, Cint, Int64, CuPtr{T}, CuPtr{UInt8}, Csize_t,
+                    Ref{Int64}), CUDA.stream(), gsa_dtype(T), nz, A.nzval, ws, length(ws), kept))
+    o0 = CuVector{Ti}(undef, A isa GenericSparseMatrixCOO ? kept[] : outer + 1)
+    o1 = CuVector{Ti}(undef, kept[]); ov = CuVector{T}(undef, kept[])
+    gsa_check(ccall((:gsa_dropzeros_copy, libgsa), Cint,
+        (CUstream, Cint, Cint, Cint, Int64, Int64, CuPtr{Ti}, CuPtr{Ti}, CuPtr{T}, Cint, CuPtr{UInt8}, CuPtr{Ti},
+         CuPtr{Ti}, CuPtr{T}), CUDA.stream(), _fmt(A), gsa_dtype(T), gsa_itype(Ti), outer, nz, p0, p1, A.nzval,
+        Cint(1), ws, o0, o1, ov))
+    return typeof(A).name.wrapper(size(A)..., o0, o1, ov)
+end
+
+# A + B for a dense B (src/core.jl:66-88): C = copy(B), then every stored entry added.
+function Base.:+(A::Union{CSRCu{T, Ti}, CSCCu{T, Ti}, COOCu{T, Ti}}, B::CuMatrix{T}) where {T <: GSAValue, Ti <: GSAIndex}
+    size(A) == size(B) || throw(DimensionMismatch(
+        "dimensions must match: A has dims $(size(A)), B has dims $(size(B))"))
+    C = copy(B)
+    p0, p1, _ = _parts(A)
+    gsa_check(ccall((:gsa_add_to_dense, libgsa), Cint,
+        (CUstream, Cint, Cint, Cint, Int64, Int64, Int64, CuPtr{Ti}, CuPtr{Ti}, CuPtr{T}, Cint, CuPtr{T}, Int64),
+        CUDA.stream(), _fmt(A), gsa_dtype(T), gsa_itype(Ti), size(A)..., length(A.nzval), p0, p1, A.nzval, Cint(1),
+        C, max(stride(C, 2), 1)))
+    return C
 end
 
 end # module
