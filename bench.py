@@ -127,6 +127,18 @@ class ClockSampler:
 
 # ---------------------------------------------------------------------------
 
+def replica_value(total_ms, world, nbytes, steps, device):
+    """Whole-job GB/s of `world` replicas that each ran `steps` steps of `nbytes`: all ranks'
+    bytes over the slowest rank's time (the max over ranks; weak scaling, no data exchange).
+    Returns (GB/s, max ms)."""
+    import torch
+    t = torch.tensor([float(total_ms)], dtype=torch.float64, device=device)
+    if world > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    max_ms = float(t.item())
+    return world * nbytes * steps / (max_ms / 1e3) / 1e9, max_ms
+
+
 def dist_setup():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -290,11 +302,7 @@ def run_gpu(args, world, rank, local):
         torch.cuda.synchronize()
         total_ms, kern_ms = timer.run(spmv_capi, args.steps, args.warmup, flush=True,
                                       kernel_events=True, lib=lib)
-        t_rank = torch.tensor([total_ms], dtype=torch.float64, device=dev)
-        if world > 1:
-            torch.distributed.all_reduce(t_rank, op=torch.distributed.ReduceOp.MAX)
-        max_ms = float(t_rank.item())
-        value = world * nbytes * args.steps / (max_ms / 1e3) / 1e9
+        value, max_ms = replica_value(total_ms, world, nbytes, args.steps, dev)
         kern_avg_s = kern_ms / args.steps / 1e3
         achieved = nbytes / kern_avg_s / 1e9
 
