@@ -28,6 +28,11 @@ template <typename I> using Off = typename std::make_unsigned<I>::type;
 #ifndef GSA_G1_UNROLL
 #define GSA_G1_UNROLL 4
 #endif
+// The same for rows shared by several lanes (2 measured 738 us on a 16-column F64 SpMM of the
+// 2048^2 Laplacian against 850 us with 4).
+#ifndef GSA_GN_UNROLL
+#define GSA_GN_UNROLL 2
+#endif
 
 template <typename V, typename I, int KC, int S, int U>
 __device__ __forceinline__ void accumulate_range(const CompressedArgs<V, I> &a, const DenseIn<V> &B,
@@ -94,7 +99,8 @@ __device__ __forceinline__ void warp_rows(const CompressedArgs<V, I> &a, int64_t
         V acc[KC];
 #pragma unroll
         for (int c = 0; c < KC; ++c) acc[c] = VT<V>::zero();
-        accumulate_range<V, I, KC, G, (G == 1 ? GSA_G1_UNROLL : 2)>(a, B, qb + (O)(lane % G), qe, c0, k, acc);
+        accumulate_range<V, I, KC, G, (G == 1 ? GSA_G1_UNROLL : GSA_GN_UNROLL)>(a, B, qb + (O)(lane % G), qe, c0, k,
+                                                                              acc);
         if (G > 1) {
 #pragma unroll
             for (int c = 0; c < KC; ++c) {
