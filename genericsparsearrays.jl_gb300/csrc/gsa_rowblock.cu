@@ -23,6 +23,7 @@
 // Without a plan such a row is one group's work like any other.
 //
 // Every row's summation order is fixed, so results are deterministic.
+#include <atomic>
 #include <vector>
 
 #include "gsa_rows.cuh"
@@ -207,12 +208,13 @@ int launch_rowblock(cudaStream_t s, const CompressedArgs<V, I> &a, int64_t k, De
     return check_cuda(cudaGetLastError(), "rowblock_kernel");
 }
 
-static int g_spmm_columns = 0;  // 0: by value size
-void set_spmm_columns(int c) { g_spmm_columns = c; }
-int get_spmm_columns() { return g_spmm_columns; }
-static int g_plan_order = 0;    // 0: the plan's choice, 1: natural order always
-void set_plan_natural(int v) { g_plan_order = v; }
-int get_plan_natural() { return g_plan_order; }
+// Process-wide tuning knobs: atomics, since any host thread may set them while others launch.
+static std::atomic<int> g_spmm_columns{0};  // 0: by value size
+void set_spmm_columns(int c) { g_spmm_columns.store(c, std::memory_order_relaxed); }
+int get_spmm_columns() { return g_spmm_columns.load(std::memory_order_relaxed); }
+static std::atomic<int> g_plan_order{0};    // 0: the plan's choice, 1: natural order always
+void set_plan_natural(int v) { g_plan_order.store(v, std::memory_order_relaxed); }
+int get_plan_natural() { return g_plan_order.load(std::memory_order_relaxed); }
 
 size_t rowblock_workspace_size(const Plan *plan, size_t vsize, int64_t k) {
     if (!plan || k == 0) return 0;

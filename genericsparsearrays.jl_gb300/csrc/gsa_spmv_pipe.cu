@@ -28,6 +28,7 @@
 //     fixup pass, in CTA order (no atomics)
 // Every mbarrier wait is bounded; a wait that gives up sets the device error
 // word (read by gsa_check_device_status) and the CTA returns.
+#include <atomic>
 #include <mutex>
 
 #include "gsa_internal.cuh"
@@ -387,10 +388,11 @@ __global__ void pipe_fixup_kernel(int64_t n, const int64_t *__restrict__ carry_r
     C.accumulate(r, 0, mul(sum, C.alpha));
 }
 
-// Threads per CTA of the pipelined kernel (256 or 512); settable for tuning.
-static int g_pipe_threads = 512;
-void set_pipe_threads(int t) { g_pipe_threads = (t == 256) ? 256 : 512; }
-int get_pipe_threads() { return g_pipe_threads; }
+// Threads per CTA of the pipelined kernel (256 or 512); settable for tuning from any host
+// thread, so an atomic read once per launch.
+static std::atomic<int> g_pipe_threads{512};
+void set_pipe_threads(int t) { g_pipe_threads.store(t == 256 ? 256 : 512, std::memory_order_relaxed); }
+int get_pipe_threads() { return g_pipe_threads.load(std::memory_order_relaxed); }
 
 template <typename V, typename I>
 size_t spmv_pipe_workspace_size(int64_t outer_n, int64_t nnz) {
@@ -440,7 +442,7 @@ template <typename V, typename I>
 int launch_spmv_pipe(cudaStream_t s, const CompressedArgs<V, I> &a, DenseIn<V> B, DenseOut<V> C,
                      void *ws, size_t ws_bytes) {
     if (a.outer_n == 0) return GSA_OK;
-    if (g_pipe_threads == 256) return launch_pipe_impl<V, I, 256>(s, a, B, C, ws, ws_bytes);
+    if (get_pipe_threads() == 256) return launch_pipe_impl<V, I, 256>(s, a, B, C, ws, ws_bytes);
     return launch_pipe_impl<V, I, 512>(s, a, B, C, ws, ws_bytes);
 }
 
@@ -520,7 +522,7 @@ static int launch_noalloc_impl(cudaStream_t s, const CompressedArgs<V, I> &a, De
 template <typename V, typename I>
 int launch_spmv_noalloc(cudaStream_t s, const CompressedArgs<V, I> &a, DenseIn<V> B, DenseOut<V> C) {
     if (a.outer_n == 0) return GSA_OK;
-    if (g_pipe_threads == 256) return launch_noalloc_impl<V, I, 256>(s, a, B, C);
+    if (get_pipe_threads() == 256) return launch_noalloc_impl<V, I, 256>(s, a, B, C);
     return launch_noalloc_impl<V, I, 512>(s, a, B, C);
 }
 

@@ -142,3 +142,43 @@ def test_sum_and_spgemm_argument_checks(lib, gsa):
     assert h.value is None
     assert lib.gsa_spgemm_compute(None, None, fake, fake) == L.ERR_INVALID_ARG
     assert lib.gsa_spgemm_destroy(None) == 0
+
+
+def test_tuning_knobs(lib, gsa):
+    """gsa_set_tuning / gsa_get_tuning round trip, reject bad values and keys, and stay
+    consistent when several host threads set them at once (the knobs are process-wide)."""
+    import threading
+    L = gsa._lib
+    keys = (L.TUNE_PIPE_THREADS, L.TUNE_SPMM_COLUMNS, L.TUNE_PLAN_ORDER)
+    saved = {key: lib.gsa_get_tuning(key) for key in keys}
+    try:
+        assert lib.gsa_set_tuning(L.TUNE_SPMM_COLUMNS, 4) == 0
+        assert lib.gsa_get_tuning(L.TUNE_SPMM_COLUMNS) == 4
+        assert lib.gsa_set_tuning(L.TUNE_SPMM_COLUMNS, 3) == L.ERR_INVALID_ARG
+        assert lib.gsa_get_tuning(L.TUNE_SPMM_COLUMNS) == 4
+        assert lib.gsa_set_tuning(L.TUNE_PLAN_ORDER, 1) == 0
+        assert lib.gsa_get_tuning(L.TUNE_PLAN_ORDER) == 1
+        assert lib.gsa_set_tuning(L.TUNE_PLAN_ORDER, 2) == L.ERR_INVALID_ARG
+        assert lib.gsa_set_tuning(999, 0) == L.ERR_INVALID_ARG
+        assert lib.gsa_get_tuning(999) == -1
+
+        values = (1, 2, 4, 8)
+        errors = []
+
+        def setter(t):
+            for i in range(2000):
+                if lib.gsa_set_tuning(L.TUNE_SPMM_COLUMNS, values[(t + i) % 4]) != 0:
+                    errors.append(t)
+                if lib.gsa_get_tuning(L.TUNE_SPMM_COLUMNS) not in values:
+                    errors.append(-t)
+
+        threads = [threading.Thread(target=setter, args=(t,)) for t in range(4)]
+        for th in threads:
+            th.start()
+        for th in threads:
+            th.join()
+        assert not errors
+        assert lib.gsa_get_tuning(L.TUNE_SPMM_COLUMNS) in values
+    finally:
+        for key, v in saved.items():
+            lib.gsa_set_tuning(key, v)
