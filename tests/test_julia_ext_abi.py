@@ -1,0 +1,180 @@
+"""The Julia extension's `ccall`s agree with include/gsa.h (CPU only; no Julia needed).
+
+Julia is not part of this toolchain, so the extension source cannot be run here; this test
+parses every `ccall((:gsa_..., libgsa), Ret, (T1, T2, ...), args...)` in it and checks, against
+the header's declaration of the same function: the number of argument types, the number of
+arguments passed, and that each Julia type has the C parameter's width and kind (pointer,
+32-bit integer, 64-bit integer, float, double).  Names chosen at run time (`_planned_entry(A)`,
+`$(QuoteNode(entry))` in a `for` over entry symbols) are resolved from the source and every
+candidate is checked.
+"""
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "gsa.h")
+EXT = os.path.join(ROOT, "genericsparsearrays.jl_gb300", "julia", "GenericSparseArraysCUDAExt.jl")
+
+
+def _split_top(s):
+    """Split s at commas outside (), {} and []."""
+    out, depth, cur = [], 0, []
+    for ch in s:
+        if ch in "({[":
+            depth += 1
+        elif ch in ")}]":
+            depth -= 1
+        if ch == "," and depth == 0:
+            out.append("".join(cur).strip())
+            cur = []
+        else:
+            cur.append(ch)
+    tail = "".join(cur).strip()
+    if tail:
+        out.append(tail)
+    return out
+
+
+def _balanced(text, i):
+    """text[i] == '('; the index just past its matching ')'."""
+    depth = 0
+    for j in range(i, len(text)):
+        if text[j] == "(":
+            depth += 1
+        elif text[j] == ")":
+            depth -= 1
+            if depth == 0:
+                return j + 1
+    raise ValueError("unbalanced parentheses")
+
+
+def c_kind(decl, enums=()):
+    t = decl.strip()
+    if "*" in t:
+        return "ptr"
+    if t.split() and t.split()[-1] in enums:
+        return "i32"
+    t = re.sub(r"\b(const|unsigned|signed)\b", lambda m: "u" if m.group(1) == "unsigned" else "", t)
+    t = t.split()[0] if t.split() else t
+    if t in ("int64_t", "uint64_t", "size_t", "ptrdiff_t", "long"):
+        return "i64"
+    if t in ("int", "int32_t", "uint32_t", "u"):
+        return "i32"
+    if t == "double":
+        return "f64"
+    if t == "float":
+        return "f32"
+    if t == "void":
+        return "void"
+    raise AssertionError(f"unknown C type {decl!r}")
+
+
+def jl_kind(t):
+    t = t.strip()
+    if re.match(r"^(Ptr|CuPtr|Ref|PtrOrCuPtr)\{", t) or t in ("CUstream", "Cstring", "CuStream"):
+        return "ptr"
+    if t in ("Cint", "Int32", "Cuint", "UInt32"):
+        return "i32"
+    if t in ("Int64", "UInt64", "Csize_t", "Clonglong", "Culonglong", "Cssize_t", "Clong", "Culong"):
+        return "i64"
+    if t in ("Float64", "Cdouble"):
+        return "f64"
+    if t in ("Float32", "Cfloat"):
+        return "f32"
+    if t == "Cvoid":
+        return "void"
+    raise AssertionError(f"unknown Julia type {t!r}")
+
+
+def header_decls():
+    text = re.sub(r"/\*.*?\*/", "", open(HEADER).read(), flags=re.S)
+    text = re.sub(r"//[^\n]*", "", text)
+    text = re.sub(r"^\s*#[^\n]*", "", text, flags=re.M)
+    text = text.replace('extern "C" {', "")
+    enums = set(re.findall(r"typedef\s+enum\s*\{[^}]*\}\s*(\w+)\s*;", text))
+    text = re.sub(r"typedef[^;{]*\{[^}]*\}[^;]*;", "", text)  # enum and struct typedefs
+    decls = {}
+    for stmt in text.split(";"):
+        m = re.match(r"^\s*([A-Za-z_][\w\s\*]*?)\b(gsa_\w+)\s*\((.*)\)\s*$", stmt, flags=re.S)
+        if not m or "typedef" in m.group(1):
+            continue
+        ret, name, params = m.group(1), m.group(2), " ".join(m.group(3).split())
+        kinds = [] if params in ("", "void") else [c_kind(re.sub(r"\w+\s*$", "", p) or p, enums)
+                                                    for p in _split_top(params)]
+        decls[name] = (c_kind(ret, enums), kinds)
+    return decls
+
+
+def _resolve(target, text, pos):
+    """gsa_ names a ccall target can take."""
+    m = re.match(r"^\(\s*:(gsa_\w+)\s*,", target)
+    if m:
+        return [m.group(1)]
+    m = re.match(r"^\(\s*(_\w+)\(", target)
+    if m:  # a function mapping a matrix type to an entry symbol
+        return re.findall(rf"^{m.group(1)}\([^)]*\)\s*=\s*:(gsa_\w+)", text, flags=re.M)
+    m = re.match(r"^\(\s*\$\(QuoteNode\((\w+)\)\)", target)
+    if m:  # a `for (..., entry, ...) in ((...), ...)` loop around an @eval
+        head = text.rfind("\nfor ", 0, pos)
+        body = text.find("@eval", head)
+        return re.findall(r":(gsa_\w+)", text[head:body])
+    raise AssertionError(f"cannot resolve ccall target {target!r}")
+
+
+def ext_ccalls():
+    text = open(EXT).read()
+    calls = []
+    for m in re.finditer(r"\bccall\(", text):
+        start = m.end() - 1
+        parts = _split_top(text[start + 1:_balanced(text, start) - 1])
+        target, ret, types, args = parts[0], parts[1], parts[2], parts[3:]
+        assert types.startswith("(") and types.endswith(")"), types
+        tlist = _split_top(types[1:-1])
+        line = text.count("\n", 0, start) + 1
+        for name in _resolve(target, text, start):
+            calls.append((line, name, ret, tlist, args))
+    return calls
+
+
+def test_extension_calls_match_header():
+    decls = header_decls()
+    calls = ext_ccalls()
+    assert len(calls) >= 25
+    seen = set()
+    for line, name, ret, tlist, args in calls:
+        where = f"{os.path.basename(EXT)}:{line} {name}"
+        assert name in decls, f"{where}: not declared in gsa.h"
+        cret, ckinds = decls[name]
+        assert len(tlist) == len(ckinds), f"{where}: {len(tlist)} argument types, gsa.h has {len(ckinds)}"
+        # `size(A)...` splats a matrix's two dimensions; any other splat only bounds the count
+        nargs = sum(2 if re.match(r"^size\(\w+\)\.\.\.$", a) else 1 for a in args)
+        if any(a.endswith("...") and not re.match(r"^size\(\w+\)\.\.\.$", a) for a in args):
+            assert nargs <= len(tlist), f"{where}: {nargs} arguments for {len(tlist)} types"
+        else:
+            assert nargs == len(tlist), f"{where}: {nargs} arguments for {len(tlist)} types"
+        for i, (jt, ck) in enumerate(zip(tlist, ckinds)):
+            assert jl_kind(jt) == ck, f"{where}: argument {i + 1} is {jt}, gsa.h wants {ck}"
+        assert jl_kind(ret) == cret or (cret == "ptr" and ret.strip() == "Cstring"), \
+            f"{where}: returns {ret}, gsa.h returns {cret}"
+        seen.add(name)
+    # the extension reaches the hot path's entry points
+    for name in ("gsa_csr_mul_planned", "gsa_csc_mul_planned", "gsa_coo_mul_planned", "gsa_coo_to_csr",
+                 "gsa_coo_to_csc", "gsa_csr_to_coo", "gsa_csc_to_coo", "gsa_spgemm_compute"):
+        assert name in seen, f"the extension never calls {name}"
+
+
+def test_parser_catches_a_mismatch(tmp_path, monkeypatch):
+    """A ccall with one argument type dropped is reported (the check is not vacuous)."""
+    text = open(EXT).read()
+    bad = text.replace("(CUstream, Cint, Cint, Int64, Int64, Int64, CuPtr{Ti}, CuPtr{Ti}, CuPtr{T}, Cint,\n"
+                       "             CuPtr{Ti}, CuPtr{Ti}, CuPtr{T}),",
+                       "(CUstream, Cint, Int64, Int64, Int64, CuPtr{Ti}, CuPtr{Ti}, CuPtr{T}, Cint,\n"
+                       "             CuPtr{Ti}, CuPtr{Ti}, CuPtr{T}),", 1)
+    assert bad != text
+    p = tmp_path / "ext.jl"
+    p.write_text(bad)
+    monkeypatch.setattr(__import__(__name__), "EXT", str(p))
+    with pytest.raises(AssertionError, match="argument types"):
+        test_extension_calls_match_header()
