@@ -178,3 +178,30 @@ def test_parser_catches_a_mismatch(tmp_path, monkeypatch):
     monkeypatch.setattr(__import__(__name__), "EXT", str(p))
     with pytest.raises(AssertionError, match="argument types"):
         test_extension_calls_match_header()
+
+
+def _header_enum():
+    text = re.sub(r"/\*.*?\*/", "", open(HEADER).read(), flags=re.S)
+    return {k: int(v) for k, v in re.findall(r"\b(GSA_[A-Z0-9_]+)\s*=\s*(\d+)", text)}
+
+
+def test_extension_codes_match_header():
+    """The extension's value-type, index-type and op codes, and its status -> exception map,
+    are the header's (and the Python binding's)."""
+    e = _header_enum()
+    text = open(EXT).read()
+    dt = dict(re.findall(r"^gsa_dtype\(::Type\{(\w+)\}\)\s*=\s*Cint\((\d+)\)", text, flags=re.M))
+    assert {k: int(v) for k, v in dt.items()} == {
+        "Float32": e["GSA_F32"], "Float64": e["GSA_F64"], "ComplexF32": e["GSA_C32"],
+        "ComplexF64": e["GSA_C64"], "Int32": e["GSA_I32"], "Int64": e["GSA_I64"]}
+    it = dict(re.findall(r"^gsa_itype\(::Type\{(\w+)\}\)\s*=\s*Cint\((\d+)\)", text, flags=re.M))
+    assert {k: int(v) for k, v in it.items()} == {"Int32": e["GSA_IDX32"], "Int64": e["GSA_IDX64"]}
+    ops = re.findall(r"^_opA\(A(?:::(\w+)(?:\{[^}]*\})?)?\)\s*=\s*\([^,]+,\s*Cint\((\d+)\)\)", text, flags=re.M)
+    assert ("", str(e["GSA_OP_N"])) in ops and ("Transpose", str(e["GSA_OP_T"])) in ops
+    assert ("Adjoint", str(e["GSA_OP_C"])) in ops
+    fmt = dict(re.findall(r"^_fmt\(::GenericSparseMatrix(\w+)\)\s*=\s*Cint\((\d+)\)", text, flags=re.M))
+    assert {k: int(v) for k, v in fmt.items()} == {"CSR": 0, "CSC": 1, "COO": 2}
+    assert re.search(rf"status == {e['GSA_ERR_DIM']} && throw\(DimensionMismatch", text)
+    m = re.search(r"status in \(([\d, ]+)\) && throw\(ArgumentError", text)
+    assert m and {int(x) for x in m.group(1).split(",")} == {
+        e["GSA_ERR_INVALID_ARG"], e["GSA_ERR_UNSUPPORTED"], e["GSA_ERR_STRUCTURE"]}
