@@ -308,12 +308,12 @@ def run_gpu(args, world, rank, local):
 
         # e2e through the public API: every step copies its x from pinned host memory to the
         # device, runs mul!, and copies its y back to pinned host memory.  Steps rotate over
-        # three streams and three buffer sets, so one step's upload, the previous step's
+        # three (--e2e-sets) streams and buffer sets, so one step's upload, the previous step's
         # product and the one before's download run at once (the host link is full duplex;
         # three sets measured 0.211 ms per step against 0.248 ms with two); a step's buffers
         # are reused only after its result is on the host.  The sequential form (one stream,
         # a synchronize per step) is reported beside it.
-        SETS = 3
+        SETS = args.e2e_sets
         xh = [torch.from_numpy(x_host).pin_memory() for _ in range(SETS)]
         yh = [torch.empty(m, dtype=torch.float64).pin_memory() for _ in range(SETS)]
         xd = [torch.empty(n, dtype=torch.float64, device=dev) for _ in range(SETS)]
@@ -398,7 +398,7 @@ def run_gpu(args, world, rank, local):
         "e2e": {"value": round(e2e_value, 2), "unit": "GB/s", "h2d_bytes_per_step": n * 8,
                 "d2h_bytes_per_step": m * 8, "ms_per_step": round(e2e_s / args.steps * 1e3, 4),
                 "matches_oracle": e2e_ok, "api": "genericsparsearrays_gb300.mul_",
-                "steps_overlap": "three streams and buffer sets: upload, product and download of consecutive steps run at once",
+                "steps_overlap": f"{SETS} streams and buffer sets: upload, product and download of consecutive steps run at once",
                 "sequential": {"value": round(nbytes * args.steps / e2e_seq_s / 1e9, 2),
                                "ms_per_step": round(e2e_seq_s / args.steps * 1e3, 4)}},
         "gpu_launches": args.steps,  # one rowblock_kernel per SpMV
@@ -719,7 +719,11 @@ def main():
     ap.add_argument("--serve-seconds", type=float, default=1.0)
     ap.add_argument("--serve-rate-low", type=float, default=400)
     ap.add_argument("--serve-seconds-low", type=float, default=2.0)
+    ap.add_argument("--e2e-sets", type=int, default=3,
+                    help="steps in flight in the end-to-end run (streams and buffer sets)")
     args = ap.parse_args()
+    if args.e2e_sets < 1:
+        ap.error("--e2e-sets must be at least 1")
     if args.warmup < 3:
         args.warmup = 3
     world, rank, local = dist_setup()
