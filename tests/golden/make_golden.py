@@ -5,9 +5,11 @@ The reference (Julia) cannot run on the machines of this build, so each case is 
 from the inputs written in the reference source (cited per case) and its expected output is
 computed with scipy.sparse, which stands in for the SparseArrays results those tests compare
 against.  Indices are 1-based, as in the reference.  Run:  python tests/golden/make_golden.py
+(`--check`: exit 1 if the committed file differs from what the script writes).
 """
 import json
 import os
+import sys
 
 import numpy as np
 import scipy.sparse as sp
@@ -45,7 +47,8 @@ def coo_from_csc(S):
             "nzval": S.data.tolist()}
 
 
-def main():
+def build_cases():
+    """The known-answer cases, keyed by name (what known_answers.json holds)."""
     cases = {}
 
     # docs/src/index.md:47-58 -- A_sparse = sparse([1,2,1,3],[1,1,2,3],[2.0,3.0,4.0,5.0],3,3),
@@ -102,10 +105,23 @@ def main():
         "source": "test/shared/matrix_coo.jl:276-281", "m": 3, "n": 3, "a": coo_from_csc(An),
         "lambda": 1.0, "expected": coo_from_csc(An + sp.identity(3))}
 
-    with open(os.path.join(HERE, "known_answers.json"), "w") as f:
-        json.dump(cases, f, indent=1, sort_keys=True)
-        f.write("\n")
+    return cases
+
+
+def render(cases):
+    return json.dumps(cases, indent=1, sort_keys=True) + "\n"
+
+
+def main(argv):
+    path = os.path.join(HERE, "known_answers.json")
+    text = render(build_cases())
+    if "--check" in argv:  # exit 1 when the committed file is not what this script writes
+        with open(path) as f:
+            return 0 if f.read() == text else 1
+    with open(path, "w") as f:
+        f.write(text)
+    return 0
 
 
 if __name__ == "__main__":
-    main()
+    sys.exit(main(sys.argv[1:]))

@@ -206,3 +206,16 @@ def test_spgemm_matches_scipy(oracle, dt, fmt):
     assert M.nnz == structure.nnz
     for o in range(ptr.size - 1):  # indices increasing in every outer entry
         assert np.all(np.diff(idx[ptr[o] - 1:ptr[o + 1] - 1]) > 0)
+
+
+def test_golden_fixtures_are_current():
+    """known_answers.json is exactly what tests/golden/make_golden.py writes (so every case in
+    it traces back to the cited reference inputs)."""
+    import importlib.util
+    path = os.path.join(os.path.dirname(__file__), "golden", "make_golden.py")
+    spec = importlib.util.spec_from_file_location("make_golden", path)
+    mg = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mg)
+    with open(os.path.join(os.path.dirname(__file__), "golden", "known_answers.json")) as f:
+        assert f.read() == mg.render(mg.build_cases())
+    assert all("source" in c for c in mg.build_cases().values())
