@@ -100,3 +100,37 @@ def laplacian_2d(g, it=np.int32, dt=np.float64):
     S = sp.csr_matrix((v, (r, c)), shape=(n, n))
     S.sort_indices()
     return S
+
+
+_C_SCALARS = {"int64_t": 8, "uint64_t": 8, "size_t": 8, "int32_t": 4, "uint32_t": 4, "int": 4,
+              "unsigned char": 1, "char": 1, "double": 8, "float": 4}
+
+
+def c_struct_layout(header_text, name):
+    """[(field, offset, size)] and the total size of `typedef struct { ... } name;` in a C
+    header, on an LP64 target with natural alignment (pointers 8 bytes)."""
+    import re
+    text = re.sub(r"/\*.*?\*/", "", header_text, flags=re.S)
+    m = re.search(r"typedef\s+struct\s*\{([^}]*)\}\s*" + name + r"\s*;", text)
+    assert m, f"struct {name} not found"
+    fields = []
+    for decl in m.group(1).split(";"):
+        decl = " ".join(decl.split())
+        if not decl:
+            continue
+        base = re.match(r"^((?:const\s+)?(?:unsigned\s+)?[A-Za-z_]\w*)", decl).group(1)
+        for d in decl[len(base):].split(","):
+            d = d.strip()
+            ptr = d.startswith("*")
+            dm = re.match(r"^\**\s*(\w+)\s*(?:\[(\d+)\])?$", d)
+            assert dm, f"cannot parse {d!r} in {name}"
+            scalar = base.replace("const ", "").strip()
+            size = 8 if ptr else _C_SCALARS[scalar]
+            fields.append((dm.group(1), size, size, int(dm.group(2) or 1)))
+    out, off, align_max = [], 0, 1
+    for fname, size, align, count in fields:
+        off = (off + align - 1) // align * align
+        out.append((fname, off, size * count))
+        off += size * count
+        align_max = max(align_max, align)
+    return out, (off + align_max - 1) // align_max * align_max

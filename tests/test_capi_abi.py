@@ -182,3 +182,17 @@ def test_tuning_knobs(lib, gsa):
     finally:
         for key, v in saved.items():
             lib.gsa_set_tuning(key, v)
+
+
+def test_group_item_layout_matches_header(gsa):
+    """batch.ITEM_DTYPE (the bytes Python hands to gsa_grouped_tiles / gsa_grouped_mul) has the
+    field order, offsets and size of gsa_group_item in include/gsa.h."""
+    from helpers import c_struct_layout
+    import importlib
+    batch = importlib.import_module(gsa.__name__ + ".batch")
+    layout, total = c_struct_layout(open(HEADER).read(), "gsa_group_item")
+    assert total == 144 == batch.ITEM_DTYPE.itemsize
+    assert [f for f, _, _ in layout] == list(batch.ITEM_DTYPE.names)
+    for fname, off, size in layout:
+        dt, py_off = batch.ITEM_DTYPE.fields[fname][:2]
+        assert (py_off, dt.itemsize) == (off, size), fname

@@ -205,3 +205,37 @@ def test_extension_codes_match_header():
     m = re.search(r"status in \(([\d, ]+)\) && throw\(ArgumentError", text)
     assert m and {int(x) for x in m.group(1).split(",")} == {
         e["GSA_ERR_INVALID_ARG"], e["GSA_ERR_UNSUPPORTED"], e["GSA_ERR_STRUCTURE"]}
+
+
+_JL_SIZES = {"Int64": 8, "UInt64": 8, "Int32": 4, "UInt32": 4, "Float64": 8, "Float32": 4}
+
+
+def test_julia_group_item_matches_header():
+    """GsaGroupItem in the extension (handed to gsa_batch_create as raw bytes) has the field
+    order, offsets and size of gsa_group_item."""
+    from helpers import c_struct_layout
+    text = open(EXT).read()
+    m = re.search(r"struct GsaGroupItem\b[^\n]*\n(.*?)\nend", text, flags=re.S)
+    assert m
+    fields = []
+    for decl in re.split(r"[;\n]", m.group(1)):
+        decl = decl.split("#")[0].strip()
+        if not decl:
+            continue
+        name, jt = [x.strip() for x in decl.split("::", 1)]
+        tm = re.match(r"^NTuple\{(\d+),\s*UInt8\}$", jt)
+        if tm:
+            size, align = int(tm.group(1)), 1
+        elif re.match(r"^(Cu)?Ptr\{", jt):
+            size = align = 8
+        else:
+            size = align = _JL_SIZES[jt]
+        fields.append((name, size, align))
+    off, got = 0, []
+    for name, size, align in fields:
+        off = (off + align - 1) // align * align
+        got.append((name, off, size))
+        off += size
+    layout, total = c_struct_layout(open(HEADER).read(), "gsa_group_item")
+    assert got == layout
+    assert (off + 7) // 8 * 8 == total == 144
