@@ -134,13 +134,26 @@ function _gsa_mul!(C::CuVecOrMat{T}, A, B, α::Number, β::Number) where {T}
     return C  # asynchronous, like the package's kernels
 end
 
-const DenseCu{T} = Union{CuVecOrMat{T}, Transpose{T, <:CuVecOrMat{T}}, Adjoint{T, <:CuVecOrMat{T}}}
+const GSAReal = Union{Float32, Float64, Int32, Int64}
+const GSAComplex = Union{ComplexF32, ComplexF64}
+
+# The package generates one method per wrapper of A and of B (trans_adj_wrappers,
+# src/core.jl:102-113: plain, Transpose of a real, Transpose of a complex, Adjoint).  The
+# methods here follow the same split, so each one is a strict subtype of the package method it
+# replaces (CuArray storage, one element type, the same element-type bound) and more specific
+# in every argument: no method ambiguity (the package runs Aqua's check, test/runtests.jl:106-111).
+# (type expression, element-type bound) of each wrapper of X:
+_wrappers(X) = ((X, :GSAValue), (:(Transpose{T, <:$X}), :GSAReal),
+                (:(Transpose{T, <:$X}), :GSAComplex), (:(Adjoint{T, <:$X}), :GSAValue))
+# the bound two wrappers share, or nothing when their bounds exclude each other
+_bound(a, b) = a === :GSAValue ? b : (b === :GSAValue || a === b ? a : nothing)
 
 for Fmt in (:CSRCu, :CSCCu, :COOCu)
-    for TA in ((Fmt), :(Transpose{T, <:$Fmt{T, Ti}}), :(Adjoint{T, <:$Fmt{T, Ti}}))
-        SA = TA == Fmt ? :($Fmt{T, Ti}) : TA
-        @eval function LinearAlgebra.mul!(C::CuVecOrMat{T}, A::$SA, B::DenseCu{T}, α::Number,
-                                          β::Number) where {T <: GSAValue, Ti <: GSAIndex}
+    for (SA, TA) in _wrappers(:($Fmt{T, Ti})), (SB, TB) in _wrappers(:(CuVecOrMat{T}))
+        Tb = _bound(TA, TB)
+        Tb === nothing && continue
+        @eval function LinearAlgebra.mul!(C::CuVecOrMat{T}, A::$SA, B::$SB, α::Number,
+                                          β::Number) where {T <: $Tb, Ti <: GSAIndex}
             return _gsa_mul!(C, A, B, α, β)
         end
     end
@@ -178,9 +191,8 @@ function _gsa_dot(x::CuVector{T}, A, y::CuVector{T}) where {T}
 end
 
 for Fmt in (:CSRCu, :CSCCu, :COOCu)
-    for TA in ((Fmt), :(Transpose{T, <:$Fmt{T, Ti}}), :(Adjoint{T, <:$Fmt{T, Ti}}))
-        SA = TA == Fmt ? :($Fmt{T, Ti}) : TA
-        @eval LinearAlgebra.dot(x::CuVector{T}, A::$SA, y::CuVector{T}) where {T <: GSAValue, Ti <: GSAIndex} =
+    for (SA, TA) in _wrappers(:($Fmt{T, Ti}))  # one method per package method, as for mul!
+        @eval LinearAlgebra.dot(x::CuVector{T}, A::$SA, y::CuVector{T}) where {T <: $TA, Ti <: GSAIndex} =
             _gsa_dot(x, A, y)
     end
 end
@@ -382,7 +394,12 @@ _parts(A::GenericSparseMatrixCSR) = (A.rowptr, A.colval, size(A, 1))
 _parts(A::GenericSparseMatrixCSC) = (A.colptr, A.rowval, size(A, 2))
 _parts(A::GenericSparseMatrixCOO) = (A.rowind, A.colind, 0)
 
-function SparseArrays.dropzeros(A::Union{CSRCu{T, Ti}, CSCCu{T, Ti}, COOCu{T, Ti}}) where {T <: GSAValue, Ti <: GSAIndex}
+# one method per format, each a subtype of the package's method for that format
+for Fmt in (:CSRCu, :CSCCu, :COOCu)
+    @eval SparseArrays.dropzeros(A::$Fmt{T, Ti}) where {T <: GSAValue, Ti <: GSAIndex} = _gsa_dropzeros(A)
+end
+
+function _gsa_dropzeros(A::Union{CSRCu{T, Ti}, CSCCu{T, Ti}, COOCu{T, Ti}}) where {T, Ti}
     nz = length(A.nzval)
     p0, p1, outer = _parts(A)
     ws = CuVector{UInt8}(undef, ccall((:gsa_dropzeros_workspace_size, libgsa), Csize_t, (Int64,), nz))
