@@ -123,8 +123,8 @@ def _resolve(target, text, pos):
     raise AssertionError(f"cannot resolve ccall target {target!r}")
 
 
-def ext_ccalls():
-    text = open(EXT).read()
+def ext_ccalls(text=None):
+    text = open(EXT).read() if text is None else text
     calls = []
     for m in re.finditer(r"\bccall\(", text):
         start = m.end() - 1
@@ -239,3 +239,17 @@ def test_julia_group_item_matches_header():
     layout, total = c_struct_layout(open(HEADER).read(), "gsa_group_item")
     assert got == layout
     assert (off + 7) // 8 * 8 == total == 144
+
+
+def test_integration_guide_snippets_match_header():
+    """The `ccall`s shown in the ```julia blocks of INTEGRATION.md match gsa.h too."""
+    guide = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    blocks = "\n".join(re.findall(r"```julia\n(.*?)```", guide, flags=re.S))
+    decls = header_decls()
+    calls = ext_ccalls(blocks)
+    assert {c[1] for c in calls} >= {"gsa_csr_mul", "gsa_batch_create", "gsa_batch_run"}
+    for line, name, ret, tlist, args in calls:
+        cret, ckinds = decls[name]
+        assert len(tlist) == len(ckinds) == len(args), (name, len(tlist), len(ckinds), len(args))
+        for i, (jt, ck) in enumerate(zip(tlist, ckinds)):
+            assert jl_kind(jt) == ck, f"{name}: argument {i + 1} is {jt}, gsa.h wants {ck}"
