@@ -168,18 +168,41 @@ MergeLayout merge_layout(int64_t outer_n) {
 }
 
 // Counting pass, scan, pointer array, and the count on the host.
-int finish_count(cudaStream_t s, int64_t outer_n, void *ws, int itype, int base, void *ptr_c, int64_t *nnz_c) {
+// The stored entry count of a compressed operand: its last pointer minus base (0 if smaller).
+int64_t stored_count(int itype, int64_t last, int base) {
+    const int64_t v = (itype == GSA_IDX32 ? (int64_t)(int32_t)last : last) - base;
+    return v > 0 ? v : 0;
+}
+
+// Scans the per-outer-entry counts, checks that the total fits (the scan is 32-bit, and Int32
+// pointers hold at most 2^31 - 1), then writes the result's pointers.  ptr_b NULL: A + λI,
+// at most one entry more per outer entry.
+int finish_count(cudaStream_t s, int64_t outer_n, void *ws, int itype, int base, const void *ptr_a,
+                 const void *ptr_b, void *ptr_c, int64_t *nnz_c) {
     const MergeLayout L = merge_layout(outer_n);
     char *w = (char *)ws;
     uint32_t *cnt = (uint32_t *)(w + L.cnt), *cptr = (uint32_t *)(w + L.cptr);
     int rc = scan_u32(s, cnt, cptr, outer_n + 1, (uint32_t *)(w + L.bsums));
     if (rc) return rc;
+    const size_t is = itype == GSA_IDX32 ? 4 : 8;
+    uint32_t total = 0;
+    int64_t last_a = 0, last_b = 0;  // the low `is` bytes are the pointer (little-endian)
+    rc = check_cuda(cudaMemcpyAsync(&total, cptr + outer_n, sizeof(total), cudaMemcpyDeviceToHost, s), "sum: count");
+    if (!rc) rc = check_cuda(cudaMemcpyAsync(&last_a, (const char *)ptr_a + outer_n * is, is, cudaMemcpyDeviceToHost, s),
+                             "sum: nnz of A");
+    if (!rc && ptr_b)
+        rc = check_cuda(cudaMemcpyAsync(&last_b, (const char *)ptr_b + outer_n * is, is, cudaMemcpyDeviceToHost, s),
+                        "sum: nnz of B");
+    if (!rc) rc = check_cuda(cudaStreamSynchronize(s), "sum: sync");
+    if (rc) return rc;
+    const int64_t bound = stored_count(itype, last_a, base) + (ptr_b ? stored_count(itype, last_b, base) : outer_n);
+    if (bound >= 0xffffffffLL)
+        return fail(GSA_ERR_UNSUPPORTED, "a sum of up to %lld entries; at most 2^32 - 2 are supported", (long long)bound);
+    if (itype == GSA_IDX32 && (int64_t)total + base > 0x7fffffffLL)
+        return fail(GSA_ERR_UNSUPPORTED, "the sum has %u entries, more than Int32 pointers can address", total);
     if (itype == GSA_IDX32) merged_pointers_kernel<int32_t><<<mg_grid(outer_n + 1), 256, 0, s>>>(outer_n, cptr, base, (int32_t *)ptr_c);
     else merged_pointers_kernel<int64_t><<<mg_grid(outer_n + 1), 256, 0, s>>>(outer_n, cptr, base, (int64_t *)ptr_c);
     rc = check_cuda(cudaGetLastError(), "merged_pointers_kernel");
-    uint32_t total = 0;
-    if (!rc) rc = check_cuda(cudaMemcpyAsync(&total, cptr + outer_n, sizeof(total), cudaMemcpyDeviceToHost, s), "sum: count");
-    if (!rc) rc = check_cuda(cudaStreamSynchronize(s), "sum: sync");
     if (!rc) *nnz_c = total;
     return rc;
 }
@@ -238,7 +261,7 @@ int gsa_compressed_add_count(void *stream, int itype, int64_t outer_n, const voi
         return fail(GSA_ERR_INVALID_ARG, "arrays must be aligned to their element size");
     MergeCountBody body{(cudaStream_t)stream, outer_n, ptr_a, idx_a, ptr_b, idx_b, base, workspace};
     int rc = dispatch_vi(GSA_F64, itype, body);
-    if (!rc) rc = finish_count((cudaStream_t)stream, outer_n, workspace, itype, base, ptr_c, nnz_c);
+    if (!rc) rc = finish_count((cudaStream_t)stream, outer_n, workspace, itype, base, ptr_a, ptr_b, ptr_c, nnz_c);
     return rc;
 }
 

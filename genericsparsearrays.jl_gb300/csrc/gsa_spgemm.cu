@@ -677,10 +677,13 @@ int spgemm_create(cudaStream_t s, gsa_spgemm *h, int64_t nnz_p, I *ptr_c) {
     }
     rc = scan_u32(s, cnt, cptr, outer_n + 1, bsums);
     if (rc) return rc;
+    uint32_t total = 0;
+    rc = read_back(s, &total, cptr + outer_n, sizeof(total), "spgemm: entry count");
+    if (rc) return rc;
+    if (sizeof(I) == 4 && (int64_t)total + h->base > 0x7fffffffLL)  // checked before any pointer is written
+        return fail(GSA_ERR_UNSUPPORTED, "the product has %u entries, more than Int32 pointers can address", total);
     pointers_kernel<I><<<sg_grid(outer_n + 1, 256, 152 * 8), 256, 0, s>>>(outer_n, cptr, h->base, ptr_c);
     rc = check_cuda(cudaGetLastError(), "spgemm: pointers_kernel");
-    uint32_t total = 0;
-    if (!rc) rc = read_back(s, &total, cptr + outer_n, sizeof(total), "spgemm: entry count");
     if (!rc) h->nnz_c = total;
     return rc;
 }

@@ -203,9 +203,11 @@ int gsa_coo_sum_copy(void *stream, int dtype, int itype, int64_t m, int64_t n, i
  * reference then drops zeros: gsa_dropzeros_* on the result); for A + λI (ptr_b = idx_b = NULL)
  * one more entry where no diagonal is stored, λ added to every stored diagonal and inserted
  * before the first larger index.  Two calls on ONE workspace of
- * gsa_compressed_add_workspace_size(outer_n) bytes: _count writes the result's pointer array
- * ptr_c (outer_n + 1, same base) and returns its entry count (synchronizes the stream); _copy
- * writes idx_c / val_c.  negate_b: B's values negated (A - B = A + (-B)).  lambda: host pointer
+ * gsa_compressed_add_workspace_size(outer_n) bytes: _count returns the result's entry count
+ * (synchronizing the stream to read it) and then writes its pointer array ptr_c (outer_n + 1,
+ * same base) on the stream; _copy writes idx_c / val_c.  At most 2^32 - 2 entries in A and B
+ * together; with Int32 indices at most 2^31 - 1 - base in the result (GSA_ERR_UNSUPPORTED, and
+ * ptr_c untouched, beyond either).  negate_b: B's values negated (A - B = A + (-B)).  lambda: host pointer
  * to one value of the dtype (A + λI only). */
 size_t gsa_compressed_add_workspace_size(int64_t outer_n);
 int gsa_compressed_add_count(void *stream, int itype, int64_t outer_n, const void *ptr_a, const void *idx_a,
@@ -224,11 +226,13 @@ int gsa_compressed_add_copy(void *stream, int dtype, int itype, int64_t outer_n,
  * dtype and itype.  C has the same format; every position that a product reaches is stored
  * (zero sums included), indices increasing within each outer entry, and each entry is the
  * sum from zero, in the reference's order, of Julia-rounded products (the reference's bits).
- * _create runs the symbolic phase: it writes C's pointer array ptr_c (m + 1 for CSR, n + 1
- * for CSC) and returns the entry count in *nnz_c (synchronizes the stream); the handle
- * keeps device scratch and refers to A's and B's arrays, which must stay unchanged until
- * _compute.  _compute writes idx_c / val_c (nnz_c each).  _destroy frees the handle.  At
- * most 2^32 - 2 products (stored A entries times the lengths of the B rows they select). */
+ * _create runs the symbolic phase: it returns the entry count in *nnz_c (synchronizing the
+ * stream to read it) and then writes C's pointer array ptr_c (m + 1 for CSR, n + 1 for CSC)
+ * on the stream; the handle keeps device scratch and refers to A's and B's arrays, which must
+ * stay unchanged until _compute.  _compute writes idx_c / val_c (nnz_c each).  _destroy frees
+ * the handle.  At most 2^32 - 2 products (stored A entries times the lengths of the B rows
+ * they select); with Int32 indices at most 2^31 - 1 - base entries (GSA_ERR_UNSUPPORTED, and
+ * ptr_c untouched, beyond that). */
 typedef struct gsa_spgemm gsa_spgemm;
 int gsa_spgemm_create(void *stream, int format, int dtype, int itype, int64_t m, int64_t k, int64_t n,
                       const void *ptr_a, const void *idx_a, const void *val_a, int64_t nnz_a, const void *ptr_b,
