@@ -219,3 +219,109 @@ def test_golden_fixtures_are_current():
     with open(os.path.join(os.path.dirname(__file__), "golden", "known_answers.json")) as f:
         assert f.read() == mg.render(mg.build_cases())
     assert all("source" in c for c in mg.build_cases().values())
+
+
+@pytest.mark.parametrize("dt", VALUE_TYPES)
+@pytest.mark.parametrize("fmt", ["csr", "csc", "coo"])
+@pytest.mark.parametrize("op", OPS)
+def test_dot_matches_numpy(oracle, dt, fmt, op):
+    """Three-argument dot(x, op(A), y) = x^H op(A) y (src/matrix_csr/matrix_csr.jl:213-277):
+    the oracle's reference-arithmetic value and its double-double value against numpy."""
+    from helpers import rand_values
+    rng = np.random.default_rng(11)
+    S = sprand(rng, 60, 45, 0.1, dt)
+    p0, p1, v = parts(S, fmt, np.int64)
+    opS = op_apply(S, op)
+    x = rand_values(rng, opS.shape[0], dt)
+    y = rand_values(rng, opS.shape[1], dt)
+    val, exact, scale = oracle.dot(fmt, op, S.shape[0], S.shape[1], p0, p1, v, 1, x, y)
+    want = np.vdot(x.astype(np.complex128), opS.astype(np.complex128) @ y.astype(np.complex128))
+    if not np.iscomplexobj(v):
+        want = want.real
+    if is_int(dt):
+        assert val == want and exact == want
+    else:
+        assert abs(exact - want) <= 1e-13 * scale
+        assert abs(val - exact) <= tol(dt) * scale
+
+
+def _canonical(S):
+    S = S.copy()
+    S.eliminate_zeros()
+    S.sort_indices()
+    return S
+
+
+@pytest.mark.parametrize("dt", [np.float64, np.complex64, np.int32])
+@pytest.mark.parametrize("it", INDEX_TYPES)
+@pytest.mark.parametrize("fmt", ["csr", "csc"])
+@pytest.mark.parametrize("neg_b", [False, True])
+def test_compressed_add_matches_scipy(oracle, dt, it, fmt, neg_b):
+    """CSR + CSR / CSC + CSC (src/matrix_csr/matrix_csr.jl:290-356, then dropzeros): on sorted,
+    duplicate-free operands the sum is scipy's, bit for bit (one add per shared position), and
+    positions that cancel are dropped."""
+    import scipy.sparse as sp
+    rng = np.random.default_rng(5)
+    A = sprand(rng, 40, 30, 0.15, dt)
+    B = sprand(rng, 40, 30, 0.15, dt)
+    # B repeats some of A's entries, so A - B cancels there
+    C = sp.coo_matrix(A)
+    keep = rng.random(C.nnz) < 0.3
+    shared = sp.csr_matrix((C.data[keep], (C.row[keep], C.col[keep])), shape=A.shape)
+    B = sp.csr_matrix(B - B.multiply(shared != 0) + shared)
+    conv = (lambda X: sp.csr_matrix(X)) if fmt == "csr" else (lambda X: sp.csc_matrix(X))
+    a, b = parts(A, fmt, it), parts(B, fmt, it)
+    outer = A.shape[0] if fmt == "csr" else A.shape[1]
+    ptr, idx, val = oracle.compressed_add(outer, a, b, neg_b=neg_b)
+    want = _canonical(conv(A - B if neg_b else A + B))
+    assert (ptr - 1).tolist() == want.indptr.tolist()
+    assert (idx - 1).tolist() == want.indices.tolist()
+    assert val.tobytes() == want.data.astype(dt).tobytes()
+    if neg_b:  # the shared positions cancel and are gone
+        assert shared.nnz > 0 and len(val) <= A.nnz + B.nnz - 2 * shared.nnz
+
+
+@pytest.mark.parametrize("dt", [np.float64, np.complex128, np.int64])
+@pytest.mark.parametrize("fmt", ["csr", "csc"])
+def test_compressed_add_diag_matches_scipy(oracle, dt, fmt):
+    """A + λI (src/matrix_csr/matrix_csr.jl:358-402): λ added to every stored diagonal, one
+    entry inserted in order where none is stored, no dropzeros (a diagonal that sums to zero
+    stays stored)."""
+    import scipy.sparse as sp
+    rng = np.random.default_rng(8)
+    A = sp.lil_matrix(sprand(rng, 30, 30, 0.12, dt))
+    for i in range(0, 30, 3):
+        A[i, i] = 2  # stored diagonals; row 0's sums to zero below
+    A = sp.csr_matrix(A)
+    lam = -2
+    a = parts(A, fmt, np.int64)
+    ptr, idx, val = oracle.compressed_add_diag(30, a, lam)
+    outer_has_diag = np.array([A[i, i] != 0 for i in range(30)])
+    assert ptr[-1] - 1 == A.nnz + int((~outer_has_diag).sum())
+    conv = sp.csr_matrix if fmt == "csr" else sp.csc_matrix
+    got = conv((val, idx - 1, ptr - 1), shape=(30, 30))
+    assert np.array_equal(got.toarray(), (A + lam * sp.identity(30, dtype=dt)).toarray().astype(dt))
+    for o in range(30):
+        assert np.all(np.diff(idx[ptr[o] - 1:ptr[o + 1] - 1]) > 0)  # rows stay sorted
+    assert got[0, 0] == 0 and (idx[ptr[0] - 1:ptr[1] - 1] == 1).any()  # zero sum kept
+
+
+@pytest.mark.parametrize("fmt", ["csr", "csc"])
+@pytest.mark.parametrize("it", INDEX_TYPES)
+def test_compressed_to_coo_matches_scipy(oracle, fmt, it):
+    """CSR / CSC -> COO (src/conversions/conversions.jl:153-169, 264-280): entries in storage
+    order, the outer index expanded."""
+    import scipy.sparse as sp
+    rng = np.random.default_rng(2)
+    S = sprand(rng, 35, 50, 0.1, np.float64)
+    p0, p1, v = parts(S, fmt, it)
+    if fmt == "csr":
+        r, c, vv = oracle.csr_to_coo(35, 50, p0, p1, v)
+        X = sp.csr_matrix(S)
+    else:
+        r, c, vv = oracle.csc_to_coo(35, 50, p0, p1, v)
+        X = sp.csc_matrix(S)
+    X.sort_indices()
+    C = X.tocoo()
+    assert (r - 1).tolist() == C.row.tolist() and (c - 1).tolist() == C.col.tolist()
+    assert vv.tobytes() == C.data.tobytes()
