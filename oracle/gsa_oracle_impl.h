@@ -279,7 +279,7 @@ static int FN(coo_to_compressed)(int colmajor, int64_t m, int64_t n, int64_t nnz
     const I *major = colmajor ? colind : rowind;
     const I *minor = colmajor ? rowind : colind;
     int64_t major_n = colmajor ? n : m, minor_n = colmajor ? m : n;
-    if (nnz == 0) {
+    if (nnz <= 0) {
         for (int64_t r = 0; r <= major_n; ++r) ptr_out[r] = (I)base;
         return 0;
     }
@@ -327,7 +327,7 @@ static int FN(coo_sum)(int64_t m, int64_t n, int64_t nnz_a, const void *ra, cons
     I *row_out = (I *)row_outv, *col_out = (I *)col_outv;
     V *val_out = (V *)val_outv;
     *kept = 0;
-    if (total == 0) return 0;
+    if (total <= 0) return 0;
     int64_t *rc = (int64_t *)malloc((size_t)total * 2 * sizeof(int64_t));
     V *vc = (V *)malloc((size_t)total * sizeof(V));
     uint64_t *keys = (uint64_t *)malloc((size_t)total * sizeof(uint64_t));
