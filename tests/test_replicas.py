@@ -1,4 +1,4 @@
-"""The N > 1 bench path (replicas only, SURVEY's multi-GPU row): every rank runs the same
+"""The N > 1 bench path (independent replicas; no collective on the data path): every rank runs the same
 product on its own GPU, and the whole-job value is all ranks' bytes over the slowest rank's
 time.  Checked here with two gloo ranks on the CPU (no GPU): the max-over-ranks reduction and
 the value every rank computes."""
