@@ -358,7 +358,7 @@ small_kernel(const uint32_t *__restrict__ list, const uint32_t *__restrict__ cou
                 __syncwarp();
             }
         }
-        uint32_t before = 0;  // run starts in earlier rounds
+        uint32_t before = 0;  // run starts in earlier passes of the loop below
         const uint32_t out0 = NUMERIC ? cptr[o] : 0;
         for (uint32_t i0 = 0; i0 < P; i0 += 32) {
             const uint32_t i = i0 + lane;

@@ -3,7 +3,7 @@
  * conversions of GenericSparseArrays.jl.
  *
  * TEST INFRASTRUCTURE, NOT PRODUCT: only tests/, __graft_entry__.smoke() and
- * bench.py's CPU-baseline leg load this library, and there only as the checker
+ * bench.py's CPU-baseline leg load this library, and there only to check results
  * (or as the timed CPU restatement of the reference).  The CUDA library never
  * links or calls it.
  *

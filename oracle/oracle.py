@@ -1,7 +1,7 @@
 """CPU oracle for the sparse x dense mul! path and the COO <-> CSR/CSC conversions.
 
 TEST INFRASTRUCTURE, NOT PRODUCT.  Only tests/, ``__graft_entry__.smoke()`` and the
-CPU-baseline leg of ``bench.py`` import this module, and only as the checker (or, for
+CPU-baseline leg of ``bench.py`` import this module, and only to check results (or, for
 the baseline, as the timed CPU restatement of the reference).  The CUDA library and
 the ``genericsparsearrays_gb300`` package never import it.
 
@@ -18,7 +18,7 @@ function cites the reference file:line it restates:
 * ``coo_to_csr`` / ``coo_to_csc`` -- src/conversions/conversions.jl:171-212,282-323.
 * ``csr_to_coo`` / ``csc_to_coo`` -- src/conversions/conversion_kernels.jl:2-35.
 
-Parity pin: Julia is absent on both machines of this build, so the restatement is
+Parity pin: Julia is not available to run the reference, so the restatement is
 pinned against the reference's known-answer fixtures (tests/golden/) and checked
 against scipy.sparse, which stands in for SparseArrays.
 """

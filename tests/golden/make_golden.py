@@ -1,7 +1,7 @@
 """Writes tests/golden/known_answers.json: the known-answer cases that the reference's own
 tests and docs hold for the sparse x dense mul! path and the conversions.
 
-The reference (Julia) cannot run on the machines of this build, so each case is rebuilt here
+The reference (Julia) cannot be run (no Julia installation), so each case is rebuilt here
 from the inputs written in the reference source (cited per case) and its expected output is
 computed with scipy.sparse, which stands in for the SparseArrays results those tests compare
 against.  Indices are 1-based, as in the reference.  Run:  python tests/golden/make_golden.py
