@@ -146,9 +146,18 @@ def dist_setup():
     return world, rank, local
 
 
+def host_threads() -> int:
+    """CPUs this process may run on.  OMP_NUM_THREADS is not consulted (torchrun sets it to 1):
+    the CPU legs run on rank 0 alone and take the whole host."""
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
 def cpu_spmv_sample(oracle, m, n, rp, cv, nz, x, budget_s=10.0, max_reps=200):
     """Time the C restatement of kernel_spmatmul_csr_N! (OpenMP, all host threads)."""
-    threads = oracle.max_threads()
+    threads = host_threads()
     y = np.zeros(m)
     oracle.mul("csr", "N", m, n, rp, cv, nz, 1, x, y, nthreads=threads)  # warm-up
     times = []
@@ -169,7 +178,7 @@ def run_reference(args, world, rank):
     wl = genericsparsearrays_gb300.workloads
     m, n, rp, cv, nz = wl.laplacian_2d(2048, itype=np.int32, dtype=np.float64)
     x = np.random.default_rng(0).uniform(-1, 1, n)
-    threads = oracle.max_threads()
+    threads = host_threads()
     y = np.zeros(m)
     for _ in range(args.warmup):
         oracle.mul("csr", "N", m, n, rp, cv, nz, 1, x, y, nthreads=threads)

@@ -52,3 +52,13 @@ def test_single_rank_is_its_own_time():
     import bench
     value, max_ms = bench.replica_value(4.0, 1, nbytes=2e9, steps=3, device=torch.device("cpu"))
     assert max_ms == 4.0 and abs(value - 3 * 2e9 / 4e-3 / 1e9) < 1e-6
+
+
+def test_cpu_legs_take_the_whole_host(monkeypatch):
+    """Under torchrun OMP_NUM_THREADS is 1; the CPU legs (run on rank 0 alone) still use every
+    CPU the process may run on."""
+    sys.path.insert(0, ROOT)
+    import bench
+    monkeypatch.setenv("OMP_NUM_THREADS", "1")
+    want = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else (os.cpu_count() or 1)
+    assert bench.host_threads() == want >= 1
