@@ -426,8 +426,8 @@ def run_extras(gsa, wl, torch, dev, lib, timer, args):
     out = {}
     steps, warm = max(5, args.steps // 4), 3
 
-    def time_call(fn):
-        total_ms, kern_ms = timer.run(fn, steps, warm, flush=True, kernel_events=True, lib=lib)
+    def time_call(fn, flush=True):
+        total_ms, kern_ms = timer.run(fn, steps, warm, flush=flush, kernel_events=True, lib=lib)
         return total_ms / steps / 1e3, kern_ms / steps / 1e3
 
     rng = np.random.default_rng(1)
@@ -530,7 +530,8 @@ def run_extras(gsa, wl, torch, dev, lib, timer, args):
     out["powerlaw_csr_dot_c64_i64"] = {"GBps": round(bp / td / 1e9, 1), "us": round(td * 1e6, 2),
                                        "note": "wall time of gsa.dot incl. the scalar's copy to the host"}
     del A, Cp
-    # n = 1e5 Poisson(10): CSR / CSC / COO (18 MB: L2-resident unless flushed; flushed here)
+    # n = 1e5 Poisson(10): CSR / CSC / COO (18 MB: L2-resident unless flushed; timed both ways,
+    # the main figures with L2 flushed, the l2_warm_* ones back to back with the operands in L2)
     m, n, rp, cv, nz = wl.random_poisson(100_000, seed=0)
     A = gsa.adapt(dev, gsa.GenericSparseMatrixCSR(m, n, rp, cv, nz))
     _, _, cp, rv, cz = wl.csr_to_csc(m, n, rp, cv, nz)
@@ -541,8 +542,11 @@ def run_extras(gsa, wl, torch, dev, lib, timer, args):
     br = spmv_bytes(m, n, cv.size, 8, 8)
     for name, M in (("csr", A), ("csc", K), ("coo", Co)):
         t, tk = time_call(lambda: gsa.mul_(y, M, x))
+        tw, tkw = time_call(lambda: gsa.mul_(y, M, x), flush=False)
         out[f"random1e5_{name}_spmv_f64_i64"] = {"GBps": round(br / t / 1e9, 1), "kernel_GBps": round(br / tk / 1e9, 1),
-                                                 "us": round(t * 1e6, 2), "kernel_us": round(tk * 1e6, 2)}
+                                                 "us": round(t * 1e6, 2), "kernel_us": round(tk * 1e6, 2),
+                                                 "l2_warm_us": round(tw * 1e6, 2), "l2_warm_kernel_us": round(tkw * 1e6, 2),
+                                                 "l2_warm_kernel_GBps": round(br / tkw / 1e9, 1)}
     return out
 
 
