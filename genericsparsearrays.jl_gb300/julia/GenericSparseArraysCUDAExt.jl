@@ -341,11 +341,16 @@ function Base.:+(A::COOCu{T, Ti}, B::COOCu{T, Ti}) where {T <: GSAValue, Ti <: G
     return _coo_sum(size(A)..., A, Cint(0), B, Cint(0), 0, zero(T))
 end
 
-function Base.:+(A::COOCu{T, Ti}, J::UniformScaling{T}) where {T <: GSAValue, Ti <: GSAIndex}
+# Any J whose λ promotes to the matrix's element type (I, -I, 2.0I on a Float64 matrix ...):
+# the reference's result type is promote_type(Tv, typeof(λ)) (src/matrix_coo/matrix_coo.jl:399);
+# when that is wider than T, the package's own method runs.
+function Base.:+(A::COOCu{T, Ti}, J::UniformScaling{S}) where {T <: GSAValue, Ti <: GSAIndex, S}
+    promote_type(T, S) === T ||
+        return invoke(Base.:+, Tuple{GenericSparseMatrixCOO, UniformScaling}, A, J)
     m, n = size(A)
     m == n || throw(DimensionMismatch("Matrix must be square to add UniformScaling."))
     iszero(J.λ) && return copy(A)
-    return _coo_sum(m, n, A, Cint(0), nothing, Cint(0), n, J.λ)
+    return _coo_sum(m, n, A, Cint(0), nothing, Cint(0), n, T(J.λ))
 end
 
 # CSR + CSR, CSC + CSC (src/matrix_csr/matrix_csr.jl:290-356, then dropzeros) and A + λI
@@ -371,17 +376,20 @@ function _compressed_sum(A::Union{CSRCu{T, Ti}, CSCCu{T, Ti}}, B, λ) where {T, 
     return B === nothing ? C : dropzeros(C)
 end
 
-for Fmt in (:CSRCu, :CSCCu)
+for (Fmt, Parent) in ((:CSRCu, :GenericSparseMatrixCSR), (:CSCCu, :GenericSparseMatrixCSC))
     @eval function Base.:+(A::$Fmt{T, Ti}, B::$Fmt{T, Ti}) where {T <: GSAValue, Ti <: GSAIndex}
         size(A) == size(B) || throw(DimensionMismatch(
             "dimensions must match: A has dims $(size(A)), B has dims $(size(B))"))
         return _compressed_sum(A, B, nothing)
     end
-    @eval function Base.:+(A::$Fmt{T, Ti}, J::UniformScaling{T}) where {T <: GSAValue, Ti <: GSAIndex}
+    # as for COO: J's λ must promote to T (src/matrix_csr/matrix_csr.jl:358-402), else the
+    # package's own method
+    @eval function Base.:+(A::$Fmt{T, Ti}, J::UniformScaling{S}) where {T <: GSAValue, Ti <: GSAIndex, S}
+        promote_type(T, S) === T || return invoke(Base.:+, Tuple{$Parent, UniformScaling}, A, J)
         m, n = size(A)
         m == n || throw(DimensionMismatch("Matrix must be square to add UniformScaling."))
         iszero(J.λ) && return copy(A)
-        return _compressed_sum(A, nothing, J.λ)
+        return _compressed_sum(A, nothing, T(J.λ))
     end
 end
 
