@@ -1,6 +1,6 @@
 """Run one benchmark workload a few times, for a profiler to capture its kernels.
 
-    python genericsparsearrays.jl_gb300/profile_cases.py CASE [--reps N]
+    python bench_support/profile_cases.py CASE [--reps N]
 
 Cases (the bench workloads, same seeds):
   laplacian_csr_f64_i32   CSR SpMV of the 2048^2 5-point Laplacian, Float64 / Int32

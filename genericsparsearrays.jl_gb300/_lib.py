@@ -21,7 +21,7 @@ IDX32, IDX64 = 0, 1
 OP_N, OP_T, OP_C = 0, 1, 2
 SUM_NEGATE = 4
 ALGO_AUTO, ALGO_MERGE, ALGO_VECTOR, ALGO_PIPE = 0, 1, 2, 3
-TUNE_PIPE_THREADS, TUNE_SPMM_COLUMNS, TUNE_PLAN_ORDER = 1, 2, 3
+TUNE_PIPE_THREADS, TUNE_SPMM_COLUMNS, TUNE_PLAN_ORDER, TUNE_WAIT_LIMIT = 1, 2, 3, 4
 BATCH_GROUPED, BATCH_GRAPH, BATCH_PER_CALL = 0, 1, 2
 
 # Every exported symbol of include/gsa.h with its ctypes signature.
@@ -32,7 +32,6 @@ SIGNATURES = {
     "gsa_version": ([], _i32),
     "gsa_last_error_string": ([], ctypes.c_char_p),
     "gsa_set_kernel_timer": ([_vp, _vp], None),
-    "gsa_probe_fma_rate": ([_vp, _i32, _i64, ctypes.POINTER(ctypes.c_double)], _i32),
     "gsa_set_tuning": ([_i32, _i32], _i32),
     "gsa_get_tuning": ([_i32], _i32),
     "gsa_csr_mul": (_MUL + [_i32, _vp, _sz], _i32),

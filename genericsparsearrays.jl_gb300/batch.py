@@ -29,11 +29,12 @@ ITEM_DTYPE = np.dtype([("rowptr", "<u8"), ("colval", "<u8"), ("nzval", "<u8"), (
 assert ITEM_DTYPE.itemsize == 144
 
 
-def bin_order_of(A) -> Tuple[int, int]:
-    """(device view, warps) of the bin order of A's plan when A's products are FP64-bound
-    (ComplexF64: every idle lane is lost FP64 time); (0, 0) otherwise.  Makes the plan on
-    first use (one synchronisation) and keeps it on the matrix."""
-    if A.dtype != torch.complex128:
+def bin_order_of(A, k: int = 1) -> Tuple[int, int]:
+    """(device view, warps) of the bin order of A's plan when a product of A with k
+    right-hand sides is FP64-bound (ComplexF64, or Float64 with k > 1: every idle lane is lost
+    FP64 time); (0, 0) otherwise.  Makes the plan on first use (one synchronisation) and keeps
+    it on the matrix."""
+    if not (A.dtype == torch.complex128 or (A.dtype == torch.float64 and k > 1)):
         return 0, 0
     plan = _gather_plan(A)
     if plan is None:
@@ -74,7 +75,8 @@ def _dense_in(t: torch.Tensor) -> Tuple[int, int, int]:
 def pack_items(products: Sequence[Product], out: Optional[np.ndarray] = None,
                use_plans: bool = True) -> Tuple[np.ndarray, torch.dtype, torch.dtype]:
     """The ``gsa_group_item`` array of a product list (checks as ``mul!`` does).  With
-    use_plans, ComplexF64 items carry their plan's bin order (see bin_order_of)."""
+    use_plans, FP64-bound items (ComplexF64, Float64 with k > 1) carry their plan's bin order
+    (see bin_order_of)."""
     if not products:
         raise ArgumentError("no products")
     dt, it = products[0][0].dtype, products[0][0].itype
@@ -102,7 +104,7 @@ def pack_items(products: Sequence[Product], out: Optional[np.ndarray] = None,
         row["B"], row["C"] = B.data_ptr(), C.data_ptr()
         row["m"], row["n"], row["nnz"], row["ldb"], row["ldc"], row["k"] = A.m, A.n, nnz(A), ldb, ldc, kb
         row["b_rowmajor"] = brow
-        row["bin_order"], row["bin_warps"] = bin_order_of(A) if use_plans else (0, 0)
+        row["bin_order"], row["bin_warps"] = bin_order_of(A, kb) if use_plans else (0, 0)
         a = _scalar_buf(alpha, dt).view(np.uint8)
         b = _scalar_buf(beta, dt).view(np.uint8)
         row["alpha"][:] = 0

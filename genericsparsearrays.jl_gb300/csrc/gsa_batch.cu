@@ -88,10 +88,9 @@ grouped_kernel(const gsa_group_item *__restrict__ items, int64_t count, int64_t 
             if (w < bin_warps) {
                 const gsa_bin_order *bo = (const gsa_bin_order *)__ldg((const unsigned long long *)&it->bin_order);
                 const gsa_bin_order bv{__ldg(&bo->nwarps),
-                                       (const int64_t *)__ldg((const unsigned long long *)&bo->perm),
-                                       (const int64_t *)__ldg((const unsigned long long *)&bo->seg),
-                                       (const uint8_t *)__ldg((const unsigned long long *)&bo->warp_bin),
-                                       (const int64_t *)__ldg((const unsigned long long *)&bo->bins)};
+                                       (const int32_t *)__ldg((const unsigned long long *)&bo->perm),
+                                       (const int32_t *)__ldg((const unsigned long long *)&bo->warp_group),
+                                       (const int64_t *)__ldg((const unsigned long long *)&bo->groups)};
                 binned_warp<V, I, KC>(a, kk, B, C, cg * KC, w, bv);
             }
         } else {

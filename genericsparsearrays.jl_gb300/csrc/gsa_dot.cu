@@ -146,15 +146,7 @@ __device__ __forceinline__ V dot_binned_rows(const CompressedArgs<V, I> &a, cons
     const bool valid = i < pend;
     int64_t o = 0;
     O b = 0, e = 0;
-    if (valid) {
-        o = __ldg(bv.perm + i);
-        const O nz = (O)a.nnz;
-        b = (O)__ldg(bv.seg + 2 * i);
-        e = (O)__ldg(bv.seg + 2 * i + 1);
-        b = b < nz ? b : nz;
-        e = e < nz ? e : nz;
-        e = e < b ? b : e;
-    }
+    if (valid) o = bin_row(a, bv, i, b, e);
     V s = dot_range<V, I, G, (G == 1 ? 1 : 2)>(a, d, b + (O)(lane % G), e);
     if (G > 1) {
 #pragma unroll
@@ -171,11 +163,9 @@ dot_binned_kernel(CompressedArgs<V, I> a, DotVecs<V> d, gsa_bin_order bv, PlanRo
     const int64_t w = (int64_t)blockIdx.x * RB_WARPS + (threadIdx.x >> 5);
     V t = VT<V>::zero();
     if (w < bv.nwarps) {
-        const int bi = __ldg(bv.warp_bin + w);
-        const int64_t first_warp = __ldg(bv.bins + 4 * bi), pos = __ldg(bv.bins + 4 * bi + 1);
-        const int64_t pend = __ldg(bv.bins + 4 * bi + 2);
-        const int G = (int)__ldg(bv.bins + 4 * bi + 3);
-        const int64_t pos0 = pos + (w - first_warp) * (32 / G);
+        int64_t pos0, pend;
+        int G;
+        bin_warp(bv, w, pos0, pend, G);
         dispatch_lanes(G, 1, [&](auto g) { t = dot_binned_rows<V, I, decltype(g)::value>(a, d, pos0, pend, bv); });
     } else if (w - bv.nwarps < L.nchunks) {  // a chunk of a row over 512 entries
         const int64_t chunk = w - bv.nwarps;
@@ -292,10 +282,11 @@ int launch_dot(cudaStream_t s, int fmt, int opA, int64_t m, int64_t n, int64_t n
         a.conjA = conjA;
         // CSR N and CSC T/C: x pairs with the outer index
         const DotVecs<V> d{x, y, csr ? !trans : trans};
-        if (plan && plan->nbin_warps > 0 && std::is_same<V, cf64>::value) {  // FP64-bound: bin order
+        if constexpr (std::is_same<V, cf64>::value)  // FP64-bound: bin order (no other instances)
+        if (plan && plan->nbin_warps > 0) {
             if (plan->outer_n != a.outer_n || plan->nnz != nnz)
                 return fail(GSA_ERR_INVALID_ARG, "plan was made for another structure");
-            const gsa_bin_order bv{plan->nbin_warps, plan->perm, plan->seg, plan->warp_bin, plan->bins};
+            const gsa_bin_order bv = plan->order;
             const PlanRows L = plan_rows(plan->bin);
             const int64_t units = ceil_div(plan->nbin_warps + plan->bin.nchunks, RB_WARPS);
             slots = units * RB_WARPS;

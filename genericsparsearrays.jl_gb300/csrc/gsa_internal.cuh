@@ -14,9 +14,11 @@
 // blocks, outer entries of more than 512 stored entries, and those of more than 32 that
 // are over 4x the average of their aligned group of 32, are cut into chunks of 512 (the
 // `nat` set, marked in its skip_mask).  When lengths vary so much inside groups of 32
-// that lanes would idle, the plan also has a bin order: the entries of at most 512
-// grouped by length (exactly up to 32, then by powers of two), each bin with its lanes
-// per entry, so that the lanes of a warp do equal work; longer ones are chunked (`bin`).
+// that lanes would idle, the plan also has a bin order: within each segment of 32768
+// consecutive outer entries, the entries of at most 512 sorted by the number of
+// multiply-adds each of their lanes does and grouped by their lanes per entry, so that the
+// lanes of a warp do equal work and a segment's entries are read close together in time;
+// longer ones are chunked (`bin`).
 struct gsa_chunk_set {
     int64_t nlong = 0, nchunks = 0;       // chunked entries and their chunks
     const int64_t *row = nullptr;         // outer index of each chunked entry
@@ -26,13 +28,13 @@ struct gsa_chunk_set {
     const uint32_t *skip_mask = nullptr;  // bit per outer entry, 1 = chunked
 };
 // A plan's bin order as the kernels read it (also copied into the plan's device memory,
-// for grouped launches whose items point at it).
+// for grouped launches whose items point at it).  A group is one lanes-per-entry class of
+// one segment.
 struct gsa_bin_order {
-    int64_t nwarps;            // warps of the bin order
-    const int64_t *perm;       // outer entries, bin by bin
-    const int64_t *seg;        // [begin, end) of each, 0-based
-    const uint8_t *warp_bin;   // bin of each warp
-    const int64_t *bins;       // per bin: first warp, first position, end position, lanes
+    int64_t nwarps;             // warps of the bin order
+    const int32_t *perm;        // outer entries, group by group (extents from the pointers)
+    const int32_t *warp_group;  // group of each warp
+    const int64_t *groups;      // per group: first warp, first position, end position, lanes
 };
 struct gsa_plan {
     int64_t outer_n = 0, nnz = 0, max_len = 0;
@@ -41,11 +43,8 @@ struct gsa_plan {
     gsa_chunk_set bin;                    // bin order: > 512 only
     // bin order (nbin_warps > 0)
     int64_t nbin_warps = 0;
-    const int64_t *perm = nullptr;        // outer entries of at most 512 entries, bin by bin
-    const int64_t *seg = nullptr;         // [begin, end) of each, 0-based
-    const uint8_t *warp_bin = nullptr;    // bin of each warp of the bin order
-    const int64_t *bins = nullptr;        // per bin: first warp, first position, end, lanes
-    const gsa_bin_order *bin_view = nullptr;  // device copy of the five fields above
+    gsa_bin_order order{};                // its arrays (device pointers)
+    const gsa_bin_order *bin_view = nullptr;  // device copy of `order`
     void *mem = nullptr;
     // COO plans (gsa_coo_plan_create): row pointers of a row-sorted COO (owned), the rest of
     // the plan describing them; coo_sorted = 0 leaves the COO kernel in charge
@@ -465,6 +464,8 @@ int launch_spmv_noalloc(cudaStream_t s, const CompressedArgs<V, I> &a, DenseIn<V
 int read_pipe_error(cudaStream_t s, int *out);
 void set_pipe_threads(int t);
 int get_pipe_threads();
+void set_wait_limit(uint32_t polls);  // polls of a bounded wait before it gives up
+uint32_t get_wait_limit();
 void set_spmm_columns(int c);   // 0 (by value size), 1, 2, 4 or 8
 int get_spmm_columns();
 void set_plan_natural(int v);   // 1: row blocks in natural order even where a plan bins them

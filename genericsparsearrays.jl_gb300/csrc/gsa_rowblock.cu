@@ -23,6 +23,7 @@
 // Without a plan such a row is one group's work like any other.
 //
 // Every row's summation order is fixed, so results are deterministic.
+#include <algorithm>
 #include <atomic>
 #include <vector>
 
@@ -39,7 +40,16 @@ namespace gsa {
 #endif
 template <typename V, int KC> constexpr int rb_min_blocks() { return KC * sizeof(V) <= 8 ? GSA_RB_MIN_BLOCKS : 0; }
 
-template <typename V> constexpr bool bins_pay() { return std::is_same<V, cf64>::value; }
+// The bin order pays where the FP64 pipe binds: ComplexF64 products (four FMAs per entry)
+// and Float64 products with several right-hand sides (one FMA per entry and column); a
+// Float64 SpMV is HBM-bound, and there the scattered rows cost more traffic than idle lanes
+// cost time (Poisson(10), 2M rows: 112 us natural vs 226 us binned).
+template <typename V> constexpr bool bins_possible() {
+    return std::is_same<V, cf64>::value || std::is_same<V, double>::value;
+}
+template <typename V> inline bool bins_pay(int64_t k) {
+    return std::is_same<V, cf64>::value || (std::is_same<V, double>::value && k > 1);
+}
 
 // One warp sums chunk `chunk` of a chunked row (entries [jb, je), 32 lanes, UNROLL loads
 // each in flight).  A row of one chunk is stored at once; otherwise the warp stores its
@@ -124,11 +134,14 @@ rowblock_kernel(CompressedArgs<V, I> a, int64_t k, DenseIn<V> B, DenseOut<V> C, 
 }
 
 // ---------------------------------------------------------------------------
-// Bin order: the plan lists the rows bin by bin (rows of equal length up to 32, then of
-// lengths within a power of two), each bin with its lanes per row; warp w of the order
-// takes 32 / G consecutive rows of its bin.  All lanes of a warp then do about the same
-// number of multiply-adds: FP64 products on GB300 are bound by the FP64 pipe, which
-// counts a warp instruction whole however few of its lanes are active.
+// Bin order: within each segment of BIN_SEGMENT rows the plan sorts the rows by the
+// multiply-adds each of their lanes does (rows up to 32 entries with a lane each, longer
+// ones with G = 2, 4, 8 or 16 lanes, each lane 17 to 32 entries) and warp w of the order
+// takes 32 / G consecutive rows of one lanes-per-row class of one segment.  The lanes of a
+// warp then do the same number of multiply-adds, or one apart: FP64 products on GB300 are
+// bound by the FP64 pipe, which counts a warp instruction whole however few of its lanes
+// are active.  A segment's rows are read close together in time, so the sectors that
+// neighbouring rows share are still in L2 when the second of them is read.
 
 template <typename V, typename I, int KC>
 __global__ void __launch_bounds__(RB_THREADS, rb_min_blocks<V, KC>())
@@ -167,9 +180,7 @@ int launch_rowblock(cudaStream_t s, const CompressedArgs<V, I> &a, int64_t k, De
     const int64_t ncg = ceil_div(k, KC);
     if (plan && (plan->outer_n != a.outer_n || plan->nnz != a.nnz))
         return fail(GSA_ERR_INVALID_ARG, "plan was made for another structure");
-    // the bin order pays where the FP64 pipe binds (ComplexF64: four FMAs per entry);
-    // elsewhere its scattered rows cost more memory traffic than idle lanes cost time
-    const bool binned = plan && plan->nbin_warps > 0 && !get_plan_natural() && bins_pay<V>();
+    const bool binned = plan && plan->nbin_warps > 0 && !get_plan_natural() && bins_pay<V>(k);
     PlanRows L{};
     int64_t chunk_warps = 0;
     const gsa_chunk_set *cs = plan ? (binned ? &plan->bin : &plan->nat) : nullptr;
@@ -191,14 +202,16 @@ int launch_rowblock(cudaStream_t s, const CompressedArgs<V, I> &a, int64_t k, De
     const int64_t blocks = units * ncg;
     if (blocks > 0x7fffffffLL) return fail(GSA_ERR_UNSUPPORTED, "too many rows");
     timer_before(s);
-    if (binned) {
-        const gsa_bin_order bv{plan->nbin_warps, plan->perm, plan->seg, plan->warp_bin, plan->bins};
-        if (KC == 1) binned_kernel<V, I, 1><<<(unsigned)blocks, RB_THREADS, 0, s>>>(a, k, B, C, ncg, bv, L);
-        else if (KC == 2) binned_kernel<V, I, 2><<<(unsigned)blocks, RB_THREADS, 0, s>>>(a, k, B, C, ncg, bv, L);
-        else if (KC == 4) binned_kernel<V, I, 4><<<(unsigned)blocks, RB_THREADS, 0, s>>>(a, k, B, C, ncg, bv, L);
-        else binned_kernel<V, I, 8><<<(unsigned)blocks, RB_THREADS, 0, s>>>(a, k, B, C, ncg, bv, L);
-        timer_after(s);
-        return check_cuda(cudaGetLastError(), "binned_kernel");
+    if constexpr (bins_possible<V>()) {  // the only types a bin order runs for: no other instances
+        if (binned) {
+            const gsa_bin_order bv = plan->order;
+            if (KC == 1) binned_kernel<V, I, 1><<<(unsigned)blocks, RB_THREADS, 0, s>>>(a, k, B, C, ncg, bv, L);
+            else if (KC == 2) binned_kernel<V, I, 2><<<(unsigned)blocks, RB_THREADS, 0, s>>>(a, k, B, C, ncg, bv, L);
+            else if (KC == 4) binned_kernel<V, I, 4><<<(unsigned)blocks, RB_THREADS, 0, s>>>(a, k, B, C, ncg, bv, L);
+            else binned_kernel<V, I, 8><<<(unsigned)blocks, RB_THREADS, 0, s>>>(a, k, B, C, ncg, bv, L);
+            timer_after(s);
+            return check_cuda(cudaGetLastError(), "binned_kernel");
+        }
     }
     if (KC == 1) rowblock_kernel<V, I, 1><<<(unsigned)blocks, RB_THREADS, 0, s>>>(a, k, B, C, ncg, nrb, L);
     else if (KC == 2) rowblock_kernel<V, I, 2><<<(unsigned)blocks, RB_THREADS, 0, s>>>(a, k, B, C, ncg, nrb, L);
@@ -232,17 +245,19 @@ size_t rowblock_workspace_size(const Plan *plan, size_t vsize, int64_t k) {
 // Plans.
 
 // Bin of a row of len <= CHUNK entries and its lanes per row: rows of equal length up to
-// 32 (a lane each), then (32, 64], (64, 128], (128, 256], (256, 512] with 2, 4, 8, 16
-// lanes -- every lane sums 16 to 32 entries before the width-G reduction.
-constexpr int NBINS = 37;
+// 32 (a lane each), then for 32 < len <= 512 the G = 2, 4, 8 or 16 lanes with 16 <
+// ceil(len / G) <= 32 and one bin per value of ceil(len / G): every lane of a warp does
+// the same number of multiply-adds, 17 to 32, before the width-G reduction.
+constexpr int NBINS = 97;
+constexpr int64_t BIN_SEGMENT = 32768;  // rows per segment of the bin order
 static int bin_of(int64_t len) {
     if (len <= 32) return (int)len;
-    if (len <= 64) return 33;
-    if (len <= 128) return 34;
-    if (len <= 256) return 35;
-    return 36;
+    int lg = 1;
+    while (((int64_t)32 << lg) < len) ++lg;  // G = 2^lg lanes: 32 * G >= len
+    const int64_t q = (len + ((int64_t)1 << lg) - 1) >> lg;  // 17 .. 32
+    return 33 + (lg - 1) * 16 + (int)(q - 17);
 }
-static int bin_lanes(int b) { return b <= 32 ? 1 : 1 << (b - 32); }
+static int bin_lanes(int b) { return b <= 32 ? 1 : 1 << (1 + (b - 33) / 16); }
 
 // Lane utilisation of the natural order: the fraction of lane-iterations that do a
 // multiply-add when a warp of 32 rows runs G lanes per row (G from the rows' average, as
@@ -281,13 +296,12 @@ static int build_plan(cudaStream_t s, int64_t outer_n, int64_t nnz, const I *ptr
     if (rc) return rc;
     rc = check_cuda(cudaStreamSynchronize(s), "plan: sync");
     if (rc) return rc;
-    std::vector<int64_t> beg((size_t)outer_n), len((size_t)outer_n);
+    std::vector<int64_t> len((size_t)outer_n);
     int64_t maxlen = 0;
     for (int64_t r = 0; r < outer_n; ++r) {
         int64_t b = (int64_t)h[r] - base, e = (int64_t)h[r + 1] - base;
         b = b < 0 ? 0 : (b > nnz ? nnz : b);
         e = e < b ? b : (e > nnz ? nnz : e);
-        beg[r] = b;
         len[r] = e - b;
         maxlen = len[r] > maxlen ? len[r] : maxlen;
     }
@@ -307,7 +321,7 @@ static int build_plan(cudaStream_t s, int64_t outer_n, int64_t nnz, const I *ptr
     }
     // bin order when the natural one would leave over a tenth of the lanes idle (only
     // FP64-bound products use it, where every idle lane is lost FP64 time)
-    const bool binned = outer_n >= 32 && natural_utilisation(len, mask_nat) < 0.9;
+    const bool binned = outer_n >= 32 && outer_n <= 0x7fffffffLL && natural_utilisation(len, mask_nat) < 0.9;
     struct HostSet {
         std::vector<int64_t> row;
         std::vector<int32_t> first, count, slot;
@@ -326,46 +340,53 @@ static int build_plan(cudaStream_t s, int64_t outer_n, int64_t nnz, const I *ptr
             for (int64_t q = 0; q < nch; ++q) h2.slot.push_back((int32_t)(h2.row.size() - 1));
         }
     }
-    std::vector<int64_t> perm, seg, bins;
-    std::vector<uint8_t> warp_bin;
-    if (binned) {  // counting sort of the unchunked rows by bin, stable
-        std::vector<int64_t> cnt(NBINS + 1, 0);
-        for (int64_t r = 0; r < outer_n; ++r)
-            if (len[r] <= CHUNK) ++cnt[(size_t)bin_of(len[r]) + 1];
-        for (int b = 0; b < NBINS; ++b) cnt[(size_t)b + 1] += cnt[(size_t)b];
-        perm.resize((size_t)cnt[NBINS]);
-        seg.resize(perm.size() * 2);
-        std::vector<int64_t> at(cnt.begin(), cnt.end() - 1);
-        for (int64_t r = 0; r < outer_n; ++r) {
-            if (len[r] > CHUNK) continue;
-            const int64_t i = at[(size_t)bin_of(len[r])]++;
-            perm[(size_t)i] = r;
-            seg[(size_t)(2 * i)] = beg[r];
-            seg[(size_t)(2 * i + 1)] = beg[r] + len[r];
-        }
-        bins.assign(4 * NBINS, 0);
-        int64_t w = 0;
-        for (int b = 0; b < NBINS; ++b) {
-            const int G = bin_lanes(b);
-            const int64_t nrows = cnt[(size_t)b + 1] - cnt[(size_t)b];
-            const int64_t nw = ceil_div(nrows, 32 / G);
-            bins[4 * b] = w;
-            bins[4 * b + 1] = cnt[(size_t)b];
-            bins[4 * b + 2] = cnt[(size_t)b + 1];
-            bins[4 * b + 3] = G;
-            for (int64_t q = 0; q < nw; ++q) warp_bin.push_back((uint8_t)b);
-            w += nw;
+    std::vector<int32_t> perm, warp_group;
+    std::vector<int64_t> groups;
+    if (binned) {  // per segment, a counting sort of the unchunked rows by bin, stable
+        std::vector<int64_t> cnt(NBINS + 1);
+        for (int64_t s0 = 0; s0 < outer_n; s0 += BIN_SEGMENT) {
+            const int64_t s1 = s0 + BIN_SEGMENT < outer_n ? s0 + BIN_SEGMENT : outer_n;
+            std::fill(cnt.begin(), cnt.end(), 0);
+            for (int64_t r = s0; r < s1; ++r)
+                if (len[r] <= CHUNK) ++cnt[(size_t)bin_of(len[r]) + 1];
+            for (int b = 0; b < NBINS; ++b) cnt[(size_t)b + 1] += cnt[(size_t)b];
+            const int64_t base_pos = (int64_t)perm.size();
+            perm.resize((size_t)(base_pos + cnt[NBINS]));
+            std::vector<int64_t> at(cnt.begin(), cnt.end() - 1);
+            for (int64_t r = s0; r < s1; ++r) {
+                if (len[r] > CHUNK) continue;
+                perm[(size_t)(base_pos + at[(size_t)bin_of(len[r])]++)] = (int32_t)r;
+            }
+            // one group per lanes-per-row class: its bins are consecutive, so its rows are
+            // sorted by the work of each lane and a warp's 32 / G rows have equal or
+            // adjacent lengths (one partial warp per class and segment, not per bin)
+            for (int b0 = 0; b0 < NBINS;) {
+                const int G = bin_lanes(b0);
+                int b1 = b0;
+                while (b1 < NBINS && bin_lanes(b1) == G) ++b1;
+                const int64_t nrows = cnt[(size_t)b1] - cnt[(size_t)b0];
+                if (nrows > 0) {
+                    const int64_t nw = ceil_div(nrows, 32 / G);
+                    const int64_t gi = (int64_t)groups.size() / 4;
+                    if (gi > 0x7fffffffLL) return fail(GSA_ERR_UNSUPPORTED, "plan: too many bin groups");
+                    groups.push_back((int64_t)warp_group.size());
+                    groups.push_back(base_pos + cnt[(size_t)b0]);
+                    groups.push_back(base_pos + cnt[(size_t)b1]);
+                    groups.push_back(G);
+                    for (int64_t q = 0; q < nw; ++q) warp_group.push_back((int32_t)gi);
+                }
+                b0 = b1;
+            }
         }
     }
     p->outer_n = outer_n;
     p->nnz = nnz;
     p->max_len = maxlen;
-    p->nbin_warps = (int64_t)warp_bin.size();
+    p->nbin_warps = (int64_t)warp_group.size();
     p->nplanned = binned ? outer_n : (int64_t)hs[0].row.size();
     if (p->nplanned == 0) return GSA_OK;
-    size_t bytes = align_up(perm.size() * 8, 256) + align_up(seg.size() * 8, 256) +
-                   align_up(warp_bin.size(), 256) + align_up(bins.size() * 8, 256) +
-                   align_up(sizeof(gsa_bin_order), 256);
+    size_t bytes = align_up(perm.size() * 4, 256) + align_up(warp_group.size() * 4, 256) +
+                   align_up(groups.size() * 8, 256) + align_up(sizeof(gsa_bin_order), 256);
     for (int t = 0; t < 2; ++t)
         bytes += align_up(hs[t].row.size() * 8, 256) + align_up(hs[t].first.size() * 4, 256) +
                  align_up(hs[t].count.size() * 4, 256) + align_up(hs[t].slot.size() * 4, 256) +
@@ -398,27 +419,19 @@ static int build_plan(cudaStream_t s, int64_t outer_n, int64_t nnz, const I *ptr
         c.chunk_slot = d_slot;
         c.skip_mask = d_mask;
     }
-    int64_t *d_perm = cv.take<int64_t>(perm.size());
-    int64_t *d_seg = cv.take<int64_t>(seg.size());
-    uint8_t *d_wb = cv.take<uint8_t>(warp_bin.size());
-    int64_t *d_bins = cv.take<int64_t>(bins.size());
-    up(d_perm, perm.data(), perm.size() * 8, "plan: order");
-    up(d_seg, seg.data(), seg.size() * 8, "plan: extents");
-    up(d_wb, warp_bin.data(), warp_bin.size(), "plan: warp bins");
-    up(d_bins, bins.data(), bins.size() * 8, "plan: bins");
+    int32_t *d_perm = cv.take<int32_t>(perm.size());
+    int32_t *d_wg = cv.take<int32_t>(warp_group.size());
+    int64_t *d_groups = cv.take<int64_t>(groups.size());
+    up(d_perm, perm.data(), perm.size() * 4, "plan: order");
+    up(d_wg, warp_group.data(), warp_group.size() * 4, "plan: warp groups");
+    up(d_groups, groups.data(), groups.size() * 8, "plan: groups");
     gsa_bin_order *d_view = cv.take<gsa_bin_order>(1);
     if (binned) {
-        const gsa_bin_order view{p->nbin_warps, d_perm, d_seg, d_wb, d_bins};
-        up(d_view, &view, sizeof(view), "plan: bin view");
+        p->order = gsa_bin_order{p->nbin_warps, d_perm, d_wg, d_groups};
+        up(d_view, &p->order, sizeof(gsa_bin_order), "plan: bin view");
     }
     if (rc) return rc;
-    if (binned) {
-        p->perm = d_perm;
-        p->seg = d_seg;
-        p->warp_bin = d_wb;
-        p->bins = d_bins;
-        p->bin_view = d_view;
-    }
+    if (binned) p->bin_view = d_view;
     return GSA_OK;
 }
 

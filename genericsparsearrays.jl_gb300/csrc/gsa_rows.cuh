@@ -205,8 +205,37 @@ __device__ __forceinline__ void warp_unit(const CompressedArgs<V, I> &a, int64_t
 }
 
 // ---------------------------------------------------------------------------
-// Bin order (a plan's): rows grouped by length, warp w of the order takes 32 / G
-// consecutive rows of its bin, G lanes each, so the lanes of a warp do equal work.
+// Bin order (a plan's): within each segment of rows, rows grouped by the multiply-adds each
+// of their lanes does; warp w of the order takes 32 / G consecutive rows of its group, G
+// lanes each, so the lanes of a warp do equal work.
+
+// Position range [pos0, pend) of warp w of a bin order and its lanes per row.
+__device__ __forceinline__ void bin_warp(const gsa_bin_order &bv, int64_t w, int64_t &pos0, int64_t &pend, int &G) {
+    const int gi = __ldg(bv.warp_group + w);
+    const int64_t first_warp = __ldg(bv.groups + 4 * gi), pos = __ldg(bv.groups + 4 * gi + 1);
+    pend = __ldg(bv.groups + 4 * gi + 2);
+    G = (int)__ldg(bv.groups + 4 * gi + 3);
+    pos0 = pos + (w - first_warp) * (32 / G);
+}
+
+// Row at position i of a bin order and its extent [b, e), clamped to [0, nnz].
+template <typename V, typename I>
+__device__ __forceinline__ int64_t bin_row(const CompressedArgs<V, I> &a, const gsa_bin_order &bv, int64_t i,
+                                           Off<I> &b, Off<I> &e) {
+    using O = Off<I>;
+    const int64_t row = __ldg(bv.perm + i);
+    if (row >= a.outer_n) {
+        b = e = 0;
+        return row;
+    }
+    const O nz = (O)a.nnz, base = (O)a.base;
+    b = (O)__ldg(a.ptr + row) - base;
+    e = (O)__ldg(a.ptr + row + 1) - base;
+    b = b < nz ? b : nz;
+    e = e < nz ? e : nz;
+    e = e < b ? b : e;
+    return row;
+}
 
 template <typename V, typename I, int KC, int G>
 __device__ __forceinline__ void binned_rows(const CompressedArgs<V, I> &a, int64_t k, const DenseIn<V> &B,
@@ -218,19 +247,11 @@ __device__ __forceinline__ void binned_rows(const CompressedArgs<V, I> &a, int64
     const bool valid = i < pend;
     int64_t row = 0;
     O b = 0, e = 0;
-    if (valid) {
-        row = __ldg(bv.perm + i);
-        const O nz = (O)a.nnz;
-        b = (O)__ldg(bv.seg + 2 * i);
-        e = (O)__ldg(bv.seg + 2 * i + 1);
-        b = b < nz ? b : nz;
-        e = e < nz ? e : nz;
-        e = e < b ? b : e;
-    }
+    if (valid) row = bin_row(a, bv, i, b, e);
     V acc[KC];
 #pragma unroll
     for (int c = 0; c < KC; ++c) acc[c] = VT<V>::zero();
-    accumulate_range<V, I, KC, G, (G == 1 ? 1 : 2)>(a, B, b + (O)(lane % G), e, c0, k, acc);
+    accumulate_range<V, I, KC, G, 2>(a, B, b + (O)(lane % G), e, c0, k, acc);
     if (G > 1) {
 #pragma unroll
         for (int c = 0; c < KC; ++c) {
@@ -250,11 +271,9 @@ template <typename V, typename I, int KC>
 __device__ __forceinline__ void binned_warp(const CompressedArgs<V, I> &a, int64_t k, const DenseIn<V> &B,
                                             const DenseOut<V> &C, int64_t c0, int64_t w,
                                             const gsa_bin_order &bv) {
-    const int bi = __ldg(bv.warp_bin + w);
-    const int64_t first_warp = __ldg(bv.bins + 4 * bi), pos = __ldg(bv.bins + 4 * bi + 1);
-    const int64_t pend = __ldg(bv.bins + 4 * bi + 2);
-    const int G = (int)__ldg(bv.bins + 4 * bi + 3);
-    const int64_t pos0 = pos + (w - first_warp) * (32 / G);
+    int64_t pos0, pend;
+    int G;
+    bin_warp(bv, w, pos0, pend, G);
     dispatch_lanes(G, 1, [&](auto g) {  // G is a power of two: picks exactly G lanes
         binned_rows<V, I, KC, decltype(g)::value>(a, k, B, C, c0, pos0, pend, bv);
     });

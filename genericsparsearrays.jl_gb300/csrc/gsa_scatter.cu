@@ -235,6 +235,65 @@ scatter_block_kernel(CompressedArgs<V, I> a, int64_t k, DenseIn<V> B, DenseOut<V
     });
 }
 
+// ---------------------------------------------------------------------------
+// Window scatter (GSA_ALGO_VECTOR, one right-hand side): a thread per outer entry, and the
+// products whose output row lies within WIN_HALO rows of the CTA's own outer range -- the
+// band of a banded matrix, where the outer entries of one CTA hit the same rows -- summed in
+// a shared-memory window first, then added with one atomic per touched row of the window.
+// Products outside the window go to the global atomics directly.  The partial sums of the
+// window are combined in shared memory: the adds move from the L2 atomic units to the SM.
+constexpr int WIN_THREADS = 128;
+constexpr int WIN_HALO = 64;
+constexpr int WIN_ROWS = WIN_THREADS + 2 * WIN_HALO;
+
+__device__ __forceinline__ void smem_add(float *p, float v) { atomicAdd(p, v); }
+__device__ __forceinline__ void smem_add(double *p, double v) { atomicAdd(p, v); }
+__device__ __forceinline__ void smem_add(cf32 *p, cf32 v) { atomicAdd(&p->re, v.re); atomicAdd(&p->im, v.im); }
+__device__ __forceinline__ void smem_add(cf64 *p, cf64 v) { atomicAdd(&p->re, v.re); atomicAdd(&p->im, v.im); }
+__device__ __forceinline__ void smem_add(int32_t *p, int32_t v) { atomicAdd((int *)p, (int)v); }
+__device__ __forceinline__ void smem_add(int64_t *p, int64_t v) {
+    atomicAdd((unsigned long long *)p, (unsigned long long)v);
+}
+
+template <typename V, typename I>
+__global__ void __launch_bounds__(WIN_THREADS)
+scatter_window_kernel(CompressedArgs<V, I> a, DenseIn<V> B, DenseOut<V> C, int64_t out_rows) {
+    using O = Off<I>;
+    __shared__ V s_acc[WIN_ROWS];
+    __shared__ uint32_t s_touched[WIN_ROWS / 32];
+    const int tid = threadIdx.x;
+    const int64_t o0 = (int64_t)blockIdx.x * WIN_THREADS;
+    const int64_t lo = o0 - WIN_HALO;  // output row of window slot 0 (may be negative)
+    for (int w = tid; w < WIN_ROWS; w += WIN_THREADS) s_acc[w] = VT<V>::zero();
+    if (tid < WIN_ROWS / 32) s_touched[tid] = 0u;
+    __syncthreads();
+    const int64_t o = o0 + tid;
+    if (o < a.outer_n) {
+        const O nz = (O)a.nnz, base = (O)a.base;
+        O j = (O)__ldg(a.ptr + o) - base;
+        O je = (O)__ldg(a.ptr + o + 1) - base;
+        j = j < nz ? j : nz;
+        je = je < nz ? je : nz;
+        const V xa = alpha_times(C, B.at(o, 0));
+        const uint64_t rows = (uint64_t)out_rows;
+        for (; j < je; ++j) {
+            const int64_t r = (int64_t)ld_stream(a.idx + j) - a.base;
+            const V pr = mul(conj_if(ld_stream(a.val + j), a.conjA), xa);
+            if ((uint64_t)r >= rows) continue;
+            const int64_t w = r - lo;
+            if (w >= 0 && w < WIN_ROWS) {
+                smem_add(&s_acc[w], pr);
+                atomicOr(&s_touched[w >> 5], 1u << (w & 31));
+            } else {
+                atomic_add(C.p + r, pr);
+            }
+        }
+    }
+    __syncthreads();
+    for (int w = tid; w < WIN_ROWS; w += WIN_THREADS)
+        if ((s_touched[w >> 5] >> (w & 31)) & 1u) atomic_add(C.p + (lo + w), s_acc[w]);
+}
+
 template <typename V, typename I>
 int launch_scatter_block(cudaStream_t s, const CompressedArgs<V, I> &a, int64_t k, DenseIn<V> B,
                          DenseOut<V> C, const Plan *plan) {
@@ -278,6 +337,14 @@ int launch_scatter(cudaStream_t s, const CompressedArgs<V, I> &a, int64_t k, Den
     int rc = launch_rmul_or_fill<V>(s, C, out_rows, k);
     if (rc) return rc;
     if (a.outer_n == 0 || a.nnz == 0 || k == 0) return GSA_OK;
+    if (algo == GSA_ALGO_VECTOR && k == 1) {
+        const int64_t blocks = ceil_div(a.outer_n, WIN_THREADS);
+        if (blocks > 0x7fffffffLL) return fail(GSA_ERR_UNSUPPORTED, "too many outer entries");
+        timer_before(s);
+        scatter_window_kernel<V, I><<<(unsigned)blocks, WIN_THREADS, 0, s>>>(a, B, C, out_rows);
+        timer_after(s);
+        return check_cuda(cudaGetLastError(), "scatter_window_kernel");
+    }
     if (algo != GSA_ALGO_MERGE) return launch_scatter_block<V, I>(s, a, k, B, C, plan);
     constexpr int TILE = ScatterShape<V>::TILE;
     const int64_t T = ceil_div(a.outer_n + a.nnz, TILE);

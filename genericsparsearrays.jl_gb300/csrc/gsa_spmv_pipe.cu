@@ -39,7 +39,12 @@ __device__ int g_pipe_error = 0;
 
 constexpr int SHORT_ROW = 32;               // thread-per-row limit
 constexpr int WARP_ROW = 1024;              // warp-per-row limit
-constexpr uint32_t WAIT_LIMIT = 1u << 24;   // bounded mbarrier polls
+constexpr uint32_t WAIT_LIMIT = 1u << 24;   // bounded mbarrier polls (default)
+// Polls before a tile's wait gives up (gsa_set_tuning(GSA_TUNE_WAIT_LIMIT); a small value
+// makes the timeout path run).  Draining copies after a give-up always uses WAIT_LIMIT.
+static std::atomic<uint32_t> g_wait_limit{WAIT_LIMIT};
+void set_wait_limit(uint32_t polls) { g_wait_limit.store(polls, std::memory_order_relaxed); }
+uint32_t get_wait_limit() { return g_wait_limit.load(std::memory_order_relaxed); }
 
 template <typename V> struct PipeShape {
     static constexpr int TILE = sizeof(V) >= 16 ? 1024 : 2048;
@@ -152,7 +157,7 @@ __device__ __forceinline__ V load_x(const CompressedArgs<V, I> &a, const DenseIn
 template <typename V, typename I, int THREADS>
 __global__ void __launch_bounds__(THREADS, THREADS >= 512 ? 2 : 3)
 spmv_pipe_kernel(CompressedArgs<V, I> a, DenseIn<V> B, DenseOut<V> C, int64_t tiles_per_cta,
-                 int64_t *__restrict__ carry_row, V *__restrict__ carry_val) {
+                 int64_t *__restrict__ carry_row, V *__restrict__ carry_val, uint32_t wait_limit) {
     using S_t = PipeSmem<V, I, THREADS>;
     constexpr int TILE = S_t::TILE;
     constexpr int WARPS = S_t::WARPS;
@@ -180,12 +185,14 @@ spmv_pipe_kernel(CompressedArgs<V, I> a, DenseIn<V> B, DenseOut<V> C, int64_t ti
                                          D0 < a.outer_n ? D0 : a.outer_n, D0);
     int64_t js = D0 - rs;
 
+    uint32_t inflight = 0u;  // bit st: stage st has copies not yet waited for (thread 0's view)
     // copies of [j0, min(j0 + TILE, nnz)) into stage st
     auto issue = [&](int st, int64_t j0) {
         j0 = j0 < 0 ? 0 : (j0 > a.nnz ? a.nnz : j0);
         const int64_t j1 = j0 + TILE < a.nnz ? j0 + TILE : a.nnz;
         const Segment sc(a.idx, j0, j1, sizeof(I)), sv(a.val, j0, j1, sizeof(V));
         if (tid == 0) {
+            inflight |= 1u << st;
             fence_proxy_async_smem();
             mbar_arrive_expect_tx(&S.bar[st], sc.interior_bytes() + sv.interior_bytes());
             if (sc.has_interior())
@@ -266,9 +273,12 @@ spmv_pipe_kernel(CompressedArgs<V, I> a, DenseIn<V> B, DenseOut<V> C, int64_t ti
         }
         // ---- wait for this tile's streams
         bool ok = false;
-        for (uint32_t w = 0; w < WAIT_LIMIT; ++w)
+        for (uint32_t w = 0; w < wait_limit; ++w)
             if ((ok = mbar_try_wait(&S.bar[st], (parity >> st) & 1u))) break;
-        if (ok) parity ^= 1u << st;
+        if (ok) {
+            parity ^= 1u << st;
+            inflight &= ~(1u << st);
+        }
         if (__syncthreads_or(!ok)) { failed = true; break; }
 
         const Segment sc(a.idx, js, js, sizeof(I)), sv(a.val, js, js, sizeof(V));
@@ -357,12 +367,16 @@ spmv_pipe_kernel(CompressedArgs<V, I> a, DenseIn<V> B, DenseOut<V> C, int64_t ti
         d0 = d1;
     }
     if (failed) {
-        // let copies still in flight land before the CTA's shared memory goes away
+        // let copies still in flight land before the CTA's shared memory goes away (the
+        // stages thread 0 issued and has not seen complete; the default bound, whatever
+        // the tile waits used)
         if (tid == 0) {
             atomicOr(&g_pipe_error, 1);
-            for (int st = 0; st < 2; ++st)
-                for (uint32_t w = 0; w < WAIT_LIMIT / 16; ++w)
+            for (int st = 0; st < 2; ++st) {
+                if (!((inflight >> st) & 1u)) continue;
+                for (uint32_t w = 0; w < WAIT_LIMIT; ++w)
                     if (mbar_try_wait(&S.bar[st], (parity >> st) & 1u)) break;
+            }
             carry_row[blockIdx.x] = -1;
         }
         return;
@@ -430,7 +444,7 @@ static int launch_pipe_impl(cudaStream_t s, const CompressedArgs<V, I> &a, Dense
     int64_t *carry_row = cv.take<int64_t>(T);
     V *carry_val = cv.take<V>(T);
     timer_before(s);
-    kern<<<(unsigned)G, THREADS, smem, s>>>(a, B, C, Q, carry_row, carry_val);
+    kern<<<(unsigned)G, THREADS, smem, s>>>(a, B, C, Q, carry_row, carry_val, get_wait_limit());
     timer_after(s);
     rc = check_cuda(cudaGetLastError(), "spmv_pipe_kernel");
     if (rc) return rc;
@@ -512,7 +526,7 @@ static int launch_noalloc_impl(cudaStream_t s, const CompressedArgs<V, I> &a, De
     if (rc) return rc;
     int64_t *carry_row = reinterpret_cast<int64_t *>(scratch);
     V *carry_val = reinterpret_cast<V *>(scratch + NOALLOC_MAX_RUNS * 8);
-    kern<<<(unsigned)G, THREADS, smem, s>>>(a, B, C, Q, carry_row, carry_val);
+    kern<<<(unsigned)G, THREADS, smem, s>>>(a, B, C, Q, carry_row, carry_val, get_wait_limit());
     rc = check_cuda(cudaGetLastError(), "spmv_pipe_kernel (noalloc)");
     if (rc) return rc;
     pipe_fixup_kernel<V><<<(unsigned)ceil_div(G, 256), 256, 0, s>>>(G, carry_row, carry_val, C);

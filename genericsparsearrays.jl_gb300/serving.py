@@ -7,9 +7,11 @@ admitted under an HBM budget and coalesced into grouped launches (continuous bat
 * ``Server``    the scheduler.  ``submit`` queues a request; every ``step`` retires the
   launches that have finished, expires requests past their deadline, and -- for each free
   launch slot (one CUDA stream each) -- admits queued requests in arrival order while the
-  budget allows and launches them together.  Requests that arrive while others are on the
-  GPU are admitted as slots and memory free up, so their work overlaps the running launch
-  on another stream.
+  budget allows and their work (FP64 multiply-adds) stays under the launch's work cap, and
+  launches them together.  The cap keeps a launch to about a millisecond of GPU time, so a
+  slot frees often; requests that arrive while others are on the GPU are admitted into
+  whichever slot frees first, and their work overlaps the running launches on the other
+  streams.
 * ``GroupedExecutor``  runs one admitted set on the slot's stream: one grouped launch
   (gsa_grouped_mul) per element type for the small products, a plain planned call for each
   large one, timed by CUDA events mapped to the host clock.
@@ -121,6 +123,7 @@ class Request:
     error: Optional[str] = None
     out_bytes: int = 0
     owns_y: bool = False
+    fma: int = 0              # FP64 multiply-adds of the product (set at submission)
 
     @property
     def k(self) -> int:
@@ -131,15 +134,27 @@ class Request:
         return self.finished - self.arrival
 
 
-class Server:
-    """Continuous batching over ``slots`` launch slots; see the module docstring."""
+def product_fma(A, k: int) -> int:
+    """FP64 multiply-adds of y = A x with k right-hand sides: one per stored entry and column,
+    four for a complex one (real types other than Float64 count one as well)."""
+    from .sparse import nnz
+    return nnz(A) * k * (4 if A.dtype.is_complex else 1)
 
-    def __init__(self, registry: Registry, executor, max_batch: int = 1024, slots: int = 2,
-                 clock: Callable[[], float] = time.perf_counter, keep_outputs: bool = True):
+
+class Server:
+    """Continuous batching over ``slots`` launch slots; see the module docstring.
+
+    ``work_cap``: FP64 multiply-adds one launch may take (a request larger than that is
+    launched alone); ``max_batch``: requests one launch may take."""
+
+    def __init__(self, registry: Registry, executor, max_batch: int = 1024, slots: int = 4,
+                 clock: Callable[[], float] = time.perf_counter, keep_outputs: bool = True,
+                 work_cap: int = 1 << 28):
         self.registry = registry
         self.keep_outputs = keep_outputs  # False: drop server-allocated outputs when done
         self.executor = executor
         self.max_batch = int(max_batch)
+        self.work_cap = int(work_cap)
         self.slots = int(slots)
         self.clock = clock
         self.queue: collections.deque = collections.deque()
@@ -147,6 +162,7 @@ class Server:
         self.finished: List[Request] = []
         self.launches = 0
         self._next_id = 0
+        self._deadlines = 0  # queued requests with a deadline (the expiry sweep runs only then)
 
     # -- client side -------------------------------------------------------------
     def submit(self, req: Request) -> int:
@@ -163,6 +179,7 @@ class Server:
             raise DimensionMismatch(f"first dimension of A, {A.m}, does not match the first dimension of C")
         req.id = self._next_id
         self._next_id += 1
+        req.fma = product_fma(A, req.k)
         req.out_bytes = 0 if req.Y is not None else A.m * req.k * _elem_size(A.dtype)
         if req.out_bytes > self.registry.budget - self.registry.resident:
             # even with every running launch retired it would not fit
@@ -171,6 +188,8 @@ class Server:
         req.state = "queued"
         if not req.arrival:
             req.arrival = self.clock()
+        if req.deadline is not None:
+            self._deadlines += 1
         self.queue.append(req)
         return req.id
 
@@ -178,6 +197,8 @@ class Server:
         for r in self.queue:
             if r.id == rid:
                 self.queue.remove(r)
+                if r.deadline is not None:
+                    self._deadlines -= 1
                 self._end(r, "cancelled", "cancelled")
                 return True
         return False  # running or finished: a launch is never interrupted
@@ -222,20 +243,29 @@ class Server:
             self.step()
 
     def _admit(self) -> List[Request]:
-        batch = []
+        batch, work = [], 0
         while self.queue and len(batch) < self.max_batch:
             r = self.queue[0]
+            if batch and work + r.fma > self.work_cap:
+                break  # the launch is full; the next free slot takes it
             if r.out_bytes and not self.registry.reserve(r.out_bytes):
                 if r.out_bytes > self.registry.budget - self.registry.resident:
                     self.queue.popleft()  # matrices registered since it was queued
+                    self._dequeued(r)
                     self._end(r, "rejected", "output does not fit the HBM budget")
                     continue
                 break
             self.queue.popleft()
+            self._dequeued(r)
             if r.Y is None:
                 r.owns_y = True
             batch.append(r)
+            work += r.fma
         return batch
+
+    def _dequeued(self, r: Request) -> None:
+        if r.deadline is not None:
+            self._deadlines -= 1
 
     def _retire(self) -> None:
         for slot in list(self.running):
@@ -253,10 +283,13 @@ class Server:
                 self._end(r, "done" if err is None else "rejected", err)
 
     def _expire(self) -> None:
+        if not self._deadlines:
+            return
         now = self.clock()
         keep = collections.deque()
         for r in self.queue:
             if r.deadline is not None and now > r.deadline:
+                self._deadlines -= 1
                 self._end(r, "expired", "deadline passed while queued")
             else:
                 keep.append(r)
@@ -286,9 +319,10 @@ def summarize(reqs: Sequence[Request], launches: Optional[int] = None) -> dict:
         lat = np.array([r.latency for r in done]) * 1e3
         t0 = min(r.arrival for r in done)
         t1 = max(r.finished for r in done)
+        span = max(t1 - t0, 1e-9)
         out.update({"p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
-                    "mean_ms": float(lat.mean()), "mul_per_s": len(done) / max(t1 - t0, 1e-9),
-                    "span_s": t1 - t0})
+                    "mean_ms": float(lat.mean()), "mul_per_s": len(done) / span,
+                    "fma_per_s": float(sum(r.fma for r in done)) / span, "span_s": t1 - t0})
     return out
 
 
@@ -297,10 +331,10 @@ class GroupedExecutor:
     grouped launch per element type for the small products (pinned item staging, no
     allocation per launch in the library), a plain planned call for each product of at least
     ``solo_fma`` multiply-adds (there a launch is cheap against the work, and the plain call
-    has the plan's chunk warps), then a timing event.  Finish times are CUDA-event times
+    has the plan's chunk warps) and for a set of one, then a timing event.  Finish times are CUDA-event times
     mapped onto the host clock through a reference event taken at construction."""
 
-    def __init__(self, device, slots: int = 2, columns: int = 0, g1_avg: int = 0,
+    def __init__(self, device, slots: int = 4, columns: int = 0, g1_avg: int = 0,
                  clock: Callable[[], float] = time.perf_counter, solo_fma: int = 1 << 24):
         import torch
         from .batch import GroupedLauncher
@@ -327,7 +361,7 @@ class GroupedExecutor:
                     shape = (A.m,) if r.X.dim() == 1 else (r.k, A.m)
                     Y = torch.empty(shape, dtype=A.dtype, device=self.device)
                     r.Y = Y if r.X.dim() == 1 else Y.t()
-                if nnz(A) * r.k >= self.solo_fma:
+                if len(work) == 1 or nnz(A) * r.k >= self.solo_fma:
                     mul_(r.Y, A, r.X, r.alpha, r.beta)
                 else:
                     groups[(A.dtype, A.itype)].append((A, r.X, r.Y, r.alpha, r.beta))
@@ -369,6 +403,7 @@ def serve_per_call(registry: Registry, requests: Sequence[Request], device,
         while clock() < r.arrival:
             pass
         A = registry[r.matrix]
+        r.fma = product_fma(A, r.k)
         if r.Y is None:
             r.Y = torch.empty((A.m,) if r.X.dim() == 1 else (r.k, A.m), dtype=A.dtype, device=dev)
             if r.X.dim() == 2:

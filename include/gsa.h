@@ -66,7 +66,10 @@ typedef enum {
     GSA_ALGO_MERGE = 1,    /* one CTA per merge-path tile (any row-length mix); gather and
                               scatter */
     GSA_ALGO_VECTOR = 2,   /* gather: a group of threads per row (short, even rows);
-                              scatter: as AUTO */
+                              scatter with one right-hand side: a thread per outer entry,
+                              products near the CTA's outer range (a band) summed in a
+                              shared-memory window, one atomic per touched row; with
+                              several right-hand sides as AUTO */
     GSA_ALGO_PIPE = 3      /* gather: persistent merge-path runs with bulk-copy double
                               buffering (one right-hand side); scatter: as AUTO */
 } gsa_algo;
@@ -76,8 +79,12 @@ typedef enum {
     GSA_TUNE_PIPE_THREADS = 1, /* threads per CTA of the pipelined SpMV: 256 or 512 */
     GSA_TUNE_SPMM_COLUMNS = 2, /* right-hand-side columns a thread accumulates in the default
                                   gather with k > 1: 0 (by value size), 1, 2, 4 or 8 */
-    GSA_TUNE_PLAN_ORDER = 3    /* 0: a planned gather runs in the plan's order (bin order
+    GSA_TUNE_PLAN_ORDER = 3,   /* 0: a planned gather runs in the plan's order (bin order
                                   where the plan chose it); 1: always in natural row order */
+    GSA_TUNE_WAIT_LIMIT = 4    /* polls a bounded device-side wait (the pipelined SpMV's
+                                  mbarrier waits for its bulk copies) makes before it gives
+                                  up, sets the device error word and returns: default
+                                  16777216; 0 gives up at once (the timeout path, for tests) */
 } gsa_tune_key;
 
 /* ---- library ------------------------------------------------------------ */
@@ -101,12 +108,6 @@ int gsa_get_tuning(int key);
  * or the whole sort of a conversion.  Pass
  * NULL, NULL to switch it off. */
 void gsa_set_kernel_timer(void *before, void *after);
-
-/* Fused multiply-adds per second the GPU retires for dtype GSA_F32 or GSA_F64 (8
- * independent chains per thread, 2048 threads per SM, `iters` steps each; synchronizes
- * the stream): the arithmetic roofline beside HBM for the product kernels, which do one
- * FMA per real multiply-add.  No counterpart in the reference. */
-int gsa_probe_fma_rate(void *stream, int dtype, int64_t iters, double *fma_per_s);
 
 /* ---- sparse x dense mul! --------------------------------------------------
  * C = beta*C + alpha * op(A) * op(B), with C (rows(op(A)) x k, column-major,

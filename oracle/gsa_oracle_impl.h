@@ -134,11 +134,44 @@ static int FN(mul)(int fmt, int opA, int64_t m, int64_t n, int64_t nnz,
     return 0;
 }
 
+/* |re + i im| without hypot's cost when the imaginary part is zero (real types). */
+static inline double FN(absv)(double re, double im) { return im == 0.0 ? fabs(re) : hypot(re, im); }
+
+/* The double-double contributions of outer entries [olo, ohi) (entries for COO) to
+ * column c of the accumulators. */
+static void FN(exact_range)(int fmt, int conjA, int trans, int64_t rows_out, int64_t c,
+                            int64_t olo, int64_t ohi, const I *p0, const I *p1, const V *val, int base,
+                            const V *B, int64_t ldb, int opB, dd *are, dd *aim, double *abssum) {
+    for (int64_t o = olo; o < ohi; ++o) {
+        int64_t jlo = (fmt == 2) ? o : (int64_t)p0[o] - base;
+        int64_t jhi = (fmt == 2) ? o + 1 : (int64_t)p0[o + 1] - base;
+        for (int64_t j = jlo; j < jhi; ++j) {
+            int64_t row, col;
+            if (fmt == 0) { row = o; col = (int64_t)p1[j] - base; }
+            else if (fmt == 1) { row = (int64_t)p1[j] - base; col = o; }
+            else { row = (int64_t)p0[j] - base; col = (int64_t)p1[j] - base; }
+            int64_t out = trans ? col : row, in = trans ? row : col;
+            double ar, ai, br, bi;
+            V_TO_C(val[j], ar, ai);
+            if (conjA) ai = -ai;
+            V_TO_C(FN(getB)(B, ldb, opB, in, c), br, bi);
+            int64_t t = out + c * rows_out;
+            are[t] = dd_add_dd(are[t], two_prod(ar, br));
+            are[t] = dd_add_dd(are[t], two_prod(-ai, bi));
+            aim[t] = dd_add_dd(aim[t], two_prod(ar, bi));
+            aim[t] = dd_add_dd(aim[t], two_prod(ai, br));
+            abssum[t] += FN(absv)(ar, ai) * FN(absv)(br, bi);
+        }
+    }
+}
+
 /* Error oracle: the same product in double-double, with the per-output scale
  * |alpha| * sum_j |a_j||b_j| + |beta||C0| that the tolerance is relative to.
  * Outputs are doubles: yre/yim and scale, each rows_out x k column-major
  * (yim is ignored for real types).  Contributions are format-agnostic: every
- * stored entry adds a(out, in) * B(in, c) to output out. */
+ * stored entry adds a(out, in) * B(in, c) to output out.  Work is split over the
+ * host threads where no two threads add into one output: over outer entries when
+ * each outer entry owns its output (CSR N, CSC T/C), else over columns of B. */
 static int FN(mul_exact)(int fmt, int opA, int64_t m, int64_t n, int64_t nnz,
                          const void *p0v, const void *p1v, const void *valv, int base,
                          int64_t k, const void *Bv, int64_t ldb, int opB,
@@ -157,28 +190,26 @@ static int FN(mul_exact)(int fmt, int opA, int64_t m, int64_t n, int64_t nnz,
     if (!are || !aim || !abssum) { free(are); free(aim); free(abssum); return 2; }
     int64_t outer_n = (fmt == 0) ? m : n;
     int64_t cnt = (fmt == 2) ? nnz : outer_n;
-    for (int64_t c = 0; c < k; ++c) {
-        for (int64_t o = 0; o < cnt; ++o) {
-            int64_t jlo = (fmt == 2) ? o : (int64_t)p0[o] - base;
-            int64_t jhi = (fmt == 2) ? o + 1 : (int64_t)p0[o + 1] - base;
-            for (int64_t j = jlo; j < jhi; ++j) {
-                int64_t row, col;
-                if (fmt == 0) { row = o; col = (int64_t)p1[j] - base; }
-                else if (fmt == 1) { row = (int64_t)p1[j] - base; col = o; }
-                else { row = (int64_t)p0[j] - base; col = (int64_t)p1[j] - base; }
-                int64_t out = trans ? col : row, in = trans ? row : col;
-                double ar, ai, br, bi;
-                V_TO_C(val[j], ar, ai);
-                if (conjA) ai = -ai;
-                V_TO_C(FN(getB)(B, ldb, opB, in, c), br, bi);
-                int64_t t = out + c * rows_out;
-                are[t] = dd_add_dd(are[t], two_prod(ar, br));
-                are[t] = dd_add_dd(are[t], two_prod(-ai, bi));
-                aim[t] = dd_add_dd(aim[t], two_prod(ar, bi));
-                aim[t] = dd_add_dd(aim[t], two_prod(ai, br));
-                abssum[t] += hypot(ar, ai) * hypot(br, bi);
-            }
+    const int own_rows = (fmt == 0 && !trans) || (fmt == 1 && trans);
+    /* small products stay on the calling thread (callers may check many at once) */
+    const int big = (double)nnz * (double)(k > 0 ? k : 1) >= (double)(1 << 20);
+    if (own_rows) {
+        const int64_t step = 4096;
+        for (int64_t c = 0; c < k; ++c) {
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 1) if (big)
+#endif
+            for (int64_t o = 0; o < cnt; o += step)
+                FN(exact_range)(fmt, conjA, trans, rows_out, c, o, o + step < cnt ? o + step : cnt, p0, p1,
+                                val, base, B, ldb, opB, are, aim, abssum);
         }
+    } else {
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 1) if (big)
+#endif
+        for (int64_t c = 0; c < k; ++c)
+            FN(exact_range)(fmt, conjA, trans, rows_out, c, 0, cnt, p0, p1, val, base, B, ldb, opB, are, aim,
+                            abssum);
     }
     double alr, ali, ber, bei;
     V_TO_C(alpha, alr, ali);

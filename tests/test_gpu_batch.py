@@ -49,14 +49,15 @@ def test_grouped_matches_per_call_and_oracle(gsa, oracle, cuda, dt):
         ye, sc = oracle.mul_exact("csr", "N", m, m, p, c, v, 1, X, Y0, alpha=alpha, beta=beta)
         assert oracle.max_rel_error(g.cpu().numpy(), ye, sc) <= 1e-12
     b.close()
-    # with plans: ComplexF64 items walk their plans' bin order
+    # with plans: ComplexF64 items and Float64 items with k > 1 walk their plans' bin order
     for p, y0 in zip(prods, Y0s):
         p[2].copy_(y0)
     items, _, _ = batch.pack_items(prods)
     if dt == np.complex128:
         assert (items["bin_warps"] > 0).sum() > len(prods) // 2
-    else:
-        assert (items["bin_warps"] == 0).all()
+    else:  # Float64: the FP64-bound products (k > 1) walk the bin order, SpMVs do not
+        assert (items["bin_warps"][items["k"] == 1] == 0).all()
+        assert (items["bin_warps"][items["k"] > 1] > 0).sum() > (items["k"] > 1).sum() // 2
     b2 = batch.BatchedMul(prods)
     b2.run("graph")
     torch.cuda.synchronize()
@@ -141,3 +142,47 @@ def test_row_major_right_hand_sides(gsa, oracle, cuda):
                                   alpha=2.0)
         assert oracle.max_rel_error(g.cpu().numpy(), ye, sc) <= 1e-12
     b.close()
+
+
+def test_full_uneven_mix_every_product(gsa, oracle, cuda):
+    """The benchmark's batched workload at full size: 4096 banded ComplexF64 CSR matrices (n
+    log-uniform in [64, 8192], half-band 3 plus Poisson(8) off-band entries per row, Int64
+    indices), k cycled 1/4/8, one grouped launch replayed from a CUDA graph with the bin
+    orders of their plans; every product against the double-double oracle (1e-12)."""
+    from concurrent.futures import ThreadPoolExecutor
+    from genericsparsearrays_gb300 import batch, workloads as wl
+    count, ks = 4096, (1, 4, 8)
+    sizes, rp, cv, nz, ro, eo = wl.banded_batch(count=count, lo=64, hi=8192, seed=11, itype=np.int64,
+                                                dtype=np.complex128, device=cuda)
+    g = torch.Generator(device=cuda).manual_seed(13)
+    prods = []
+    for i, m in enumerate(sizes):
+        A = gsa.GenericSparseMatrixCSR(m, m, rp[int(ro[i]) + i: int(ro[i + 1]) + i + 1],
+                                       cv[int(eo[i]): int(eo[i + 1])], nz[int(eo[i]): int(eo[i + 1])])
+        k = ks[i % len(ks)]
+        shape = (m,) if k == 1 else (k, m)
+        X = torch.complex(torch.rand(shape, generator=g, device=cuda, dtype=torch.float64) * 2 - 1,
+                          torch.rand(shape, generator=g, device=cuda, dtype=torch.float64) * 2 - 1)
+        Y = torch.full(shape, float("nan"), dtype=torch.complex128, device=cuda)  # beta = 0 never reads Y
+        if k > 1:
+            X, Y = X.t(), Y.t()
+        prods.append((A, X, Y, 1, 0))
+    del rp, cv, nz
+    b = batch.BatchedMul(prods)
+    b.run("graph")
+    b.run("graph")  # a replay of the captured graph
+    torch.cuda.synchronize()
+    host = [(A.m, A.rowptr.cpu().numpy(), A.colval.cpu().numpy(), A.nzval.cpu().numpy(),
+             np.asfortranarray(X.cpu().numpy()), Y.cpu().numpy()) for A, X, Y, _, _ in prods]
+    b.close()
+
+    def err(h):
+        m, p, c, v, X, Y = h
+        ye, sc = oracle.mul_exact("csr", "N", m, m, p, c, v, 1, X, np.zeros(Y.shape, np.complex128))
+        return oracle.max_rel_error(Y, ye, sc)
+
+    with ThreadPoolExecutor(max_workers=oracle.max_threads()) as ex:
+        errs = list(ex.map(err, host))
+    assert len(errs) == count
+    worst = int(np.argmax(errs))
+    assert errs[worst] <= 1e-12, f"product {worst}: {errs[worst]:.3e}"

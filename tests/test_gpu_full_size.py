@@ -42,21 +42,23 @@ def test_laplacian_spmv_csr_csc(gsa, oracle, cuda, wl, it, dt):
     assert rel_err_vs(y.cpu().numpy(), ref, scale) <= tol
 
 
-def test_laplacian_spmm_k16(gsa, oracle, cuda, wl):
-    m, n, rp, cv, nz = wl.laplacian_2d(2048, itype=np.int32, dtype=np.float64)
+@pytest.mark.parametrize("it", [np.int32, np.int64])
+@pytest.mark.parametrize("dt", [np.float64, np.float32])
+def test_laplacian_spmm_k16(gsa, oracle, cuda, wl, it, dt):
+    """SpMM with a 16-column column-major X, CSR and CSC, every value/index type pair of the
+    benchmark, against the double-double oracle (1e-12 for Float64, 1e-5 for Float32)."""
+    m, n, rp, cv, nz = wl.laplacian_2d(2048, itype=it, dtype=dt)
     rng = np.random.default_rng(1)
-    X = np.asfortranarray(rng.uniform(-1, 1, (n, 16)))
-    Y = np.zeros((m, 16), order="F")
-    oracle.mul("csr", "N", m, n, rp, cv, nz, 1, X, Y, nthreads=oracle.max_threads())
-    S = sp.csr_matrix((nz, cv.astype(np.int64) - 1, rp.astype(np.int64) - 1), shape=(m, n))
-    scale = abs(S) @ np.abs(X)
+    X = np.asfortranarray(rng.uniform(-1, 1, (n, 16)).astype(dt))
+    ye, sc = oracle.mul_exact("csr", "N", m, n, rp, cv, nz, 1, X, np.zeros((m, 16), dtype=dt, order="F"))
+    tol = 1e-12 if dt == np.float64 else 1e-5
+    Xd = torch.from_numpy(X).to(cuda)
     A = gsa.adapt(cuda, gsa.GenericSparseMatrixCSR(m, n, rp, cv, nz))
-    Yd = A @ torch.from_numpy(X).to(cuda)
-    assert rel_err_vs(Yd.cpu().numpy(), Y, scale) <= 1e-12
+    assert oracle.max_rel_error((A @ Xd).cpu().numpy(), ye, sc) <= tol
+    del A
     _, _, cp, rv, cz = wl.csr_to_csc(m, n, rp, cv, nz)
     K = gsa.adapt(cuda, gsa.GenericSparseMatrixCSC(m, n, cp, rv, cz))
-    Yk = K @ torch.from_numpy(X).to(cuda)
-    assert rel_err_vs(Yk.cpu().numpy(), Y, scale) <= 1e-12
+    assert oracle.max_rel_error((K @ Xd).cpu().numpy(), ye, sc) <= tol
 
 
 @pytest.mark.parametrize("it", [np.int32, np.int64])
@@ -91,6 +93,29 @@ def test_power_law_complex_csr_coo(gsa, oracle, cuda, wl):
     rows = wl.csr_rows(rp)
     C = gsa.adapt(cuda, gsa.GenericSparseMatrixCOO(m, n, rows, cv, nz))
     assert oracle.max_rel_error((C @ xd).cpu().numpy(), ye, sc) <= 1e-12
+
+
+def test_power_law_complex_coo_random_order_atomics(gsa, oracle, cuda, wl):
+    """The power-law ComplexF64 COO with its triplets in a seeded random order, through the
+    atomic COO kernel (gsa_coo_mul: segmented shuffle over adjacent equal rows, then one
+    atomic per run), against the double-double oracle; alpha and beta general."""
+    import ctypes
+    L = gsa._lib
+    lib = L.load()
+    m, n, rp, cv, nz = wl.power_law(1_000_000, seed=0, itype=np.int64, dtype=np.complex128)
+    _, _, r, c, v = wl.permuted_coo(m, n, rp, cv, nz, seed=13)
+    rng = np.random.default_rng(4)
+    x = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    y0 = rng.standard_normal(m) + 1j * rng.standard_normal(m)
+    alpha, beta = np.array([0.75 - 0.5j]), np.array([-1.25 + 0.25j])
+    ye, sc = oracle.mul_exact("csr", "N", m, n, rp, cv, nz, 1, x, y0, alpha=alpha[0], beta=beta[0])
+    d = [torch.from_numpy(a).to(cuda) for a in (r, c, v, x, y0)]
+    stream = ctypes.c_void_p(torch.cuda.current_stream(cuda).cuda_stream)
+    st = lib.gsa_coo_mul(stream, L.C64, L.IDX64, m, n, int(v.size), *(ctypes.c_void_p(t.data_ptr()) for t in d[:3]),
+                         1, L.OP_N, 1, ctypes.c_void_p(d[3].data_ptr()), n, L.OP_N, ctypes.c_void_p(d[4].data_ptr()),
+                         m, alpha.ctypes.data_as(ctypes.c_void_p), beta.ctypes.data_as(ctypes.c_void_p))
+    L.check(st)
+    assert oracle.max_rel_error(d[4].cpu().numpy(), ye, sc) <= 1e-12
 
 
 def test_random_poisson_three_formats(gsa, oracle, cuda, wl):

@@ -340,3 +340,33 @@ def test_row_sorted_coo_uses_row_pointers(gsa, oracle, cuda, dt, it):
                 gsa.mul_(C, wrap(gsa, A, opA), torch.from_numpy(X).to(cuda), 2, 3)
                 check(oracle, "coo", opA, m, n, r, c, v, X, "N", C0, C, 2, 3, dt)
         assert (A._plan is not None) == (order == "sorted")
+
+
+@pytest.mark.parametrize("it", INDEX_TYPES)
+@pytest.mark.parametrize("dt", VALUE_TYPES)
+def test_window_scatter(gsa, oracle, cuda, dt, it):
+    """GSA_ALGO_VECTOR on the scatter directions (CSC N, CSR T/C) with one right-hand side:
+    products near the CTA's outer range summed in a shared-memory window first.  A banded
+    matrix (half-band 70, wider than the window's halo) plus random far entries and empty
+    columns, alpha and beta general, against the oracle (integers bit-exact)."""
+    import scipy.sparse as sp
+    rng = np.random.default_rng(zlib.crc32(f"win-{np.dtype(it)}-{np.dtype(dt)}".encode()))
+    m = n = 3000
+    offs = list(range(-70, 71, 7))
+    S = sp.diags([np.ones(n - abs(o)) for o in offs], offs, shape=(m, n), format="csr")
+    S = (S + sprand(rng, m, n, 0.002, np.float64)).tocsr()
+    S = S.tolil()
+    S[:, 1500:1510] = 0  # empty columns
+    S = S.tocsr()
+    S.eliminate_zeros()
+    S.sort_indices()
+    S = sp.csr_matrix((rand_values(rng, S.nnz, dt), S.indices, S.indptr), shape=(m, n))
+    for fmt, opA in (("csc", "N"), ("csr", "T"), ("csr", "C")):
+        p0, p1, v = parts(S, fmt, it)
+        A = wrap(gsa, make(gsa, fmt, m, n, p0, p1, v, cuda), opA)
+        x = rand_values(rng, n, dt)
+        C0 = rand_values(rng, m, dt)
+        C = torch.from_numpy(C0).to(cuda)
+        alpha, beta = (3, 2) if not is_complex(dt) else (0.5 - 1j, 2 + 0.25j)
+        gsa.mul_(C, A, torch.from_numpy(x).to(cuda), alpha, beta, algo=gsa.ALGO_VECTOR)
+        check(oracle, fmt, opA, m, n, p0, p1, v, x, "N", C0, C, alpha, beta, dt)

@@ -52,12 +52,12 @@ class FakeExecutor:
         return None
 
 
-def setup(budget=10_000, per_launch=1.0, fail_on=(), slots=2, max_batch=64):
+def setup(budget=10_000, per_launch=1.0, fail_on=(), slots=2, max_batch=64, work_cap=1 << 28):
     clk = Clock()
     reg = serving.Registry(budget)
     mid = reg.add(FakeMatrix(100, 100, 50))  # 101*4 + 50*4 + 50*8 = 1004 bytes
     ex = FakeExecutor(clk, per_launch, fail_on)
-    srv = serving.Server(reg, ex, max_batch=max_batch, slots=slots, clock=clk)
+    srv = serving.Server(reg, ex, max_batch=max_batch, slots=slots, clock=clk, work_cap=work_cap)
     return clk, reg, mid, ex, srv
 
 
@@ -177,3 +177,24 @@ def test_run_realtime_with_manual_clock():
     assert st["done"] == 50
     assert st["launches"] < 50       # coalesced
     assert st["p99_ms"] >= st["p50_ms"] > 0
+
+
+def test_work_cap_splits_launches():
+    """A launch takes queued requests while their multiply-adds stay under the work cap (50
+    per SpMV of the 50-entry matrix, 150 with k = 3); a request over the cap goes alone, and
+    the next free slot takes the rest in arrival order."""
+    clk, reg, mid, ex, srv = setup(slots=3, work_cap=120)
+    ids = [srv.submit(req(mid)) for _ in range(3)] + [srv.submit(req(mid, k=3))] + [srv.submit(req(mid))]
+    assert [r.fma for r in srv.queue] == [50, 50, 50, 150, 50]
+    srv.step()
+    assert [w for _, w, _ in ex.launched] == [[ids[0], ids[1]], [ids[2]], [ids[3]]]
+    assert [s for s, _, _ in ex.launched] == [0, 1, 2]
+    clk.t = 1.0
+    srv.step()
+    assert ex.launched[-1][1] == [ids[4]]
+    clk.t = 2.0
+    srv.step()
+    assert not srv.busy()
+    assert sum(r.state == "done" for r in srv.finished) == 5
+    st = srv.stats()
+    assert st["fma_per_s"] == pytest.approx(350 / 2.0)
