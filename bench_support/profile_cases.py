@@ -34,6 +34,8 @@ def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("case")
     ap.add_argument("--reps", type=int, default=3)
+    ap.add_argument("--columns", type=int, default=1,
+                    help="batched_mix: right-hand-side columns per thread (the autotuner's pick on GB300: 1)")
     args = ap.parse_args(argv)
     sys.path.insert(0, ROOT)
     import torch
@@ -98,7 +100,7 @@ def main(argv=None):
         sys.path.insert(0, ROOT)
         import bench
         prods, _ = bench.batched_products(gsa, wl, torch, dev)
-        b = batch.BatchedMul(prods)
+        b = batch.BatchedMul(prods, columns=args.columns)
         run = lambda: b.run("grouped")
     else:
         raise SystemExit(f"unknown case {c}")

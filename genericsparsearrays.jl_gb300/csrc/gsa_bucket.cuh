@@ -8,17 +8,17 @@
 //
 // Two levels, so that no pass writes single entries to random addresses (a random 8-byte
 // store costs a whole DRAM sector, and more):
-//   A. coarse_hist_kernel: a fixed grid of CTAs, each owning one contiguous span of the
-//      entries, counts its span's entries per coarse bucket (2^cs consecutive rows, at most
-//      4096 rows and 8192 buckets) in shared memory and stores the counts bucket-major; one
-//      exclusive scan of that (bucket, CTA) table gives every CTA the first slot of its run in
-//      every bucket, and the buckets' starts.
-//   B. coarse_run_kernel: the same CTAs place their spans: one shared-memory cursor per
-//      bucket, one shared atomic per entry, no global atomics and no barriers, so each warp
-//      streams its entries with its loads in flight.  A CTA's run in a bucket is contiguous,
-//      so its writes to it land in sectors that L2 merges.  Each entry is one record: the key
-//      row-in-bucket << (mb + pb) | minor << pb | position (sorting a row by it is sorting by
-//      (minor, position)) and the value (conversions), one 16- or 32-byte store.
+//   A. coarse_count_kernel: entries per coarse bucket (2^cs consecutive rows, at most 4096
+//      rows and 8192 buckets), histograms in shared memory; one scan of the bucket counts.
+//   B. coarse_place_kernel: a CTA takes a tile of 2048 entries, ranks them per coarse bucket
+//      in shared memory and reserves one contiguous run per bucket with one global atomic
+//      (made by the bucket's first entry of the tile; no pass over all buckets per tile), so
+//      the tile's writes land in runs that L2 merges into whole sectors: all tiles append at
+//      one moving frontier per bucket.  While a tile is processed, the bulk-copy engine
+//      prefetches the CTA's next tile into L2 (fine_kernel does the same with its next
+//      bucket's records).  Each entry is one
+//      record: the key row-in-bucket << (mb + pb) | minor << pb | position (sorting a row by it
+//      is sorting by (minor, position)) and the value (conversions), one 16- or 32-byte store.
 //   C. fine_kernel: a CTA per coarse bucket counts its rows in shared memory, scans them --
 //      the row pointers of the result -- and places the bucket's entries in row order into
 //      shared memory (96 KB of staging; cs is chosen so that an average bucket fills at most
@@ -56,8 +56,7 @@ constexpr int WARP_CTA_THREADS = 256;
 constexpr int MERGE_ITEMS = 8;
 constexpr int ROWS_MAX = 4096;     // rows per coarse bucket
 constexpr int COARSE_MAX = 8192;   // coarse buckets, the invalid-row bucket included
-constexpr int PB_THREADS = 256, PB_ITEMS = 4;  // passes A and B: threads, entries in flight per thread
-constexpr int PB_CTAS_PER_SM = 8;
+constexpr int PB_THREADS = 256, PB_ITEMS = 8;
 constexpr int PC_THREADS = 512;
 constexpr int STAGE_BYTES = 96 * 1024;  // fine_kernel's shared staging of one coarse bucket
 
@@ -134,18 +133,10 @@ template <class Emit> struct PackedEmit {
     }
 };
 
-// CTAs of passes A and B (both use the same spans): enough to fill the GPU, each span at
-// least a few rounds of PB_THREADS * PB_ITEMS entries.
-inline int64_t span_ctas(int64_t nnz) {
-    int64_t g = ceil_div(nnz, (int64_t)PB_THREADS * PB_ITEMS * 4);
-    const int64_t cap = (int64_t)152 * PB_CTAS_PER_SM;
-    return g < 1 ? 1 : (g > cap ? cap : g);
-}
-
 struct Layout {
     Coarse co;
-    int64_t ncnt, G, nhist;
-    size_t cnt, cstart, start, bsums, hist, key1, rec1, key2, val2, list, counters, bytes;
+    int64_t ncnt;
+    size_t cnt, cstart, start, bsums, key1, rec1, key2, val2, list, counters, bytes;
 };
 
 // vsize: bytes of a carried value (0: none)
@@ -154,16 +145,12 @@ inline Layout layout(int64_t major_n, int64_t minor_n, int64_t nnz, size_t vsize
     L.co = coarse_plan(major_n, minor_n, nnz, (int)(STAGE_BYTES / (8 + vsize)));
     const int64_t n = nnz > 0 ? nnz : 1;
     L.ncnt = (L.co.ok ? L.co.nb : major_n) + 2;
-    L.G = span_ctas(nnz);
-    L.nhist = L.co.ok ? L.co.nb * L.G + 1 : 1;  // the (bucket, CTA) table and its total
-    int64_t nscan = L.ncnt > major_n + 2 ? L.ncnt : major_n + 2;
-    nscan = nscan > L.nhist ? nscan : L.nhist;
+    const int64_t nscan = L.ncnt > major_n + 2 ? L.ncnt : major_n + 2;
     Carver cv(nullptr);
     L.cnt = cv.reserve<uint32_t>(L.ncnt);
     L.cstart = cv.reserve<uint32_t>(L.ncnt);
     L.start = cv.reserve<uint32_t>(major_n + 2);
     L.bsums = cv.reserve<uint32_t>(ceil_div(nscan, (int64_t)sc_tile) + 1);
-    L.hist = cv.reserve<uint32_t>(L.nhist);
     L.key1 = cv.reserve<uint64_t>(n);
     L.key2 = cv.reserve<uint64_t>(n);
     L.rec1 = L.co.ok ? cv.reserve<unsigned char>((size_t)n * rec_size(vsize)) : 0;
@@ -238,90 +225,102 @@ __device__ __forceinline__ void list_long_rows(bool valid, uint32_t len, uint32_
 
 // ---- two-level form --------------------------------------------------------
 
-// Pass A: CTA c counts the entries of its span [c * span, (c + 1) * span) per coarse bucket
-// and stores the counts at hist[d * gridDim.x + c] (bucket-major, so that one exclusive scan
-// orders the runs by bucket, then by CTA).
 template <class Src>
 __global__ void __launch_bounds__(PB_THREADS)
-coarse_hist_kernel(Src src, int64_t nnz, int64_t major_n, int cs, int64_t nb, int64_t span,
-                   uint32_t *__restrict__ hist) {
-    extern __shared__ uint32_t h[];  // nb counters
-    for (int64_t d = threadIdx.x; d < nb; d += PB_THREADS) h[d] = 0;
+coarse_count_kernel(Src src, int64_t nnz, int64_t major_n, int cs, int64_t nb, uint32_t *__restrict__ cnt) {
+    __shared__ uint32_t h[COARSE_MAX];
+    for (int64_t d = threadIdx.x; d < nb; d += blockDim.x) h[d] = 0;
     __syncthreads();
-    const int64_t e0 = (int64_t)blockIdx.x * span;
-    const int64_t e1 = e0 + span < nnz ? e0 + span : nnz;
-    for (int64_t i0 = e0 + threadIdx.x; i0 < e1; i0 += (int64_t)PB_THREADS * PB_ITEMS) {
-        int64_t mj[PB_ITEMS];
-#pragma unroll
-        for (int q = 0; q < PB_ITEMS; ++q) {
-            const int64_t i = i0 + (int64_t)q * PB_THREADS;
-            mj[q] = i < e1 ? src.major(i) : -2;
-        }
-#pragma unroll
-        for (int q = 0; q < PB_ITEMS; ++q) {
-            if (mj[q] == -2) continue;
-            const int64_t d = (uint64_t)mj[q] < (uint64_t)major_n ? mj[q] >> cs : nb - 1;
-            atomicAdd(&h[d], 1u);
-        }
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nnz; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t mj = src.major(i);
+        const int64_t d = (uint64_t)mj < (uint64_t)major_n ? mj >> cs : nb - 1;
+        atomicAdd(&h[d], 1u);
     }
     __syncthreads();
-    const int64_t G = gridDim.x;
-    for (int64_t d = threadIdx.x; d < nb; d += PB_THREADS) hist[d * G + blockIdx.x] = h[d];
+    for (int64_t d = threadIdx.x; d < nb; d += blockDim.x)
+        if (h[d]) atomicAdd(&cnt[d], h[d]);
 }
 
-// The buckets' starts from the scanned (bucket, CTA) table: cstart[d] = off[d * G], and
-// cstart[nb] = nnz (the table's last entry).
-__global__ void coarse_starts_kernel(const uint32_t *__restrict__ off, int64_t nb, int64_t G,
-                                     uint32_t *__restrict__ cstart) {
-    const int64_t d = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (d <= nb) cstart[d] = off[d * G];
-}
-
-// Pass B: CTA c places the entries of its span.  Its cursor in bucket d starts at the
-// scanned off[d * G + c]; every entry takes the next slot of its bucket with one shared
-// atomic and is stored there as one record.  Entries are read once; PB_ITEMS of a thread's
-// loads are issued before their atomics.
 template <class Src, class VT>
-__global__ void __launch_bounds__(PB_THREADS)
-coarse_run_kernel(Src src, const VT *__restrict__ vals_in, int64_t nnz, int64_t major_n, Coarse co, int64_t span,
-                  const uint32_t *__restrict__ off, Rec<VT> *__restrict__ rec1) {
-    constexpr bool HAS_VAL = !std::is_same<VT, NoValue>::value;
-    extern __shared__ uint32_t s_cur[];  // nb cursors
+__global__ void __launch_bounds__(PB_THREADS, 3)
+coarse_place_kernel(Src src, const VT *__restrict__ vals_in, int64_t nnz, int64_t major_n, Coarse co,
+                    uint32_t *__restrict__ cfill, Rec<VT> *__restrict__ rec1) {
     const int cs = co.cs;
-    const int64_t nb = co.nb, G = gridDim.x;
-    for (int64_t d = threadIdx.x; d < nb; d += PB_THREADS) s_cur[d] = __ldg(off + d * G + blockIdx.x);
+    const int64_t nb = co.nb;
+    // per bucket: the tile's count, then (in place) the first slot of the tile's run; zero
+    // between tiles (each entry clears its own bucket's word)
+    __shared__ uint32_t s_run[COARSE_MAX];
+    constexpr bool HAS_VAL = !std::is_same<VT, NoValue>::value;
+    constexpr int64_t TILE = (int64_t)PB_THREADS * PB_ITEMS;
+    for (int64_t d = threadIdx.x; d < nb; d += blockDim.x) s_run[d] = 0;
     __syncthreads();
-    const int64_t e0 = (int64_t)blockIdx.x * span;
-    const int64_t e1 = e0 + span < nnz ? e0 + span : nnz;
-    for (int64_t i0 = e0 + threadIdx.x; i0 < e1; i0 += (int64_t)PB_THREADS * PB_ITEMS) {
-        int64_t mjs[PB_ITEMS], mns[PB_ITEMS];
+    for (int64_t t0 = (int64_t)blockIdx.x * TILE; t0 < nnz; t0 += (int64_t)gridDim.x * TILE) {
+        // the CTA's next tile into L2 while this one is ranked, reserved and stored
+        const int64_t tn = t0 + (int64_t)gridDim.x * TILE;
+        if (threadIdx.x == 0 && tn < nnz) {
+            const int64_t te = tn + TILE < nnz ? tn + TILE : nnz;
+            src.prefetch(tn, te);
+            if constexpr (HAS_VAL) prefetch_l2(vals_in + tn, (size_t)(te - tn) * sizeof(VT));
+        }
+        // every entry is read once: its indices and value stay in registers across the
+        // reservation
+        uint32_t packed[PB_ITEMS];  // bucket << 16 | rank in the tile's run
+        uint64_t key[PB_ITEMS];     // row in the bucket << (mb + pb) | minor << pb | position
         typename std::conditional<HAS_VAL, VT, char>::type val[PB_ITEMS];
+        int64_t mjs[PB_ITEMS], mns[PB_ITEMS];
+        // all loads first, so that they are in flight together (the shared-memory atomics below
+        // would otherwise keep each entry's loads behind the previous entry's atomic)
 #pragma unroll
         for (int q = 0; q < PB_ITEMS; ++q) {
-            const int64_t e = i0 + (int64_t)q * PB_THREADS;
+            const int64_t e = t0 + (int64_t)q * PB_THREADS + threadIdx.x;
             mjs[q] = -1;
             mns[q] = 0;
-            if (e < e1) {
+            if (e < nnz) {
                 src.get(e, mjs[q], mns[q]);
                 if constexpr (HAS_VAL) val[q] = vals_in[e];
             }
         }
 #pragma unroll
         for (int q = 0; q < PB_ITEMS; ++q) {
-            const int64_t e = i0 + (int64_t)q * PB_THREADS;
-            if (e >= e1) continue;
+            const int64_t e = t0 + (int64_t)q * PB_THREADS + threadIdx.x;
             const int64_t mj = mjs[q], mn = mns[q];
             const bool in = (uint64_t)mj < (uint64_t)major_n;
             const uint32_t d = (uint32_t)(in ? mj >> cs : nb - 1);
             const uint64_t lrow = in ? (uint64_t)(mj - ((int64_t)d << cs)) : 0;
             // the minor index masked to its field, so that an index outside the matrix cannot
             // reach the row bits
-            const uint64_t key =
-                shl64(lrow, co.mb + co.pb) | ((((uint64_t)mn) & low_mask(co.mb)) << co.pb) | (uint64_t)e;
-            const uint32_t slot = atomicAdd(&s_cur[d], 1u);
-            if constexpr (HAS_VAL) rec1[slot] = Rec<VT>{key, val[q]};
-            else rec1[slot] = Rec<VT>{key};
+            key[q] = shl64(lrow, co.mb + co.pb) | ((((uint64_t)mn) & low_mask(co.mb)) << co.pb) | (uint64_t)e;
+            packed[q] = e < nnz ? (d << 16) | atomicAdd(&s_run[d], 1u) : 0u;
         }
+        __syncthreads();
+        // one reservation per bucket the tile touches, made by the bucket's first entry of the
+        // tile (rank 0): the tile's count becomes the first slot of its run (cfill starts at
+        // the buckets' first slots); a thread's reservations are independent atomics in flight
+#pragma unroll
+        for (int q = 0; q < PB_ITEMS; ++q) {
+            const int64_t e = t0 + (int64_t)q * PB_THREADS + threadIdx.x;
+            if (e < nnz && (packed[q] & 0xffffu) == 0) {
+                const uint32_t d = packed[q] >> 16;
+                s_run[d] = atomicAdd(&cfill[d], s_run[d]);
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int q = 0; q < PB_ITEMS; ++q) {
+            const int64_t e = t0 + (int64_t)q * PB_THREADS + threadIdx.x;
+            if (e < nnz) {
+                const uint32_t slot = s_run[packed[q] >> 16] + (packed[q] & 0xffffu);
+                if constexpr (HAS_VAL) rec1[slot] = Rec<VT>{key[q], val[q]};
+                else rec1[slot] = Rec<VT>{key[q]};
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int q = 0; q < PB_ITEMS; ++q) {
+            const int64_t e = t0 + (int64_t)q * PB_THREADS + threadIdx.x;
+            if (e < nnz) s_run[packed[q] >> 16] = 0;
+        }
+        __syncthreads();
     }
 }
 
@@ -361,6 +360,11 @@ fine_kernel(int64_t major_n, Coarse co, const uint32_t *__restrict__ cstart, con
     for (int64_t bk = blockIdx.x; bk < nb; bk += gridDim.x) {
         const uint32_t B0 = cstart[bk], B1 = cstart[bk + 1];
         const uint32_t E = B1 - B0;
+        // this CTA's next bucket's records into L2 while this one is sorted
+        if (threadIdx.x == 0 && bk + gridDim.x < nb) {
+            const uint32_t N0 = cstart[bk + gridDim.x], N1 = cstart[bk + gridDim.x + 1];
+            prefetch_l2(rec1 + N0, (size_t)(N1 - N0) * sizeof(Rec<VT>));
+        }
         const bool invalid = bk == nb - 1;
         const int64_t row0 = invalid ? major_n : bk << cs;
         const int64_t rspan = major_n - row0 < (int64_t)rmax ? major_n - row0 : (int64_t)rmax;
@@ -673,28 +677,22 @@ int sort(cudaStream_t s, int64_t major_n, int64_t minor_n, int64_t nnz, const Sr
     if (L.co.ok) {
         const Coarse co = L.co;
         uint32_t *cstart = (uint32_t *)(w + L.cstart);
-        uint32_t *hist = (uint32_t *)(w + L.hist);
         Rec<VT> *rec1 = (Rec<VT> *)(w + L.rec1);
         VT *val2 = VS ? (VT *)(w + L.val2) : nullptr;
-        const int64_t G = L.G, span = ceil_div(nnz > 0 ? nnz : 1, G);
-        const size_t hsmem = (size_t)co.nb * sizeof(uint32_t);
-        rc = check_cuda(cudaFuncSetAttribute(coarse_hist_kernel<Src>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)hsmem),
-                        "bucket: coarse_hist_kernel shared memory");
-        if (!rc)
-            rc = check_cuda(cudaFuncSetAttribute(coarse_run_kernel<Src, VT>,
-                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)hsmem),
-                            "bucket: coarse_run_kernel shared memory");
-        if (!rc) rc = check_cuda(cudaMemsetAsync(hist + co.nb * G, 0, sizeof(uint32_t), s), "bucket: clear");
-        if (rc) return rc;
-        coarse_hist_kernel<Src><<<(unsigned)G, PB_THREADS, hsmem, s>>>(src, nnz, major_n, co.cs, co.nb, span, hist);
-        rc = check_cuda(cudaGetLastError(), "bucket coarse_hist_kernel");
-        if (!rc) rc = scan(s, hist, hist, L.nhist, bsums);  // hist[nb * G] = nnz
-        if (rc) return rc;
-        coarse_starts_kernel<<<(unsigned)ceil_div(co.nb + 1, 256), 256, 0, s>>>(hist, co.nb, G, cstart);
         if (nnz > 0)
-            coarse_run_kernel<Src, VT><<<(unsigned)G, PB_THREADS, hsmem, s>>>(src, vals_in, nnz, major_n, co, span,
-                                                                             hist, rec1);
+            coarse_count_kernel<Src><<<grid_for(nnz, PB_THREADS * PB_ITEMS, cap), PB_THREADS, 0, s>>>(
+                src, nnz, major_n, co.cs, co.nb, cnt);
+        rc = check_cuda(cudaGetLastError(), "bucket coarse_count_kernel");
+        if (!rc) rc = scan(s, cnt, cstart, co.nb + 1, bsums);  // cstart[nb] = nnz
+        // the fill cursors start at the buckets' first slots
+        if (!rc)
+            rc = check_cuda(cudaMemcpyAsync(cnt, cstart, (size_t)(co.nb + 1) * sizeof(uint32_t),
+                                            cudaMemcpyDeviceToDevice, s),
+                            "bucket: cursors");
+        if (rc) return rc;
+        if (nnz > 0)
+            coarse_place_kernel<Src, VT><<<grid_for(nnz, PB_THREADS * PB_ITEMS, cap), PB_THREADS, 0, s>>>(
+                src, vals_in, nnz, major_n, co, cnt, rec1);
         const size_t smem = fine_smem_bytes<VT>(co.cs);
         rc = check_cuda(cudaFuncSetAttribute(fine_kernel<VT, Emit>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)smem),

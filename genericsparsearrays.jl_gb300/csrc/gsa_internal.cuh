@@ -197,6 +197,18 @@ template <> __device__ __forceinline__ cf64 ld_stream(const cf64 *p) {
     return cf64{v.x, v.y};
 }
 
+// Asks the bulk-copy engine to bring the bytes of [p, p + bytes) that lie on whole 16-byte
+// pieces into L2, without waiting and without touching shared memory (a hint: no data comes
+// back).  Only for ranges inside one array: the pieces are rounded inwards.
+__device__ __forceinline__ void prefetch_l2(const void *p, size_t bytes) {
+    const uintptr_t a = ((uintptr_t)p + 15) & ~(uintptr_t)15;
+    const uintptr_t e = ((uintptr_t)p + bytes) & ~(uintptr_t)15;
+    for (uintptr_t q = a; q < e; q += (uintptr_t)1 << 16) {
+        const uint32_t n = (uint32_t)(e - q < ((uintptr_t)1 << 16) ? e - q : ((uintptr_t)1 << 16));
+        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(q), "r"(n) : "memory");
+    }
+}
+
 // Atomic accumulate (complex: one atomic per component).
 __device__ __forceinline__ void atomic_add(float *p, float v) { atomicAdd(p, v); }
 __device__ __forceinline__ void atomic_add(double *p, double v) { atomicAdd(p, v); }
@@ -470,6 +482,8 @@ void set_spmm_columns(int c);   // 0 (by value size), 1, 2, 4 or 8
 int get_spmm_columns();
 void set_plan_natural(int v);   // 1: row blocks in natural order even where a plan bins them
 int get_plan_natural();
+void set_stage_rows(int v);     // 1: thread-per-row warps stage their span with 16-byte loads
+int get_stage_rows();
 
 // Scatter: out[idx_j, c] += conj?(val_j) * (op(B)(o, c) * alpha), after the beta pass.
 // ALGO_MERGE: merge-path tiles (workspace: tile coordinates); otherwise outer blocks with

@@ -134,6 +134,89 @@ rowblock_kernel(CompressedArgs<V, I> a, int64_t k, DenseIn<V> B, DenseOut<V> C, 
 }
 
 // ---------------------------------------------------------------------------
+// Staged rows (GSA_TUNE_STAGE_ROWS = 1; one right-hand side, Float32 or Float64 values, Int32
+// indices): the entries of a warp's 32 thread-per-row rows are one contiguous span, which the
+// warp copies into shared memory with 16-byte loads -- a lane moves whole 16-byte pieces of
+// idx and val, two or three warp instructions where the direct path issues one scalar load
+// per entry and lane -- before each lane sums its own row from shared memory.  Warps whose
+// rows take several lanes, spans longer than STAGE_CAP entries, spans whose 16-byte pieces
+// would pass the end of the arrays and arrays that are not 16-byte aligned take the direct
+// path of rowblock_kernel.  Each row is summed in the same order as there (bit-identical).
+constexpr int STAGE_CAP = 256;
+
+template <typename V> constexpr bool stage_rows_type() {
+    return std::is_same<V, float>::value || std::is_same<V, double>::value;
+}
+
+// 12 resident CTAs of 128 threads: 40 registers, and 96 KB (Float32) or 144 KB (Float64) of
+// staging per SM
+template <typename V, typename I>
+__global__ void __launch_bounds__(RB_THREADS, 12)
+rowblock_staged_kernel(CompressedArgs<V, I> a, DenseIn<V> B, DenseOut<V> C, int64_t nrb, PlanRows L) {
+    static_assert(sizeof(I) == 4, "staged rows take 32-bit offsets");
+    constexpr int PIECE = 4;  // entries per 16 bytes of indices (and the unit of the span's ends)
+    __shared__ __align__(16) I s_idx[RB_WARPS][STAGE_CAP];
+    __shared__ __align__(16) V s_val[RB_WARPS][STAGE_CAP];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int64_t unit = blockIdx.x;
+    if (unit >= nrb) {  // chunked rows: a warp per chunk
+        chunk_unit<V, I, 1>(a, 1, B, C, 0, 0u, 1, (unit - nrb) * RB_WARPS + w, L);
+        return;
+    }
+    const int64_t row0 = unit * RB_THREADS + (threadIdx.x & ~31);
+    if (row0 >= a.outer_n) return;  // a warp past the last row (uniform: the whole warp leaves)
+    uint32_t b, e;
+    int skip;
+    const int64_t avg = warp_extent(a, row0, L.skip_mask, b, e, skip);
+    // lane 0's row exists, so the span [S, E) covers at least one row: S <= b_0 <= e_0 <= E
+    const bool valid = row0 + lane < a.outer_n;
+    const uint32_t S = __reduce_min_sync(0xffffffffu, valid ? b : 0xffffffffu) & ~(uint32_t)(PIECE - 1);
+    const uint32_t E = __reduce_max_sync(0xffffffffu, valid ? e : 0u);
+    const uint32_t T = (E + PIECE - 1) & ~(uint32_t)(PIECE - 1);
+    if (avg > G1_AVG || T < S || T - S > (uint32_t)STAGE_CAP || (int64_t)T > a.nnz) {
+        dispatch_lanes(avg, G1_AVG, [&](auto g) {
+            warp_rows<V, I, 1, decltype(g)::value>(a, 1, B, C, 0, row0, b, e, skip);
+        });
+        return;
+    }
+    // the span [S, T) in 16-byte pieces
+    const int4 *gi = reinterpret_cast<const int4 *>(a.idx + S);
+    int4 *si = reinterpret_cast<int4 *>(&s_idx[w][0]);
+    for (uint32_t q = lane; q < (T - S) / PIECE; q += 32) si[q] = __ldcs(gi + q);
+    constexpr int VPIECE = 16 / sizeof(V);
+    using V4 = typename std::conditional<sizeof(V) == 4, float4, double2>::type;
+    const V4 *gv = reinterpret_cast<const V4 *>(a.val + S);
+    V4 *sv = reinterpret_cast<V4 *>(&s_val[w][0]);
+    for (uint32_t q = lane; q < (T - S) / VPIECE; q += 32) sv[q] = __ldcs(gv + q);
+    __syncwarp();
+    const uint32_t inner = a.inner_n < 0xffffffffLL ? (uint32_t)a.inner_n : 0xffffffffu;
+    const uint32_t base = (uint32_t)a.base;
+    V acc = VT<V>::zero();
+    uint32_t j = b - S;
+    const uint32_t je = e - S;
+    for (; j + 3 < je; j += 4) {  // four gathers in flight
+        uint32_t ci[4];
+        V av[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            ci[u] = (uint32_t)s_idx[w][j + u] - base;
+            av[u] = s_val[w][j + u];
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) acc = mac(acc, av[u], ci[u] < inner ? B.at((int64_t)ci[u], 0) : VT<V>::zero());
+    }
+    for (; j < je; ++j) {
+        const uint32_t c1 = (uint32_t)s_idx[w][j] - base;
+        acc = mac(acc, s_val[w][j], c1 < inner ? B.at((int64_t)c1, 0) : VT<V>::zero());
+    }
+    if (valid && !skip) C.store(row0 + lane, 0, acc);
+}
+
+static std::atomic<int> g_stage_rows{0};
+void set_stage_rows(int v) { g_stage_rows.store(v, std::memory_order_relaxed); }
+int get_stage_rows() { return g_stage_rows.load(std::memory_order_relaxed); }
+
+// ---------------------------------------------------------------------------
 // Bin order: within each segment of BIN_SEGMENT rows the plan sorts the rows by the
 // multiply-adds each of their lanes does (rows up to 32 entries with a lane each, longer
 // ones with G = 2, 4, 8 or 16 lanes, each lane 17 to 32 entries) and warp w of the order
@@ -211,6 +294,14 @@ int launch_rowblock(cudaStream_t s, const CompressedArgs<V, I> &a, int64_t k, De
             else binned_kernel<V, I, 8><<<(unsigned)blocks, RB_THREADS, 0, s>>>(a, k, B, C, ncg, bv, L);
             timer_after(s);
             return check_cuda(cudaGetLastError(), "binned_kernel");
+        }
+    }
+    if constexpr (stage_rows_type<V>() && sizeof(I) == 4) {
+        const bool aligned = ((uintptr_t)a.idx % 16 == 0) && ((uintptr_t)a.val % 16 == 0);
+        if (KC == 1 && get_stage_rows() && aligned) {
+            rowblock_staged_kernel<V, I><<<(unsigned)blocks, RB_THREADS, 0, s>>>(a, B, C, nrb, L);
+            timer_after(s);
+            return check_cuda(cudaGetLastError(), "rowblock_staged_kernel");
         }
     }
     if (KC == 1) rowblock_kernel<V, I, 1><<<(unsigned)blocks, RB_THREADS, 0, s>>>(a, k, B, C, ncg, nrb, L);

@@ -81,6 +81,10 @@ typedef enum {
                                   gather with k > 1: 0 (by value size), 1, 2, 4 or 8 */
     GSA_TUNE_PLAN_ORDER = 3,   /* 0: a planned gather runs in the plan's order (bin order
                                   where the plan chose it); 1: always in natural row order */
+    GSA_TUNE_STAGE_ROWS = 5,   /* 1: in the default gather with one right-hand side, Float32 /
+                                  Float64 values and Int32 indices, warps of thread-per-row
+                                  rows copy their contiguous entry span into shared memory with
+                                  16-byte loads before summing; 0 (default): direct loads */
     GSA_TUNE_WAIT_LIMIT = 4    /* polls a bounded device-side wait (the pipelined SpMV's
                                   mbarrier waits for its bulk copies) makes before it gives
                                   up, sets the device error word and returns: default
@@ -252,9 +256,15 @@ int gsa_spgemm_destroy(gsa_spgemm *handle);
  * array of 8192 slots (192 KiB, held on every GPU that loads the library until
  * the process exits); a call that would need more slots returns
  * GSA_ERR_INVALID_ARG.  The first call on a device looks up the array's device
- * address, so make it before any stream capture.  All calls share the array:
- * calls that overlap on the GPU race on it.  Same tolerance and determinism as
- * gsa_csr_mul. */
+ * address, and under CUDA's default lazy module loading it is also the call that
+ * loads the library's code and the array onto that device -- which takes device
+ * memory.  So make the first call on each device at set-up, while device memory is
+ * still free and before any stream capture (or run with CUDA_MODULE_LOADING=EAGER);
+ * later calls take no device memory.  All calls share the array: calls that overlap
+ * on the GPU race on it.  It runs the pipelined merge-path kernel (GSA_ALGO_PIPE),
+ * about three times slower than gsa_csr_mul's default row blocks on the 2048^2
+ * Laplacian: it is the entry for callers that cannot allocate, not the fast one.
+ * Same tolerance and determinism as gsa_csr_mul. */
 int gsa_csr_spmv_noalloc(void *stream, int dtype, int itype, int64_t m, int64_t n, int64_t nnz,
                          const void *rowptr, const void *colval, const void *nzval, int base,
                          const void *x, void *y, const void *alpha, const void *beta);

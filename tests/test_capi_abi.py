@@ -149,7 +149,7 @@ def test_tuning_knobs(lib, gsa):
     consistent when several host threads set them at once (the knobs are process-wide)."""
     import threading
     L = gsa._lib
-    keys = (L.TUNE_PIPE_THREADS, L.TUNE_SPMM_COLUMNS, L.TUNE_PLAN_ORDER, L.TUNE_WAIT_LIMIT)
+    keys = (L.TUNE_PIPE_THREADS, L.TUNE_SPMM_COLUMNS, L.TUNE_PLAN_ORDER, L.TUNE_WAIT_LIMIT, L.TUNE_STAGE_ROWS)
     saved = {key: lib.gsa_get_tuning(key) for key in keys}
     try:
         assert lib.gsa_set_tuning(L.TUNE_SPMM_COLUMNS, 4) == 0
@@ -160,6 +160,10 @@ def test_tuning_knobs(lib, gsa):
         assert lib.gsa_get_tuning(L.TUNE_PLAN_ORDER) == 1
         assert lib.gsa_set_tuning(L.TUNE_PLAN_ORDER, 2) == L.ERR_INVALID_ARG
         assert lib.gsa_get_tuning(L.TUNE_WAIT_LIMIT) == saved[L.TUNE_WAIT_LIMIT] == 1 << 24
+        assert lib.gsa_get_tuning(L.TUNE_STAGE_ROWS) == saved[L.TUNE_STAGE_ROWS] == 0
+        assert lib.gsa_set_tuning(L.TUNE_STAGE_ROWS, 1) == 0
+        assert lib.gsa_get_tuning(L.TUNE_STAGE_ROWS) == 1
+        assert lib.gsa_set_tuning(L.TUNE_STAGE_ROWS, 2) == L.ERR_INVALID_ARG
         assert lib.gsa_set_tuning(L.TUNE_WAIT_LIMIT, 0) == 0
         assert lib.gsa_get_tuning(L.TUNE_WAIT_LIMIT) == 0
         assert lib.gsa_set_tuning(L.TUNE_WAIT_LIMIT, -1) == L.ERR_INVALID_ARG

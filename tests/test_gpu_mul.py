@@ -370,3 +370,46 @@ def test_window_scatter(gsa, oracle, cuda, dt, it):
         alpha, beta = (3, 2) if not is_complex(dt) else (0.5 - 1j, 2 + 0.25j)
         gsa.mul_(C, A, torch.from_numpy(x).to(cuda), alpha, beta, algo=gsa.ALGO_VECTOR)
         check(oracle, fmt, opA, m, n, p0, p1, v, x, "N", C0, C, alpha, beta, dt)
+
+
+@pytest.mark.parametrize("dt", [np.float32, np.float64])
+def test_staged_rows_match_direct(gsa, oracle, cuda, dt):
+    """GSA_TUNE_STAGE_ROWS = 1 (warps of thread-per-row rows copy their entry span with 16-byte
+    loads): bit-identical to the direct loads (same summation order), within the oracle's
+    tolerance; with long rows taken by a plan, empty rows, a last CTA with a warp past the last
+    row, the last warp's span at the end of the arrays, and misaligned arrays (a view one entry
+    in), which take the direct path."""
+    from genericsparsearrays_gb300 import workloads
+    L = gsa._lib
+    lib = L.load()
+    m, n, rp, cv, nz = workloads.random_poisson(50_001, mean=4.0, seed=12, itype=np.int32, dtype=dt)
+    lens = np.diff(rp.astype(np.int64))
+    lens[::997] = 0          # empty rows
+    lens[5:4000:401] = 700   # long rows (plan chunks)
+    rng = np.random.default_rng(13)
+    rp = np.concatenate([[1], 1 + np.cumsum(lens)]).astype(np.int32)
+    cv = np.concatenate([np.sort(rng.choice(n, size=l, replace=False)) for l in lens]).astype(np.int32) + 1
+    nz = rng.uniform(-1, 1, cv.size).astype(dt)
+    x = rng.uniform(-1, 1, n).astype(dt)
+    ye, sc = oracle.mul_exact("csr", "N", m, n, rp, cv, nz, 1, x, np.zeros(m, dt))
+    tol = 1e-12 if dt == np.float64 else 1e-5
+    xd = torch.from_numpy(x).to(cuda)
+    cv_pad = torch.from_numpy(np.concatenate([[1], cv]).astype(np.int32)).to(cuda)
+    nz_pad = torch.from_numpy(np.concatenate([[0], nz]).astype(dt)).to(cuda)
+    A = gsa.adapt(cuda, gsa.GenericSparseMatrixCSR(m, n, rp, cv, nz))
+    Am = gsa.adapt(cuda, gsa.GenericSparseMatrixCSR(m, n, rp, cv, nz))
+    Am.colval, Am.nzval = cv_pad[1:], nz_pad[1:]  # the constructor copies: point at the views
+    assert Am.colval.data_ptr() % 16 == 4
+    saved = lib.gsa_get_tuning(L.TUNE_STAGE_ROWS)
+    try:
+        for M in (A, Am):
+            ys = []
+            for stage in (0, 1):
+                assert lib.gsa_set_tuning(L.TUNE_STAGE_ROWS, stage) == L.OK
+                y = torch.full((m,), float("nan"), dtype=xd.dtype, device=cuda)
+                gsa.mul_(y, M, xd)
+                ys.append(y.cpu().numpy())
+            assert np.array_equal(ys[0], ys[1])
+            assert oracle.max_rel_error(ys[1], ye, sc) <= tol
+    finally:
+        lib.gsa_set_tuning(L.TUNE_STAGE_ROWS, saved)

@@ -253,3 +253,27 @@ def test_integration_guide_snippets_match_header():
         assert len(tlist) == len(ckinds) == len(args), (name, len(tlist), len(ckinds), len(args))
         for i, (jt, ck) in enumerate(zip(tlist, ckinds)):
             assert jl_kind(jt) == ck, f"{name}: argument {i + 1} is {jt}, gsa.h wants {ck}"
+
+
+def test_invoke_fallbacks_name_reference_methods():
+    """Every `invoke(Base.:+, Tuple{Parent, UniformScaling}, ...)` of the extension (its fallback
+    when lambda does not promote to the matrix's element type) names a method the reference
+    defines: tests/golden/reference_methods.json lists the reference's `Base.:+(::Matrix,
+    ::UniformScaling)` methods with their file:line.  The `@eval` loop's `$Parent` is resolved
+    from the loop's `(Fmt, Parent)` pairs.  (The fallback itself has not run: no Julia here.)"""
+    import json
+    src = open(EXT).read()
+    ref = json.load(open(os.path.join(ROOT, "tests", "golden", "reference_methods.json")))
+    defined = {(r["method"], tuple(r["args"])) for r in ref}
+    assert len(defined) == 3
+    loop = re.search(r"for \(Fmt, Parent\) in \(([^\n]*)\)\n", src)
+    parents = re.findall(r"\(:\w+, :(\w+)\)", loop.group(1)) if loop else []
+    assert parents == ["GenericSparseMatrixCSR", "GenericSparseMatrixCSC"]
+    calls = re.findall(r"invoke\((Base\.:\+), Tuple\{(\$?\w+), (\w+)\}", src)
+    assert calls, "no invoke fallback found"
+    seen = set()
+    for method, first, second in calls:
+        for parent in (parents if first == "$Parent" else [first]):
+            assert (method, (parent, second)) in defined, (method, parent, second)
+            seen.add(parent)
+    assert seen == {"GenericSparseMatrixCOO", "GenericSparseMatrixCSR", "GenericSparseMatrixCSC"}
