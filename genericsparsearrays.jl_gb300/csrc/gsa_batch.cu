@@ -36,7 +36,7 @@ __device__ __forceinline__ V scalar_at(const unsigned char *p) {
 template <typename V, typename I, int KC>
 __global__ void __launch_bounds__(RB_THREADS)
 grouped_kernel(const gsa_group_item *__restrict__ items, int64_t count, int64_t ntiles, int base,
-               int g1_avg) {
+               int g1_avg, int x_pairs) {
     // Each warp finds its tile's item on its own -- lane 0 searches forward from the
     // warp's previous item (a CTA's tiles ascend), the warp reads the item's fields with
     // uniform loads -- so warps never wait for one another between tiles.
@@ -75,6 +75,8 @@ grouped_kernel(const gsa_group_item *__restrict__ items, int64_t count, int64_t 
         B.rs = brow ? ldb : 1;
         B.cs = brow ? 1 : ldb;
         B.conj = false;
+        B.pairs = KC >= 2 && x_pairs && std::is_same<V, double>::value && brow && (ldb & 1) == 0 &&
+                  ((uintptr_t)B.p & 15) == 0;
         DenseOut<V> C;
         C.p = (V *)__ldg((const unsigned long long *)&it->C);
         C.ld = __ldg(&it->ldc);
@@ -117,7 +119,7 @@ struct GroupedBody {
         int64_t grid = (int64_t)sms * (per_sm > 0 ? per_sm : 1);
         if (grid > ntiles) grid = ntiles;
         timer_before(s);
-        kern<<<(unsigned)grid, RB_THREADS, 0, s>>>(items, count, ntiles, base, g1);
+        kern<<<(unsigned)grid, RB_THREADS, 0, s>>>(items, count, ntiles, base, g1, get_x_pairs());
         timer_after(s);
         return check_cuda(cudaGetLastError(), "grouped_kernel");
     }

@@ -11,12 +11,8 @@
 //   A. coarse_count_kernel: entries per coarse bucket (2^cs consecutive rows, at most 4096
 //      rows and 8192 buckets), histograms in shared memory; one scan of the bucket counts.
 //   B. coarse_place_kernel: a CTA takes a tile of 2048 entries, ranks them per coarse bucket
-//      in shared memory and reserves one contiguous run per bucket with one global atomic
-//      (made by the bucket's first entry of the tile; no pass over all buckets per tile), so
-//      the tile's writes land in runs that L2 merges into whole sectors: all tiles append at
-//      one moving frontier per bucket.  While a tile is processed, the bulk-copy engine
-//      prefetches the CTA's next tile into L2 (fine_kernel does the same with its next
-//      bucket's records).  Each entry is one
+//      in shared memory and reserves one contiguous run per bucket with one global atomic,
+//      so the tile's writes land in runs that L2 merges into whole sectors.  Each entry is one
 //      record: the key row-in-bucket << (mb + pb) | minor << pb | position (sorting a row by it
 //      is sorting by (minor, position)) and the value (conversions), one 16- or 32-byte store.
 //   C. fine_kernel: a CTA per coarse bucket counts its rows in shared memory, scans them --
@@ -247,21 +243,13 @@ coarse_place_kernel(Src src, const VT *__restrict__ vals_in, int64_t nnz, int64_
                     uint32_t *__restrict__ cfill, Rec<VT> *__restrict__ rec1) {
     const int cs = co.cs;
     const int64_t nb = co.nb;
-    // per bucket: the tile's count, then (in place) the first slot of the tile's run; zero
-    // between tiles (each entry clears its own bucket's word)
+    // per bucket: the tile's count, then (in place) the first slot of the tile's run
     __shared__ uint32_t s_run[COARSE_MAX];
     constexpr bool HAS_VAL = !std::is_same<VT, NoValue>::value;
     constexpr int64_t TILE = (int64_t)PB_THREADS * PB_ITEMS;
-    for (int64_t d = threadIdx.x; d < nb; d += blockDim.x) s_run[d] = 0;
-    __syncthreads();
     for (int64_t t0 = (int64_t)blockIdx.x * TILE; t0 < nnz; t0 += (int64_t)gridDim.x * TILE) {
-        // the CTA's next tile into L2 while this one is ranked, reserved and stored
-        const int64_t tn = t0 + (int64_t)gridDim.x * TILE;
-        if (threadIdx.x == 0 && tn < nnz) {
-            const int64_t te = tn + TILE < nnz ? tn + TILE : nnz;
-            src.prefetch(tn, te);
-            if constexpr (HAS_VAL) prefetch_l2(vals_in + tn, (size_t)(te - tn) * sizeof(VT));
-        }
+        for (int64_t d = threadIdx.x; d < nb; d += blockDim.x) s_run[d] = 0;
+        __syncthreads();
         // every entry is read once: its indices and value stay in registers across the
         // reservation
         uint32_t packed[PB_ITEMS];  // bucket << 16 | rank in the tile's run
@@ -293,16 +281,19 @@ coarse_place_kernel(Src src, const VT *__restrict__ vals_in, int64_t nnz, int64_
             packed[q] = e < nnz ? (d << 16) | atomicAdd(&s_run[d], 1u) : 0u;
         }
         __syncthreads();
-        // one reservation per bucket the tile touches, made by the bucket's first entry of the
-        // tile (rank 0): the tile's count becomes the first slot of its run (cfill starts at
-        // the buckets' first slots); a thread's reservations are independent atomics in flight
+        // one reservation per bucket the tile touches; eight independent atomics in flight
+        // per thread (cfill starts at the buckets' first slots)
+        for (int64_t d0 = threadIdx.x; d0 < nb; d0 += (int64_t)PB_THREADS * 8) {
+            uint32_t c[8], got[8];
 #pragma unroll
-        for (int q = 0; q < PB_ITEMS; ++q) {
-            const int64_t e = t0 + (int64_t)q * PB_THREADS + threadIdx.x;
-            if (e < nnz && (packed[q] & 0xffffu) == 0) {
-                const uint32_t d = packed[q] >> 16;
-                s_run[d] = atomicAdd(&cfill[d], s_run[d]);
+            for (int u = 0; u < 8; ++u) {
+                const int64_t d = d0 + (int64_t)u * PB_THREADS;
+                c[u] = d < nb ? s_run[d] : 0;
+                got[u] = c[u] ? atomicAdd(&cfill[d], c[u]) : 0;
             }
+#pragma unroll
+            for (int u = 0; u < 8; ++u)
+                if (c[u]) s_run[d0 + (int64_t)u * PB_THREADS] = got[u];
         }
         __syncthreads();
 #pragma unroll
@@ -313,12 +304,6 @@ coarse_place_kernel(Src src, const VT *__restrict__ vals_in, int64_t nnz, int64_
                 if constexpr (HAS_VAL) rec1[slot] = Rec<VT>{key[q], val[q]};
                 else rec1[slot] = Rec<VT>{key[q]};
             }
-        }
-        __syncthreads();
-#pragma unroll
-        for (int q = 0; q < PB_ITEMS; ++q) {
-            const int64_t e = t0 + (int64_t)q * PB_THREADS + threadIdx.x;
-            if (e < nnz) s_run[packed[q] >> 16] = 0;
         }
         __syncthreads();
     }
@@ -360,11 +345,6 @@ fine_kernel(int64_t major_n, Coarse co, const uint32_t *__restrict__ cstart, con
     for (int64_t bk = blockIdx.x; bk < nb; bk += gridDim.x) {
         const uint32_t B0 = cstart[bk], B1 = cstart[bk + 1];
         const uint32_t E = B1 - B0;
-        // this CTA's next bucket's records into L2 while this one is sorted
-        if (threadIdx.x == 0 && bk + gridDim.x < nb) {
-            const uint32_t N0 = cstart[bk + gridDim.x], N1 = cstart[bk + gridDim.x + 1];
-            prefetch_l2(rec1 + N0, (size_t)(N1 - N0) * sizeof(Rec<VT>));
-        }
         const bool invalid = bk == nb - 1;
         const int64_t row0 = invalid ? major_n : bk << cs;
         const int64_t rspan = major_n - row0 < (int64_t)rmax ? major_n - row0 : (int64_t)rmax;

@@ -747,6 +747,11 @@ int gsa_set_tuning(int key, int value) {
         set_stage_rows(value);
         return GSA_OK;
     }
+    if (key == GSA_TUNE_X_PAIRS) {
+        if (value != 0 && value != 1) return fail(GSA_ERR_INVALID_ARG, "x pairs must be 0 or 1");
+        set_x_pairs(value);
+        return GSA_OK;
+    }
     if (key == GSA_TUNE_WAIT_LIMIT) {
         if (value < 0) return fail(GSA_ERR_INVALID_ARG, "wait limit must be >= 0");
         set_wait_limit(value == 0 ? 0u : (uint32_t)value);
@@ -760,6 +765,7 @@ int gsa_get_tuning(int key) {
     if (key == GSA_TUNE_SPMM_COLUMNS) return get_spmm_columns();
     if (key == GSA_TUNE_PLAN_ORDER) return get_plan_natural();
     if (key == GSA_TUNE_STAGE_ROWS) return get_stage_rows();
+    if (key == GSA_TUNE_X_PAIRS) return get_x_pairs();
     if (key == GSA_TUNE_WAIT_LIMIT) {
         const uint32_t w = get_wait_limit();
         return w > 0x7fffffffu ? 0x7fffffff : (int)w;

@@ -379,11 +379,6 @@ template <typename I>
 struct PairSource {
     const I *mj, *mn;
     int base;
-    // the indices of entries [i0, i1) into L2 ahead of their loads
-    __device__ __forceinline__ void prefetch(int64_t i0, int64_t i1) const {
-        prefetch_l2(mj + i0, (size_t)(i1 - i0) * sizeof(I));
-        prefetch_l2(mn + i0, (size_t)(i1 - i0) * sizeof(I));
-    }
     __device__ __forceinline__ int64_t major(int64_t i) const { return (int64_t)__ldg(mj + i) - base; }
     __device__ __forceinline__ void get(int64_t i, int64_t &a, int64_t &b) const {
         a = (int64_t)__ldg(mj + i) - base;
@@ -732,7 +727,6 @@ template <typename I>
 struct SumSource {
     SumSources s;
     int base;
-    __device__ __forceinline__ void prefetch(int64_t, int64_t) const {}  // entries from up to three sources
     __device__ __forceinline__ void get(int64_t i, int64_t &col, int64_t &row) const {
         if (i < s.nnz[0] + s.nnz[1]) {
             const int w = i < s.nnz[0] ? 0 : 1;

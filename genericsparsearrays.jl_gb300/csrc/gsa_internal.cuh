@@ -8,6 +8,8 @@
 #include <stddef.h>
 #include <math.h>
 
+#include <type_traits>
+
 #include "../../include/gsa.h"
 
 // A plan (gsa_plan_create), device arrays in one allocation.  In the natural order of row
@@ -197,18 +199,6 @@ template <> __device__ __forceinline__ cf64 ld_stream(const cf64 *p) {
     return cf64{v.x, v.y};
 }
 
-// Asks the bulk-copy engine to bring the bytes of [p, p + bytes) that lie on whole 16-byte
-// pieces into L2, without waiting and without touching shared memory (a hint: no data comes
-// back).  Only for ranges inside one array: the pieces are rounded inwards.
-__device__ __forceinline__ void prefetch_l2(const void *p, size_t bytes) {
-    const uintptr_t a = ((uintptr_t)p + 15) & ~(uintptr_t)15;
-    const uintptr_t e = ((uintptr_t)p + bytes) & ~(uintptr_t)15;
-    for (uintptr_t q = a; q < e; q += (uintptr_t)1 << 16) {
-        const uint32_t n = (uint32_t)(e - q < ((uintptr_t)1 << 16) ? e - q : ((uintptr_t)1 << 16));
-        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(q), "r"(n) : "memory");
-    }
-}
-
 // Atomic accumulate (complex: one atomic per component).
 __device__ __forceinline__ void atomic_add(float *p, float v) { atomicAdd(p, v); }
 __device__ __forceinline__ void atomic_add(double *p, double v) { atomicAdd(p, v); }
@@ -256,14 +246,23 @@ template <> __device__ __forceinline__ cf64 shfl_down(cf64 v, int d) {
 
 // ---------------------------------------------------------------------------
 // Dense operand views.  op(B)(i, c) = B[i*rs + c*cs], conjugated if conj.
+// pairs: the caller checked that op(B)(i, c) and op(B)(i, c + 1) for even c are one aligned
+// 16-byte piece (Float64, unit column stride, even row stride, 16-byte aligned p), so a
+// thread's columns of one row may be read two at a time.
 template <typename V> struct DenseIn {
     const V *p;
     int64_t rs, cs;
     bool conj;
+    bool pairs = false;
     __device__ __forceinline__ V at(int64_t i, int64_t c) const {
         return conj_if(ldg(p + i * rs + c * cs), conj);
     }
 };
+
+// Whether a Float64 operand's rows can be read two columns at a time (see DenseIn::pairs).
+template <typename V> inline bool pairs_ok(const DenseIn<V> &B) {
+    return std::is_same<V, double>::value && B.cs == 1 && (B.rs & 1) == 0 && ((uintptr_t)B.p & 15) == 0;
+}
 
 // 0 + x without an FP add: x, except that -0 becomes +0 (integer compare and select,
 // so the FP64 pipe is not used).
@@ -484,6 +483,8 @@ void set_plan_natural(int v);   // 1: row blocks in natural order even where a p
 int get_plan_natural();
 void set_stage_rows(int v);     // 1: thread-per-row warps stage their span with 16-byte loads
 int get_stage_rows();
+void set_x_pairs(int v);        // 1 (default): Float64 row-major B read two columns per load
+int get_x_pairs();
 
 // Scatter: out[idx_j, c] += conj?(val_j) * (op(B)(o, c) * alpha), after the beta pass.
 // ALGO_MERGE: merge-path tiles (workspace: tile coordinates); otherwise outer blocks with

@@ -212,6 +212,10 @@ rowblock_staged_kernel(CompressedArgs<V, I> a, DenseIn<V> B, DenseOut<V> C, int6
     if (valid && !skip) C.store(row0 + lane, 0, acc);
 }
 
+static std::atomic<int> g_x_pairs{1};
+void set_x_pairs(int v) { g_x_pairs.store(v, std::memory_order_relaxed); }
+int get_x_pairs() { return g_x_pairs.load(std::memory_order_relaxed); }
+
 static std::atomic<int> g_stage_rows{0};
 void set_stage_rows(int v) { g_stage_rows.store(v, std::memory_order_relaxed); }
 int get_stage_rows() { return g_stage_rows.load(std::memory_order_relaxed); }
@@ -261,6 +265,7 @@ int launch_rowblock(cudaStream_t s, const CompressedArgs<V, I> &a, int64_t k, De
     if (k == 1) KC = 1;
     if (KC > k) KC = k <= 1 ? 1 : (k <= 2 ? 2 : (k <= 4 ? 4 : 8));
     const int64_t ncg = ceil_div(k, KC);
+    B.pairs = KC >= 2 && get_x_pairs() && pairs_ok(B);
     if (plan && (plan->outer_n != a.outer_n || plan->nnz != a.nnz))
         return fail(GSA_ERR_INVALID_ARG, "plan was made for another structure");
     const bool binned = plan && plan->nbin_warps > 0 && !get_plan_natural() && bins_pay<V>(k);

@@ -34,10 +34,59 @@ template <typename I> using Off = typename std::make_unsigned<I>::type;
 #define GSA_GN_UNROLL 2
 #endif
 
+// The same for Float64 with B.pairs: op(B)(i, c0 + c) read two columns per 16-byte load (c0
+// and c even), the multiply-adds in the same order as accumulate_range's.
+template <typename I, int KC, int S, int U>
+__device__ __forceinline__ void accumulate_pairs(const CompressedArgs<double, I> &a, const DenseIn<double> &B,
+                                                 Off<I> jb, Off<I> je, int64_t c0, int64_t k,
+                                                 double (&acc)[KC]) {
+    using O = Off<I>;
+    const I *__restrict__ idx = a.idx;
+    const double *__restrict__ val = a.val;
+    const O inner = sizeof(O) == 8 ? (O)a.inner_n
+                                   : (O)(a.inner_n < 0xffffffffLL ? a.inner_n : 0xffffffffLL);
+    const O base = (O)a.base;
+    auto row_fma = [&](O ci, double av) {
+        const bool ok = ci < inner;
+        const double *q = B.p + (int64_t)(ok ? ci : 0) * B.rs + c0;
+#pragma unroll
+        for (int c = 0; c < KC; c += 2) {
+            if (c0 + c + 1 < k) {
+                const double2 x = ok ? __ldg(reinterpret_cast<const double2 *>(q + c)) : make_double2(0.0, 0.0);
+                acc[c] = fma(av, x.x, acc[c]);
+                acc[c + 1] = fma(av, x.y, acc[c + 1]);
+            } else if (c0 + c < k) {
+                acc[c] = fma(av, ok ? __ldg(q + c) : 0.0, acc[c]);
+            }
+        }
+    };
+    O j = jb;
+    if (U > 1) {
+        for (; j + (O)((U - 1) * S) < je; j += U * S) {
+            O ci[U];
+            double av[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                ci[u] = (O)idx[j + u * S] - base;
+                av[u] = val[j + u * S];
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u) row_fma(ci[u], av[u]);
+        }
+    }
+    for (; j < je; j += S) row_fma((O)idx[j] - base, val[j]);
+}
+
 template <typename V, typename I, int KC, int S, int U>
 __device__ __forceinline__ void accumulate_range(const CompressedArgs<V, I> &a, const DenseIn<V> &B,
                                                  Off<I> jb, Off<I> je, int64_t c0, int64_t k,
                                                  V (&acc)[KC]) {
+    if constexpr (std::is_same<V, double>::value && KC >= 2) {
+        if (B.pairs) {
+            accumulate_pairs<I, KC, S, U>(a, B, jb, je, c0, k, acc);
+            return;
+        }
+    }
     using O = Off<I>;
     const I *__restrict__ idx = a.idx;
     const V *__restrict__ val = a.val;

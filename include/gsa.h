@@ -84,7 +84,13 @@ typedef enum {
     GSA_TUNE_STAGE_ROWS = 5,   /* 1: in the default gather with one right-hand side, Float32 /
                                   Float64 values and Int32 indices, warps of thread-per-row
                                   rows copy their contiguous entry span into shared memory with
-                                  16-byte loads before summing; 0 (default): direct loads */
+                                  16-byte loads before summing (measured slower on GB300: a
+                                  second memory round trip before the gathers); 0 (default):
+                                  direct loads */
+    GSA_TUNE_X_PAIRS = 6,      /* 1 (default): with Float64 values, several right-hand sides and a
+                                  row-major B (unit column stride, even row stride, 16-byte
+                                  aligned), a thread reads its columns of one row of B two at a
+                                  time with 16-byte loads; 0: one load per column */
     GSA_TUNE_WAIT_LIMIT = 4    /* polls a bounded device-side wait (the pipelined SpMV's
                                   mbarrier waits for its bulk copies) makes before it gives
                                   up, sets the device error word and returns: default

@@ -413,3 +413,33 @@ def test_staged_rows_match_direct(gsa, oracle, cuda, dt):
             assert oracle.max_rel_error(ys[1], ye, sc) <= tol
     finally:
         lib.gsa_set_tuning(L.TUNE_STAGE_ROWS, saved)
+
+
+@pytest.mark.parametrize("it", INDEX_TYPES)
+def test_row_major_pairs_match_single_loads(gsa, oracle, cuda, it):
+    """Float64 SpMM with a row-major X (the served layout: the first k columns of an n x 32
+    block): two columns per 16-byte load (GSA_TUNE_X_PAIRS = 1, the default) gives the bits of
+    one load per column, for odd and even k, planned and plain, and is within the oracle's
+    tolerance; an odd row stride falls back to single loads."""
+    L = gsa._lib
+    lib = L.load()
+    rng = np.random.default_rng(31)
+    S = sprand(rng, 3000, 2500, 0.006, np.float64)
+    p0, p1, v = parts(S, "csr", it)
+    A = make(gsa, "csr", 3000, 2500, p0, p1, v, cuda)
+    for ld in (32, 33):
+        block = rand_values(rng, (2500, ld), np.float64)
+        Bd = torch.from_numpy(block).to(cuda)
+        for k in (2, 5, 8, 16, 32 if ld == 32 else 31):
+            X = Bd[:, :k]
+            ye, sc = oracle.mul_exact("csr", "N", 3000, 2500, p0, p1, v, 1, np.asfortranarray(block[:, :k]),
+                                      np.zeros((3000, k), order="F"))
+            got = []
+            for pairs in (1, 0):
+                assert lib.gsa_set_tuning(L.TUNE_X_PAIRS, pairs) == L.OK
+                Y = torch.empty((k, 3000), dtype=torch.float64, device=cuda).t()
+                gsa.mul_(Y, A, X)
+                got.append(Y.cpu().numpy())
+            lib.gsa_set_tuning(L.TUNE_X_PAIRS, 1)
+            assert np.array_equal(got[0], got[1]), (ld, k)
+            assert oracle.max_rel_error(got[0], ye, sc) <= 1e-12
