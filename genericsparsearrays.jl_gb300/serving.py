@@ -366,8 +366,9 @@ class GroupedExecutor:
                 else:
                     groups[(A.dtype, A.itype)].append((A, r.X, r.Y, r.alpha, r.beta))
             for (dt, _), prods in groups.items():
-                # rows of a row-major X: 8 complex / 4 real values per thread share lines
-                cols = self.columns or (8 if dt == torch.complex128 else 4)
+                # rows of a row-major X: a thread takes 8 columns of a row (its values share
+                # cache lines; Float64 ones are read two per 16-byte load)
+                cols = self.columns or 8
                 self.launchers[slot].launch(prods, s, columns=cols)
             ev = torch.cuda.Event(enable_timing=True)
             ev.record(s)
