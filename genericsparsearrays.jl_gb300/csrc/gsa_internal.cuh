@@ -248,7 +248,7 @@ template <> __device__ __forceinline__ cf64 shfl_down(cf64 v, int d) {
 // Dense operand views.  op(B)(i, c) = B[i*rs + c*cs], conjugated if conj.
 // pairs: the caller checked that op(B)(i, c) and op(B)(i, c + 1) for even c are one aligned
 // 16-byte piece (Float64, unit column stride, even row stride, 16-byte aligned p), so a
-// thread's columns of one row may be read two at a time.
+// thread's columns of one row may be read two at a time (by kernels of 4 or 8 columns).
 template <typename V> struct DenseIn {
     const V *p;
     int64_t rs, cs;

@@ -81,7 +81,9 @@ template <typename V, typename I, int KC, int S, int U>
 __device__ __forceinline__ void accumulate_range(const CompressedArgs<V, I> &a, const DenseIn<V> &B,
                                                  Off<I> jb, Off<I> je, int64_t c0, int64_t k,
                                                  V (&acc)[KC]) {
-    if constexpr (std::is_same<V, double>::value && KC >= 2) {
+    // only in the 4- and 8-column kernels (what a row-major B takes): compiled into the
+    // 2-column kernel of a column-major B it cost 8 registers and 12 % of the Laplacian SpMM
+    if constexpr (std::is_same<V, double>::value && KC >= 4) {
         if (B.pairs) {
             accumulate_pairs<I, KC, S, U>(a, B, jb, je, c0, k, acc);
             return;

@@ -89,8 +89,9 @@ typedef enum {
                                   direct loads */
     GSA_TUNE_X_PAIRS = 6,      /* 1 (default): with Float64 values, several right-hand sides and a
                                   row-major B (unit column stride, even row stride, 16-byte
-                                  aligned), a thread reads its columns of one row of B two at a
-                                  time with 16-byte loads; 0: one load per column */
+                                  aligned), a thread of 4 or 8 columns reads its columns of one
+                                  row of B two at a time with 16-byte loads; 0: one load per
+                                  column */
     GSA_TUNE_WAIT_LIMIT = 4    /* polls a bounded device-side wait (the pipelined SpMV's
                                   mbarrier waits for its bulk copies) makes before it gives
                                   up, sets the device error word and returns: default
