@@ -743,7 +743,7 @@ int gsa_set_tuning(int key, int value) {
         return GSA_OK;
     }
     if (key == GSA_TUNE_STAGE_ROWS) {
-        if (value != 0 && value != 1) return fail(GSA_ERR_INVALID_ARG, "stage rows must be 0 or 1");
+        if (value < 0 || value > 2) return fail(GSA_ERR_INVALID_ARG, "stage rows must be 0, 1 or 2");
         set_stage_rows(value);
         return GSA_OK;
     }

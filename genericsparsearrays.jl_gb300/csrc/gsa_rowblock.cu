@@ -212,6 +212,71 @@ rowblock_staged_kernel(CompressedArgs<V, I> a, DenseIn<V> B, DenseOut<V> C, int6
     if (valid && !skip) C.store(row0 + lane, 0, acc);
 }
 
+// Vector rows (GSA_TUNE_STAGE_ROWS = 2; same types as the staged rows): each lane of a
+// thread-per-row warp reads its own row's indices and values in aligned 16-byte pieces
+// straight into registers -- one 16-byte index load and one or two value loads per four
+// entries, where the direct path issues a scalar load per entry and array -- and multiplies the
+// entries of each piece that lie in its row, in order (bit-identical to the direct path).  A
+// lane whose last piece would pass the end of the arrays uses scalar loads.
+template <typename V, typename I>
+__global__ void __launch_bounds__(RB_THREADS, rb_min_blocks<V, 1>())
+rowblock_vec_kernel(CompressedArgs<V, I> a, DenseIn<V> B, DenseOut<V> C, int64_t nrb, PlanRows L) {
+    static_assert(sizeof(I) == 4, "vector rows take 32-bit offsets");
+    const int w = threadIdx.x >> 5;
+    const int64_t unit = blockIdx.x;
+    if (unit >= nrb) {  // chunked rows: a warp per chunk
+        chunk_unit<V, I, 1>(a, 1, B, C, 0, 0u, 1, (unit - nrb) * RB_WARPS + w, L);
+        return;
+    }
+    const int64_t row0 = unit * RB_THREADS + (threadIdx.x & ~31);
+    if (row0 >= a.outer_n) return;  // a warp past the last row (uniform)
+    uint32_t b, e;
+    int skip;
+    const int64_t avg = warp_extent(a, row0, L.skip_mask, b, e, skip);
+    if (avg > G1_AVG) {
+        dispatch_lanes(avg, G1_AVG, [&](auto g) {
+            warp_rows<V, I, 1, decltype(g)::value>(a, 1, B, C, 0, row0, b, e, skip);
+        });
+        return;
+    }
+    const int lane = threadIdx.x & 31;
+    const uint32_t inner = a.inner_n < 0xffffffffLL ? (uint32_t)a.inner_n : 0xffffffffu;
+    const uint32_t base = (uint32_t)a.base;
+    V acc = VT<V>::zero();
+    if ((int64_t)((e + 3u) & ~3u) <= a.nnz) {
+#pragma unroll 2
+        for (uint32_t c = b & ~3u; c < e; c += 4) {
+            const int4 iv = __ldcs(reinterpret_cast<const int4 *>(a.idx + c));
+            V v[4];
+            if constexpr (sizeof(V) == 4) {
+                const float4 f = __ldcs(reinterpret_cast<const float4 *>(a.val + c));
+                v[0] = f.x; v[1] = f.y; v[2] = f.z; v[3] = f.w;
+            } else {
+                const double2 d0 = __ldcs(reinterpret_cast<const double2 *>(a.val + c));
+                const double2 d1 = __ldcs(reinterpret_cast<const double2 *>(a.val + c + 2));
+                v[0] = d0.x; v[1] = d0.y; v[2] = d1.x; v[3] = d1.y;
+            }
+            const uint32_t ci[4] = {(uint32_t)iv.x - base, (uint32_t)iv.y - base, (uint32_t)iv.z - base,
+                                    (uint32_t)iv.w - base};
+            V x[4];
+#pragma unroll
+            for (int t = 0; t < 4; ++t) {
+                const bool in = c + t >= b && c + t < e;
+                x[t] = in && ci[t] < inner ? B.at((int64_t)ci[t], 0) : VT<V>::zero();
+            }
+#pragma unroll
+            for (int t = 0; t < 4; ++t)
+                if (c + t >= b && c + t < e) acc = mac(acc, v[t], x[t]);
+        }
+    } else {
+        for (uint32_t j = b; j < e; ++j) {
+            const uint32_t c1 = (uint32_t)a.idx[j] - base;
+            acc = mac(acc, a.val[j], c1 < inner ? B.at((int64_t)c1, 0) : VT<V>::zero());
+        }
+    }
+    if (row0 + lane < a.outer_n && !skip) C.store(row0 + lane, 0, acc);
+}
+
 static std::atomic<int> g_x_pairs{1};
 void set_x_pairs(int v) { g_x_pairs.store(v, std::memory_order_relaxed); }
 int get_x_pairs() { return g_x_pairs.load(std::memory_order_relaxed); }
@@ -304,10 +369,15 @@ int launch_rowblock(cudaStream_t s, const CompressedArgs<V, I> &a, int64_t k, De
     }
     if constexpr (stage_rows_type<V>() && sizeof(I) == 4) {
         const bool aligned = ((uintptr_t)a.idx % 16 == 0) && ((uintptr_t)a.val % 16 == 0);
-        if (KC == 1 && get_stage_rows() && aligned) {
+        if (KC == 1 && get_stage_rows() == 1 && aligned) {
             rowblock_staged_kernel<V, I><<<(unsigned)blocks, RB_THREADS, 0, s>>>(a, B, C, nrb, L);
             timer_after(s);
             return check_cuda(cudaGetLastError(), "rowblock_staged_kernel");
+        }
+        if (KC == 1 && get_stage_rows() == 2 && aligned) {
+            rowblock_vec_kernel<V, I><<<(unsigned)blocks, RB_THREADS, 0, s>>>(a, B, C, nrb, L);
+            timer_after(s);
+            return check_cuda(cudaGetLastError(), "rowblock_vec_kernel");
         }
     }
     if (KC == 1) rowblock_kernel<V, I, 1><<<(unsigned)blocks, RB_THREADS, 0, s>>>(a, k, B, C, ncg, nrb, L);

@@ -85,8 +85,9 @@ typedef enum {
                                   Float64 values and Int32 indices, warps of thread-per-row
                                   rows copy their contiguous entry span into shared memory with
                                   16-byte loads before summing (measured slower on GB300: a
-                                  second memory round trip before the gathers); 0 (default):
-                                  direct loads */
+                                  second memory round trip before the gathers); 2: each lane
+                                  reads its own row in aligned 16-byte pieces into registers;
+                                  0 (default): direct loads */
     GSA_TUNE_X_PAIRS = 6,      /* 1 (default): with Float64 values, several right-hand sides and a
                                   row-major B (unit column stride, even row stride, 16-byte
                                   aligned), a thread of 4 or 8 columns reads its columns of one

@@ -164,7 +164,7 @@ def test_tuning_knobs(lib, gsa):
         assert lib.gsa_get_tuning(L.TUNE_STAGE_ROWS) == saved[L.TUNE_STAGE_ROWS] == 0
         assert lib.gsa_set_tuning(L.TUNE_STAGE_ROWS, 1) == 0
         assert lib.gsa_get_tuning(L.TUNE_STAGE_ROWS) == 1
-        assert lib.gsa_set_tuning(L.TUNE_STAGE_ROWS, 2) == L.ERR_INVALID_ARG
+        assert lib.gsa_set_tuning(L.TUNE_STAGE_ROWS, 3) == L.ERR_INVALID_ARG
         assert lib.gsa_get_tuning(L.TUNE_X_PAIRS) == saved[L.TUNE_X_PAIRS] == 1
         assert lib.gsa_set_tuning(L.TUNE_X_PAIRS, 0) == 0 and lib.gsa_get_tuning(L.TUNE_X_PAIRS) == 0
         assert lib.gsa_set_tuning(L.TUNE_X_PAIRS, 3) == L.ERR_INVALID_ARG

@@ -375,7 +375,8 @@ def test_window_scatter(gsa, oracle, cuda, dt, it):
 @pytest.mark.parametrize("dt", [np.float32, np.float64])
 def test_staged_rows_match_direct(gsa, oracle, cuda, dt):
     """GSA_TUNE_STAGE_ROWS = 1 (warps of thread-per-row rows copy their entry span with 16-byte
-    loads): bit-identical to the direct loads (same summation order), within the oracle's
+    loads) and 2 (each lane reads its row in 16-byte pieces into registers): bit-identical to the
+    direct loads (same summation order), within the oracle's
     tolerance; with long rows taken by a plan, empty rows, a last CTA with a warp past the last
     row, the last warp's span at the end of the arrays, and misaligned arrays (a view one entry
     in), which take the direct path."""
@@ -404,12 +405,12 @@ def test_staged_rows_match_direct(gsa, oracle, cuda, dt):
     try:
         for M in (A, Am):
             ys = []
-            for stage in (0, 1):
+            for stage in (0, 1, 2):
                 assert lib.gsa_set_tuning(L.TUNE_STAGE_ROWS, stage) == L.OK
                 y = torch.full((m,), float("nan"), dtype=xd.dtype, device=cuda)
                 gsa.mul_(y, M, xd)
                 ys.append(y.cpu().numpy())
-            assert np.array_equal(ys[0], ys[1])
+            assert np.array_equal(ys[0], ys[1]) and np.array_equal(ys[0], ys[2])
             assert oracle.max_rel_error(ys[1], ye, sc) <= tol
     finally:
         lib.gsa_set_tuning(L.TUNE_STAGE_ROWS, saved)
