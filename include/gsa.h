@@ -86,8 +86,9 @@ typedef enum {
                                   rows copy their contiguous entry span into shared memory with
                                   16-byte loads before summing (measured slower on GB300: a
                                   second memory round trip before the gathers); 2: each lane
-                                  reads its own row in aligned 16-byte pieces into registers;
-                                  0 (default): direct loads */
+                                  reads its own row in aligned 16-byte pieces into registers
+                                  (4-5 % faster on rows of about 4 entries, slower on the
+                                  Float64 Laplacian); 0 (default): direct loads */
     GSA_TUNE_X_PAIRS = 6,      /* 1 (default): with Float64 values, several right-hand sides and a
                                   row-major B (unit column stride, even row stride, 16-byte
                                   aligned), a thread of 4 or 8 columns reads its columns of one
