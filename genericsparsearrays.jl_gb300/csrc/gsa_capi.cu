@@ -738,7 +738,7 @@ int gsa_set_tuning(int key, int value) {
         return GSA_OK;
     }
     if (key == GSA_TUNE_PLAN_ORDER) {
-        if (value != 0 && value != 1) return fail(GSA_ERR_INVALID_ARG, "plan order must be 0 or 1");
+        if (value < 0 || value > 2) return fail(GSA_ERR_INVALID_ARG, "plan order must be 0, 1 or 2");
         set_plan_natural(value);
         return GSA_OK;
     }

@@ -334,7 +334,10 @@ int launch_rowblock(cudaStream_t s, const CompressedArgs<V, I> &a, int64_t k, De
     B.pairs = KC >= 2 && get_x_pairs() && pairs_ok(B);
     if (plan && (plan->outer_n != a.outer_n || plan->nnz != a.nnz))
         return fail(GSA_ERR_INVALID_ARG, "plan was made for another structure");
-    const bool binned = plan && plan->nbin_warps > 0 && !get_plan_natural() && bins_pay<V>(k);
+    // plan order 0: the bin order where it pays; 1: natural always; 2: the bin order for every
+    // FP64 product whose plan has one
+    const int order = get_plan_natural();
+    const bool binned = plan && plan->nbin_warps > 0 && order != 1 && (order == 2 || bins_pay<V>(k));
     PlanRows L{};
     int64_t chunk_warps = 0;
     const gsa_chunk_set *cs = plan ? (binned ? &plan->bin : &plan->nat) : nullptr;

@@ -79,8 +79,11 @@ typedef enum {
     GSA_TUNE_PIPE_THREADS = 1, /* threads per CTA of the pipelined SpMV: 256 or 512 */
     GSA_TUNE_SPMM_COLUMNS = 2, /* right-hand-side columns a thread accumulates in the default
                                   gather with k > 1: 0 (by value size), 1, 2, 4 or 8 */
-    GSA_TUNE_PLAN_ORDER = 3,   /* 0: a planned gather runs in the plan's order (bin order
-                                  where the plan chose it); 1: always in natural row order */
+    GSA_TUNE_PLAN_ORDER = 3,   /* 0: a planned gather runs in the plan's bin order where the
+                                  plan has one and the product is FP64-bound (ComplexF64, or
+                                  Float64 with several right-hand sides); 1: always in natural
+                                  row order; 2: in the bin order for every Float64 / ComplexF64
+                                  product whose plan has one */
     GSA_TUNE_STAGE_ROWS = 5,   /* 1: in the default gather with one right-hand side, Float32 /
                                   Float64 values and Int32 indices, warps of thread-per-row
                                   rows copy their contiguous entry span into shared memory with

@@ -159,7 +159,8 @@ def test_tuning_knobs(lib, gsa):
         assert lib.gsa_get_tuning(L.TUNE_SPMM_COLUMNS) == 4
         assert lib.gsa_set_tuning(L.TUNE_PLAN_ORDER, 1) == 0
         assert lib.gsa_get_tuning(L.TUNE_PLAN_ORDER) == 1
-        assert lib.gsa_set_tuning(L.TUNE_PLAN_ORDER, 2) == L.ERR_INVALID_ARG
+        assert lib.gsa_set_tuning(L.TUNE_PLAN_ORDER, 2) == 0 and lib.gsa_get_tuning(L.TUNE_PLAN_ORDER) == 2
+        assert lib.gsa_set_tuning(L.TUNE_PLAN_ORDER, 3) == L.ERR_INVALID_ARG
         assert lib.gsa_get_tuning(L.TUNE_WAIT_LIMIT) == saved[L.TUNE_WAIT_LIMIT] == 1 << 24
         assert lib.gsa_get_tuning(L.TUNE_STAGE_ROWS) == saved[L.TUNE_STAGE_ROWS] == 0
         assert lib.gsa_set_tuning(L.TUNE_STAGE_ROWS, 1) == 0

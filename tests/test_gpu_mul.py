@@ -279,8 +279,9 @@ def test_sparse_rows_span_many_tiles(gsa, oracle, cuda, dt):
 @pytest.mark.parametrize("k", [1, 3])
 def test_plan_orders(gsa, oracle, cuda, dt, k):
     """Power-law rows: the plan puts them in bin order (rows grouped by length) and chunks
-    rows over 512; the natural order (GSA_TUNE_PLAN_ORDER = 1) with the same plan, and both
-    for CSR N and the same arrays as a transposed CSC, match the oracle."""
+    rows over 512; the natural order (GSA_TUNE_PLAN_ORDER = 1) and the bin order for every FP64
+    product (= 2) with the same plan, each for CSR N and the same arrays as a transposed CSC,
+    match the oracle."""
     from genericsparsearrays_gb300 import _lib, workloads
     lib = _lib.load()
     m, n, rp, cv, nz = workloads.power_law(n=60_000, cap=5_000, seed=5, itype=np.int64, dtype=np.float64)
@@ -289,7 +290,7 @@ def test_plan_orders(gsa, oracle, cuda, dt, k):
     X = np.asfortranarray(rand_values(rng, (n, k), dt))
     C0 = np.asfortranarray(rand_values(rng, (m, k), dt))
     try:
-        for natural in (0, 1):
+        for natural in (0, 1, 2):
             assert lib.gsa_set_tuning(_lib.TUNE_PLAN_ORDER, natural) == 0
             for fmt in ("csr", "csc_t"):
                 if fmt == "csr":
