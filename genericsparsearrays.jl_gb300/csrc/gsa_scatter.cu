@@ -391,6 +391,15 @@ coo_kernel(int64_t nnz, const I *__restrict__ out_idx, const I *__restrict__ in_
         const int64_t prev_key = __shfl_up_sync(0xffffffffu, key, 1);
         const int64_t next_key = __shfl_down_sync(0xffffffffu, key, 1);
         const bool tail = valid && (lane == 31 || next_key != key);
+        // no run longer than one entry in this warp (COO in random order): every valid entry
+        // is its own tail, and the segmented sum -- five rounds of adds on the FP64 pipe -- is
+        // skipped (warp-uniform)
+        const bool runs = __any_sync(0xffffffffu, valid && !tail);
+        if (!runs) {
+            for (int64_t c = 0; c < k; ++c)
+                if (valid) atomic_add(C.p + key + c * C.ld, mul(av, mul(B.at(in, c), C.alpha)));
+            continue;
+        }
         int run_start = (lane == 0 || prev_key != key) ? lane : 0;
 #pragma unroll
         for (int off = 1; off < 32; off <<= 1) {
