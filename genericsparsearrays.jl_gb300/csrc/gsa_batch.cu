@@ -36,14 +36,16 @@ __device__ __forceinline__ V scalar_at(const unsigned char *p) {
 template <typename V, typename I, int KC>
 __global__ void __launch_bounds__(RB_THREADS)
 grouped_kernel(const gsa_group_item *__restrict__ items, int64_t count, int64_t ntiles, int base,
-               int g1_avg, int x_pairs) {
+               int g1_avg, int x_pairs, const int32_t *__restrict__ tile_item) {
     // Each warp finds its tile's item on its own -- lane 0 searches forward from the
     // warp's previous item (a CTA's tiles ascend), the warp reads the item's fields with
     // uniform loads -- so warps never wait for one another between tiles.
     const int lane = threadIdx.x & 31;
     int64_t lo = 0;
     for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
-        if (lane == 0 && lo + 1 < count && __ldg(&items[lo + 1].first_tile) <= t) {
+        if (tile_item) {  // a batch's table: the tile's item in one load
+            lo = __ldg(tile_item + t);
+        } else if (lane == 0 && lo + 1 < count && __ldg(&items[lo + 1].first_tile) <= t) {
             int64_t l = lo + 1, h = count - 1;  // last item with first_tile <= t, in (lo, count)
             while (l < h) {
                 const int64_t mid = (l + h + 1) >> 1;
@@ -52,7 +54,7 @@ grouped_kernel(const gsa_group_item *__restrict__ items, int64_t count, int64_t 
             }
             lo = l;
         }
-        lo = __shfl_sync(0xffffffffu, lo, 0);
+        if (!tile_item) lo = __shfl_sync(0xffffffffu, lo, 0);
         const gsa_group_item *it = items + lo;
         const int64_t kk = __ldg(&it->k);
         const int64_t ncg = (kk + KC - 1) / KC;
@@ -105,6 +107,7 @@ int default_columns(int dtype) { return dtype_size(dtype) == 8 ? 2 : 4; }  // co
 
 struct GroupedBody {
     cudaStream_t s; const gsa_group_item *items; int64_t count, ntiles; int base, KC, g1;
+    const int32_t *tile_item;
     template <typename V, typename I> int operator()() {
         if (ntiles == 0) return GSA_OK;
         auto kern = KC == 1 ? grouped_kernel<V, I, 1>
@@ -119,17 +122,17 @@ struct GroupedBody {
         int64_t grid = (int64_t)sms * (per_sm > 0 ? per_sm : 1);
         if (grid > ntiles) grid = ntiles;
         timer_before(s);
-        kern<<<(unsigned)grid, RB_THREADS, 0, s>>>(items, count, ntiles, base, g1, get_x_pairs());
+        kern<<<(unsigned)grid, RB_THREADS, 0, s>>>(items, count, ntiles, base, g1, get_x_pairs(), tile_item);
         timer_after(s);
         return check_cuda(cudaGetLastError(), "grouped_kernel");
     }
 };
 
 int grouped_mul(cudaStream_t s, int dtype, int itype, int base, const gsa_group_item *d_items,
-                int64_t count, int64_t ntiles, int columns, int g1) {
+                int64_t count, int64_t ntiles, int columns, int g1, const int32_t *tile_item = nullptr) {
     // one right-hand side everywhere runs KC = 1; otherwise the batch's KC
     const int KC = columns > 0 ? columns : default_columns(dtype);
-    GroupedBody body{s, d_items, count, ntiles, base, KC, g1 > 0 ? g1 : G1_AVG};
+    GroupedBody body{s, d_items, count, ntiles, base, KC, g1 > 0 ? g1 : G1_AVG, tile_item};
     return dispatch_vi(dtype, itype, body);
 }
 
@@ -138,11 +141,13 @@ int grouped_mul(cudaStream_t s, int dtype, int itype, int base, const gsa_group_
 using namespace gsa;
 
 // A batch: items kept on the device (and on the host for the per-call mode), tiles
-// counted once, an optional captured graph of the grouped launch.
+// counted once with a tile -> item table (so a warp finds its tile's item in one load instead
+// of a search), an optional captured graph of the grouped launch.
 struct gsa_batch {
     int dtype = 0, itype = 0, base = 1, columns = 0, g1 = 0;
     std::vector<gsa_group_item> host;
     gsa_group_item *dev = nullptr;
+    int32_t *tiles = nullptr;
     int64_t ntiles = 0;
     cudaStream_t capture = nullptr;
     cudaGraph_t graph = nullptr;
@@ -222,16 +227,29 @@ int gsa_batch_create(void *stream, int dtype, int itype, int base, const gsa_gro
                         (long long)i);
         }
     int rc = gsa_grouped_tiles(dtype, b->host.data(), count, columns, &b->ntiles);
+    if (!rc && count > 0x7fffffffLL) rc = fail(GSA_ERR_UNSUPPORTED, "batch: more than 2^31 - 1 items");
+    std::vector<int32_t> table;
     if (!rc && count > 0) {
+        table.resize((size_t)b->ntiles);
+        for (int64_t i = 0; i < count; ++i) {
+            const int64_t t1 = i + 1 < count ? b->host[(size_t)i + 1].first_tile : b->ntiles;
+            for (int64_t t = b->host[(size_t)i].first_tile; t < t1; ++t) table[(size_t)t] = (int32_t)i;
+        }
         rc = check_cuda(cudaMalloc(&b->dev, sizeof(gsa_group_item) * count), "batch: device items");
+        if (!rc && b->ntiles > 0) rc = check_cuda(cudaMalloc(&b->tiles, sizeof(int32_t) * b->ntiles), "batch: tiles");
         if (!rc)
             rc = check_cuda(cudaMemcpyAsync(b->dev, b->host.data(), sizeof(gsa_group_item) * count,
                                             cudaMemcpyHostToDevice, (cudaStream_t)stream),
                             "batch: item upload");
+        if (!rc && b->ntiles > 0)
+            rc = check_cuda(cudaMemcpyAsync(b->tiles, table.data(), sizeof(int32_t) * b->ntiles,
+                                            cudaMemcpyHostToDevice, (cudaStream_t)stream),
+                            "batch: tile upload");
         if (!rc) rc = check_cuda(cudaStreamSynchronize((cudaStream_t)stream), "batch: sync");
     }
     if (rc) {
         if (b->dev) cudaFree(b->dev);
+        if (b->tiles) cudaFree(b->tiles);
         delete b;
         return rc;
     }
@@ -244,7 +262,7 @@ int gsa_batch_run(gsa_batch *b, void *stream, int mode) {
     cudaStream_t s = (cudaStream_t)stream;
     const int64_t count = (int64_t)b->host.size();
     if (mode == GSA_BATCH_GROUPED)
-        return grouped_mul(s, b->dtype, b->itype, b->base, b->dev, count, b->ntiles, b->columns, b->g1);
+        return grouped_mul(s, b->dtype, b->itype, b->base, b->dev, count, b->ntiles, b->columns, b->g1, b->tiles);
     if (mode == GSA_BATCH_GRAPH) {
         if (!b->exec) {
             int rc = check_cuda(cudaStreamCreateWithFlags(&b->capture, cudaStreamNonBlocking), "batch: stream");
@@ -252,7 +270,7 @@ int gsa_batch_run(gsa_batch *b, void *stream, int mode) {
             rc = check_cuda(cudaStreamBeginCapture(b->capture, cudaStreamCaptureModeThreadLocal), "batch: capture");
             if (rc) return rc;
             const int lrc = grouped_mul(b->capture, b->dtype, b->itype, b->base, b->dev, count, b->ntiles,
-                                        b->columns, b->g1);
+                                        b->columns, b->g1, b->tiles);
             rc = check_cuda(cudaStreamEndCapture(b->capture, &b->graph), "batch: end capture");
             if (lrc) return lrc;
             if (rc) return rc;
@@ -282,6 +300,10 @@ int gsa_batch_destroy(gsa_batch *b) {
     if (b->graph) cudaGraphDestroy(b->graph);
     if (b->capture) cudaStreamDestroy(b->capture);
     int rc = b->dev ? check_cuda(cudaFree(b->dev), "batch: free") : GSA_OK;
+    if (b->tiles) {
+        const int rc2 = check_cuda(cudaFree(b->tiles), "batch: free");
+        rc = rc ? rc : rc2;
+    }
     delete b;
     return rc;
 }

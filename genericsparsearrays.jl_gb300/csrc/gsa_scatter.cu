@@ -368,12 +368,11 @@ template <typename V, typename I>
 __global__ void __launch_bounds__(256)
 coo_kernel(int64_t nnz, const I *__restrict__ out_idx, const I *__restrict__ in_idx,
            const V *__restrict__ val, int base, bool conjA, int64_t k, DenseIn<V> B,
-           DenseOut<V> C, int64_t out_rows, int64_t in_rows, bool prescaled) {
-    // op(B)(in, c) * alpha: read from the prescaled copy, or formed here (alpha == 1 of a real
-    // type needs no multiply: exact)
+           DenseOut<V> C, int64_t out_rows, int64_t in_rows) {
+    // op(B)(in, c) * alpha (alpha == 1 of a real type needs no multiply: exact)
     auto xa = [&](int64_t in, int64_t c) -> V {
         const V x = B.at(in, c);
-        return prescaled || C.alpha_one ? x : mul(x, C.alpha);
+        return C.alpha_one ? x : mul(x, C.alpha);
     };
     const int lane = threadIdx.x & 31;
     const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -424,16 +423,6 @@ coo_kernel(int64_t nnz, const I *__restrict__ out_idx, const I *__restrict__ in_
     }
 }
 
-// out[i + c * rows] = op(B)(i, c) * alpha: the scaled right-hand side the COO kernel reads when
-// each value of B serves several entries (the same products as forming them per entry).
-template <typename V>
-__global__ void scale_rows_kernel(DenseIn<V> B, V alpha, int64_t rows, int64_t k, V *__restrict__ out) {
-    const int64_t total = rows * k;
-    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total;
-         t += (int64_t)gridDim.x * blockDim.x)
-        out[t] = mul(B.at(t % rows, t / rows), alpha);
-}
-
 template <typename V, typename I>
 int launch_coo(cudaStream_t s, int64_t nnz, const I *out_idx, const I *in_idx, const V *val,
                int base, bool conjA, int64_t k, DenseIn<V> B, DenseOut<V> C, int64_t out_rows,
@@ -441,42 +430,14 @@ int launch_coo(cudaStream_t s, int64_t nnz, const I *out_idx, const I *in_idx, c
     int rc = launch_rmul_or_fill<V>(s, C, out_rows, k);
     if (rc) return rc;
     if (nnz == 0 || k == 0) return GSA_OK;
-    // op(B) * alpha formed once (stream-ordered scratch) when every value of B serves at least
-    // one entry on average: half the FP64 work of a complex entry, the same bits; without the
-    // scratch (allocation refused) each entry forms its own product
-    void *xs = nullptr;
-    DenseIn<V> Bx = B;
-    bool prescaled = false;
-    if (!C.alpha_one && in_rows > 0 && in_rows * k <= nnz) {
-        if (cudaMallocAsync(&xs, (size_t)(in_rows * k) * sizeof(V), s) == cudaSuccess) {
-            int64_t sb = ceil_div(in_rows * k, 256);
-            if (sb > 152 * 16) sb = 152 * 16;
-            scale_rows_kernel<V><<<(unsigned)sb, 256, 0, s>>>(B, C.alpha, in_rows, k, (V *)xs);
-            rc = check_cuda(cudaGetLastError(), "scale_rows_kernel");
-            if (rc) {
-                cudaFreeAsync(xs, s);
-                return rc;
-            }
-            Bx.p = (const V *)xs;
-            Bx.rs = 1;
-            Bx.cs = in_rows;
-            Bx.conj = false;
-            prescaled = true;
-        } else {
-            cudaGetLastError();
-            xs = nullptr;
-        }
-    }
     int64_t warps = ceil_div(nnz, 32);
     int64_t blocks = ceil_div(warps, 8);
     if (blocks > 152 * 16) blocks = 152 * 16;
     timer_before(s);
-    coo_kernel<V, I><<<(unsigned)blocks, 256, 0, s>>>(nnz, out_idx, in_idx, val, base, conjA, k, Bx,
-                                                       C, out_rows, in_rows, prescaled);
+    coo_kernel<V, I><<<(unsigned)blocks, 256, 0, s>>>(nnz, out_idx, in_idx, val, base, conjA, k, B,
+                                                       C, out_rows, in_rows);
     timer_after(s);
-    rc = check_cuda(cudaGetLastError(), "coo_kernel");
-    if (xs) cudaFreeAsync(xs, s);
-    return rc;
+    return check_cuda(cudaGetLastError(), "coo_kernel");
 }
 
 #define GSA_INST_SCATTER(V, I)                                                                  \

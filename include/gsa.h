@@ -155,10 +155,7 @@ int gsa_csc_mul(void *stream, int dtype, int itype, int64_t m, int64_t n, int64_
  * _T!, src/matrix_coo/matrix_coo_kernels.jl:1-43).  Any storage order and
  * duplicates are accepted; runs of equal output rows are reduced in registers
  * before the atomics (warps without such a run, as in a COO of random order, go
- * straight to the atomics).  Takes no workspace argument: when every value of
- * op(B) serves at least one entry on average (rows(op(B)) * k <= nnz) and alpha
- * is not a real one, op(B) * alpha is formed once into stream-ordered scratch
- * (cudaMallocAsync / cudaFreeAsync on the call's stream; without it, per entry). */
+ * straight to the atomics).  Needs no workspace. */
 int gsa_coo_mul(void *stream, int dtype, int itype, int64_t m, int64_t n, int64_t nnz,
                 const void *rowind, const void *colind, const void *nzval, int base, int opA,
                 int64_t k, const void *B, int64_t ldb, int opB, void *C, int64_t ldc,
