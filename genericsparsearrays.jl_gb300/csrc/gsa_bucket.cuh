@@ -55,13 +55,6 @@ constexpr int COARSE_MAX = 8192;   // coarse buckets, the invalid-row bucket inc
 constexpr int PB_THREADS = 256, PB_ITEMS = 8;
 constexpr int PC_THREADS = 512;
 constexpr int STAGE_BYTES = 96 * 1024;  // fine_kernel's shared staging of one coarse bucket
-// Words between two buckets' fill cursors in pass B: every tile reserves its runs with atomics
-// on the cursors, and cursors packed into shared cache lines put all tiles' atomics on a few
-// hot lines of L2.
-#ifndef GSA_CURSOR_STRIDE
-#define GSA_CURSOR_STRIDE 32
-#endif
-constexpr int CURSOR_STRIDE = GSA_CURSOR_STRIDE;
 
 struct NoValue {};  // the COO sums carry no values (they sum by input position)
 
@@ -139,7 +132,7 @@ template <class Emit> struct PackedEmit {
 struct Layout {
     Coarse co;
     int64_t ncnt;
-    size_t cnt, cstart, start, bsums, cur, key1, rec1, key2, val2, list, counters, bytes;
+    size_t cnt, cstart, start, bsums, key1, rec1, key2, val2, list, counters, bytes;
 };
 
 // vsize: bytes of a carried value (0: none)
@@ -151,7 +144,6 @@ inline Layout layout(int64_t major_n, int64_t minor_n, int64_t nnz, size_t vsize
     const int64_t nscan = L.ncnt > major_n + 2 ? L.ncnt : major_n + 2;
     Carver cv(nullptr);
     L.cnt = cv.reserve<uint32_t>(L.ncnt);
-    L.cur = L.co.ok ? cv.reserve<uint32_t>((size_t)(L.co.nb + 1) * CURSOR_STRIDE) : 0;
     L.cstart = cv.reserve<uint32_t>(L.ncnt);
     L.start = cv.reserve<uint32_t>(major_n + 2);
     L.bsums = cv.reserve<uint32_t>(ceil_div(nscan, (int64_t)sc_tile) + 1);
@@ -297,7 +289,7 @@ coarse_place_kernel(Src src, const VT *__restrict__ vals_in, int64_t nnz, int64_
             for (int u = 0; u < 8; ++u) {
                 const int64_t d = d0 + (int64_t)u * PB_THREADS;
                 c[u] = d < nb ? s_run[d] : 0;
-                got[u] = c[u] ? atomicAdd(&cfill[d * CURSOR_STRIDE], c[u]) : 0;
+                got[u] = c[u] ? atomicAdd(&cfill[d], c[u]) : 0;
             }
 #pragma unroll
             for (int u = 0; u < 8; ++u)
@@ -315,12 +307,6 @@ coarse_place_kernel(Src src, const VT *__restrict__ vals_in, int64_t nnz, int64_
         }
         __syncthreads();
     }
-}
-
-// cur[d * CURSOR_STRIDE] = cstart[d], d < n: pass B's fill cursors.
-__global__ void spread_cursors_kernel(const uint32_t *__restrict__ cstart, int64_t n, uint32_t *__restrict__ cur) {
-    const int64_t d = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (d < n) cur[d * CURSOR_STRIDE] = cstart[d];
 }
 
 // Dynamic shared memory of fine_kernel: the staged keys and values, then row offsets and
@@ -678,16 +664,15 @@ int sort(cudaStream_t s, int64_t major_n, int64_t minor_n, int64_t nnz, const Sr
                 src, nnz, major_n, co.cs, co.nb, cnt);
         rc = check_cuda(cudaGetLastError(), "bucket coarse_count_kernel");
         if (!rc) rc = scan(s, cnt, cstart, co.nb + 1, bsums);  // cstart[nb] = nnz
-        // the fill cursors start at the buckets' first slots (one per CURSOR_STRIDE words)
-        uint32_t *cur = (uint32_t *)(w + L.cur);
-        if (!rc) {
-            spread_cursors_kernel<<<(unsigned)ceil_div(co.nb + 1, 256), 256, 0, s>>>(cstart, co.nb + 1, cur);
-            rc = check_cuda(cudaGetLastError(), "bucket: cursors");
-        }
+        // the fill cursors start at the buckets' first slots
+        if (!rc)
+            rc = check_cuda(cudaMemcpyAsync(cnt, cstart, (size_t)(co.nb + 1) * sizeof(uint32_t),
+                                            cudaMemcpyDeviceToDevice, s),
+                            "bucket: cursors");
         if (rc) return rc;
         if (nnz > 0)
             coarse_place_kernel<Src, VT><<<grid_for(nnz, PB_THREADS * PB_ITEMS, cap), PB_THREADS, 0, s>>>(
-                src, vals_in, nnz, major_n, co, cur, rec1);
+                src, vals_in, nnz, major_n, co, cnt, rec1);
         const size_t smem = fine_smem_bytes<VT>(co.cs);
         rc = check_cuda(cudaFuncSetAttribute(fine_kernel<VT, Emit>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)smem),
