@@ -22,7 +22,7 @@ OP_N, OP_T, OP_C = 0, 1, 2
 SUM_NEGATE = 4
 ALGO_AUTO, ALGO_MERGE, ALGO_VECTOR, ALGO_PIPE = 0, 1, 2, 3
 (TUNE_PIPE_THREADS, TUNE_SPMM_COLUMNS, TUNE_PLAN_ORDER, TUNE_WAIT_LIMIT, TUNE_STAGE_ROWS,
- TUNE_X_PAIRS) = 1, 2, 3, 4, 5, 6
+ TUNE_X_PAIRS, TUNE_SORT_STAGED) = 1, 2, 3, 4, 5, 6, 7
 BATCH_GROUPED, BATCH_GRAPH, BATCH_PER_CALL = 0, 1, 2
 
 # Every exported symbol of include/gsa.h with its ctypes signature.

@@ -23,7 +23,9 @@
 //      (bitonic sort of 16384-entry chunks in shared memory, merged pairwise; values then
 //      gathered by input position).  A bucket larger than the staging is placed in global
 //      memory instead, with its rows of more than 16 entries listed for warp_kernel and
-//      cta_kernel.
+//      cta_kernel.  Where rows average at most 8 entries, fine_stage_kernel runs this pass
+//      instead: one CTA per SM, the next bucket's records copied into shared memory while the
+//      current one is sorted, the bucket's output written with coalesced stores.
 // Matrices with more than 8191 x 4096 rows take the one-level form (count, place, and
 // small_kernel per row), whose stores are random.
 //
@@ -48,6 +50,7 @@ constexpr int SMALL = 16;          // a thread sorts rows of up to 16 entries in
 constexpr int WARP_MAX = 256;      // a warp sorts rows of up to 256 entries
 constexpr int CTA_THREADS = 1024;
 constexpr int CTA_TILE = 16384;    // a CTA sorts 16384 entries in shared memory at once (128 KB)
+constexpr int RANK_MAX = 1024;     // a CTA ranks rows of up to 1024 entries by counting
 constexpr int WARP_CTA_THREADS = 256;
 constexpr int MERGE_ITEMS = 8;
 constexpr int ROWS_MAX = 4096;     // rows per coarse bucket
@@ -106,6 +109,28 @@ template <class VT> struct Rec<VT, false> {
     uint64_t key;
 };
 constexpr size_t rec_size(size_t vsize) { return vsize == 0 ? 8 : (vsize <= 8 ? 16 : 32); }
+
+// Stores a record with every byte written, the alignment padding as zeros (4-byte values
+// leave 4 bytes, 16-byte values 8 bytes): a sector left partly unwritten makes the L2 read it
+// from DRAM before writing it back, which doubled pass B's reads for ComplexF64.
+template <class VT> __device__ __forceinline__ void store_rec(Rec<VT> *p, uint64_t key, const VT &v) {
+    static_assert(sizeof(VT) == 4 || sizeof(VT) == 8 || sizeof(VT) == 16, "record values of 4, 8 or 16 bytes");
+    if constexpr (sizeof(VT) == 16) {
+        ulonglong2 head, tail;
+        head.x = key;
+        head.y = 0;
+        memcpy(&tail, &v, 16);
+        reinterpret_cast<ulonglong2 *>(p)[0] = head;
+        reinterpret_cast<ulonglong2 *>(p)[1] = tail;
+    } else {
+        ulonglong2 w;
+        w.x = key;
+        w.y = 0;
+        memcpy(&w.y, &v, sizeof(VT));
+        *reinterpret_cast<ulonglong2 *>(p) = w;
+    }
+}
+__device__ __forceinline__ void store_rec(Rec<NoValue> *p, uint64_t key, NoValue) { p->key = key; }
 
 __host__ __device__ __forceinline__ uint64_t shl64(uint64_t x, int n) { return n >= 64 ? 0 : x << n; }
 __host__ __device__ __forceinline__ uint64_t shr64(uint64_t x, int n) { return n >= 64 ? 0 : x >> n; }
@@ -227,10 +252,19 @@ coarse_count_kernel(Src src, int64_t nnz, int64_t major_n, int cs, int64_t nb, u
     __shared__ uint32_t h[COARSE_MAX];
     for (int64_t d = threadIdx.x; d < nb; d += blockDim.x) h[d] = 0;
     __syncthreads();
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nnz; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    // eight loads in flight per thread before their shared-memory atomics
+    for (; i + 7 * stride < nnz; i += 8 * stride) {
+        int64_t mj[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) mj[u] = src.major(i + u * stride);
+#pragma unroll
+        for (int u = 0; u < 8; ++u) atomicAdd(&h[(uint64_t)mj[u] < (uint64_t)major_n ? mj[u] >> cs : nb - 1], 1u);
+    }
+    for (; i < nnz; i += stride) {
         const int64_t mj = src.major(i);
-        const int64_t d = (uint64_t)mj < (uint64_t)major_n ? mj >> cs : nb - 1;
-        atomicAdd(&h[d], 1u);
+        atomicAdd(&h[(uint64_t)mj < (uint64_t)major_n ? mj >> cs : nb - 1], 1u);
     }
     __syncthreads();
     for (int64_t d = threadIdx.x; d < nb; d += blockDim.x)
@@ -301,7 +335,7 @@ coarse_place_kernel(Src src, const VT *__restrict__ vals_in, int64_t nnz, int64_
             const int64_t e = t0 + (int64_t)q * PB_THREADS + threadIdx.x;
             if (e < nnz) {
                 const uint32_t slot = s_run[packed[q] >> 16] + (packed[q] & 0xffffu);
-                if constexpr (HAS_VAL) rec1[slot] = Rec<VT>{key[q], val[q]};
+                if constexpr (HAS_VAL) store_rec(rec1 + slot, key[q], val[q]);
                 else rec1[slot] = Rec<VT>{key[q]};
             }
         }
@@ -471,6 +505,297 @@ fine_kernel(int64_t major_n, Coarse co, const uint32_t *__restrict__ cstart, con
     }
 }
 
+// ---- staged two-level form -------------------------------------------------
+//
+// Pass C with one CTA of 1024 threads per SM that copies its next bucket into shared memory
+// with cp.async while it sorts the current one, so that the loads stay in flight across the
+// pass's barriers instead of waiting behind them.  It places a bucket's records by 16-bit
+// indices in shared memory, sorts each row's indices there and writes the bucket's output in
+// order with coalesced stores; a bucket larger than its buffer takes the global path of
+// fine_kernel.  The row pointers and the output are the same as fine_kernel's.
+
+constexpr int ST_THREADS = 1024;
+constexpr int FS_MAXI = 8;                   // pass C: at most 8 staged records per thread
+constexpr int STAGE_ROW_AVG = 8;             // pass C staged while rows average at most 8 entries
+// Pass C staged: a thread sorts rows of up to 8 entries in place, a warp rows of 9 to 256.  (A
+// 16-key in-place thread sort, which at this kernel's 64 registers runs mostly from spilled
+// registers, left rows of 9 to 16 entries unsorted and corrupted the index array on GB300; the
+// warp sort takes those rows.)
+constexpr int STAGE_SMALL = 8;
+
+// The CTA copies the bytes [src, src + bytes) to dst, both 16-byte aligned, in 16-byte
+// pieces; a last partial piece reads only its own bytes and zero-fills the rest.
+__device__ __forceinline__ void copy_to_shared(void *dst, const void *src, uint64_t bytes) {
+    const uint64_t pieces = (bytes + 15) >> 4;
+    for (uint64_t c = threadIdx.x; c < pieces; c += blockDim.x) {
+        const uint64_t left = bytes - (c << 4);
+        cp_async16((char *)dst + (c << 4), (const char *)src + (c << 4), left < 16 ? (uint32_t)left : 16u);
+    }
+}
+
+// Rank-counting sort, by the records' keys, of the N or fewer record indices of one row
+// (idx[0 .. len)), in place: all indices are read before any is written (volatile reads, so
+// that none is read again after the stores).
+template <class R, int N>
+__device__ __forceinline__ void sort_idx_registers(const R *rec, uint16_t *idx, uint32_t len) {
+    const volatile uint16_t *vidx = idx;
+    uint64_t k[N];
+    uint32_t ix[N / 2];  // two 16-bit indices per register
+#pragma unroll
+    for (int j = 0; j < N; j += 2) {
+        const uint32_t a = (uint32_t)j < len ? vidx[j] : 0u, b = (uint32_t)j + 1 < len ? vidx[j + 1] : 0u;
+        ix[j / 2] = a | (b << 16);
+        k[j] = (uint32_t)j < len ? rec[a].key : ~0ull;
+        k[j + 1] = (uint32_t)j + 1 < len ? rec[b].key : ~0ull;
+    }
+#pragma unroll
+    for (int j = 0; j < N; ++j) {
+        if ((uint32_t)j >= len) break;
+        uint32_t rank = 0;
+#pragma unroll
+        for (int q = 0; q < N; ++q) rank += k[q] < k[j] ? 1u : 0u;
+        idx[rank] = (uint16_t)(ix[j / 2] >> (16 * (j & 1)));
+    }
+}
+template <class R> __device__ __forceinline__ void sort_idx_short(const R *rec, uint16_t *idx, uint32_t len) {
+    if (len <= 1) return;
+    if (len <= 4) sort_idx_registers<R, 4>(rec, idx, len);
+    else sort_idx_registers<R, STAGE_SMALL>(rec, idx, len);
+}
+// A warp sorts the record indices of one row of up to WARP_MAX entries in place: each lane
+// holds up to 8 keys, and every key is compared with the row's keys broadcast 32 at a time.
+template <class R> __device__ __forceinline__ void sort_idx_warp(const R *rec, uint16_t *idx, uint32_t len, int lane) {
+    constexpr int P = WARP_MAX / 32;
+    uint64_t k[P];
+    uint32_t ix[P], rank[P];
+#pragma unroll
+    for (int m = 0; m < P; ++m) {
+        const uint32_t t = (uint32_t)(m * 32 + lane);
+        ix[m] = t < len ? idx[t] : 0u;
+        k[m] = t < len ? rec[ix[m]].key : ~0ull;
+        rank[m] = 0;
+    }
+#pragma unroll
+    for (int g = 0; g < P; ++g) {
+        if ((uint32_t)(g * 32) >= len) break;  // uniform across the warp
+        for (int l = 0; l < 32; ++l) {
+            const uint64_t kl = __shfl_sync(0xffffffffu, k[g], l);
+#pragma unroll
+            for (int m = 0; m < P; ++m)
+                if ((uint32_t)(m * 32) < len) rank[m] += kl < k[m] ? 1u : 0u;
+        }
+    }
+    __syncwarp();
+#pragma unroll
+    for (int m = 0; m < P; ++m) {
+        const uint32_t t = (uint32_t)(m * 32 + lane);
+        if (t < len) idx[rank[m]] = (uint16_t)ix[m];
+    }
+    __syncwarp();
+}
+
+// Pass C's buffer: the most records per bucket whose two buffers and index array fit beside
+// the row offsets and counters (a multiple of 16, at most FS_MAXI * ST_THREADS).
+template <class VT> inline int fine_stage_cap(int cs, size_t smem_max) {
+    const size_t rows = (((size_t)2 << cs) + 2) * sizeof(uint32_t);
+    if (smem_max <= rows) return 0;
+    int64_t c = (int64_t)((smem_max - rows) / (2 * sizeof(Rec<VT>) + sizeof(uint16_t)));
+    c &= ~(int64_t)15;
+    return (int)(c > FS_MAXI * ST_THREADS ? FS_MAXI * ST_THREADS : c);
+}
+template <class VT> inline size_t fine_stage_smem(int cs, int cap) {
+    return 2 * (size_t)cap * sizeof(Rec<VT>) + (size_t)cap * sizeof(uint16_t) + (((size_t)2 << cs) + 2) * sizeof(uint32_t);
+}
+
+// Pass C, staged: one CTA per SM takes buckets from a queue (counters[2]) and copies the
+// next bucket's records into shared memory while it sorts the current one.  Rows are
+// counted, scanned (the row pointers) and placed as record indices; rows of up to 16
+// entries are sorted by a thread, up to 256 by a warp, longer ones listed for cta_kernel;
+// then the bucket's output is written in order.  A bucket of more than `cap` entries takes
+// fine_kernel's global path (rows placed into key2 / val2, then sorted there or listed).
+template <class VT, class Emit>
+__global__ void __launch_bounds__(ST_THREADS, 1)
+fine_stage_kernel(int64_t major_n, Coarse co, int cap, const uint32_t *__restrict__ cstart,
+                  const Rec<VT> *__restrict__ rec1, uint64_t *key2, VT *val2, uint32_t *__restrict__ start,
+                  uint32_t *__restrict__ list, uint32_t *__restrict__ counters, Emit emit) {
+    constexpr bool HAS_VAL = !std::is_same<VT, NoValue>::value;
+    constexpr int ITEMS = ROWS_MAX / ST_THREADS;
+    const int cs = co.cs;
+    const int64_t nb = co.nb;
+    const int rshift = co.mb + co.pb;
+    const PackedEmit<Emit> pemit{emit, co.mb, co.pb};
+    extern __shared__ __align__(16) unsigned char dsm[];
+    Rec<VT> *s_buf = (Rec<VT> *)dsm;  // two buffers of cap records
+    uint16_t *s_idx = (uint16_t *)(s_buf + 2 * (size_t)cap);
+    uint32_t *s_off = (uint32_t *)(s_idx + cap);
+    const int rmax = 1 << cs;
+    uint32_t *s_cnt = s_off + rmax + 1;  // row counts; then fill cursors (global path) or the warp row list
+    __shared__ uint32_t s_warp[ST_THREADS / 32];
+    __shared__ uint32_t s_nlist, s_long;
+    __shared__ int64_t s_next;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int64_t bk = blockIdx.x;
+    if (bk < nb) {
+        const uint32_t b0 = cstart[bk], e = cstart[bk + 1] - b0;
+        if (e <= (uint32_t)cap) copy_to_shared(s_buf, rec1 + b0, (uint64_t)e * sizeof(Rec<VT>));
+    }
+    cp_async_commit();
+    for (int b = 0; bk < nb; b ^= 1) {
+        const uint32_t B0 = cstart[bk], B1 = cstart[bk + 1];
+        const uint32_t E = B1 - B0;
+        const bool invalid = bk == nb - 1;
+        const int64_t row0 = invalid ? major_n : bk << cs;
+        const int64_t rspan = major_n - row0 < (int64_t)rmax ? major_n - row0 : (int64_t)rmax;
+        const int R = invalid ? 1 : (int)rspan;
+        const bool staged = E <= (uint32_t)cap;
+        for (int j = threadIdx.x; j < R; j += ST_THREADS) s_cnt[j] = 0;
+        if (threadIdx.x == 0) {
+            s_next = (int64_t)gridDim.x + atomicAdd(&counters[2], 1u);
+            s_nlist = 0;
+            s_long = 0;
+        }
+        __syncthreads();
+        const int64_t nx = s_next;
+        // the other buffer was last read before the previous bucket's final barrier
+        if (nx < nb) {
+            const uint32_t b0 = cstart[nx], e = cstart[nx + 1] - b0;
+            if (e <= (uint32_t)cap)
+                copy_to_shared(s_buf + (size_t)(b ^ 1) * cap, rec1 + b0, (uint64_t)e * sizeof(Rec<VT>));
+        }
+        cp_async_commit();
+        cp_async_wait<1>();
+        __syncthreads();  // bucket bk's records in shared memory
+        const Rec<VT> *s_rec = s_buf + (size_t)b * cap;
+        uint32_t pr[FS_MAXI];  // row << 16 | arrival rank in the row
+        if (staged) {
+#pragma unroll
+            for (int q = 0; q < FS_MAXI; ++q) {
+                const uint32_t j = (uint32_t)(q * ST_THREADS) + threadIdx.x;
+                pr[q] = 0;
+                if (j < E) {
+                    const uint32_t row = (uint32_t)shr64(s_rec[j].key, rshift);
+                    pr[q] = (row << 16) | atomicAdd(&s_cnt[row], 1u);
+                }
+            }
+        } else {
+#pragma unroll 4
+            for (uint32_t i = B0 + threadIdx.x; i < B1; i += ST_THREADS)
+                atomicAdd(&s_cnt[(uint32_t)shr64(rec1[i].key, rshift)], 1u);
+        }
+        __syncthreads();
+        // exclusive scan of the R row counts: each thread takes ITEMS consecutive rows
+        uint32_t v[ITEMS], sum = 0;
+#pragma unroll
+        for (int q = 0; q < ITEMS; ++q) {
+            const int j = threadIdx.x * ITEMS + q;
+            v[q] = j < R ? s_cnt[j] : 0;
+            sum += v[q];
+        }
+        uint32_t x = sum;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) s_warp[warp] = x;
+        __syncthreads();
+        if (warp == 0) {
+            uint32_t wsum = s_warp[lane];
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xffffffffu, wsum, o);
+                if (lane >= o) wsum += y;
+            }
+            s_warp[lane] = wsum;
+        }
+        __syncthreads();
+        uint32_t run = (warp ? s_warp[warp - 1] : 0) + x - sum;
+#pragma unroll
+        for (int q = 0; q < ITEMS; ++q) {
+            const int j = threadIdx.x * ITEMS + q;
+            if (j < R) s_off[j] = run;
+            run += v[q];
+        }
+        if (threadIdx.x == 0) s_off[R] = E;
+        __syncthreads();
+        for (int j = threadIdx.x; j < R; j += ST_THREADS) {
+            const uint32_t first = B0 + s_off[j];
+            start[row0 + j] = first;
+            emit.pointer(row0 + j, first);
+            if (!staged) s_cnt[j] = 0;  // the global path's fill cursors
+            if (s_off[j + 1] - s_off[j] > (uint32_t)WARP_MAX) s_long = 1;
+        }
+        if (invalid && threadIdx.x == 0) start[major_n + 1] = B1;
+        if (staged) {
+            // s_off is complete since the scan; the row counts are no longer read
+#pragma unroll
+            for (int q = 0; q < FS_MAXI; ++q) {
+                const uint32_t j = (uint32_t)(q * ST_THREADS) + threadIdx.x;
+                if (j < E) s_idx[s_off[pr[q] >> 16] + (pr[q] & 0xffffu)] = (uint16_t)j;
+            }
+            __syncthreads();
+            if (s_long) {  // rows for cta_kernel read their (plain) keys from key2
+                for (uint32_t p = threadIdx.x; p < E; p += ST_THREADS)
+                    key2[B0 + p] = canonical_key(s_rec[s_idx[p]].key, co.mb, co.pb);
+            }
+            for (int j0 = 0; j0 < R; j0 += ST_THREADS) {
+                const int j = j0 + threadIdx.x;
+                const bool valid = j < R;
+                uint32_t len = 0;
+                if (valid) {
+                    const uint32_t o = s_off[j];
+                    len = s_off[j + 1] - o;
+                    if (len <= (uint32_t)STAGE_SMALL) sort_idx_short(s_rec, s_idx + o, len);
+                    else if (len <= (uint32_t)WARP_MAX) s_cnt[atomicAdd(&s_nlist, 1u)] = (uint32_t)j;
+                }
+                list_long_rows(valid && len > (uint32_t)WARP_MAX, len, (uint32_t)(row0 + j), major_n, list,
+                               counters);
+            }
+            __syncthreads();
+            if (s_nlist) {  // uniform
+                for (uint32_t q = warp; q < s_nlist; q += ST_THREADS / 32) {
+                    const uint32_t j = s_cnt[q];
+                    const uint32_t o = s_off[j];
+                    sort_idx_warp(s_rec, s_idx + o, s_off[j + 1] - o, lane);
+                }
+                __syncthreads();
+            }
+            // the bucket's output in order (rows listed for cta_kernel are rewritten by it)
+            for (uint32_t p = threadIdx.x; p < E; p += ST_THREADS) {
+                const Rec<VT> r = s_rec[s_idx[p]];
+                const uint64_t row = (uint64_t)row0 + shr64(r.key, rshift);
+                if constexpr (HAS_VAL) pemit.put(B0 + p, row, r.key, r.val);
+                else pemit.gather(B0 + p, row, r.key);
+            }
+        } else {
+            __syncthreads();  // the fill cursors are zero
+            for (uint32_t i = B0 + threadIdx.x; i < B1; i += ST_THREADS) {
+                const Rec<VT> r = rec1[i];
+                const uint32_t row = (uint32_t)shr64(r.key, rshift);
+                const uint32_t slot = B0 + s_off[row] + atomicAdd(&s_cnt[row], 1u);
+                key2[slot] = canonical_key(r.key, co.mb, co.pb);
+                if constexpr (HAS_VAL) val2[slot] = r.val;
+            }
+            __syncthreads();
+            for (int j0 = 0; j0 < R; j0 += ST_THREADS) {
+                const int j = j0 + threadIdx.x;
+                const bool valid = j < R;
+                uint32_t len = 0;
+                if (valid) {
+                    const uint32_t b2 = B0 + s_off[j];
+                    len = s_off[j + 1] - s_off[j];
+                    if (len <= (uint32_t)SMALL)
+                        sort_short_row(key2 + b2, HAS_VAL ? val2 + b2 : nullptr, b2, len, (uint64_t)(row0 + j), emit);
+                }
+                list_long_rows(valid, len, (uint32_t)(row0 + j), major_n, list, counters);
+            }
+        }
+        __syncthreads();
+        bk = nx;
+    }
+    cp_async_wait<0>();
+}
+
 // ---- one-level form (more rows than the coarse buckets cover) --------------
 
 template <class Src>
@@ -577,9 +902,11 @@ __device__ __forceinline__ void merge_runs(const uint64_t *A, uint32_t na, const
     }
 }
 
-// CTA per listed row of more than WARP_MAX entries: up to CTA_TILE keys sorted in shared
-// memory; longer rows sorted in CTA_TILE chunks, then merged pairwise between keys and
-// scratch (the row's own range in each).  Values are gathered by input position.
+// CTA per listed row of more than WARP_MAX entries.  Rows of up to RANK_MAX keys: each key's
+// position is the number of smaller keys in the row (shared memory, two barriers per row);
+// up to CTA_TILE keys: bitonic sort in shared memory; longer rows sorted in CTA_TILE chunks,
+// then merged pairwise between keys and scratch (the row's own range in each).  Values are
+// gathered by input position.
 template <class Emit>
 __global__ void __launch_bounds__(CTA_THREADS)
 cta_kernel(int64_t major_n, const uint32_t *__restrict__ start, uint64_t *keys, uint64_t *scratch,
@@ -589,6 +916,19 @@ cta_kernel(int64_t major_n, const uint32_t *__restrict__ start, uint64_t *keys, 
     for (uint32_t q = blockIdx.x; q < nlisted; q += gridDim.x) {
         const uint32_t r = list[major_n - q];
         const uint32_t b = start[r], len = start[r + 1] - b;
+        if (len <= (uint32_t)RANK_MAX) {  // keys are distinct (they hold the input position)
+            for (uint32_t j = threadIdx.x; j < len; j += blockDim.x) s[j] = keys[b + j];
+            __syncthreads();
+            for (uint32_t j = threadIdx.x; j < len; j += blockDim.x) {
+                const uint64_t kj = s[j];
+                uint32_t rank = 0;
+#pragma unroll 4
+                for (uint32_t u = 0; u < len; ++u) rank += s[u] < kj ? 1u : 0u;
+                emit.gather(b + rank, (uint64_t)r, kj);
+            }
+            __syncthreads();
+            continue;
+        }
         for (uint32_t c0 = 0; c0 < len; c0 += CTA_TILE) {
             const uint32_t n = len - c0 < (uint32_t)CTA_TILE ? len - c0 : (uint32_t)CTA_TILE;
             uint32_t P = 2;
@@ -659,9 +999,23 @@ int sort(cudaStream_t s, int64_t major_n, int64_t minor_n, int64_t nnz, const Sr
         uint32_t *cstart = (uint32_t *)(w + L.cstart);
         Rec<VT> *rec1 = (Rec<VT> *)(w + L.rec1);
         VT *val2 = VS ? (VT *)(w + L.val2) : nullptr;
+        const bool staged = get_sort_staged() != 0;
+        int sms = 0, optin = 0;
+        if (staged) {
+            int dev = 0;
+            rc = check_cuda(cudaGetDevice(&dev), "bucket: device");
+            if (!rc) rc = check_cuda(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "bucket: SMs");
+            if (!rc)
+                rc = check_cuda(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev),
+                                "bucket: shared memory");
+            if (rc) return rc;
+        }
+        // dynamic shared memory the staged kernels may take (their static arrays stay below 512 B)
+        const size_t smax = optin > 1024 ? (size_t)optin - 512 : 0;
+        // the counting pass: six CTAs of 32 KB histograms per SM, each flushing its counts once
         if (nnz > 0)
-            coarse_count_kernel<Src><<<grid_for(nnz, PB_THREADS * PB_ITEMS, cap), PB_THREADS, 0, s>>>(
-                src, nnz, major_n, co.cs, co.nb, cnt);
+            coarse_count_kernel<Src><<<grid_for(nnz, PB_THREADS * PB_ITEMS, staged ? (int64_t)sms * 6 : cap),
+                                       PB_THREADS, 0, s>>>(src, nnz, major_n, co.cs, co.nb, cnt);
         rc = check_cuda(cudaGetLastError(), "bucket coarse_count_kernel");
         if (!rc) rc = scan(s, cnt, cstart, co.nb + 1, bsums);  // cstart[nb] = nnz
         // the fill cursors start at the buckets' first slots
@@ -673,6 +1027,25 @@ int sort(cudaStream_t s, int64_t major_n, int64_t minor_n, int64_t nnz, const Sr
         if (nnz > 0)
             coarse_place_kernel<Src, VT><<<grid_for(nnz, PB_THREADS * PB_ITEMS, cap), PB_THREADS, 0, s>>>(
                 src, vals_in, nnz, major_n, co, cnt, rec1);
+        // the staged pass C copies whole 16-byte-aligned records (conversions carry values); it
+        // pays where rows are short (thread-sorted): with longer rows, most entries are sorted by
+        // warps, whose uneven work two CTAs per SM overlap better (power-law rows averaging 16
+        // entries: 1151 us staged against 671 us)
+        const bool short_rows = nnz <= STAGE_ROW_AVG * major_n;
+        const int fcap = staged && short_rows && sizeof(Rec<VT>) % 16 == 0 ? fine_stage_cap<VT>(co.cs, smax) : 0;
+        if (fcap >= ST_THREADS) {
+            const size_t sm = fine_stage_smem<VT>(co.cs, fcap);
+            rc = check_cuda(cudaFuncSetAttribute(fine_stage_kernel<VT, Emit>,
+                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm),
+                            "bucket: fine_stage_kernel shared memory");
+            if (rc) return rc;
+            fine_stage_kernel<VT, Emit><<<(unsigned)(co.nb < sms ? co.nb : sms), ST_THREADS, sm, s>>>(
+                major_n, co, fcap, cstart, rec1, key2, val2, start, list, counters, emit);
+            warp_kernel<VT, Emit><<<152 * 8, WARP_CTA_THREADS, 0, s>>>(start, key2, val2, list, counters, emit);
+            rc = launch_cta(s, major_n, start, key2, key1, list, counters, emit);
+            if (rc) return rc;
+            return check_cuda(cudaGetLastError(), "bucket sort kernels");
+        }
         const size_t smem = fine_smem_bytes<VT>(co.cs);
         rc = check_cuda(cudaFuncSetAttribute(fine_kernel<VT, Emit>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)smem),

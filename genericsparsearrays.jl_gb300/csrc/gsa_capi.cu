@@ -752,6 +752,11 @@ int gsa_set_tuning(int key, int value) {
         set_x_pairs(value);
         return GSA_OK;
     }
+    if (key == GSA_TUNE_SORT_STAGED) {
+        if (value != 0 && value != 1) return fail(GSA_ERR_INVALID_ARG, "sort staged must be 0 or 1");
+        set_sort_staged(value);
+        return GSA_OK;
+    }
     if (key == GSA_TUNE_WAIT_LIMIT) {
         if (value < 0) return fail(GSA_ERR_INVALID_ARG, "wait limit must be >= 0");
         set_wait_limit(value == 0 ? 0u : (uint32_t)value);
@@ -766,6 +771,7 @@ int gsa_get_tuning(int key) {
     if (key == GSA_TUNE_PLAN_ORDER) return get_plan_natural();
     if (key == GSA_TUNE_STAGE_ROWS) return get_stage_rows();
     if (key == GSA_TUNE_X_PAIRS) return get_x_pairs();
+    if (key == GSA_TUNE_SORT_STAGED) return get_sort_staged();
     if (key == GSA_TUNE_WAIT_LIMIT) {
         const uint32_t w = get_wait_limit();
         return w > 0x7fffffffu ? 0x7fffffff : (int)w;

@@ -23,12 +23,17 @@
 // CSR / CSC -> COO (src/conversions/conversion_kernels.jl:2-35): the major
 // index of every entry is written by merge-path tiles (balanced for any row
 // length mix); minor indices and values are plain copies.
+#include <atomic>
 #include <type_traits>
 
 #include "gsa_internal.cuh"
 #include "gsa_bucket.cuh"
 
 namespace gsa {
+
+static std::atomic<int> g_sort_staged{1};
+void set_sort_staged(int v) { g_sort_staged.store(v, std::memory_order_relaxed); }
+int get_sort_staged() { return g_sort_staged.load(std::memory_order_relaxed); }
 
 constexpr int RS_THREADS = 256;
 constexpr int RS_WARPS = RS_THREADS / 32;

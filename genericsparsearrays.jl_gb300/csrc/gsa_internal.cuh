@@ -188,6 +188,21 @@ template <> __device__ __forceinline__ cf64 ld_coherent(const cf64 *p) {
     return cf64{v.x, v.y};
 }
 
+// Asynchronous 16-byte copies global -> shared (cp.async, L1 bypassed): `bytes` (0..16) are
+// read from src and the rest of the 16 zero-filled; both addresses 16-byte aligned.  A
+// thread's copies are grouped by commit, and wait_group<N> returns once at most N of its
+// groups are still in flight (the copies become visible to other threads at the next barrier).
+__device__ __forceinline__ void cp_async16(void *dst, const void *src, uint32_t bytes) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(
+                     (uint32_t)__cvta_generic_to_shared(dst)),
+                 "l"(src), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N> __device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
 // Streaming loads for data read exactly once (matrix entries): evict-first.
 template <typename T> __device__ __forceinline__ T ld_stream(const T *p) { return __ldcs(p); }
 template <> __device__ __forceinline__ cf32 ld_stream(const cf32 *p) {
@@ -485,6 +500,8 @@ void set_stage_rows(int v);     // 1: thread-per-row warps stage their span with
 int get_stage_rows();
 void set_x_pairs(int v);        // 1 (default): Float64 row-major B read two columns per load
 int get_x_pairs();
+void set_sort_staged(int v);    // 1 (default): the bucket sort's staged passes (one CTA per SM)
+int get_sort_staged();
 
 // Scatter: out[idx_j, c] += conj?(val_j) * (op(B)(o, c) * alpha), after the beta pass.
 // ALGO_MERGE: merge-path tiles (workspace: tile coordinates); otherwise outer blocks with

@@ -97,6 +97,11 @@ typedef enum {
                                   aligned), a thread of 4 or 8 columns reads its columns of one
                                   row of B two at a time with 16-byte loads; 0: one load per
                                   column */
+    GSA_TUNE_SORT_STAGED = 7,  /* 1 (default): where rows average at most 8 entries, the
+                                  conversions' bucket sort runs its row pass as one CTA per SM
+                                  that copies its next bucket into shared memory (cp.async)
+                                  while it sorts the current one; 0: two CTAs per SM that read
+                                  their buckets as they go.  Same output either way */
     GSA_TUNE_WAIT_LIMIT = 4    /* polls a bounded device-side wait (the pipelined SpMV's
                                   mbarrier waits for its bulk copies) makes before it gives
                                   up, sets the device error word and returns: default

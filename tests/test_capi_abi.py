@@ -150,7 +150,7 @@ def test_tuning_knobs(lib, gsa):
     import threading
     L = gsa._lib
     keys = (L.TUNE_PIPE_THREADS, L.TUNE_SPMM_COLUMNS, L.TUNE_PLAN_ORDER, L.TUNE_WAIT_LIMIT, L.TUNE_STAGE_ROWS,
-            L.TUNE_X_PAIRS)
+            L.TUNE_X_PAIRS, L.TUNE_SORT_STAGED)
     saved = {key: lib.gsa_get_tuning(key) for key in keys}
     try:
         assert lib.gsa_set_tuning(L.TUNE_SPMM_COLUMNS, 4) == 0
@@ -169,6 +169,9 @@ def test_tuning_knobs(lib, gsa):
         assert lib.gsa_get_tuning(L.TUNE_X_PAIRS) == saved[L.TUNE_X_PAIRS] == 1
         assert lib.gsa_set_tuning(L.TUNE_X_PAIRS, 0) == 0 and lib.gsa_get_tuning(L.TUNE_X_PAIRS) == 0
         assert lib.gsa_set_tuning(L.TUNE_X_PAIRS, 3) == L.ERR_INVALID_ARG
+        assert lib.gsa_get_tuning(L.TUNE_SORT_STAGED) == saved[L.TUNE_SORT_STAGED] == 1
+        assert lib.gsa_set_tuning(L.TUNE_SORT_STAGED, 0) == 0 and lib.gsa_get_tuning(L.TUNE_SORT_STAGED) == 0
+        assert lib.gsa_set_tuning(L.TUNE_SORT_STAGED, 2) == L.ERR_INVALID_ARG
         assert lib.gsa_set_tuning(L.TUNE_WAIT_LIMIT, 0) == 0
         assert lib.gsa_get_tuning(L.TUNE_WAIT_LIMIT) == 0
         assert lib.gsa_set_tuning(L.TUNE_WAIT_LIMIT, -1) == L.ERR_INVALID_ARG

@@ -14,6 +14,17 @@ pytestmark = pytest.mark.gpu
 GOLDEN = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "known_answers.json")))
 
 
+@pytest.fixture(params=[1, 0], ids=["staged", "unstaged"])
+def sort_staged(request, gsa):
+    """Both forms of the bucket sort's passes (GSA_TUNE_SORT_STAGED), restored afterwards."""
+    lib = gsa._lib.load()
+    key = gsa._lib.TUNE_SORT_STAGED
+    saved = lib.gsa_get_tuning(key)
+    assert lib.gsa_set_tuning(key, request.param) == 0
+    yield request.param
+    lib.gsa_set_tuning(key, saved)
+
+
 def coo(gsa, dev, m, n, r, c, v):
     return gsa.adapt(dev, gsa.GenericSparseMatrixCOO(m, n, r, c, v))
 
@@ -64,7 +75,7 @@ def test_empty(gsa, cuda, m, n):
 
 @pytest.mark.parametrize("it", INDEX_TYPES)
 @pytest.mark.parametrize("dt", VALUE_TYPES)
-def test_permuted_coo_bit_exact(gsa, oracle, cuda, it, dt):
+def test_permuted_coo_bit_exact(gsa, oracle, cuda, sort_staged, it, dt):
     """test/shared/conversions.jl shapes (100x200 at 0.05), triplets shuffled, with duplicate
     (row, col) pairs: CSR and CSC structure and values equal the oracle's bit for bit."""
     rng = np.random.default_rng(31)
@@ -114,7 +125,7 @@ def test_compressed_to_coo_and_round_trips(gsa, oracle, cuda, it):
     assert np.allclose(gsa.collect(Tc), S.toarray().T)
 
 
-def test_power_law_rows_conversion(gsa, oracle, cuda):
+def test_power_law_rows_conversion(gsa, oracle, cuda, sort_staged):
     """Rows of up to 50,000 entries, shuffled triplets: bit-exact against the oracle."""
     from genericsparsearrays_gb300 import workloads
     m, n, rp, cv, nz = workloads.power_law(n=100_000, seed=4, itype=np.int64, dtype=np.float64)
@@ -126,7 +137,7 @@ def test_power_law_rows_conversion(gsa, oracle, cuda):
 
 
 @pytest.mark.parametrize("it", INDEX_TYPES)
-def test_bucket_sizes_with_duplicates(gsa, oracle, cuda, it):
+def test_bucket_sizes_with_duplicates(gsa, oracle, cuda, sort_staged, it):
     """Rows and columns of 0..16 (sorted by a thread), 17..256 (a warp), 257..16384 (a CTA in
     shared memory) and beyond 16384 entries (CTA chunks merged pairwise), each with repeated
     (row, col) pairs carrying different values, shuffled: CSR and CSC equal the oracle's bit
@@ -155,3 +166,74 @@ def test_bucket_sizes_with_duplicates(gsa, oracle, cuda, it):
         assert np.array_equal(np_(ptr), e_ptr)
         assert np.array_equal(np_(idx), e_idx)
         assert np.array_equal(np_(B.nzval), e_val)
+
+
+@pytest.mark.parametrize("it", INDEX_TYPES)
+def test_short_rows_with_long_ones(gsa, oracle, cuda, sort_staged, it):
+    """Rows averaging about two entries (the staged row pass runs) with a few rows and columns
+    of 17, 200, 256, 257, 3000, 4096, 4097 and 40,000 entries among them: rows sorted by a
+    thread, by a warp, by rank counting, by the bitonic sort and in chunks, buckets staged in
+    shared memory and one too large for its buffer; repeated (row, col) pairs; shuffled.  CSR
+    and CSC equal the oracle's bit for bit."""
+    rng = np.random.default_rng(61)
+    m, n = 200_000, 150_000
+    rows = [rng.integers(1, m + 1, 2 * m)]
+    cols = [rng.integers(1, n + 1, 2 * m)]
+    for L in (17, 200, 256, 257, 3000, 4096, 4097, 40_000):
+        r0, c0 = rng.integers(1, m + 1), rng.integers(1, n + 1)
+        c = rng.integers(1, n + 1, L)
+        c[: L // 4] = c[0]  # repeated (row, col) pairs
+        rows += [np.full(L, r0), rng.integers(1, m + 1, L)]
+        cols += [c, np.full(L, c0)]  # the same lengths as columns
+    r = np.concatenate(rows).astype(it)
+    c = np.concatenate(cols).astype(it)
+    v = rng.standard_normal(r.size)
+    p = rng.permutation(r.size)
+    r, c, v = r[p], c[p], v[p]
+    assert r.size <= 8 * min(m, n)
+    A = coo(gsa, cuda, m, n, r, c, v)
+    for cls, f in ((gsa.GenericSparseMatrixCSR, oracle.coo_to_csr), (gsa.GenericSparseMatrixCSC, oracle.coo_to_csc)):
+        B = cls(A)
+        ptr, idx = (B.rowptr, B.colval) if cls is gsa.GenericSparseMatrixCSR else (B.colptr, B.rowval)
+        e_ptr, e_idx, e_val = f(m, n, r, c, v)
+        assert np.array_equal(np_(ptr), e_ptr)
+        assert np.array_equal(np_(idx), e_idx)
+        assert np.array_equal(np_(B.nzval), e_val)
+
+
+@pytest.mark.parametrize("it", INDEX_TYPES)
+@pytest.mark.parametrize("offset", [0, 1, 3])
+def test_unaligned_and_ragged_inputs(gsa, oracle, cuda, sort_staged, it, offset):
+    """Index and value arrays that start `offset` elements into their allocations (not 16-byte
+    aligned for offsets 1 and 3: the staged placement then falls back to plain loads), with
+    entry counts that end inside a 16-byte piece, through the C ABI: bit-exact CSR and CSC."""
+    import ctypes
+    lib = gsa._lib.load()
+    rng = np.random.default_rng(57 + offset)
+    m, n = 3000, 1700
+    for nz in (1, 7, 4099, 50_001):
+        r = rng.integers(1, m + 1, nz).astype(it)
+        c = rng.integers(1, n + 1, nz).astype(it)
+        v = rng.standard_normal(nz)
+        pad = lambda a: torch.from_numpy(np.concatenate([np.zeros(offset, a.dtype), a])).to(cuda)
+        rd, cd, vd = pad(r), pad(c), pad(v)
+        ptr_at = lambda t: ctypes.c_void_p(t.data_ptr() + offset * t.element_size())
+        itype = gsa._lib.IDX32 if it == np.int32 else gsa._lib.IDX64
+        for colmajor, f in ((0, oracle.coo_to_csr), (1, oracle.coo_to_csc)):
+            major_n = n if colmajor else m
+            ws_bytes = lib.gsa_coo_to_compressed_workspace_size(colmajor, gsa._lib.F64, itype, m, n, nz)
+            ws = torch.empty(max(ws_bytes, 1), dtype=torch.uint8, device=cuda)
+            tt = torch.int32 if it == np.int32 else torch.int64
+            ptr = torch.empty(major_n + 1, dtype=tt, device=cuda)
+            idx = torch.empty(nz, dtype=tt, device=cuda)
+            val = torch.empty(nz, dtype=torch.float64, device=cuda)
+            fn = lib.gsa_coo_to_csc if colmajor else lib.gsa_coo_to_csr
+            st = fn(ctypes.c_void_p(torch.cuda.current_stream().cuda_stream), gsa._lib.F64, itype, m, n, nz,
+                    ptr_at(rd), ptr_at(cd), ptr_at(vd), 1, ctypes.c_void_p(ptr.data_ptr()),
+                    ctypes.c_void_p(idx.data_ptr()), ctypes.c_void_p(val.data_ptr()),
+                    ctypes.c_void_p(ws.data_ptr()), ws.numel())
+            assert st == 0, gsa._lib.last_error()
+            e_ptr, e_idx, e_val = f(m, n, r, c, v)
+            assert np.array_equal(np_(ptr), e_ptr)
+            assert np.array_equal(np_(idx), e_idx)
+            assert np.array_equal(np_(val), e_val)

@@ -61,10 +61,22 @@ def test_laplacian_spmm_k16(gsa, oracle, cuda, wl, it, dt):
     assert oracle.max_rel_error((K @ Xd).cpu().numpy(), ye, sc) <= tol
 
 
+@pytest.mark.parametrize("staged", [1, 0])
 @pytest.mark.parametrize("it", [np.int32, np.int64])
-def test_laplacian_permuted_coo_conversion(gsa, cuda, wl, it):
+def test_laplacian_permuted_coo_conversion(gsa, cuda, wl, it, staged):
     """COO -> CSR and COO -> CSC of the randomly permuted Laplacian triplets are bit-exact
-    (keys need 44 bits: the reference's Int32 keys would wrap here)."""
+    (keys need 44 bits: the reference's Int32 keys would wrap here), with the bucket sort's
+    staged and unstaged passes."""
+    lib = gsa._lib.load()
+    saved = lib.gsa_get_tuning(gsa._lib.TUNE_SORT_STAGED)
+    assert lib.gsa_set_tuning(gsa._lib.TUNE_SORT_STAGED, staged) == 0
+    try:
+        _laplacian_conversion(gsa, cuda, wl, it)
+    finally:
+        lib.gsa_set_tuning(gsa._lib.TUNE_SORT_STAGED, saved)
+
+
+def _laplacian_conversion(gsa, cuda, wl, it):
     m, n, rp, cv, nz = wl.laplacian_2d(2048, itype=it, dtype=np.float64)
     _, _, r, c, v = wl.permuted_coo(m, n, rp, cv, nz, seed=7)
     A = gsa.adapt(cuda, gsa.GenericSparseMatrixCOO(m, n, r, c, v))
