@@ -39,6 +39,13 @@ namespace gsa {
 #define GSA_RB_MIN_BLOCKS 16
 #endif
 template <typename V, int KC> constexpr int rb_min_blocks() { return KC * sizeof(V) <= 8 ? GSA_RB_MIN_BLOCKS : 0; }
+// The bin order's ComplexF64 SpMV is held to 8 resident CTAs, which lets the compiler keep 64
+// registers (48 without the bound) and more loads in flight: power-law n = 10^6 160 us against
+// 170 us on one GB300 (10 CTAs at 48 registers: 167 us, 12 at 40: 177 us); the grouped kernel
+// gained nothing from the same bounds.
+template <typename V, int KC> constexpr int binned_min_blocks() {
+    return std::is_same<V, cf64>::value && KC == 1 ? 8 : rb_min_blocks<V, KC>();
+}
 
 // The bin order pays where the FP64 pipe binds: ComplexF64 products (four FMAs per entry)
 // and Float64 products with several right-hand sides (one FMA per entry and column); a
@@ -296,7 +303,7 @@ int get_stage_rows() { return g_stage_rows.load(std::memory_order_relaxed); }
 // neighbouring rows share are still in L2 when the second of them is read.
 
 template <typename V, typename I, int KC>
-__global__ void __launch_bounds__(RB_THREADS, rb_min_blocks<V, KC>())
+__global__ void __launch_bounds__(RB_THREADS, binned_min_blocks<V, KC>())
 binned_kernel(CompressedArgs<V, I> a, int64_t k, DenseIn<V> B, DenseOut<V> C, int64_t ncg, gsa_bin_order bv,
               PlanRows L) {
     const unsigned cta = blockIdx.x;
