@@ -271,8 +271,14 @@ coarse_count_kernel(Src src, int64_t nnz, int64_t major_n, int cs, int64_t nb, u
         if (h[d]) atomicAdd(&cnt[d], h[d]);
 }
 
+// Resident CTAs of the placement: 4 (64 registers, half the SM's warps) measured 631 us for
+// the permuted Laplacian F64/I64 conversion against 666 us with 3 (80 registers), 664 with 5 and
+// 683 with 6 (both spilling); the power-law ComplexF64 conversion is the same within noise.
+#ifndef GSA_PB_MIN_BLOCKS
+#define GSA_PB_MIN_BLOCKS 4
+#endif
 template <class Src, class VT>
-__global__ void __launch_bounds__(PB_THREADS, 3)
+__global__ void __launch_bounds__(PB_THREADS, GSA_PB_MIN_BLOCKS)
 coarse_place_kernel(Src src, const VT *__restrict__ vals_in, int64_t nnz, int64_t major_n, Coarse co,
                     uint32_t *__restrict__ cfill, Rec<VT> *__restrict__ rec1) {
     const int cs = co.cs;
