@@ -20,8 +20,8 @@
 //      shared memory (96 KB of staging; cs is chosen so that an average bucket fills at most
 //      half of it).  Rows of up to 16 entries are sorted there by a thread in registers (rank
 //      counting), rows of up to 256 by a warp, and emitted; longer rows go to cta_kernel
-//      (bitonic sort of 16384-entry chunks in shared memory, merged pairwise; values then
-//      gathered by input position).  A bucket larger than the staging is placed in global
+//      (rank counting up to 1024 entries, else a bitonic sort of 16384-entry chunks in shared
+//      memory, merged pairwise; values then gathered by input position).  A bucket larger than the staging is placed in global
 //      memory instead, with its rows of more than 16 entries listed for warp_kernel and
 //      cta_kernel.  Where rows average at most 8 entries, fine_stage_kernel runs this pass
 //      instead: one CTA per SM, the next bucket's records copied into shared memory while the

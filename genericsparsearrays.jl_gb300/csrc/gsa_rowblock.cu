@@ -41,10 +41,13 @@ namespace gsa {
 template <typename V, int KC> constexpr int rb_min_blocks() { return KC * sizeof(V) <= 8 ? GSA_RB_MIN_BLOCKS : 0; }
 // The bin order's ComplexF64 SpMV is held to 8 resident CTAs, which lets the compiler keep 64
 // registers (48 without the bound) and more loads in flight: power-law n = 10^6 160 us against
-// 170 us on one GB300 (10 CTAs at 48 registers: 167 us, 12 at 40: 177 us); the grouped kernel
-// gained nothing from the same bounds.
+// 170 us on one GB300 (12 CTAs at 40 registers: 177 us, 10 at 48: 167 us, 7 at 72: 163 us, 6 at
+// 74: 169 us, 5 at 88: 178 us); the grouped kernel gained nothing from the same bounds.
+#ifndef GSA_BINNED_C64_MIN_BLOCKS
+#define GSA_BINNED_C64_MIN_BLOCKS 8
+#endif
 template <typename V, int KC> constexpr int binned_min_blocks() {
-    return std::is_same<V, cf64>::value && KC == 1 ? 8 : rb_min_blocks<V, KC>();
+    return std::is_same<V, cf64>::value && KC == 1 ? GSA_BINNED_C64_MIN_BLOCKS : rb_min_blocks<V, KC>();
 }
 
 // The bin order pays where the FP64 pipe binds: ComplexF64 products (four FMAs per entry)
